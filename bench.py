@@ -1,0 +1,432 @@
+"""Throughput of the FastGB hot path on GB300: fused waveform + log-likelihood.
+
+Workload (one step = one pass over the whole batch): 200,000 Galactic
+binaries, f0 log-uniform on [1e-4, 2.5e-2] Hz, N chosen per binary by
+frequency band from {64, 128, 256, 512, 1024, 2048}, amp log-U(1e-23, 1e-21),
+fdot log-U(1e-18, 1e-15), fddot = 11/3 fdot^2/f0, angles isotropic; T = 4 x
+31,557,600 s, dt = 5 s; data = the injected sum of all binaries plus
+Gaussian noise drawn from the analytic A/E PSD on the full 0-0.1 Hz grid
+(L = 12,623,041 bins, A and E, complex128).  Synthetic, seeded.
+
+``value``: binaries/s of the mixed-precision fused kernel (one persistent
+work-queue launch per step; parameters, data and PSD resident in HBM).
+``e2e``: the same metric through ``GBGPU.get_ll`` with the parameters copied
+from pinned host memory every step and the log-likelihoods read back.
+The plain-FP64 form of the same kernel is timed on the same batch
+(``fp64_binaries_per_s``).  ``--impl reference`` times the reference's CPU
+path (its algorithm restated in the oracle) on the host cores instead.
+"""
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+T_OBS = 4 * 31557600.0
+DT = 5.0
+B_DEFAULT = 200_000
+BANDS = [(1e-4, 5e-4, 64), (5e-4, 1e-3, 128), (1e-3, 3e-3, 256), (3e-3, 6e-3, 512),
+         (6e-3, 1.2e-2, 1024), (1.2e-2, 2.5e-2 + 1e-12, 2048)]
+METRIC = "binaries/s (wave+loglike) & grads/s, mixed vs plain FP64, 1 GB300, <=1e-6 rel ll"
+
+
+def draw_workload(B, seed):
+    rng = np.random.default_rng(seed)
+    f0 = 10 ** rng.uniform(-4, np.log10(2.5e-2), B)
+    fdot = 10 ** rng.uniform(-18, -15, B)
+    p = np.array([10 ** rng.uniform(-23, -21, B), f0, fdot, 11.0 / 3.0 * fdot ** 2 / f0,
+                  rng.uniform(0, 2 * np.pi, B), np.arccos(rng.uniform(-1, 1, B)),
+                  rng.uniform(0, np.pi, B), rng.uniform(0, 2 * np.pi, B),
+                  np.arcsin(rng.uniform(-1, 1, B))])
+    Ns = np.zeros(B, np.int64)
+    for lo, hi, n in BANDS:
+        Ns[(f0 >= lo) & (f0 < hi)] = n
+    assert np.all(Ns > 0)
+    return p, Ns
+
+
+def alg_bytes(Ns):
+    """Algorithmic HBM bytes of one fused launch: per binary the A/E data
+    (2 x 16 B) and PSD (2 x 8 B) windows of N bins, 9 FP64 parameters and
+    two complex128 outputs: 48 N + 72 + 32."""
+    return float(np.sum(48 * Ns + 104))
+
+
+class ClockSampler:
+    """nvidia-smi SM clock / throttle sampling while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        import torch
+        try:
+            self.index = "GPU-" + str(torch.cuda.get_device_properties(index).uuid)
+        except Exception:
+            self.index = str(index)
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4)
+                          if len(r) > 5 + i and r[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+# ------------------------------------------------------------------ CPU side
+def _cpu_warm(_):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import fastgb_oracle as O
+    O._lib()
+    return 0
+
+
+def _cpu_task(args):
+    """One oracle chunk: waveform (NumPy) + native get_ll (C) for binaries of
+    one N whose windows lie in the given data slice."""
+    import time as _t
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import fastgb_oracle as O
+    p, N, dA, dE, S, s0 = args
+    t0 = _t.perf_counter()
+    O.get_ll(p, [dA, dE], [S, S], N, T=T_OBS, dt=DT, start_freq_ind=s0)
+    return _t.perf_counter() - t0, p.shape[1]
+
+
+def cpu_baseline(p, Ns, dA, dE, S, workers, per_class=(256, 256, 128, 64, 32, 24)):
+    """Times the oracle port on a bounded sample of every N class with a spawn
+    pool of ``workers`` processes and extrapolates to the workload's N mix."""
+    import multiprocessing as mp
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import fastgb_oracle as O
+    O._lib()                                  # build/load before the pool starts
+    tasks = []
+    sample = {}
+    for (lo, hi, n), m in zip(BANDS, per_class):
+        idx = np.nonzero(Ns == n)[0][:m]
+        idx = idx[np.argsort(p[1, idx])]
+        sample[n] = len(idx)
+        chunk = max(1, len(idx) // max(1, workers // 2))
+        for c in range(0, len(idx), chunk):
+            sel = idx[c:c + chunk]
+            si = O.start_indices(p[1, sel], n, T_OBS, DT)
+            a, b = int(si.min()) - 1, int(si.max()) + n + 1
+            tasks.append((p[:, sel].copy(), n, dA[a:b].copy(), dE[a:b].copy(), S[a:b].copy(), a))
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(workers) as pool:
+        pool.map(_cpu_warm, range(workers), chunksize=1)     # imports done before timing
+        t0 = time.perf_counter()
+        res = pool.map(_cpu_task, tasks, chunksize=1)
+        wall = time.perf_counter() - t0
+    busy = {}
+    for (task, (dt_, nb)) in zip(tasks, res):
+        busy[task[1]] = busy.get(task[1], 0.0) + dt_
+    per_bin = {n: busy[n] / sample[n] for n in busy}
+    total_cpu = sum(per_bin[n] * np.count_nonzero(Ns == n) for n in per_bin)
+    eff = sum(busy.values()) / wall                    # effective parallel workers
+    value = len(Ns) / (total_cpu / max(eff, 1e-9))
+    return {"value": value, "unit": "binaries/s", "cores": int(workers), "kind": "port",
+            "sample": (f"oracle (NumPy waveform + C get_ll) on {sum(sample.values())} binaries "
+                       f"({', '.join(f'{sample[n]}xN={n}' for n in sorted(sample))}), "
+                       f"{workers} spawn workers, wall {wall:.1f} s, extrapolated by "
+                       f"per-N cost to the {len(Ns)}-binary mix"),
+            "seconds_per_binary": {str(n): per_bin[n] for n in sorted(per_bin)}}
+
+
+# ------------------------------------------------------------------ GPU side
+def make_data(gb, p, Ns, seed):
+    """Injected sum of all binaries + Gaussian noise from the analytic A/E PSD."""
+    import torch
+    from gbgpu_gb300.sensitivity import A1TDISens
+    T = int(T_OBS / DT) * DT
+    L = int(int(T_OBS / DT) / 2) + 1
+    f = np.arange(L) / T
+    S = np.empty(L)
+    S[1:] = A1TDISens.get_Sn(f[1:])
+    S[0] = np.inf
+    Sd = torch.as_tensor(S, device="cuda")
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    sig = torch.sqrt(Sd * (T / 4.0))
+    sig[0] = 0.0
+    data = []
+    for _ in range(2):
+        re = torch.randn(L, device="cuda", dtype=torch.float64, generator=g)
+        im = torch.randn(L, device="cuda", dtype=torch.float64, generator=g)
+        data.append(torch.complex(re * sig, im * sig))
+    # the sources, one N class at a time (the FP64 fused fill kernel)
+    tmpl = torch.zeros((1, 2, L), dtype=torch.complex128, device="cuda")
+    acc = torch.zeros_like(tmpl)
+    for n in np.unique(Ns):
+        sel = Ns == n
+        gb.generate_global_template(p[:, sel].T, np.zeros(int(sel.sum()), np.int32), tmpl,
+                                    N=int(n), T=T_OBS, dt=DT, precision="fp64")
+        acc += tmpl
+    data[0] += acc[0, 0]
+    data[1] += acc[0, 1]
+    w = 4.0 / T / Sd
+    w[0] = 0.0
+    d_d = float((w * (data[0].abs() ** 2 + data[1].abs() ** 2)).sum().item())
+    return data, Sd, d_d, S
+
+
+def run_gpu(args, rank, world):
+    import torch
+    import torch.distributed as dist
+    from gbgpu_gb300 import GBGPU
+    from gbgpu_gb300 import _native as nat
+    import ctypes
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    B = args.binaries
+    p, Ns = draw_workload(B, args.seed + rank)
+    gb = GBGPU(precision="mixed")
+    data, Sd, d_d, S_host = make_data(gb, p, Ns, args.seed + rank)
+    gb.d_d = d_d
+    L = data[0].shape[0]
+
+    params_d = torch.as_tensor(p, device="cuda").contiguous()
+    plans = {prec: gb._plan(Ns, int(T_OBS / DT) * DT, prec, False, 9)
+             for prec in ("mixed", "fp64")}
+    d_h = torch.empty(B, dtype=torch.complex128, device="cuda")
+    h_h = torch.empty(B, dtype=torch.complex128, device="cuda")
+    zeros = torch.zeros(B, dtype=torch.int32, device="cuda")
+    la = nat.LLArgs()
+    la.A_data, la.E_data = data[0].data_ptr(), data[1].data_ptr()
+    la.A_psd = la.E_psd = Sd.data_ptr()
+    la.data_length, la.num_data, la.num_psd = L, 1, 1
+    la.data_index = la.noise_index = zeros.data_ptr()
+    la.df = 1.0 / (int(T_OBS / DT) * DT)
+    wargs = {k: v.args(params_d) for k, v in plans.items()}
+    lib = nat.lib()
+    stream = torch.cuda.current_stream()
+    sh = nat.stream_handle(stream)
+
+    def step(prec):
+        rc = lib.gbx_waveform_ll(ctypes.byref(wargs[prec]), ctypes.byref(la),
+                                 ctypes.c_void_p(d_h.data_ptr()), ctypes.c_void_p(h_h.data_ptr()), sh)
+        if rc:
+            nat.check(rc, "gbx_waveform_ll")
+
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def timed(prec, K, W):
+        for _ in range(W):
+            step(prec)
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(K)]
+        t_wall = time.perf_counter()
+        for a, b in ev:
+            flush.zero_()                     # evict L2 between timed steps
+            a.record(stream)
+            step(prec)
+            b.record(stream)
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall
+        ms = [a.elapsed_time(b) for a, b in ev]
+        return float(np.mean(ms)), t_wall
+
+    # accuracy of the mixed form on the full batch against the FP64 form
+    step("fp64")
+    hh64 = h_h.clone()
+    dh64 = d_h.clone()
+    step("mixed")
+    torch.cuda.synchronize()
+    like64 = -0.5 * (d_d + hh64.real - 2 * dh64.real)
+    likem = -0.5 * (d_d + h_h.real - 2 * d_h.real)
+    scaled = ((likem - like64).abs() / torch.clamp(hh64.real, min=1.0)).max().item()
+
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        ms_mixed, wall_mixed = timed("mixed", args.steps, args.warmup)
+    ms_fp64, _ = timed("fp64", max(1, min(args.steps, 3)), 1)
+
+    # e2e through the public API: host params -> device, like -> host
+    p_pin = torch.from_numpy(np.ascontiguousarray(p)).pin_memory()
+    for _ in range(max(1, args.warmup)):
+        gb.get_ll(p_pin, data, [Sd, Sd], N=Ns, T=T_OBS, dt=DT, precision="mixed")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        gb.get_ll(p_pin, data, [Sd, Sd], N=Ns, T=T_OBS, dt=DT, precision="mixed")
+    e2e_s = (time.perf_counter() - t0) / args.steps
+
+    t_max = ms_mixed
+    e2e_max = e2e_s
+    if world > 1:
+        t = torch.tensor([ms_mixed, e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max, e2e_max = float(t[0]), float(t[1])
+    value = world * B / (t_max / 1e3)
+    ab = alg_bytes(Ns)
+    achieved = ab / (ms_mixed / 1e3) / 1e9
+    peak, peak_src = hbm_peak()
+    traffic = profiled_traffic()
+    out = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "binaries/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": t_max,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+f64 (FP64 phase/delay/accumulation, FP32 slow part and FFT)",
+        "data": "synthetic (seeded binaries; injected sum + Gaussian noise from the analytic A/E PSD)",
+        "config": {"workload": "config1: 200k binaries, uneven N in {64..2048} by f0 band, "
+                               "T=4x31557600 s, dt=5 s, L=12,623,041 bins x A,E complex128",
+                   "binaries_per_gpu": B, "N_mix": {str(n): int(np.count_nonzero(Ns == n))
+                                                    for n in np.unique(Ns)},
+                   "precision": "mixed", "l2": "flushed (256 MB write) before every timed step; "
+                   "data+PSD (606 MB) also exceed L2",
+                   "parallelism": f"replicas x{world} (binaries sharded, no collective)"},
+        "gpu_launches": args.steps,
+        "fp64_binaries_per_s": B / (ms_fp64 / 1e3),
+        "mixed_over_fp64": ms_fp64 / ms_mixed,
+        "mixed_max_scaled_dlogL_vs_fp64": scaled,
+        "grads_per_s": None,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "note": f"peak {peak_src}; the kernel is FP64-pipe bound (carrier phase), "
+                             "so the HBM fraction is low by design"},
+        "e2e": {"value": world * B / e2e_max, "unit": "binaries/s",
+                "h2d_bytes_per_step": int(p.nbytes), "d2h_bytes_per_step": int(B * 8)},
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(p, Ns, data[0].cpu().numpy(), data[1].cpu().numpy(),
+                                           S_host, workers=args.cpu_workers)
+    return out
+
+
+def hbm_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "of measured (MEASURED_PEAKS.json hbm_gbs)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "of fallback (6.8 TB/s)"
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the fused kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "wave_ll_mixed_config1.txt")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def run_reference(args):
+    """CPU reference arm: the reference's algorithm (oracle port) on all host cores."""
+    p, Ns = draw_workload(args.binaries, args.seed)
+    from gbgpu_gb300.sensitivity import A1TDISens
+    T = int(T_OBS / DT) * DT
+    L = int(int(T_OBS / DT) / 2) + 1
+    rng = np.random.default_rng(args.seed)
+    f = np.arange(L) / T
+    S = np.empty(L)
+    S[1:] = A1TDISens.get_Sn(f[1:])
+    S[0] = np.inf
+    sig = np.sqrt(S * T / 4.0)
+    sig[0] = 0.0
+    dA = (rng.standard_normal(L) + 1j * rng.standard_normal(L)) * sig
+    dE = (rng.standard_normal(L) + 1j * rng.standard_normal(L)) * sig
+    workers = os.cpu_count() or 1
+    vals = []
+    base = None
+    for _ in range(max(1, args.steps)):
+        base = cpu_baseline(p, Ns, dA, dE, S, workers=workers,
+                            per_class=(64, 64, 32, 16, 8, 8))
+        vals.append(base["value"])
+    v = float(np.median(vals))
+    base["value"] = v
+    return {"metric": METRIC, "value": v, "unit": "binaries/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded; noise-only data for the CPU timing)",
+            "config": {"workload": "config1: 200k binaries, uneven N in {64..2048} by f0 band, "
+                                   "T=4x31557600 s, dt=5 s, L=12,623,041 bins x A,E complex128"},
+            "impl": "reference", "cpu_baseline": base,
+            "e2e": {"value": v, "unit": "binaries/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--binaries", type=int, default=B_DEFAULT)
+    ap.add_argument("--seed", type=int, default=2026)
+    ap.add_argument("--cpu-workers", type=int, default=os.cpu_count() or 1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        print(json.dumps(run_reference(args)), flush=True)
+        return
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    out = run_gpu(args, rank, world)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,51 @@
+// Shared device helpers for the GB300 FastGB kernels (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/gbgpu_gb300.h"
+
+namespace gbx {
+
+constexpr int kBlock = 256;        // threads per CTA for the waveform family
+constexpr int kTileMin = 512;      // minimum samples per tile (P = kTileMin / N binaries)
+constexpr int kMaxPack = 16;       // kTileMin / 32
+constexpr int kTwN = 8192;         // twiddle table period (largest supported N)
+constexpr double kPi = 3.141592653589793238462643383279502884;
+constexpr double kTwoPi = 6.283185307179586476925286766559005768;
+constexpr double kInvTwoPi = 0.159154943091895335768883763372514362;
+constexpr double kCSI = 299792458.0;
+
+// ---------------------------------------------------------------- complex
+template <typename R> struct C2;
+template <> struct C2<float> { using T = float2; };
+template <> struct C2<double> { using T = double2; };
+
+__device__ __forceinline__ float2 mk(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ double2 mk(double a, double b) { return make_double2(a, b); }
+
+template <typename V> __device__ __forceinline__ V cadd(V a, V b) { V r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename V> __device__ __forceinline__ V csub(V a, V b) { V r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template <typename V> __device__ __forceinline__ V cmul(V a, V b)
+{
+    V r;
+    r.x = a.x * b.x - a.y * b.y;
+    r.y = a.x * b.y + a.y * b.x;
+    return r;
+}
+template <typename V, typename S> __device__ __forceinline__ V cscale(V a, S s)
+{
+    V r; r.x = a.x * s; r.y = a.y * s; return r;
+}
+
+// bit reversal of the low `bits` bits
+__device__ __forceinline__ int bitrev(int k, int bits) { return (int)(__brev((unsigned)k) >> (32 - bits)); }
+
+// ---------------------------------------------------------------- status
+__device__ __forceinline__ void flag(int *status, int bit)
+{
+    if (status) atomicOr(status, bit);
+}
+
+}  // namespace gbx

@@ -1,0 +1,160 @@
+// Drop-in replacements for the reference's two native kernels
+// (gbgpu/cutils/gbgpu_utils.cu): batched <d|h>, <h|h> over point-major
+// templates, and the scatter-add of templates into global buffers.
+// One warp per binary: lanes walk the N-point window, so the data and PSD
+// windows (contiguous in memory) are read with coalesced 16-/8-byte loads.
+#include "gbx_common.cuh"
+#include "gbx_internal.h"
+
+namespace gbx {
+
+__global__ void __launch_bounds__(256) get_ll_kernel(
+    double2 *__restrict__ d_h, double2 *__restrict__ h_h, const double2 *__restrict__ A_t,
+    const double2 *__restrict__ E_t, const double2 *__restrict__ A_d,
+    const double2 *__restrict__ E_d, const double *__restrict__ A_p,
+    const double *__restrict__ E_p, double df, const int *__restrict__ start_ind, int M,
+    int num_bin, const int *__restrict__ data_index, const int *__restrict__ noise_index,
+    int L, long long tsi, long long tsb, int *status)
+{
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < num_bin; b += warps) {
+        const int s = start_ind[b];
+        const size_t doff = (size_t)(data_index ? data_index[b] : 0) * L;
+        const size_t noff = (size_t)(noise_index ? noise_index[b] : 0) * L;
+        double dr = 0.0, di = 0.0, hh = 0.0;
+        bool out = false;
+        for (int i = lane; i < M; i += 32) {
+            const int j = s + i;
+            if (j < 0 || j >= L) {
+                out = true;
+                continue;
+            }
+            const double2 hA = __ldg(A_t + i * tsi + b * tsb);
+            const double2 hE = __ldg(E_t + i * tsi + b * tsb);
+            const double2 dA = __ldg(A_d + doff + j), dE = __ldg(E_d + doff + j);
+            const double wA = 1.0 / __ldg(A_p + noff + j), wE = 1.0 / __ldg(E_p + noff + j);
+            // conj(d) h / S and conj(h) h / S  (gbgpu_utils.cu:172-178)
+            dr += (dA.x * hA.x + dA.y * hA.y) * wA + (dE.x * hE.x + dE.y * hE.y) * wE;
+            di += (dA.x * hA.y - dA.y * hA.x) * wA + (dE.x * hE.y - dE.y * hE.x) * wE;
+            hh += (hA.x * hA.x + hA.y * hA.y) * wA + (hE.x * hE.x + hE.y * hE.y) * wE;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            dr += __shfl_xor_sync(0xffffffffu, dr, o);
+            di += __shfl_xor_sync(0xffffffffu, di, o);
+            hh += __shfl_xor_sync(0xffffffffu, hh, o);
+        }
+        if (__any_sync(0xffffffffu, out) && lane == 0) flag(status, GBX_FLAG_WINDOW);
+        if (lane == 0) {
+            const double s4 = 4. * df;
+            d_h[b] = make_double2(s4 * dr, s4 * di);
+            h_h[b] = make_double2(s4 * hh, 0.0);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) fill_global_kernel(
+    double2 *__restrict__ A_g, double2 *__restrict__ E_g, const double2 *__restrict__ A_t,
+    const double2 *__restrict__ E_t, const int *__restrict__ start_ind, int M, int num_bin,
+    const int *__restrict__ group_index, int L, long long gstride, long long tsi, long long tsb,
+    int num_groups, int *status)
+{
+    const int lane = threadIdx.x & 31;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    for (int b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < num_bin; b += warps) {
+        const int s = start_ind[b];
+        const int g = group_index[b];
+        if (num_groups > 0 && (g < 0 || g >= num_groups)) {
+            if (lane == 0) flag(status, GBX_FLAG_INDEX);
+            continue;
+        }
+        const size_t goff = (size_t)g * gstride;
+        for (int i = lane; i < M; i += 32) {
+            const int j = s + i;
+            if (j < 0 || j >= L) continue;    // gbgpu_utils.cu:88-91
+            const double2 a = __ldg(A_t + i * tsi + b * tsb);
+            const double2 e = __ldg(E_t + i * tsi + b * tsb);
+            atomicAdd(&A_g[goff + j].x, a.x);
+            atomicAdd(&A_g[goff + j].y, a.y);
+            atomicAdd(&E_g[goff + j].x, e.x);
+            atomicAdd(&E_g[goff + j].y, e.y);
+        }
+    }
+}
+
+static int grid_for(int num_bin)
+{
+    int blocks = (num_bin + 7) / 8;
+    int cap = num_sms() * 8;
+    return blocks < cap ? (blocks > 0 ? blocks : 1) : cap;
+}
+
+}  // namespace gbx
+
+using namespace gbx;
+
+extern "C" int gbx_get_ll_ex(void *d_h, void *h_h, const void *A_template,
+                             const void *E_template, const void *A_data, const void *E_data,
+                             const double *A_psd, const double *E_psd, double df,
+                             const int *start_ind, int M, int num_bin, const int *data_index,
+                             const int *noise_index, int data_length, long long t_stride_i,
+                             long long t_stride_b, int *status, void *stream)
+{
+    if (num_bin < 0 || M < 0 || data_length < 0) return set_error(GBX_ERR_ARG, "negative size");
+    if (num_bin == 0) return GBX_OK;
+    if (!d_h || !h_h || !A_template || !E_template || !A_data || !E_data || !A_psd || !E_psd ||
+        !start_ind)
+        return set_error(GBX_ERR_ARG, "NULL pointer");
+    int rc = ensure_init((cudaStream_t)stream);
+    if (rc) return rc;
+    get_ll_kernel<<<grid_for(num_bin), 256, 0, (cudaStream_t)stream>>>(
+        (double2 *)d_h, (double2 *)h_h, (const double2 *)A_template, (const double2 *)E_template,
+        (const double2 *)A_data, (const double2 *)E_data, A_psd, E_psd, df, start_ind, M, num_bin,
+        data_index, noise_index, data_length, t_stride_i, t_stride_b, status);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_error(e, "get_ll launch");
+    return GBX_OK;
+}
+
+extern "C" int gbx_get_ll(void *d_h, void *h_h, const void *A_template, const void *E_template,
+                          const void *A_data, const void *E_data, const double *A_psd,
+                          const double *E_psd, double df, const int *start_ind, int M,
+                          int num_bin, const int *data_index, const int *noise_index,
+                          int data_length, int *status, void *stream)
+{
+    return gbx_get_ll_ex(d_h, h_h, A_template, E_template, A_data, E_data, A_psd, E_psd, df,
+                         start_ind, M, num_bin, data_index, noise_index, data_length,
+                         (long long)num_bin, 1LL, status, stream);
+}
+
+extern "C" int gbx_fill_global_ex(void *A_glob, void *E_glob, const void *A_template,
+                                  const void *E_template, const int *start_ind, int M,
+                                  int num_bin, const int *group_index, int data_length,
+                                  int num_groups, long long group_stride, long long t_stride_i,
+                                  long long t_stride_b, int *status, void *stream)
+{
+    if (num_bin < 0 || M < 0 || data_length < 0) return set_error(GBX_ERR_ARG, "negative size");
+    if (num_bin == 0) return GBX_OK;
+    if (!A_glob || !E_glob || !A_template || !E_template || !start_ind || !group_index)
+        return set_error(GBX_ERR_ARG, "NULL pointer");
+    if (group_stride < data_length) return set_error(GBX_ERR_ARG, "group_stride < data_length");
+    int rc = ensure_init((cudaStream_t)stream);
+    if (rc) return rc;
+    fill_global_kernel<<<grid_for(num_bin), 256, 0, (cudaStream_t)stream>>>(
+        (double2 *)A_glob, (double2 *)E_glob, (const double2 *)A_template,
+        (const double2 *)E_template, start_ind, M, num_bin, group_index, data_length,
+        group_stride, t_stride_i, t_stride_b, num_groups, status);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_error(e, "fill_global launch");
+    return GBX_OK;
+}
+
+extern "C" int gbx_fill_global(void *A_glob, void *E_glob, const void *A_template,
+                               const void *E_template, const int *start_ind, int M, int num_bin,
+                               const int *group_index, int data_length, int *status, void *stream)
+{
+    return gbx_fill_global_ex(A_glob, E_glob, A_template, E_template, start_ind, M, num_bin,
+                              group_index, data_length, 0, (long long)data_length,
+                              (long long)num_bin, 1LL, status, stream);
+}

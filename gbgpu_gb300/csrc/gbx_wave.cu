@@ -1,0 +1,997 @@
+// FastGB waveform family for GB300 (sm_103a): one CTA builds a tile of
+// binaries (P = max(1, 512/N) of them) entirely in shared memory -- slow part,
+// N-point FFT, fftshift/heterodyne and TDI combination -- and then either
+// writes the reference's output arrays, folds the window into <d|h>, <h|h>
+// against the data and PSD, or scatter-adds it into global templates.
+//
+// Reference: gbgpu/gbgpu.py:108-578 (waveform), gbgpu/thirdbody.py:155-428
+// (third body), gbgpu/cutils/gbgpu_utils.cu:54-185 (likelihood / fill loops).
+#include <math.h>
+#include <string.h>
+
+#include "gbx_common.cuh"
+#include "gbx_internal.h"
+
+namespace gbx {
+
+__device__ double2 g_tw_d[kTwN / 2];
+__device__ float2 g_tw_f[kTwN / 2];
+
+__global__ void tw_init_kernel()
+{
+    int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m < kTwN / 2) {
+        double s, c;
+        sincospi(-2.0 * (double)m / (double)kTwN, &s, &c);
+        g_tw_d[m] = make_double2(c, s);
+        g_tw_f[m] = make_float2((float)c, (float)s);
+    }
+}
+
+template <typename R> __device__ __forceinline__ typename C2<R>::T tw(int m);
+template <> __device__ __forceinline__ float2 tw<float>(int m) { return g_tw_f[m]; }
+template <> __device__ __forceinline__ double2 tw<double>(int m) { return g_tw_d[m]; }
+
+// ----------------------------------------------------------------------------
+// per-binary constants (shared memory)
+// ----------------------------------------------------------------------------
+struct Bin {
+    double f0, fdot, fddot, phi0;
+    double om, om_m_dfa;           // 2 pi f0, 2 pi f0 - 2 pi q/T   (gbgpu.py:462-464)
+    double pifdot, pi3fddot;       // pi fdot, pi/3 fddot           (gbgpu.py:495-500)
+    double k[3];
+    double ep[6], ec[6];           // e+ and ex, order xx yy zz xy xz yz
+    double2 DP, DC;                // polarisation factors divided by amp
+    double2 scale;                 // amp * 0.5 T / N [* tdi2 factor]
+    double A2, varpi, e2, n2, T2;  // third body (n2, T2 in SI)
+    float kf[3], epf[6], ecf[6];
+    float2 DPf, DCf;
+    float f0f, fdotf, fddotf;
+    float w0h, w0l, w1, w2;        // f(t)/fstar = (w0h + w0l) + w1 t + w2 t^2 (w0 split hi/lo)
+    float A2f, e2f, varpif, sinvarpif;
+    int start;                     // start index - start_freq_ind
+    int b;                         // binary index
+    int di, ni, gi;                // data / noise / group rows
+    int eS, eD;                    // power-of-two scalings of the mixed likelihood
+    int valid;
+};
+
+struct KParams {
+    gbx_wave_args a;
+    // likelihood
+    const double2 *A_data, *E_data;
+    const double *A_psd, *E_psd;
+    int L, num_data, num_psd;
+    const int *data_index, *noise_index;
+    double df;
+    double2 *d_h, *h_h;
+    // waveform outputs
+    double2 *XYZ, *AET;
+    int *start_out;
+    // fill
+    double2 *A_glob, *E_glob;
+    const int *group_index;
+    int num_groups;
+    long long gstride;             // elements between consecutive groups of A_glob / E_glob
+    int P;                         // binaries per tile in uniform mode
+    int maxS;                      // largest tile (samples) the shared memory is sized for
+};
+
+enum { MODE_WAVE = 0, MODE_LL = 1, MODE_FILL = 2 };
+
+__device__ __forceinline__ double quad_form(const double *e, double x, double y, double z)
+{
+    return e[0] * x * x + e[1] * y * y + e[2] * z * z +
+           2.0 * (e[3] * x * y + e[4] * x * z + e[5] * y * z);
+}
+__device__ __forceinline__ float quad_form(const float *e, float x, float y, float z)
+{
+    float xx = x * x, yy = y * y, zz = z * z, xy = x * y, xz = x * z, yz = y * z;
+    return fmaf(e[0], xx, fmaf(e[1], yy, fmaf(e[2], zz, 2.0f * fmaf(e[3], xy, fmaf(e[4], xz, e[5] * yz)))));
+}
+
+// sin(a)/a from its Taylor series (error < 1e-11 for |a| <= 1.6), falls back
+// to sinf(a)/a for larger arguments.
+__device__ __forceinline__ float sinc_f(float a)
+{
+    float x = a * a;
+    if (x < 2.56f) {
+        float p = -1.0f / 1307674368000.0f;
+        p = fmaf(p, x, 1.0f / 6227020800.0f);
+        p = fmaf(p, x, -1.0f / 39916800.0f);
+        p = fmaf(p, x, 1.0f / 362880.0f);
+        p = fmaf(p, x, -1.0f / 5040.0f);
+        p = fmaf(p, x, 1.0f / 120.0f);
+        p = fmaf(p, x, -1.0f / 6.0f);
+        return fmaf(p, x, 1.0f);
+    }
+    return sinf(a) / a;
+}
+
+// FP64 -> FP32 with an exact power-of-two scaling, done on the integer pipe.
+// Rounds to nearest (ties away), flushes results below FP32's normal range to
+// signed zero and saturates to infinity above it.
+__device__ __forceinline__ float d2f_scaled(double x, int e)
+{
+    unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    unsigned hi = (unsigned)(bits >> 32), lo = (unsigned)bits;
+    unsigned sign = hi & 0x80000000u;
+    int ex = (int)((hi >> 20) & 0x7ffu);
+    int ne = ex - 1023 + 127 + e;
+    unsigned mag = ((unsigned)ne << 23) + (((hi & 0xfffffu) << 3) | (lo >> 29)) + ((lo >> 28) & 1u);
+    mag = (ne >= 255) ? 0x7f800000u : mag;
+    mag = (ne <= 0 || ex == 0) ? 0u : mag;
+    return __uint_as_float(sign | mag);
+}
+
+// ----------------------------------------------------------------------------
+// third body: line-of-sight velocity (gbgpu/thirdbody.py:228-380)
+// ----------------------------------------------------------------------------
+__device__ double vlos_fp64(double t, const Bin &B)
+{
+    // Kepler inverse exactly as gbgpu/thirdbody.py:243-320
+    double l = B.n2 * (t - B.T2);
+    double e = B.e2;
+    bool neg = l < 0.0;
+    l = fabs(l);
+    bool over2pi = l > 2.0 * kPi;
+    double mult = 0.0;
+    if (over2pi) {
+        mult = floor(l / (2.0 * kPi));
+        l -= mult * 2.0 * kPi;
+    }
+    bool overpi = l > kPi;
+    if (overpi) l = 2.0 * kPi - l;
+    double alpha = (1.0 - e) / (4.0 * e + 0.5);
+    double beta = 0.5 * l / (4.0 * e + 0.5);
+    double z = sqrt(beta * beta + alpha * alpha * alpha);
+    z = neg ? beta - z : beta + z;
+    z = (z < 0.0) ? -pow(-z, 1.0 / 3.0) : pow(z, 1.0 / 3.0);
+    double s = z - alpha / z;
+    double w = s - 0.078 * s * s * s * s * s / (1.0 + e);
+    double u0 = l + e * (3.0 * w - 4.0 * w * w * w);
+    double su0, cu0;
+    sincos(u0, &su0, &cu0);
+    double f = u0 - e * su0 - l;
+    double f1 = 1.0 - e * cu0;
+    double f2 = u0 - f - l;
+    double f3 = 1.0 - f1;
+    double f4 = -f2;
+    f2 *= 0.5;
+    f3 *= 0.166666666666667;
+    f4 *= 0.0416666666666667;
+    double u1 = -f / f1;
+    double u2 = -f / (f1 + f2 * u1);
+    double u3 = -f / (f1 + f2 * u2 + f3 * u2 * u2);
+    double u4 = -f / (f1 + f2 * u3 + f3 * u3 * u3 + f4 * u3 * u3 * u3);
+    double u = u0 + u4;
+    if (overpi) u = 2.0 * kPi - u;
+    if (over2pi) u = 2.0 * kPi * mult + u;
+    if (neg) u = -u;
+    // true anomaly (gbgpu/thirdbody.py:339-350)
+    if (e > 1e-6) {
+        double bt = (1.0 - sqrt(1.0 - e * e)) / e;
+        double su, cu;
+        sincos(u, &su, &cu);
+        u += 2.0 * atan2(bt * su, 1.0 - bt * cu);
+    }
+    return B.A2 * (sin(u + B.varpi) + e * sin(B.varpi));
+}
+
+// Same model with the Kepler solve in FP32.  The mean anomaly and its 2 pi
+// reductions stay in FP64; since only sin/cos of the anomaly are used, the
+// un-reduction is applied modulo 2 pi, which keeps |u| <= pi in FP32.
+__device__ float vlos_mixed(double t, const Bin &B)
+{
+    double ld = B.n2 * (t - B.T2);
+    bool neg = ld < 0.0;
+    ld = fabs(ld);
+    if (ld > 2.0 * kPi) ld -= floor(ld * kInvTwoPi) * 2.0 * kPi;
+    bool overpi = ld > kPi;
+    if (overpi) ld = 2.0 * kPi - ld;
+    float l = (float)ld;
+    float e = B.e2f;
+    float alpha = (1.0f - e) / (4.0f * e + 0.5f);
+    float beta = 0.5f * l / (4.0f * e + 0.5f);
+    float z = sqrtf(beta * beta + alpha * alpha * alpha);
+    z = neg ? beta - z : beta + z;
+    z = cbrtf(z);
+    float s = z - alpha / z;
+    float s2 = s * s;
+    float w = s - 0.078f * s2 * s2 * s / (1.0f + e);
+    float u0 = l + e * (3.0f * w - 4.0f * w * w * w);
+    float su0, cu0;
+    sincosf(u0, &su0, &cu0);
+    float f = u0 - e * su0 - l;
+    float f1 = 1.0f - e * cu0;
+    float f2 = 0.5f * (e * su0);
+    float f3 = (1.0f / 6.0f) * (e * cu0);
+    float f4 = -(1.0f / 24.0f) * (e * su0);
+    float u1 = -f / f1;
+    float u2 = -f / (f1 + f2 * u1);
+    float u3 = -f / (f1 + f2 * u2 + f3 * u2 * u2);
+    float u4 = -f / (f1 + f2 * u3 + f3 * u3 * u3 + f4 * u3 * u3 * u3);
+    float u = u0 + u4;
+    if (overpi) u = -u;
+    if (neg) u = -u;
+    if (e > 1e-6f) {
+        float bt = (1.0f - sqrtf(1.0f - e * e)) / e;
+        float su, cu;
+        sincosf(u, &su, &cu);
+        u += 2.0f * atan2f(bt * su, 1.0f - bt * cu);
+    }
+    return B.A2f * (sinf(u + B.varpif) + e * B.sinvarpif);
+}
+
+// ----------------------------------------------------------------------------
+// per-binary set-up (gbgpu.py:212-266, 296-309)
+// ----------------------------------------------------------------------------
+__device__ void setup_bin(Bin &B, const KParams &K, int b, int N, int mode)
+{
+    const gbx_wave_args &a = K.a;
+    const int nb = a.num_bin;
+    const double *p = a.params;
+    double amp = p[b], f0 = p[nb + b], fdot = p[2 * nb + b], fddot = p[3 * nb + b];
+    double phi0 = p[4 * nb + b], iota = p[5 * nb + b], psi = p[6 * nb + b];
+    double lam = p[7 * nb + b], beta = p[8 * nb + b];
+    const double T = a.T;
+    B.b = b;
+    B.valid = 1;
+    B.f0 = f0; B.fdot = fdot; B.fddot = fddot; B.phi0 = phi0;
+    double q = rint(f0 * T);
+    // om - 2 pi q/T cancels about seven digits; the two products are rounded
+    // separately (no FMA contraction) so the phase slope carries the same
+    // rounding as the reference's (om - df) (gbgpu.py:462-464, 497)
+    B.om = __dmul_rn(2.0 * kPi, f0);
+    B.om_m_dfa = __dsub_rn(B.om, __dmul_rn(2.0 * kPi, q / T));
+    B.pifdot = kPi * fdot;
+    B.pi3fddot = (1.0 / 3.0 * kPi) * fddot;
+    double ci = cos(iota);
+    double s2p, c2p;
+    sincos(2.0 * psi, &s2p, &c2p);
+    double Ap = 1.0 + ci * ci, Ac = -2.0 * ci;
+    B.DP = make_double2(Ap * c2p, -Ac * s2p);
+    B.DC = make_double2(-Ap * s2p, -Ac * c2p);
+    double theta = kPi / 2.0 - beta;
+    double st, ct, sp, cp;
+    sincos(theta, &st, &ct);
+    sincos(lam, &sp, &cp);
+    double u[3] = {ct * cp, ct * sp, -st};
+    double v[3] = {sp, -cp, 0.0};
+    B.k[0] = -st * cp; B.k[1] = -st * sp; B.k[2] = -ct;
+    const int ia[6] = {0, 1, 2, 0, 0, 1}, ib[6] = {0, 1, 2, 1, 2, 2};
+    for (int c = 0; c < 6; c++) {
+        B.ep[c] = v[ia[c]] * v[ib[c]] - u[ia[c]] * u[ib[c]];
+        B.ec[c] = u[ia[c]] * v[ib[c]] + v[ia[c]] * u[ib[c]];
+        B.epf[c] = (float)B.ep[c];
+        B.ecf[c] = (float)B.ec[c];
+    }
+    for (int c = 0; c < 3; c++) B.kf[c] = (float)B.k[c];
+    B.DPf = make_float2((float)B.DP.x, (float)B.DP.y);
+    B.DCf = make_float2((float)B.DC.x, (float)B.DC.y);
+    B.f0f = (float)f0; B.fdotf = (float)fdot; B.fddotf = (float)fddot;
+    {
+        // f/fstar with the constant term kept as an unevaluated float pair so
+        // the FP32 transfer frequency carries no per-binary rounding bias
+        const double fstar = kCSI / (a.armlength * 2.0 * kPi);
+        double w0 = f0 / fstar;
+        B.w0h = (float)w0;
+        B.w0l = (float)(w0 - (double)B.w0h);
+        B.w1 = (float)(fdot / fstar);
+        B.w2 = (float)(0.5 * fddot / fstar);
+    }
+    // start index, bit-exact with round(((q - N/2)/T)/(1/T))  (gbgpu.py:296, 387)
+    double fmin = (q - (double)N / 2.0) / T;
+    double kmin = rint(fmin / (1.0 / T));
+    B.start = (int)kmin - a.start_freq_ind;
+    // output scaling (gbgpu.py:298-309): amp * 0.5 T / N [* 2i sin 2wL e^{-2iwL}]
+    double fc = 0.5 * T / (double)N;
+    double2 sc = make_double2(amp * fc, 0.0);
+    if (a.tdi2) {
+        double omL = 2.0 * kPi * f0 * (a.armlength / kCSI);
+        double s2, c2;
+        sincos(2.0 * omL, &s2, &c2);
+        // 2i s (c - i s) = 2 s^2 + 2i s c
+        double2 t2 = make_double2(2.0 * s2 * s2, 2.0 * s2 * c2);
+        sc = make_double2(fc * t2.x * amp, fc * t2.y * amp);
+    }
+    B.scale = sc;
+    if (a.nparams >= 14) {
+        B.A2 = p[9 * nb + b];
+        B.varpi = p[10 * nb + b];
+        B.e2 = p[11 * nb + b];
+        double P2 = p[12 * nb + b];
+        B.n2 = 2.0 * kPi / (P2 * a.year);
+        B.T2 = p[13 * nb + b] * a.year;
+        B.A2f = (float)B.A2;
+        B.e2f = (float)B.e2;
+        double vr = B.varpi - 2.0 * kPi * floor(B.varpi * kInvTwoPi);
+        B.varpif = (float)vr;
+        B.sinvarpif = (float)sin(B.varpi);
+    }
+    B.di = B.ni = B.gi = 0;
+    B.eS = B.eD = 0;
+    if (mode == MODE_LL) {
+        int di = K.data_index ? K.data_index[b] : 0;
+        int ni = K.noise_index ? K.noise_index[b] : 0;
+        if (di < 0 || di >= K.num_data || ni < 0 || ni >= K.num_psd) {
+            flag(a.status, GBX_FLAG_INDEX);
+            B.valid = 0;
+            di = ni = 0;
+        }
+        B.di = di; B.ni = ni;
+        // power-of-two scalings so that S*2^eS and d*2^eD are O(1) in FP32
+        int jm = B.start + N / 2;
+        jm = jm < 0 ? 0 : (jm >= K.L ? K.L - 1 : jm);
+        double Sm = K.A_psd[(size_t)ni * K.L + jm];
+        int lg = (Sm > 0.0 && isfinite(Sm)) ? ilogb(Sm) : 0;
+        B.eS = -lg;
+        B.eD = -(lg >> 1) - 14;
+    } else if (mode == MODE_FILL) {
+        int gi = K.group_index[b];
+        if (gi < 0 || gi >= K.num_groups) {
+            flag(a.status, GBX_FLAG_INDEX);
+            B.valid = 0;
+            gi = 0;
+        }
+        B.gi = gi;
+    }
+}
+
+// ----------------------------------------------------------------------------
+// slow part at one sample (gbgpu.py:399-540 and 348-375)
+// writes fctr2 * {X, Y, Z} (amplitude divided out) into out[0..2]
+// ----------------------------------------------------------------------------
+template <bool THIRD>
+__device__ __forceinline__ void slow_fp64(const Bin &B, int n, int N, double tm, double inv_c_unused,
+                                          const double *__restrict__ tab, double fstar,
+                                          const double *psi, const double *vl, double2 out[3])
+{
+    double Pc[3][3], r[3][3];
+#pragma unroll
+    for (int s = 0; s < 3; s++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            Pc[s][c] = __ldg(tab + (size_t)(3 * s + c) * N + n);
+            r[s][c] = __ldg(tab + (size_t)(9 + 3 * s + c) * N + n);
+        }
+    double kdotr[3], kP[3], xi[3], fonfs[3], kp[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+        kdotr[a] = B.k[0] * r[a][0] + B.k[1] * r[a][1] + B.k[2] * r[a][2];
+#pragma unroll
+    for (int s = 0; s < 3; s++) {
+        kP[s] = B.k[0] * Pc[s][0] + B.k[1] * Pc[s][1] + B.k[2] * Pc[s][2];
+        xi[s] = tm - kP[s];
+        double fi = B.f0 + B.fdot * xi[s] + 0.5 * B.fddot * xi[s] * xi[s];
+        if (THIRD) fi *= 1.0 + vl[s] / kCSI;
+        fonfs[s] = fi / fstar;
+        double argS = B.phi0 + B.om_m_dfa * tm + B.pifdot * xi[s] * xi[s] +
+                      B.pi3fddot * xi[s] * xi[s] * xi[s];
+        if (THIRD) argS += psi[s];
+        kp[s] = B.om * kP[s] - argS;
+    }
+    double2 A[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        double pp = quad_form(B.ep, r[a][0], r[a][1], r[a][2]);
+        double cc = quad_form(B.ec, r[a][0], r[a][1], r[a][2]);
+        A[a] = make_double2(pp * B.DP.x + cc * B.DC.x, pp * B.DP.y + cc * B.DC.y);
+    }
+    // links (ij, sym arm, spacecraft, sign of kdotr): 12,23,31,21,32,13
+    double2 G[6];
+    const int arm[6] = {0, 1, 2, 0, 1, 2};
+    const int sc[6] = {0, 1, 2, 1, 2, 0};
+    const double sg[6] = {1.0, 1.0, 1.0, -1.0, -1.0, -1.0};
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+        double arg = 0.5 * fonfs[sc[q]] * (1.0 + sg[q] * kdotr[arm[q]]);
+        double sn, cs;
+        sincos(arg + kp[sc[q]], &sn, &cs);
+        double amp = 0.25 * sin(arg) / arg;
+        double2 e = make_double2(amp * cs, -amp * sn);
+        G[q] = cmul(e, A[arm[q]]);
+    }
+    double f = B.f0 + B.fdot * tm + 0.5 * B.fddot * tm * tm;
+    double omL = f / fstar;
+    double so, co;
+    sincos(omL, &so, &co);
+    double2 fc = make_double2(co, -so);
+    double2 fc2 = make_double2(4.0 * omL * so * co, -4.0 * omL * so * so);
+    // X = G21 - G31 + (G12 - G13) fc, cyclic (gbgpu.py:370-372)
+    double2 X = cadd(csub(G[3], G[2]), cmul(csub(G[0], G[5]), fc));
+    double2 Y = cadd(csub(G[4], G[0]), cmul(csub(G[1], G[3]), fc));
+    double2 Z = cadd(csub(G[5], G[1]), cmul(csub(G[2], G[4]), fc));
+    out[0] = cmul(fc2, X);
+    out[1] = cmul(fc2, Y);
+    out[2] = cmul(fc2, Z);
+}
+
+template <bool THIRD>
+__device__ __forceinline__ void slow_mixed(const Bin &B, int n, int N, double tm,
+                                           const double *__restrict__ tab, float inv_fstar,
+                                           const double *psi, const float *vl, float2 out[3])
+{
+    const float *tabf = reinterpret_cast<const float *>(tab + (size_t)18 * N);
+    float r[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) r[a][c] = __ldg(tabf + (size_t)(3 * a + c) * N + n);
+    float kdotr[3], fonfs[3], phh[3], phl[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+        kdotr[a] = fmaf(B.kf[0], r[a][0], fmaf(B.kf[1], r[a][1], B.kf[2] * r[a][2]));
+    const double base = B.phi0 + B.om_m_dfa * tm;
+#pragma unroll
+    for (int s = 0; s < 3; s++) {
+        // FP64: light-travel delay, delayed time and carrier phase
+        double kP = B.k[0] * __ldg(tab + (size_t)(3 * s) * N + n) +
+                    B.k[1] * __ldg(tab + (size_t)(3 * s + 1) * N + n) +
+                    B.k[2] * __ldg(tab + (size_t)(3 * s + 2) * N + n);
+        double xi = tm - kP;
+        double argS = fma(xi * xi, fma(B.pi3fddot, xi, B.pifdot), base);
+        if (THIRD) argS += psi[s];
+        double kp = fma(B.om, kP, -argS);
+        double red = fma(-rint(kp * kInvTwoPi), kTwoPi, kp);
+        phh[s] = (float)red;
+        phl[s] = (float)(red - (double)phh[s]);
+        // FP32: instantaneous frequency over the transfer frequency
+        float xf = (float)xi;
+        float fo = B.w0h + fmaf(fmaf(B.w2, xf, B.w1), xf, B.w0l);
+        if (THIRD) fo *= 1.0f + vl[s] * (float)(1.0 / kCSI);
+        fonfs[s] = fo;
+    }
+    float2 A[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        float pp = quad_form(B.epf, r[a][0], r[a][1], r[a][2]);
+        float cc = quad_form(B.ecf, r[a][0], r[a][1], r[a][2]);
+        A[a] = make_float2(fmaf(pp, B.DPf.x, cc * B.DCf.x), fmaf(pp, B.DPf.y, cc * B.DCf.y));
+    }
+    float2 G[6];
+    const int arm[6] = {0, 1, 2, 0, 1, 2};
+    const int sc[6] = {0, 1, 2, 1, 2, 0};
+    const float sg[6] = {1.f, 1.f, 1.f, -1.f, -1.f, -1.f};
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+        float arg = 0.5f * fonfs[sc[q]] * fmaf(sg[q], kdotr[arm[q]], 1.0f);
+        // arg + phase as an exact float sum (TwoSum) plus the FP64 remainder
+        float hi = arg + phh[sc[q]];
+        float bb = hi - arg;
+        float lo = ((arg - (hi - bb)) + (phh[sc[q]] - bb)) + phl[sc[q]];
+        float sn, cs;
+        sincosf(hi, &sn, &cs);
+        // exp(-i(hi + lo)) ~ (cs - i sn)(1 - i lo)
+        float er = fmaf(-sn, lo, cs);
+        float ei = -fmaf(cs, lo, sn);
+        float amp = 0.25f * sinc_f(arg);
+        float2 e = make_float2(amp * er, amp * ei);
+        G[q] = cmul(e, A[arm[q]]);
+    }
+    float tf = (float)tm;
+    float omL = B.w0h + fmaf(fmaf(B.w2, tf, B.w1), tf, B.w0l);
+    float so, co;
+    sincosf(omL, &so, &co);
+    float2 fc = make_float2(co, -so);
+    float g4 = 4.0f * omL * so;
+    float2 fc2 = make_float2(g4 * co, -g4 * so);
+    float2 X = cadd(csub(G[3], G[2]), cmul(csub(G[0], G[5]), fc));
+    float2 Y = cadd(csub(G[4], G[0]), cmul(csub(G[1], G[3]), fc));
+    float2 Z = cadd(csub(G[5], G[1]), cmul(csub(G[2], G[4]), fc));
+    out[0] = cmul(fc2, X);
+    out[1] = cmul(fc2, Y);
+    out[2] = cmul(fc2, Z);
+}
+
+// ----------------------------------------------------------------------------
+// in-place radix-2 decimation-in-frequency FFT over `nsub` contiguous
+// sub-arrays of length N in shared memory; output in bit-reversed order.
+// ----------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ void fft_dif(typename C2<R>::T *buf, int nsub, int lg)
+{
+    using V = typename C2<R>::T;
+    const int N = 1 << lg;
+    const int half = N >> 1;
+    const int total = nsub * half;
+    for (int hl = lg - 1; hl >= 0; hl--) {
+        const int h = 1 << hl;
+        const int tstride = kTwN >> (hl + 1);   // W_{2h}^r = W_{kTwN}^{r * kTwN/(2h)}
+        for (int beta = threadIdx.x; beta < total; beta += kBlock) {
+            int a = beta >> (lg - 1);
+            int j = beta & (half - 1);
+            int g = j >> hl;
+            int r = j & (h - 1);
+            int i0 = (a << lg) + (g << (hl + 1)) + r;
+            V x0 = buf[i0], x1 = buf[i0 + h];
+            V w = tw<R>(r * tstride);
+            buf[i0] = cadd(x0, x1);
+            buf[i0 + h] = cmul(csub(x0, x1), w);
+        }
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// ----------------------------------------------------------------------------
+// the kernel
+// ----------------------------------------------------------------------------
+template <typename R, int MODE, bool THIRD>
+__global__ void __launch_bounds__(kBlock, 2) wave_kernel(const KParams K)
+{
+    using V = typename C2<R>::T;
+    extern __shared__ __align__(16) unsigned char smem[];
+    Bin *bins = reinterpret_cast<Bin *>(smem);
+    double *red = reinterpret_cast<double *>(smem + sizeof(Bin) * kMaxPack);  // [maxS/32][3]
+    V *buf = reinterpret_cast<V *>(smem + sizeof(Bin) * kMaxPack + sizeof(double) * 3 * (K.maxS >> 5));
+    __shared__ int s_tile;
+
+    const gbx_wave_args &a = K.a;
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31;
+    const int ntiles = a.tiles ? a.ntiles : (a.num_bin + K.P - 1) / K.P;
+    const double fstar = kCSI / (a.armlength * 2.0 * kPi);
+    const float inv_fstar = (float)(1.0 / fstar);
+    int iter = 0;
+
+    for (;;) {
+        if (tid == 0) {
+            if (a.queue) s_tile = atomicAdd(a.queue, 1);
+            else s_tile = blockIdx.x + iter * gridDim.x;
+        }
+        __syncthreads();
+        const int tile = s_tile;
+        iter++;
+        if (tile >= ntiles) break;
+        int lg, first, cnt;
+        if (a.tiles) {
+            lg = a.tiles[4 * tile];
+            first = a.tiles[4 * tile + 1];
+            cnt = a.tiles[4 * tile + 2];
+        } else {
+            lg = 31 - __clz(a.N);
+            first = tile * K.P;
+            cnt = min(K.P, a.num_bin - first);
+        }
+        const int N = 1 << lg;
+        const double *tab = (lg >= 5 && lg <= GBX_MAX_LOG2N)
+                                ? reinterpret_cast<const double *>(a.orbit[lg]) : nullptr;
+        const int maxcnt = max(1, kTileMin >> lg);
+        if (tab == nullptr || cnt < 1 || cnt > maxcnt || first < 0 || first + cnt > a.num_bin ||
+            (cnt << lg) > K.maxS || (sizeof(R) == 8 && lg > 12)) {
+            flag(a.status, GBX_FLAG_TILE);
+            __syncthreads();
+            continue;
+        }
+        if (tid < cnt) {
+            int slot = first + tid;
+            int b = a.order ? a.order[slot] : slot;
+            if (b < 0 || b >= a.num_bin) {
+                flag(a.status, GBX_FLAG_TILE);
+                memset(&bins[tid], 0, sizeof(Bin));
+                bins[tid].b = -1;
+            } else {
+                setup_bin(bins[tid], K, b, N, MODE);
+            }
+        }
+        __syncthreads();
+
+        const int S = cnt << lg;                 // samples in this tile
+        const double step = a.T / (double)N;     // tm = n T/N (gbgpu.py:269)
+
+        double *psi = nullptr;
+        R *vl = nullptr;
+        if (THIRD) {
+            // third-body pre-passes (gbgpu/thirdbody.py:155-226):
+            // A) v_LOS and g = v_LOS f_GW at every (sample, spacecraft)
+            psi = reinterpret_cast<double *>(buf + 3 * (size_t)maxcnt * N);
+            vl = reinterpret_cast<R *>(psi + 3 * (size_t)maxcnt * N);
+            double *inc = reinterpret_cast<double *>(buf);
+            for (int m = tid; m < S; m += kBlock) {
+                const int p = m >> lg, n = m & (N - 1);
+                const Bin &B = bins[p];
+                const double tm = (double)n * step;
+#pragma unroll
+                for (int s = 0; s < 3; s++) {
+                    double kP = B.k[0] * __ldg(tab + (size_t)(3 * s) * N + n) +
+                                B.k[1] * __ldg(tab + (size_t)(3 * s + 1) * N + n) +
+                                B.k[2] * __ldg(tab + (size_t)(3 * s + 2) * N + n);
+                    double xi = tm - kP;
+                    double v = (sizeof(R) == 8) ? vlos_fp64(xi, B) : (double)vlos_mixed(xi, B);
+                    double fgw = B.f0 + B.fdot * xi + 0.5 * B.fddot * xi * xi;
+                    psi[(p * 3 + s) * N + n] = v * fgw;
+                    vl[(p * 3 + s) * N + n] = (R)v;
+                }
+            }
+            __syncthreads();
+            // B) trapezoid increments (xi_n - xi_{n-1}) (g_{n-1} + g_n) pi / c
+            for (int m = tid; m < S; m += kBlock) {
+                const int p = m >> lg, n = m & (N - 1);
+                const Bin &B = bins[p];
+#pragma unroll
+                for (int s = 0; s < 3; s++) {
+                    double v = 0.0;
+                    if (n > 0) {
+                        double d = step;
+#pragma unroll
+                        for (int c = 0; c < 3; c++)
+                            d -= B.k[c] * (__ldg(tab + (size_t)(3 * s + c) * N + n) -
+                                           __ldg(tab + (size_t)(3 * s + c) * N + n - 1));
+                        // xi_n - xi_{n-1} = step - (kP_n - kP_{n-1})
+                        v = d * (psi[(p * 3 + s) * N + n - 1] + psi[(p * 3 + s) * N + n]) / 2.0 *
+                            kPi * 2.0 / kCSI;
+                    }
+                    inc[(p * 3 + s) * N + n] = v;
+                }
+            }
+            __syncthreads();
+            // C) inclusive prefix sum along n for every (binary, spacecraft): warp per row
+            const int chunk = N >> 5;
+            for (int row = warp; row < 3 * cnt; row += kBlock / 32) {
+                const double *src = inc + (size_t)row * N + lane * chunk;
+                double *dst = psi + (size_t)row * N + lane * chunk;
+                double t = 0.0;
+                for (int c = 0; c < chunk; c++) t += src[c];
+                double incl = t;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    double y = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += y;
+                }
+                double run = incl - t;
+                for (int c = 0; c < chunk; c++) {
+                    run += src[c];
+                    dst[c] = run;
+                }
+            }
+            __syncthreads();
+        }
+
+        // slow part -> buf[(p*3 + channel)*N + n]
+        for (int m = tid; m < S; m += kBlock) {
+            const int p = m >> lg, n = m & (N - 1);
+            const Bin &B = bins[p];
+            const double tm = (double)n * step;
+            double ps[3] = {0.0, 0.0, 0.0};
+            R vv[3] = {0, 0, 0};
+            if (THIRD) {
+#pragma unroll
+                for (int s = 0; s < 3; s++) {
+                    ps[s] = psi[(p * 3 + s) * N + n];
+                    vv[s] = vl[(p * 3 + s) * N + n];
+                }
+            }
+            V o[3];
+            if constexpr (sizeof(R) == 8) {
+                double vd[3] = {(double)vv[0], (double)vv[1], (double)vv[2]};
+                slow_fp64<THIRD>(B, n, N, tm, 0.0, tab, fstar, ps, vd, reinterpret_cast<double2 *>(o));
+            } else {
+                float vf[3] = {(float)vv[0], (float)vv[1], (float)vv[2]};
+                slow_mixed<THIRD>(B, n, N, tm, tab, inv_fstar, ps, vf, reinterpret_cast<float2 *>(o));
+            }
+#pragma unroll
+            for (int c = 0; c < 3; c++) buf[(p * 3 + c) * N + n] = o[c];
+        }
+        __syncthreads();
+
+        fft_dif<R>(buf, 3 * cnt, lg);
+
+        // ------------------------------------------------------------ epilogue
+        const R is2 = (R)0.70710678118654752440, is6 = (R)0.40824829046386301637;
+        if (MODE == MODE_WAVE) {
+            for (int m = tid; m < S; m += kBlock) {
+                const int p = m >> lg, i = m & (N - 1);
+                const Bin &B = bins[p];
+                if (B.b < 0) continue;
+                const int pos = bitrev((i + (N >> 1)) & (N - 1), lg);   // fftshift
+                V X = buf[(p * 3 + 0) * N + pos], Y = buf[(p * 3 + 1) * N + pos],
+                  Z = buf[(p * 3 + 2) * N + pos];
+                double2 Xd = cmul(make_double2((double)X.x, (double)X.y), B.scale);
+                double2 Yd = cmul(make_double2((double)Y.x, (double)Y.y), B.scale);
+                double2 Zd = cmul(make_double2((double)Z.x, (double)Z.y), B.scale);
+                const size_t o = (size_t)B.b * 3 * N + i;
+                if (K.XYZ) {
+                    K.XYZ[o] = Xd;
+                    K.XYZ[o + N] = Yd;
+                    K.XYZ[o + 2 * N] = Zd;
+                }
+                if (K.AET) {
+                    // utility.py:24-38
+                    const double r2 = 1.4142135623730951, r6 = 2.449489742783178,
+                                 r3 = 1.7320508075688772;
+                    K.AET[o] = make_double2((Zd.x - Xd.x) / r2, (Zd.y - Xd.y) / r2);
+                    K.AET[o + N] = make_double2((Xd.x - 2.0 * Yd.x + Zd.x) / r6,
+                                                (Xd.y - 2.0 * Yd.y + Zd.y) / r6);
+                    K.AET[o + 2 * N] = make_double2((Xd.x + Yd.x + Zd.x) / r3,
+                                                    (Xd.y + Yd.y + Zd.y) / r3);
+                }
+                if (i == 0 && K.start_out) K.start_out[B.b] = B.start;
+            }
+        } else if (MODE == MODE_FILL) {
+            for (int m = tid; m < S; m += kBlock) {
+                const int p = m >> lg, i = m & (N - 1);
+                const Bin &B = bins[p];
+                const int j = B.start + i;
+                if (!B.valid || j < 0 || j >= K.L) continue;
+                const int pos = bitrev((i + (N >> 1)) & (N - 1), lg);
+                V X = buf[(p * 3 + 0) * N + pos], Y = buf[(p * 3 + 1) * N + pos],
+                  Z = buf[(p * 3 + 2) * N + pos];
+                double2 Ah = cmul(make_double2((double)((Z.x - X.x) * is2), (double)((Z.y - X.y) * is2)), B.scale);
+                double2 Eh = cmul(make_double2((double)((X.x - 2 * Y.x + Z.x) * is6),
+                                               (double)((X.y - 2 * Y.y + Z.y) * is6)), B.scale);
+                const size_t o = (size_t)B.gi * K.gstride + j;
+                atomicAdd(&K.A_glob[o].x, Ah.x);
+                atomicAdd(&K.A_glob[o].y, Ah.y);
+                atomicAdd(&K.E_glob[o].x, Eh.x);
+                atomicAdd(&K.E_glob[o].y, Eh.y);
+            }
+        } else {  // MODE_LL
+            for (int m0 = 0; m0 < S; m0 += kBlock) {
+                const int m = m0 + tid;
+                double dr = 0.0, di = 0.0, hh = 0.0;
+                if (m < S) {
+                    const int p = m >> lg, i = m & (N - 1);
+                    const Bin &B = bins[p];
+                    const int j = B.start + i;
+                    if (B.valid && j >= 0 && j < K.L) {
+                        const int pos = bitrev((i + (N >> 1)) & (N - 1), lg);
+                        V X = buf[(p * 3 + 0) * N + pos], Y = buf[(p * 3 + 1) * N + pos],
+                          Z = buf[(p * 3 + 2) * N + pos];
+                        const size_t jd = (size_t)B.di * K.L + j, jn = (size_t)B.ni * K.L + j;
+                        const double2 dA = __ldg(K.A_data + jd), dE = __ldg(K.E_data + jd);
+                        const double SA = __ldg(K.A_psd + jn), SE = __ldg(K.E_psd + jn);
+                        if constexpr (sizeof(R) == 8) {
+                            double2 hA = cmul(make_double2((Z.x - X.x) * is2, (Z.y - X.y) * is2), B.scale);
+                            double2 hE = cmul(make_double2((X.x - 2.0 * Y.x + Z.x) * is6,
+                                                           (X.y - 2.0 * Y.y + Z.y) * is6), B.scale);
+                            const double wA = 1.0 / SA, wE = 1.0 / SE;
+                            // conj(d) h / S  (gbgpu_utils.cu:172-178)
+                            dr = (dA.x * hA.x + dA.y * hA.y) * wA + (dE.x * hE.x + dE.y * hE.y) * wE;
+                            di = (dA.x * hA.y - dA.y * hA.x) * wA + (dE.x * hE.y - dE.y * hE.x) * wE;
+                            hh = (hA.x * hA.x + hA.y * hA.y) * wA + (hE.x * hE.x + hE.y * hE.y) * wE;
+                        } else {
+                            float2 hA = make_float2((Z.x - X.x) * (float)is2, (Z.y - X.y) * (float)is2);
+                            float2 hE = make_float2((X.x - 2.f * Y.x + Z.x) * (float)is6,
+                                                    (X.y - 2.f * Y.y + Z.y) * (float)is6);
+                            const float wA = 1.0f / d2f_scaled(SA, B.eS);
+                            const float wE = 1.0f / d2f_scaled(SE, B.eS);
+                            const float aR = d2f_scaled(dA.x, B.eD), aI = d2f_scaled(dA.y, B.eD);
+                            const float eR = d2f_scaled(dE.x, B.eD), eI = d2f_scaled(dE.y, B.eD);
+                            float fr = fmaf(aR, hA.x, aI * hA.y) * wA + fmaf(eR, hE.x, eI * hE.y) * wE;
+                            float fi = fmaf(aR, hA.y, -aI * hA.x) * wA + fmaf(eR, hE.y, -eI * hE.x) * wE;
+                            float fh = fmaf(hA.x, hA.x, hA.y * hA.y) * wA + fmaf(hE.x, hE.x, hE.y * hE.y) * wE;
+                            dr = fr; di = fi; hh = fh;
+                        }
+                    } else if (B.valid) {
+                        flag(a.status, GBX_FLAG_WINDOW);
+                    }
+                }
+                dr = warp_sum(dr);
+                di = warp_sum(di);
+                hh = warp_sum(hh);
+                if (lane == 0 && m0 + (warp << 5) < S) {
+                    const int e = (m0 + (warp << 5)) >> 5;
+                    red[3 * e] = dr;
+                    red[3 * e + 1] = di;
+                    red[3 * e + 2] = hh;
+                }
+            }
+            __syncthreads();
+            if (tid < cnt) {
+                const Bin &B = bins[tid];
+                const int e0 = (tid << lg) >> 5, e1 = ((tid + 1) << lg) >> 5;
+                double sr = 0.0, si = 0.0, sh = 0.0;
+                for (int e = e0; e < e1; e++) {
+                    sr += red[3 * e];
+                    si += red[3 * e + 1];
+                    sh += red[3 * e + 2];
+                }
+                const double s4 = 4.0 * K.df;
+                double2 dh, hv;
+                if constexpr (sizeof(R) == 8) {
+                    dh = make_double2(s4 * sr, s4 * si);
+                    hv = make_double2(s4 * sh, 0.0);
+                } else {
+                    // undo the power-of-two scalings and apply amp * 0.5T/N [* tdi2]
+                    const double cd = s4 * ldexp(1.0, B.eS - B.eD);
+                    const double ch = s4 * ldexp(1.0, B.eS) *
+                                      (B.scale.x * B.scale.x + B.scale.y * B.scale.y);
+                    dh = cmul(make_double2(cd * sr, cd * si), B.scale);
+                    hv = make_double2(ch * sh, 0.0);
+                }
+                if (!B.valid) {
+                    dh = make_double2(0.0, 0.0);
+                    hv = make_double2(0.0, 0.0);
+                }
+                if (B.b >= 0) {
+                    K.d_h[B.b] = dh;
+                    K.h_h[B.b] = hv;
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ----------------------------------------------------------------------------
+// host side
+// ----------------------------------------------------------------------------
+static size_t smem_bytes(int prec, bool third, int maxS)
+{
+    size_t head = sizeof(Bin) * kMaxPack + sizeof(double) * 3 * (size_t)(maxS >> 5);
+    size_t rc = prec == GBX_FP64 ? sizeof(double2) : sizeof(float2);
+    size_t r = prec == GBX_FP64 ? sizeof(double) : sizeof(float);
+    size_t s = head + 3 * (size_t)maxS * rc;
+    if (third) s += 3 * (size_t)maxS * (sizeof(double) + r);
+    return s;
+}
+
+template <typename R, int MODE, bool THIRD>
+static int launch_one(const KParams &K, int maxS, cudaStream_t st)
+{
+    auto kern = wave_kernel<R, MODE, THIRD>;
+    size_t sm = smem_bytes(sizeof(R) == 8 ? GBX_FP64 : GBX_MIXED, THIRD, maxS);
+    if (sm > 227 * 1024) return set_error(GBX_ERR_UNSUPPORTED, "tile needs %zu B of shared memory", sm);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute");
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, sm);
+    if (e != cudaSuccess) return cuda_error(e, "occupancy");
+    if (per_sm < 1) per_sm = 1;
+    int nsm = num_sms();
+    int ntiles = K.a.tiles ? K.a.ntiles : (K.a.num_bin + K.P - 1) / K.P;
+    int grid = per_sm * nsm;
+    if (grid > ntiles) grid = ntiles;
+    if (grid < 1) return GBX_OK;
+    if (K.a.queue) {
+        e = cudaMemsetAsync(K.a.queue, 0, sizeof(int), st);
+        if (e != cudaSuccess) return cuda_error(e, "queue reset");
+    }
+    kern<<<grid, kBlock, sm, st>>>(K);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_error(e, "wave_kernel launch");
+    return GBX_OK;
+}
+
+template <int MODE>
+static int dispatch(KParams &K, int maxS, cudaStream_t st)
+{
+    K.maxS = maxS;
+    const bool third = K.a.nparams >= 14;
+    if (K.a.precision == GBX_FP64) {
+        return third ? launch_one<double, MODE, true>(K, maxS, st)
+                     : launch_one<double, MODE, false>(K, maxS, st);
+    }
+    return third ? launch_one<float, MODE, true>(K, maxS, st)
+                 : launch_one<float, MODE, false>(K, maxS, st);
+}
+
+// validates the shared arguments; returns max samples per tile in *maxS
+static int check_wave(const gbx_wave_args *a, int *maxS)
+{
+    if (!a || !a->params) return set_error(GBX_ERR_ARG, "NULL wave args / params");
+    if (a->num_bin < 0) return set_error(GBX_ERR_ARG, "num_bin < 0");
+    if (a->nparams != 9 && a->nparams != 14) return set_error(GBX_ERR_ARG, "nparams must be 9 or 14");
+    if (a->precision != GBX_FP64 && a->precision != GBX_MIXED)
+        return set_error(GBX_ERR_ARG, "unknown precision %d", a->precision);
+    if (!(a->T > 0.0) || !(a->armlength > 0.0)) return set_error(GBX_ERR_ARG, "T and armlength must be > 0");
+    if (a->nparams == 14 && !(a->year > 0.0)) return set_error(GBX_ERR_ARG, "year must be > 0");
+    const int maxlg = a->precision == GBX_FP64 ? 12 : GBX_MAX_LOG2N;
+    if (a->tiles == nullptr) {
+        int N = a->N;
+        if (N < 32 || (N & (N - 1)) != 0) return set_error(GBX_ERR_UNSUPPORTED, "N=%d: need a power of two >= 32", N);
+        int lg = 31 - __builtin_clz((unsigned)N);
+        if (lg > maxlg) return set_error(GBX_ERR_UNSUPPORTED, "N=%d above the limit of this precision", N);
+        if (!a->orbit[lg]) return set_error(GBX_ERR_ARG, "no orbit table for N=%d", N);
+        *maxS = N > kTileMin ? N : kTileMin;
+    } else {
+        if (a->ntiles < 0) return set_error(GBX_ERR_ARG, "ntiles < 0");
+        // the largest N with a table bounds the tile size
+        int mx = 0;
+        for (int k = 5; k <= maxlg; k++)
+            if (a->orbit[k]) mx = k;
+        if (mx == 0) return set_error(GBX_ERR_ARG, "no orbit tables");
+        *maxS = (1 << mx) > kTileMin ? (1 << mx) : kTileMin;
+    }
+    return GBX_OK;
+}
+
+static KParams base_params(const gbx_wave_args *a)
+{
+    KParams K;
+    memset(&K, 0, sizeof(K));
+    K.a = *a;
+    if (a->tiles == nullptr) {
+        int P = kTileMin / a->N;
+        K.P = P < 1 ? 1 : P;
+    } else {
+        K.P = 1;
+    }
+    return K;
+}
+
+}  // namespace gbx
+
+using namespace gbx;
+
+int gbx_twiddle_init(cudaStream_t st)
+{
+    tw_init_kernel<<<(kTwN / 2 + 255) / 256, 256, 0, st>>>();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_error(e, "twiddle init");
+    return GBX_OK;
+}
+
+extern "C" int gbx_waveform(const gbx_wave_args *a, void *XYZ_out, void *AET_out, int *start_out,
+                            void *stream)
+{
+    int maxS = 0;
+    int rc = check_wave(a, &maxS);
+    if (rc) return rc;
+    if (a->tiles) return set_error(GBX_ERR_ARG, "gbx_waveform takes a uniform N");
+    rc = ensure_init((cudaStream_t)stream);
+    if (rc) return rc;
+    KParams K = base_params(a);
+    K.XYZ = (double2 *)XYZ_out;
+    K.AET = (double2 *)AET_out;
+    K.start_out = start_out;
+    return dispatch<MODE_WAVE>(K, maxS, (cudaStream_t)stream);
+}
+
+extern "C" int gbx_waveform_ll(const gbx_wave_args *a, const gbx_ll_args *l, void *d_h, void *h_h,
+                               void *stream)
+{
+    int maxS = 0;
+    int rc = check_wave(a, &maxS);
+    if (rc) return rc;
+    if (!l || !l->A_data || !l->E_data || !l->A_psd || !l->E_psd || !d_h || !h_h)
+        return set_error(GBX_ERR_ARG, "NULL likelihood pointer");
+    if (l->data_length <= 0 || l->num_data < 1 || l->num_psd < 1)
+        return set_error(GBX_ERR_ARG, "data_length / num_data / num_psd must be positive");
+    rc = ensure_init((cudaStream_t)stream);
+    if (rc) return rc;
+    KParams K = base_params(a);
+    K.A_data = (const double2 *)l->A_data;
+    K.E_data = (const double2 *)l->E_data;
+    K.A_psd = l->A_psd;
+    K.E_psd = l->E_psd;
+    K.L = l->data_length;
+    K.num_data = l->num_data;
+    K.num_psd = l->num_psd;
+    K.data_index = l->data_index;
+    K.noise_index = l->noise_index;
+    K.df = l->df;
+    K.d_h = (double2 *)d_h;
+    K.h_h = (double2 *)h_h;
+    return dispatch<MODE_LL>(K, maxS, (cudaStream_t)stream);
+}
+
+extern "C" int gbx_waveform_fill(const gbx_wave_args *a, void *A_glob, void *E_glob,
+                                 const int *group_index, int num_groups, int data_length,
+                                 long long group_stride, void *stream)
+{
+    int maxS = 0;
+    int rc = check_wave(a, &maxS);
+    if (rc) return rc;
+    if (!A_glob || !E_glob || !group_index) return set_error(GBX_ERR_ARG, "NULL fill pointer");
+    if (data_length <= 0 || num_groups < 1) return set_error(GBX_ERR_ARG, "bad template shape");
+    if (group_stride == 0) group_stride = data_length;
+    if (group_stride < data_length) return set_error(GBX_ERR_ARG, "group_stride < data_length");
+    rc = ensure_init((cudaStream_t)stream);
+    if (rc) return rc;
+    KParams K = base_params(a);
+    K.A_glob = (double2 *)A_glob;
+    K.E_glob = (double2 *)E_glob;
+    K.group_index = group_index;
+    K.num_groups = num_groups;
+    K.gstride = group_stride;
+    K.L = data_length;
+    return dispatch<MODE_FILL>(K, maxS, (cudaStream_t)stream);
+}

@@ -1,0 +1,732 @@
+"""GBGPU class API on the GB300 kernels.
+
+Mirrors gbgpu/gbgpu.py: ``GBGPUBase`` / ``GBGPU`` with ``run_wave`` (:108-316),
+the output properties (:318-346, :542-578), ``get_ll`` (:580-735),
+``fill_global_template`` (:737-837), ``generate_global_template`` (:839-878),
+``inject_signal`` (:880-946), ``information_matrix`` (:957-1138) and the
+extension hooks (:1140-1327).  Arrays live on the GPU as torch tensors; NumPy
+inputs are accepted and copied to the device.  The waveform, likelihood and
+template fill run in the CUDA kernels of ``libgbgpu_gb300.so``; ``get_ll`` and
+``generate_global_template`` use fused kernels so the waveform never goes
+through device memory, and the waveform attributes (``XYZf``, ``AETf``,
+``start_inds`` ...) are then produced on first access.
+"""
+
+import abc
+import ctypes
+import hashlib
+import warnings
+
+import numpy as np
+import torch
+
+from . import _native as nat
+from .backend import get_backend
+from .constants import C_SI, YRSID_SI
+from .orbits import EqualArmlengthOrbits, Orbits
+from .utility import get_N
+
+_PRECISIONS = {"fp64": nat.GBX_FP64, "mixed": nat.GBX_MIXED}
+_TILE_MIN = 512
+
+
+def _is_pow2(n):
+    return n >= 1 and (n & (n - 1)) == 0
+
+
+def _to_device(x, dtype, device):
+    if isinstance(x, torch.Tensor):
+        return x.to(device=device, dtype=dtype)
+    return torch.as_tensor(np.asarray(x), dtype=dtype, device=device)
+
+
+def _to_host(x):
+    if isinstance(x, torch.Tensor):
+        return x.detach().cpu().numpy()
+    return np.asarray(x)
+
+
+def plan_tiles(N_per_bin):
+    """Tile list for a batch of uneven N: binaries sorted by decreasing N,
+    packed max(1, 512/N) per tile.  Returns (order int32, tiles int32 (t, 4))."""
+    Ns = np.asarray(N_per_bin, dtype=np.int64).reshape(-1)
+    if Ns.size and (np.any(Ns < 32) or np.any(Ns & (Ns - 1))):
+        raise NotImplementedError("per-binary N must be powers of two >= 32")
+    order = np.argsort(-Ns, kind="stable").astype(np.int32)
+    sortedN = Ns[order]
+    tiles = []
+    pos = 0
+    for N in sorted(set(Ns.tolist()), reverse=True):
+        cnt = int(np.count_nonzero(sortedN == N))
+        P = max(1, _TILE_MIN // N)
+        first = pos + np.arange(0, cnt, P)
+        count = np.minimum(P, pos + cnt - first)
+        lg = int(N).bit_length() - 1
+        tiles.append(np.stack([np.full_like(first, lg), first, count, np.zeros_like(first)], 1))
+        pos += cnt
+    tiles = np.concatenate(tiles).astype(np.int32) if tiles else np.zeros((0, 4), np.int32)
+    return order, tiles
+
+
+class WavePlan:
+    """Device-resident description of a batch (orbit tables, tiles, queue)."""
+
+    def __init__(self, owner, N, T, precision, tdi2=False, nparams=9):
+        self.owner = owner
+        self.T = float(T)
+        self.precision = precision
+        self.tdi2 = bool(tdi2)
+        self.nparams = nparams
+        dev = owner.device
+        if np.ndim(N) == 0:
+            self.uniform = True
+            self.N = int(N)
+            Ns = [self.N]
+            self.order = self.tiles = None
+            self.ntiles = 0
+        else:
+            self.uniform = False
+            self.N = 0
+            Ns_arr = np.asarray(N, dtype=np.int64).reshape(-1)
+            order, tiles = plan_tiles(Ns_arr)
+            Ns = sorted(set(Ns_arr.tolist()))
+            self.order = torch.as_tensor(order, device=dev)
+            self.tiles = torch.as_tensor(tiles.reshape(-1), device=dev)
+            self.ntiles = len(tiles)
+        self.tables = {}
+        for n in Ns:
+            n = int(n)
+            if not _is_pow2(n) or n < 32:
+                raise NotImplementedError(f"N={n}: the CUDA path supports powers of two >= 32")
+            self.tables[n.bit_length() - 1] = owner._orbit_table(n, self.T)
+        self.queue = torch.zeros(1, dtype=torch.int32, device=dev) if not self.uniform else None
+
+    def args(self, params, start_freq_ind=0, status=None):
+        a = nat.WaveArgs()
+        a.params = params.data_ptr()
+        a.num_bin = params.shape[1]
+        a.nparams = params.shape[0]
+        a.N = self.N
+        a.precision = _PRECISIONS[self.precision]
+        a.tdi2 = int(self.tdi2)
+        a.start_freq_ind = int(start_freq_ind)
+        a.T = self.T
+        a.armlength = float(self.owner.orbits.armlength)
+        a.year = YRSID_SI
+        for lg, t in self.tables.items():
+            a.orbit[lg] = t.data_ptr()
+        a.order = self.order.data_ptr() if self.order is not None else None
+        a.tiles = self.tiles.data_ptr() if self.tiles is not None else None
+        a.ntiles = self.ntiles
+        a.queue = self.queue.data_ptr() if self.queue is not None else None
+        a.status = status.data_ptr() if status is not None else None
+        return a
+
+
+class GBGPUBase(abc.ABC):
+    """Batched FastGB Galactic-binary waveforms, likelihoods and templates.
+
+    Args:
+        orbits: object with ``get_pos(t, sc)``, ``armlength`` and ``t_base``
+            (default: analytic ``EqualArmlengthOrbits``).
+        force_backend: accepted for API compatibility; only the GPU exists.
+        precision: ``"fp64"`` (plain form) or ``"mixed"`` (FP64 phase, FP32
+            slow part and FFT) for the fused likelihood / fill kernels.
+    """
+
+    NPARAMS = 9
+
+    def __init__(self, orbits: Orbits = None, force_backend=None, precision="fp64", device=None):
+        self._backend = get_backend(force_backend)
+        self.device = torch.device(device) if device is not None else torch.device(
+            "cuda", torch.cuda.current_device())
+        if precision not in _PRECISIONS:
+            raise ValueError(f"precision must be one of {list(_PRECISIONS)}")
+        self.precision = precision
+        self.d_d = None
+        self._tables = {}
+        self._plans = {}
+        self._status = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self._lazy = None
+        self._XYZf = self._AETf = self._start_inds = None
+        self.orbits = orbits
+
+    # ------------------------------------------------------------- plumbing
+    @property
+    def backend(self):
+        return self._backend
+
+    @property
+    def xp(self):
+        return torch
+
+    @classmethod
+    def supported_backends(cls):
+        return ["gpu"]
+
+    @property
+    def get_ll_func(self):
+        return self.backend.get_ll
+
+    @property
+    def fill_global_func(self):
+        return self.backend.fill_global
+
+    @property
+    def orbits(self):
+        return self._orbits
+
+    @orbits.setter
+    def orbits(self, orbits):
+        if orbits is None:
+            self._orbits = EqualArmlengthOrbits()
+        elif not (hasattr(orbits, "get_pos") and hasattr(orbits, "armlength")):
+            raise ValueError("Input orbits must provide get_pos(t, sc), armlength and t_base")
+        else:
+            self._orbits = orbits
+        self._orbits.configure(linear_interp_setup=True)
+        self._tables = {}
+        self._plans = {}
+
+    @property
+    def citation(self):
+        return ("Katz et al. arXiv:2205.03461; Cornish & Littenberg arXiv:0704.1808; "
+                "Robson et al. arXiv:1806.00500")
+
+    def _orbit_table(self, N, T):
+        key = (int(N), float(T))
+        tab = self._tables.get(key)
+        if tab is None:
+            tm = np.linspace(0, T, num=N, endpoint=False)
+            pos = np.stack([self.orbits.get_pos(tm, np.full(N, s, dtype=np.int32))
+                            for s in (1, 2, 3)])
+            pos_d = torch.as_tensor(np.ascontiguousarray(pos, dtype=np.float64), device=self.device)
+            nbytes = nat.lib().gbx_orbit_table_bytes(N)
+            tab = torch.empty((nbytes + 15) // 16 * 2, dtype=torch.float64, device=self.device)
+            rc = nat.lib().gbx_orbit_table(ctypes.c_void_p(tab.data_ptr()),
+                                          ctypes.c_void_p(pos_d.data_ptr()), int(N),
+                                          float(self.orbits.armlength), nat.stream_handle())
+            nat.check(rc, "gbx_orbit_table")
+            self._tables[key] = tab
+        return tab
+
+    def _check_T(self, T):
+        if T > np.max(self.orbits.t_base):
+            raise ValueError(
+                f"Observation time ({T}) is larger than length of time in orbital information "
+                f"({np.max(self.orbits.t_base)})")
+
+    def _plan(self, N, T, precision, tdi2, nparams):
+        """WavePlan cache: tile schedules and orbit tables are built once per
+        distinct (N or N-array contents, T, precision, tdi2, nparams)."""
+        if np.ndim(N) == 0:
+            key = (int(N), float(T), precision, bool(tdi2), nparams)
+        else:
+            arr = np.ascontiguousarray(N, dtype=np.int64)
+            key = (hashlib.blake2b(arr.view(np.uint8), digest_size=16).digest(), arr.shape[0],
+                   float(T), precision, bool(tdi2), nparams)
+        plan = self._plans.get(key)
+        if plan is None:
+            if len(self._plans) > 32:
+                self._plans.clear()
+            plan = WavePlan(self, N, T, precision, tdi2, nparams)
+            self._plans[key] = plan
+        return plan
+
+    def _params(self, base, add_args):
+        if isinstance(base, (np.ndarray, torch.Tensor)) and base.ndim == 2 and not add_args:
+            return _to_device(base, torch.float64, self.device).contiguous()
+        cols = [torch.atleast_1d(_to_device(x, torch.float64, self.device)) for x in base]
+        B = cols[0].shape[0]
+        rows = [c.expand(B) if c.shape[0] == 1 and B > 1 else c for c in cols]
+        for x in add_args:
+            c = torch.atleast_1d(_to_device(x, torch.float64, self.device))
+            rows.append(c.expand(B) if c.shape[0] == 1 and B > 1 else c)
+        return torch.stack(rows).contiguous()
+
+    def _resolve_N(self, N, amp, f0, T, args, oversample):
+        if N is None:
+            N = self.special_get_N(_to_host(amp), _to_host(f0), T, *[_to_host(a) for a in args],
+                                   oversample=oversample)
+            return int(np.max(N))
+        if np.ndim(N) == 0:
+            return int(N)
+        return np.asarray(_to_host(N), dtype=np.int64).reshape(-1)
+
+    # -------------------------------------------------------------- waveform
+    def run_wave(self, amp, f0, fdot, fddot, phi0, iota, psi, lam, beta, *args, N=None,
+                 T=4 * YRSID_SI, dt=10.0, oversample=1, tdi2=False):
+        """Batched X/Y/Z and A/E/T windows (reference gbgpu/gbgpu.py:108-316)."""
+        N_obs = int(T / dt)
+        T = N_obs * dt
+        self._check_T(T)
+        add_args = self.prepare_additional_args(*args) if len(args) else ()
+        N = self._resolve_N(N, amp, f0, T, args, oversample)
+        if np.ndim(N) != 0:
+            raise NotImplementedError("run_wave takes one N per call (as the reference)")
+        params = self._params((amp, f0, fdot, fddot, phi0, iota, psi, lam, beta), add_args)
+        self._wave_from_params(params, N, T, tdi2)
+
+    def _wave_from_params(self, params, N, T, tdi2):
+        B = params.shape[1]
+        self.num_bin = B
+        self.N = N
+        self.df = 1 / T
+        plan = self._plan(N, T, "fp64", tdi2, params.shape[0])
+        XYZ = torch.empty((B, 3, N), dtype=torch.complex128, device=self.device)
+        AET = torch.empty((B, 3, N), dtype=torch.complex128, device=self.device)
+        start = torch.empty(B, dtype=torch.int32, device=self.device)
+        if B:
+            a = plan.args(params)
+            rc = nat.lib().gbx_waveform(ctypes.byref(a), nat.ptr(XYZ), nat.ptr(AET), nat.ptr(start),
+                                        nat.stream_handle())
+            nat.check(rc, "gbx_waveform")
+        self._lazy = None
+        self._XYZf, self._AETf = XYZ, AET
+        self._start_inds = start.to(torch.int64)
+
+    def _materialize(self):
+        if self._lazy is not None:
+            params, N, T, tdi2 = self._lazy
+            self._lazy = None
+            if np.ndim(N) != 0:
+                raise RuntimeError("waveform arrays are only defined for a single N per batch")
+            self._wave_from_params(params, N, T, tdi2)
+
+    @property
+    def XYZf(self):
+        self._materialize()
+        return self._XYZf
+
+    @XYZf.setter
+    def XYZf(self, v):
+        self._XYZf = v
+
+    @property
+    def AETf(self):
+        self._materialize()
+        return self._AETf
+
+    @AETf.setter
+    def AETf(self, v):
+        self._AETf = v
+
+    @property
+    def start_inds(self):
+        self._materialize()
+        return self._start_inds
+
+    @start_inds.setter
+    def start_inds(self, v):
+        self._start_inds = v
+
+    @property
+    def kmin(self):
+        return self.start_inds
+
+    @property
+    def X_out(self):
+        return self.XYZf[:, 0].T.flatten()
+
+    @property
+    def Y_out(self):
+        return self.XYZf[:, 1].T.flatten()
+
+    @property
+    def Z_out(self):
+        return self.XYZf[:, 2].T.flatten()
+
+    @property
+    def A_out(self):
+        return self.AETf[:, 0].T.flatten()
+
+    @property
+    def E_out(self):
+        return self.AETf[:, 1].T.flatten()
+
+    @property
+    def T_out(self):
+        return self.AETf[:, 2].T.flatten()
+
+    @property
+    def A(self):
+        return self.AETf[:, 0]
+
+    @property
+    def E(self):
+        return self.AETf[:, 1]
+
+    @property
+    def T(self):
+        return self.AETf[:, 2]
+
+    @property
+    def X(self):
+        return self.XYZf[:, 0]
+
+    @property
+    def Y(self):
+        return self.XYZf[:, 1]
+
+    @property
+    def Z(self):
+        return self.XYZf[:, 2]
+
+    @property
+    def freqs(self):
+        k = torch.arange(self.N, device=self.device)[None, :] + self.start_inds[:, None]
+        return k.to(torch.float64) * self.df
+
+    # ------------------------------------------------------------ likelihood
+    def _prepare_data(self, data, psd, data_index, noise_index, num_bin):
+        if not isinstance(data[0], (torch.Tensor, np.ndarray)):
+            raise TypeError("Make sure the data arrays are torch tensors (or NumPy arrays).")
+        d0 = data[0]
+        if d0.ndim == 1:
+            if data_index is not None:
+                raise ValueError("If inputing 1D data, cannot use data_index kwarg.")
+            if noise_index is not None:
+                raise ValueError("If inputing 1D data, cannot use noise_index kwarg.")
+            data_length = d0.shape[0]
+        elif d0.ndim == 2:
+            data_length = d0.shape[1]
+        else:
+            raise ValueError("data must be 1-D or 2-D")
+        dd = [_to_device(x, torch.complex128, self.device).reshape(-1).contiguous() for x in data]
+        pp = [_to_device(x, torch.float64, self.device).reshape(-1).contiguous() for x in psd]
+        if data_index is None:
+            data_index = torch.zeros(num_bin, dtype=torch.int32, device=self.device)
+        if noise_index is None:
+            noise_index = torch.zeros(num_bin, dtype=torch.int32, device=self.device)
+        # reference checks (gbgpu.py:681-686)
+        assert len(data_index) == num_bin
+        assert len(data_index) == len(noise_index)
+        assert str(data_index.dtype).endswith("int32")
+        assert str(noise_index.dtype).endswith("int32")
+        data_index = _to_device(data_index, torch.int32, self.device).contiguous()
+        noise_index = _to_device(noise_index, torch.int32, self.device).contiguous()
+        return dd, pp, data_length, data_index, noise_index
+
+    def _fused_ll(self, params, N, T, tdi2, dd, pp, data_length, data_index, noise_index,
+                  start_freq_ind, precision):
+        B = params.shape[1]
+        d_h = torch.empty(B, dtype=torch.complex128, device=self.device)
+        h_h = torch.empty(B, dtype=torch.complex128, device=self.device)
+        if B == 0:
+            return d_h, h_h
+        plan = self._plan(N, T, precision, tdi2, params.shape[0])
+        self._status.zero_()
+        a = plan.args(params, start_freq_ind, self._status)
+        la = nat.LLArgs()
+        la.A_data, la.E_data = dd[0].data_ptr(), dd[1].data_ptr()
+        la.A_psd, la.E_psd = pp[0].data_ptr(), pp[1].data_ptr()
+        la.data_length = int(data_length)
+        la.num_data = int(dd[0].numel() // data_length)
+        la.num_psd = int(pp[0].numel() // data_length)
+        la.data_index = data_index.data_ptr()
+        la.noise_index = noise_index.data_ptr()
+        la.df = 1.0 / T
+        rc = nat.lib().gbx_waveform_ll(ctypes.byref(a), ctypes.byref(la), nat.ptr(d_h),
+                                       nat.ptr(h_h), nat.stream_handle())
+        nat.check(rc, "gbx_waveform_ll")
+        return d_h, h_h
+
+    def _check_status(self):
+        st = int(self._status.item())
+        if st & nat.GBX_FLAG_INDEX:
+            raise ValueError("a data/noise/group index is out of range")
+        if st & nat.GBX_FLAG_WINDOW:
+            warnings.warn("some template windows extend past the data arrays; "
+                          "those bins were left out of the inner products")
+        if st & nat.GBX_FLAG_TILE:
+            raise RuntimeError("malformed tile schedule")
+
+    def get_ll(self, params, data, psd, phase_marginalize=False, start_freq_ind=0,
+               data_index=None, noise_index=None, **kwargs):
+        """Batched log-likelihood -1/2 (<d|d> + <h|h> - 2 <d|h>) (gbgpu.py:580-735).
+
+        ``params`` is (nparams, B).  Extra keywords go to the waveform
+        (N, T, dt, oversample, tdi2) plus ``precision`` ("fp64" / "mixed").
+        ``N`` may also be an array with one power-of-two N per binary; the
+        batch then runs as one persistent work-queue launch.
+        """
+        if self.d_d is None:
+            raise ValueError(
+                "self.d_d attribute must be set before computing log-Likelihood. This attribute "
+                "is the data with data inner product (<d|d>).")
+        precision = kwargs.pop("precision", self.precision)
+        if precision not in _PRECISIONS:
+            raise ValueError(f"precision must be one of {list(_PRECISIONS)}")
+        N = kwargs.pop("N", None)
+        T = kwargs.pop("T", 4 * YRSID_SI)
+        dt = kwargs.pop("dt", 10.0)
+        oversample = kwargs.pop("oversample", 1)
+        tdi2 = kwargs.pop("tdi2", False)
+        if kwargs:
+            raise TypeError(f"unexpected keyword arguments {list(kwargs)}")
+        T = int(T / dt) * dt
+        self._check_T(T)
+        if isinstance(params, (np.ndarray, torch.Tensor)) and params.ndim == 2 and \
+                params.shape[0] == self.NPARAMS:
+            prm = _to_device(params, torch.float64, self.device).contiguous()
+            base = [params[0], params[1]]
+            extra = [params[i] for i in range(9, self.NPARAMS)]
+            if extra:
+                self.prepare_additional_args(*extra)
+            if N is None:
+                N = self._resolve_N(N, base[0], base[1], T, extra, oversample)
+            elif np.ndim(N) != 0:
+                N = np.asarray(_to_host(N), dtype=np.int64).reshape(-1)
+            else:
+                N = int(N)
+        else:
+            p = list(params)
+            base, extra = p[:9], p[9:]
+            add_args = self.prepare_additional_args(*extra) if extra else ()
+            N = self._resolve_N(N, base[0], base[1], T, extra, oversample)
+            prm = self._params(base, add_args)
+        B = prm.shape[1]
+        self.num_bin = B
+        self.N = N
+        self.df = df = 1 / T
+        dd, pp, L, di, ni = self._prepare_data(data, psd, data_index, noise_index, B)
+        d_h, h_h = self._fused_ll(prm, N, T, tdi2, dd, pp, L, di, ni, start_freq_ind, precision)
+        self._lazy = (prm, N, T, tdi2)
+        if phase_marginalize:
+            self.non_marg_d_h = d_h.cpu().numpy().copy()
+            d_h = torch.abs(d_h).to(torch.complex128)
+        self.h_h = h_h
+        self.d_h = d_h
+        d_d = torch.as_tensor(self.d_d, device=self.device)
+        like = -1.0 / 2.0 * (d_d + h_h - 2 * d_h).real
+        out = like.cpu().numpy()
+        self._check_status()
+        return out
+
+    # --------------------------------------------------------- global fill
+    def fill_global_template(self, group_index, templates, A, E, start_inds, N=None,
+                             start_freq_ind=0):
+        """Sum waveforms into templates[g, 0:2] (gbgpu.py:737-837), in place.
+
+        Channels 0 and 1 of ``templates`` are overwritten with the new sums,
+        as in the reference; other channels are untouched.
+        """
+        total_groups, nchannels, data_length = templates.shape
+        num_bin = len(group_index)
+        if nchannels < 2:
+            raise ValueError("Calculates for A and E channels.")
+        elif nchannels > 2:
+            warnings.warn("Only calculating A and E channels here currently.")
+        if not isinstance(templates, (torch.Tensor, np.ndarray)):
+            raise TypeError("Make sure the data arrays are the same type as template arrays.")
+        host_out = isinstance(templates, np.ndarray)
+        tt = _to_device(templates, torch.complex128, self.device)
+        work = tt if tt.is_contiguous() else tt.contiguous()
+        gi = _to_device(group_index, torch.int32, self.device).contiguous()
+        si = (_to_device(start_inds, torch.int64, self.device) - start_freq_ind).to(torch.int32).contiguous()
+        A = _to_device(A, torch.complex128, self.device)
+        E = _to_device(E, torch.complex128, self.device)
+        if A.ndim > 2 or E.ndim > 2:
+            raise ValueError("A_in, E_in have maximum allowable dimension of 2.")
+        elif A.ndim == 2:
+            N = A.shape[1]
+            assert E.ndim == 2
+            if A.stride() != E.stride():
+                A, E = A.contiguous(), E.contiguous()
+            tsb, tsi = A.stride()
+        elif A.ndim == 1:
+            if N is None:
+                raise ValueError("If providing a 1D flattened array for A and E, the N kwarg "
+                                 "also needs to be provided.")
+            A, E = A.contiguous(), E.contiguous()
+            tsi, tsb = num_bin, 1
+        work[:, 0:2].zero_()
+        self._status.zero_()
+        if num_bin:
+            rc = nat.lib().gbx_fill_global_ex(
+                ctypes.c_void_p(work[0, 0].data_ptr()), ctypes.c_void_p(work[0, 1].data_ptr()),
+                ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(E.data_ptr()),
+                ctypes.c_void_p(si.data_ptr()), int(N), int(num_bin),
+                ctypes.c_void_p(gi.data_ptr()), int(data_length), int(total_groups),
+                int(nchannels * data_length), int(tsi), int(tsb),
+                ctypes.c_void_p(self._status.data_ptr()), nat.stream_handle())
+            nat.check(rc, "gbx_fill_global_ex")
+        self._finish_fill(templates, tt, work, host_out)
+
+    def _finish_fill(self, templates, tt, work, host_out):
+        if work is not tt:
+            tt.copy_(work)
+        if host_out:
+            templates[...] = tt.cpu().numpy()
+        elif tt is not templates:
+            templates.copy_(tt)
+        if int(self._status.item()) & nat.GBX_FLAG_INDEX:
+            raise ValueError("group_index out of range")
+
+    def generate_global_template(self, params, group_index, templates, start_freq_ind=0,
+                                 **kwargs):
+        """Waveforms straight into templates (gbgpu.py:839-878), fused on the GPU.
+
+        ``params`` is (B, nparams), transposed relative to ``get_ll``.
+        """
+        precision = kwargs.pop("precision", self.precision)
+        N = kwargs.pop("N", None)
+        T = kwargs.pop("T", 4 * YRSID_SI)
+        dt = kwargs.pop("dt", 10.0)
+        oversample = kwargs.pop("oversample", 1)
+        tdi2 = kwargs.pop("tdi2", False)
+        T = int(T / dt) * dt
+        self._check_T(T)
+        pT = _to_device(params, torch.float64, self.device).T
+        base, extra = [pT[i] for i in range(9)], [pT[i] for i in range(9, pT.shape[0])]
+        add_args = self.prepare_additional_args(*extra) if extra else ()
+        N = self._resolve_N(N, base[0], base[1], T, extra, oversample)
+        prm = self._params(base, add_args)
+        B = prm.shape[1]
+        self.num_bin, self.N, self.df = B, N, 1 / T
+        total_groups, nchannels, data_length = templates.shape
+        if nchannels < 2:
+            raise ValueError("Calculates for A and E channels.")
+        host_out = isinstance(templates, np.ndarray)
+        tt = _to_device(templates, torch.complex128, self.device)
+        work = tt if tt.is_contiguous() else tt.contiguous()
+        gi = _to_device(group_index, torch.int32, self.device).contiguous()
+        work[:, 0:2].zero_()
+        self._status.zero_()
+        if B:
+            plan = self._plan(N, T, precision, tdi2, prm.shape[0])
+            a = plan.args(prm, start_freq_ind, self._status)
+            rc = nat.lib().gbx_waveform_fill(
+                ctypes.byref(a), ctypes.c_void_p(work[0, 0].data_ptr()),
+                ctypes.c_void_p(work[0, 1].data_ptr()), ctypes.c_void_p(gi.data_ptr()),
+                int(total_groups), int(data_length), int(nchannels * data_length),
+                nat.stream_handle())
+            nat.check(rc, "gbx_waveform_fill")
+        self._lazy = (prm, N, T, tdi2)
+        self._finish_fill(templates, tt, work, host_out)
+
+    # ------------------------------------------------------------- injection
+    def inject_signal(self, *args, fmax=None, T=4.0 * YRSID_SI, dt=10.0, **kwargs):
+        """Binary 0 placed on a 0..fmax grid, as NumPy (A, E) (gbgpu.py:880-946)."""
+        if fmax is None:
+            fmax = 1 / (2 * dt)
+        self._check_T(T)
+        N_obs = int(T / dt)
+        T = N_obs * dt
+        kwargs["T"] = T
+        kwargs["dt"] = dt
+        self.df = df = 1 / T
+        f = np.arange(0.0, fmax + df, df)
+        num = len(f)
+        A_out = np.zeros(num, dtype=np.complex128)
+        E_out = np.zeros(num, dtype=np.complex128)
+        self.run_wave(*args, **kwargs)
+        start = int(self.start_inds[0].item())
+        A_temp = self.A_out.squeeze().cpu().numpy()
+        E_temp = self.E_out.squeeze().cpu().numpy()
+        A_out[start:start + self.N] = A_temp
+        E_out[start:start + self.N] = E_temp
+        return A_out, E_out
+
+    # ---------------------------------------------------- information matrix
+    def _apply_parameter_transforms(self, params, parameter_transforms):
+        for ind_trans, trans in parameter_transforms.items():
+            if isinstance(ind_trans, int):
+                params[ind_trans] = trans(params[ind_trans])
+            else:
+                params[np.asarray(ind_trans)] = trans(*params[np.asarray(ind_trans)])
+        return params
+
+    def information_matrix(self, params, eps=1e-9, parameter_transforms={}, inds=None, N=1024,
+                           psd_func=None, psd_kwargs={}, easy_central_difference=False,
+                           return_gpu=False, **kwargs):
+        """Fisher matrices from central differences of run_wave (gbgpu.py:957-1138)."""
+        if psd_func is None:
+            from .sensitivity import A1TDISens
+            psd_func = A1TDISens.get_Sn
+        if N is None:
+            raise ValueError("N must be provided up front for Infromation Matrix.")
+        kwargs["N"] = N
+        params = np.atleast_2d(_to_host(params))
+        num_params = len(params)
+        num_bins = len(params[0])
+        if inds is None:
+            inds = np.arange(num_params)
+        num_derivs = len(inds)
+        info = torch.zeros((num_bins, num_derivs, num_derivs), dtype=torch.float64,
+                           device=self.device)
+        dh = torch.zeros((num_bins, num_derivs, 2, N), dtype=torch.complex128, device=self.device)
+
+        def wave(step):
+            p = self._apply_parameter_transforms(step * params, parameter_transforms)
+            self.run_wave(*p, **kwargs)
+            return torch.stack([self.A, self.E], 1)
+
+        for i, ind in enumerate(inds):
+            up1 = np.ones_like(params)
+            up1[ind] += eps
+            dn1 = np.ones_like(params)
+            dn1[ind] -= eps
+            h_up = wave(up1)
+            h_dn = wave(dn1)
+            if easy_central_difference:
+                dh[:, i] = (h_up - h_dn) / (2 * eps)
+            else:
+                up2 = np.ones_like(params)
+                up2[ind] += 2 * eps
+                h_up2 = wave(up2)
+                if not bool(torch.all(self.start_inds == self.start_inds[0])):
+                    raise ValueError(
+                        "The user should decrease steps size (eps) because the frequency bins "
+                        "are changing during derivative calculation, which is not allowed.")
+                dn2 = np.ones_like(params)
+                dn2[ind] -= 2 * eps
+                h_dn2 = wave(dn2)
+                dh[:, i] = (-h_up2 + h_dn2 + 8 * (h_up - h_dn)) / (12 * eps)
+        freqs = self.freqs
+        psd = torch.as_tensor(np.asarray(psd_func(_to_host(freqs), **psd_kwargs)),
+                              device=self.device)
+        for i in range(num_derivs):
+            for j in range(i, num_derivs):
+                ip = 4 * self.df * torch.sum((dh[:, i].conj() * dh[:, j]).real / psd[:, None, :],
+                                             dim=(1, 2))
+                info[:, i, j] = ip
+                info[:, j, i] = ip
+        if not return_gpu:
+            return info.cpu().numpy()
+        return info
+
+    # ----------------------------------------------------------------- hooks
+    @abc.abstractmethod
+    def add_to_argS(self, argS, f0, fdot, fddot, xi, *args):
+        raise NotImplementedError
+
+    @abc.abstractmethod
+    def prepare_additional_args(self, *args):
+        raise NotImplementedError
+
+    @abc.abstractmethod
+    def special_get_N(self, amp, f0, T, *args, oversample=1):
+        raise NotImplementedError
+
+    @abc.abstractmethod
+    def shift_frequency(self, fi, xi, *args):
+        raise NotImplementedError
+
+
+class GBGPU(GBGPUBase):
+    """Circular Galactic binaries (reference gbgpu/gbgpu.py:1233-1327)."""
+
+    def prepare_additional_args(self, *args):
+        raise ValueError(
+            "If providing more args than the base args, must be a class derived from GBGPUBase "
+            "with an adjusted 'prepare_additional_args' method.")
+
+    def special_get_N(self, amp, f0, T, *args, oversample=1):
+        return get_N(amp, f0, T, oversample=oversample)
+
+    def shift_frequency(self, fi, xi, *args):
+        return fi
+
+    def add_to_argS(self, argS, f0, fdot, fddot, xi, *args):
+        return argS

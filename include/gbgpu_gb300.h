@@ -1,0 +1,201 @@
+/*
+ * gbgpu_gb300 -- C ABI of the GB300 (sm_103a) FastGB hot path.
+ *
+ * Every entry point takes caller-owned DEVICE pointers, plain sizes and a
+ * CUDA stream handle (cudaStream_t passed as void*, NULL = legacy default
+ * stream), launches asynchronously on that stream and returns a status code
+ * (GBX_OK = 0).  Nothing is allocated per call, nothing is synchronised, and
+ * no call ever terminates the process (the reference's gpuAssert calls
+ * exit(), gbgpu/cutils/global.h:46-54).  Complex arrays are interleaved
+ * double[2] (complex128), the layout of the reference's
+ * gcmplx::complex<double> (gbgpu/cutils/global.h:66).
+ */
+#ifndef GBGPU_GB300_H
+#define GBGPU_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes returned by every entry point ---- */
+#define GBX_OK 0
+#define GBX_ERR_ARG 1          /* NULL pointer, negative size, bad index array ... */
+#define GBX_ERR_UNSUPPORTED 2  /* N not a power of two or outside the supported range */
+#define GBX_ERR_CUDA 3         /* the CUDA runtime reported an error (see gbx_last_error) */
+
+/* ---- bits OR-ed by kernels into the optional device status word ---- */
+#define GBX_FLAG_WINDOW 1      /* a template window left [0, data_length): those bins count as 0 */
+#define GBX_FLAG_INDEX 2       /* a data_index / noise_index / group_index out of range: binary skipped */
+#define GBX_FLAG_TILE 4        /* malformed tile descriptor: tile skipped */
+
+/* ---- precision of the waveform family ---- */
+#define GBX_FP64 0             /* every step in FP64 (the plain form) */
+#define GBX_MIXED 1            /* FP64 carrier phase, delays and reductions; FP32 slow part + FFT */
+
+#define GBX_MAX_LOG2N 13       /* N = 2^k, 5 <= k <= 13 (FP64 form: k <= 12) */
+
+int gbx_version(void);
+
+/* Message for the most recent non-zero status returned on this host thread. */
+const char *gbx_last_error(void);
+
+/* Number of SMs and compute capability (major*10 + minor) of the current device. */
+int gbx_device_info(int *num_sms, int *arch);
+
+/*
+ * One-time set-up on the current device (FFT twiddle tables).  Every entry
+ * point does it on first use and synchronises its stream once to do so; call
+ * gbx_init() first when the first call would otherwise be made while a
+ * stream is being captured into a CUDA graph.
+ */
+int gbx_init(void);
+
+/*
+ * Drop-in for get_ll_wrap (reference: gbgpu/cutils/gbgpu_utils.hh:11-13,
+ * kernel gbgpu/cutils/gbgpu_utils.cu:124-210).  Same argument order and
+ * meaning: for each binary b,
+ *   d_h[b] = 4 df sum_{i<M} sum_{A,E} conj(d[di*L + s_b + i]) h[i*num_bin + b] / S[ni*L + s_b + i]
+ *   h_h[b] = 4 df sum_{i<M} sum_{A,E} |h[i*num_bin + b]|^2 / S[ni*L + s_b + i]
+ * with templates in the reference's point-major layout (element i*num_bin+b).
+ * Differences: bins outside [0, data_length) contribute zero and set
+ * GBX_FLAG_WINDOW in *status (the reference reads out of bounds); the call is
+ * asynchronous on `stream` (the reference synchronises the device).
+ * `status` may be NULL.
+ */
+int gbx_get_ll(void *d_h, void *h_h, const void *A_template, const void *E_template,
+               const void *A_data, const void *E_data, const double *A_psd,
+               const double *E_psd, double df, const int *start_ind, int M,
+               int num_bin, const int *data_index, const int *noise_index,
+               int data_length, int *status, void *stream);
+
+/*
+ * gbx_get_ll with explicit template strides: element (b, i) of a template is
+ * read at A_template[i * t_stride_i + b * t_stride_b] (in complex elements).
+ * (num_bin, 1) is the reference's point-major layout; (1, M) reads a
+ * (num_bin, M) row-major array without the transpose the reference makes.
+ */
+int gbx_get_ll_ex(void *d_h, void *h_h, const void *A_template, const void *E_template,
+                  const void *A_data, const void *E_data, const double *A_psd,
+                  const double *E_psd, double df, const int *start_ind, int M, int num_bin,
+                  const int *data_index, const int *noise_index, int data_length,
+                  long long t_stride_i, long long t_stride_b, int *status, void *stream);
+
+/*
+ * Drop-in for fill_global_wrap (reference: gbgpu/cutils/gbgpu_utils.hh:6-7,
+ * kernel gbgpu/cutils/gbgpu_utils.cu:54-122):
+ *   glob[group_index[b]*L + start_ind[b] + i] += template[i*num_bin + b]
+ * for 0 <= start_ind[b] + i < data_length, channels A and E, accumulated with
+ * native FP64 atomics (the reference emulates them with a CAS loop).
+ */
+int gbx_fill_global(void *A_glob, void *E_glob, const void *A_template,
+                    const void *E_template, const int *start_ind, int M, int num_bin,
+                    const int *group_index, int data_length, int *status, void *stream);
+
+/*
+ * gbx_fill_global with strides: group g of a channel starts at element
+ * g * group_stride (>= data_length), so channels 0 and 1 of a caller's
+ * (G, nch, L) template array are filled in place with group_stride = nch*L --
+ * the reference instead fills two G*L temporaries and copies them back
+ * (gbgpu/gbgpu.py:796-837).  Template strides as in gbx_get_ll_ex.  When
+ * num_groups > 0, group indices outside [0, num_groups) are skipped and
+ * flagged with GBX_FLAG_INDEX.
+ */
+int gbx_fill_global_ex(void *A_glob, void *E_glob, const void *A_template,
+                       const void *E_template, const int *start_ind, int M, int num_bin,
+                       const int *group_index, int data_length, int num_groups,
+                       long long group_stride, long long t_stride_i, long long t_stride_b,
+                       int *status, void *stream);
+
+/*
+ * Orbit table for one N.  `sc_pos` is the (3, N, 3) FP64 array of spacecraft
+ * positions [m] at tm_n = n T/N for spacecraft 1, 2, 3 -- exactly what the
+ * reference obtains from orbits.get_pos (gbgpu/gbgpu.py:390-397).  The table
+ * holds P_s/c and the arm unit vectors r_12, r_23, r_31 = (P_j - P_i)/L
+ * (gbgpu/gbgpu.py:424-427) in FP64 and FP32; it is what the waveform family
+ * reads.  `table` must hold gbx_orbit_table_bytes(N) bytes, 16-byte aligned.
+ */
+size_t gbx_orbit_table_bytes(int N);
+int gbx_orbit_table(void *table, const double *sc_pos, int N, double armlength,
+                    void *stream);
+
+/*
+ * Batch description shared by the waveform family.  Parameters are a
+ * (nparams, num_bin) row-major FP64 array -- the reference's `params` layout
+ * for get_ll (gbgpu/gbgpu.py:597-599): amp, f0, fdot, fddot, phi0, iota, psi,
+ * lam, beta, followed for the third-body model by A2, varpi, e2, P2 [yr],
+ * T2 [yr] (gbgpu/thirdbody.py:39-80).
+ *
+ * Uniform N: set N and leave tiles NULL.  Uneven N: set N = 0 and pass a tile
+ * list; tile t is four ints {log2 N, first slot, count, 0}; slots map to
+ * binaries through `order` (NULL = identity) and count <= max(1, 512/N).
+ * With `queue` non-NULL the tiles are taken from a device work-queue counter
+ * (reset by the call, so concurrent calls must not share it); tiles should be
+ * sorted by decreasing N for load balance.
+ */
+typedef struct gbx_wave_args {
+    const double *params;
+    int num_bin;
+    int nparams;                 /* 9, or 14 for the third-body model */
+    int N;                       /* uniform N (power of two) or 0 with tiles */
+    int precision;               /* GBX_FP64 or GBX_MIXED */
+    int tdi2;                    /* 0: TDI 1st generation, 1: multiply by 2i sin(2wL) e^{-2iwL} */
+    int start_freq_ind;          /* subtracted from every start index */
+    double T;                    /* observation time, already int(T/dt)*dt */
+    double armlength;            /* m */
+    double year;                 /* seconds per year used for P2, T2 (third body) */
+    const void *orbit[GBX_MAX_LOG2N + 1];   /* table for N = 2^k, NULL if unused */
+    const int *order;
+    const int *tiles;
+    int ntiles;
+    int *queue;
+    int *status;                 /* optional device word for GBX_FLAG_* bits */
+} gbx_wave_args;
+
+/* Data side of the likelihood: (num_data, L) complex128 data, (num_psd, L) PSD. */
+typedef struct gbx_ll_args {
+    const void *A_data;
+    const void *E_data;
+    const double *A_psd;
+    const double *E_psd;
+    int data_length;
+    int num_data;
+    int num_psd;
+    const int *data_index;       /* NULL = all zeros */
+    const int *noise_index;      /* NULL = all zeros */
+    double df;
+} gbx_ll_args;
+
+/*
+ * run_wave (reference gbgpu/gbgpu.py:108-316): X/Y/Z and A/E/T frequency-domain
+ * windows as (num_bin, 3, N) complex128 (either output may be NULL) and the
+ * start indices (int32, start_freq_ind subtracted).  Uniform N only.
+ */
+int gbx_waveform(const gbx_wave_args *a, void *XYZ_out, void *AET_out, int *start_out,
+                 void *stream);
+
+/*
+ * Fused run_wave + get_ll (reference gbgpu/gbgpu.py:580-712 with the native
+ * kernel gbgpu_utils.cu:124-185): d_h and h_h (complex128, num_bin) without
+ * writing the waveform to memory.  Uniform or uneven N.
+ */
+int gbx_waveform_ll(const gbx_wave_args *a, const gbx_ll_args *l, void *d_h, void *h_h,
+                    void *stream);
+
+/*
+ * Fused run_wave + fill_global (reference gbgpu/gbgpu.py:839-878): scatter-adds
+ * A and E of every binary into A_glob/E_glob[group_index[b]*L + j] with FP64
+ * atomics.  Group g starts at element g * group_stride (0 = data_length).
+ * The caller zeroes the templates first when it wants the reference's
+ * overwrite semantics (gbgpu/gbgpu.py:796-801, 836-837).
+ */
+int gbx_waveform_fill(const gbx_wave_args *a, void *A_glob, void *E_glob,
+                      const int *group_index, int num_groups, int data_length,
+                      long long group_stride, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBGPU_GB300_H */

@@ -1,0 +1,306 @@
+"""CUDA path against the reference's golden vectors and the CPU oracle.
+
+Tolerances: start indices bit-exact; the FP64 form within 1e-10 relative
+(normwise per binary for waveform windows, per value for <d|h>, <h|h>,
+templates); the mixed form within |dlogL| <= 1e-6 max(1, SNR^2) with
+SNR^2 = <h|h>, plus a stated per-output bound on the raw terms.
+"""
+
+import numpy as np
+import pytest
+
+import fastgb_oracle as O
+from conftest import load_golden, rel_err
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+WAVE_CASES = ["wave_n128", "wave_n256_tdi2", "wave_n64_1yr", "wave_n512_hf",
+              "wave_n2048_hf", "wave_b1"]
+FP64_TOL = 1e-10
+MIXED_LL_TOL = 1e-6
+
+
+def dev(x, dtype=None):
+    t = torch.as_tensor(np.asarray(x), device="cuda")
+    return t.to(dtype) if dtype is not None else t
+
+
+@pytest.fixture(scope="module")
+def gbgpu():
+    from gbgpu_gb300 import GBGPU
+    return GBGPU
+
+
+@pytest.mark.parametrize("case", WAVE_CASES)
+def test_run_wave_matches_reference(gbgpu, case):
+    g = load_golden(case)
+    gb = gbgpu()
+    gb.run_wave(*g["params"], N=int(g["N"]), T=float(g["T"]), dt=float(g["dt"]),
+                tdi2=bool(g["tdi2"]))
+    np.testing.assert_array_equal(gb.start_inds.cpu().numpy(), g["start_inds"])
+    assert np.max(rel_err(gb.XYZf.cpu().numpy(), g["XYZf"], axis=(1, 2))) < FP64_TOL
+    assert np.max(rel_err(gb.AETf.cpu().numpy(), g["AETf"], axis=(1, 2))) < FP64_TOL
+    assert rel_err(gb.A_out.cpu().numpy(), g["A_out"]) < FP64_TOL
+    np.testing.assert_allclose(gb.freqs.cpu().numpy(), g["freqs"], rtol=1e-15)
+    assert gb.A.shape == (len(g["start_inds"]), int(g["N"]))
+
+
+@pytest.mark.parametrize("case", ["ll_basic", "ll_multi", "ll_phasemarg"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_get_ll_matches_reference(gbgpu, case, precision):
+    g = load_golden(case)
+    gb = gbgpu()
+    gb.d_d = float(g["d_d"])
+    kw = {}
+    if "data_index" in g:
+        kw["data_index"] = dev(g["data_index"], torch.int32)
+    if "noise_index" in g:
+        kw["noise_index"] = dev(g["noise_index"], torch.int32)
+    like = gb.get_ll(g["params"], [dev(g["A_data"]), dev(g["E_data"])],
+                     [dev(g["A_psd"]), dev(g["E_psd"])], N=int(g["N"]), T=float(g["T"]),
+                     dt=float(g["dt"]), tdi2=bool(g["tdi2"]),
+                     start_freq_ind=int(g["start_freq_ind"]),
+                     phase_marginalize=bool(g["phase_marginalize"]), precision=precision, **kw)
+    d_h = gb.d_h.cpu().numpy()
+    h_h = gb.h_h.cpu().numpy()
+    snr2 = np.abs(g["h_h"].real)
+    if precision == "fp64":
+        np.testing.assert_allclose(d_h, g["d_h"], rtol=FP64_TOL, atol=0)
+        np.testing.assert_allclose(h_h.real, g["h_h"].real, rtol=FP64_TOL, atol=0)
+        np.testing.assert_allclose(like, g["like"], rtol=FP64_TOL)
+    else:
+        assert np.max(np.abs(like - g["like"]) / np.maximum(1.0, snr2)) < MIXED_LL_TOL
+        # stated per-output bound of the mixed form: |d(h_h)| <= 1e-6 h_h
+        assert np.max(np.abs(h_h.real - g["h_h"].real) / snr2) < 1e-6
+    if bool(g["phase_marginalize"]):
+        np.testing.assert_allclose(gb.non_marg_d_h, g["non_marg_d_h"],
+                                   rtol=FP64_TOL if precision == "fp64" else 1e-5)
+    # the waveform attributes are produced on demand after the fused call
+    np.testing.assert_array_equal(gb.start_inds.cpu().numpy(), g["start_inds"])
+
+
+def test_backend_get_ll_dropin_matches_oracle(gbgpu):
+    """backend.get_ll with the reference's 15-argument list (gbgpu_utils_wrap.pyx:20-48)."""
+    g = load_golden("ll_multi")
+    W = O.waveform(g["params"], int(g["N"]), T=float(g["T"]), dt=float(g["dt"]), tdi2=True)
+    B = W["AETf"].shape[0]
+    L = g["A_data"].shape[-1]
+    si = (W["start_inds"] - int(g["start_freq_ind"])).astype(np.int32)
+    di, ni = g["data_index"], g["noise_index"]
+    A_pm, E_pm = O.point_major(W["AETf"][:, 0]), O.point_major(W["AETf"][:, 1])
+    ref_dh, ref_hh = O.get_ll_native(A_pm, E_pm, g["A_data"].ravel(), g["E_data"].ravel(),
+                                     g["A_psd"].ravel(), g["E_psd"].ravel(), W["df"], si,
+                                     int(g["N"]), B, di, ni, L)
+    gb = gbgpu()
+    d_h = torch.zeros(B, dtype=torch.complex128, device="cuda")
+    h_h = torch.zeros(B, dtype=torch.complex128, device="cuda")
+    gb.backend.get_ll(d_h, h_h, dev(A_pm), dev(E_pm), dev(g["A_data"].ravel()),
+                      dev(g["E_data"].ravel()), dev(g["A_psd"].ravel()),
+                      dev(g["E_psd"].ravel()), W["df"], dev(si), int(g["N"]), B, dev(di),
+                      dev(ni), L)
+    np.testing.assert_allclose(d_h.cpu().numpy(), ref_dh, rtol=1e-12)
+    np.testing.assert_allclose(h_h.cpu().numpy().real, ref_hh.real, rtol=1e-12)
+
+
+def test_fill_global_template_matches_reference(gbgpu):
+    g = load_golden("fill_basic")
+    gb = gbgpu()
+    t = dev(g["templates_before"]).clone()
+    gb.fill_global_template(dev(g["group_index"]), t, dev(g["A"]), dev(g["E"]),
+                            dev(g["start_inds"]), start_freq_ind=int(g["start_freq_ind"]))
+    t = t.cpu().numpy()
+    ref = g["templates_after"]
+    np.testing.assert_array_equal(t[:, 2], ref[:, 2])          # untouched channel
+    assert rel_err(t[:, :2], ref[:, :2]) < 1e-13
+    # NumPy templates are filled in place as well
+    tn = g["templates_before"].copy()
+    gb.fill_global_template(g["group_index"], tn, g["A"], g["E"], g["start_inds"],
+                            start_freq_ind=int(g["start_freq_ind"]))
+    assert rel_err(tn, ref) < 1e-13
+
+
+def test_backend_fill_global_dropin(gbgpu):
+    g = load_golden("fill_basic")
+    A, E = g["A"], g["E"]
+    B, N = A.shape
+    G = g["templates_after"].shape[0]
+    L = g["templates_after"].shape[-1]
+    si = (g["start_inds"] - int(g["start_freq_ind"])).astype(np.int32)
+    rA = np.zeros(G * L, np.complex128)
+    rE = np.zeros(G * L, np.complex128)
+    O.fill_global_native(rA, rE, O.point_major(A), O.point_major(E), si, N, B,
+                         g["group_index"], L)
+    gb = gbgpu()
+    tA = torch.zeros(G * L, dtype=torch.complex128, device="cuda")
+    tE = torch.zeros(G * L, dtype=torch.complex128, device="cuda")
+    gb.backend.fill_global(tA, tE, dev(O.point_major(A)), dev(O.point_major(E)), dev(si), N, B,
+                           dev(g["group_index"]), L)
+    assert rel_err(tA.cpu().numpy(), rA) < 1e-13
+    assert rel_err(tE.cpu().numpy(), rE) < 1e-13
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_generate_global_template_matches_reference(gbgpu, precision):
+    g = load_golden("fill_basic")
+    gb = gbgpu()
+    t = torch.zeros(g["generated"].shape, dtype=torch.complex128, device="cuda")
+    gb.generate_global_template(g["params"].T, dev(g["group_index"]), t, N=int(g["N"]),
+                                T=float(g["T"]), dt=float(g["dt"]),
+                                start_freq_ind=int(g["start_freq_ind"]), precision=precision)
+    err = rel_err(t.cpu().numpy(), g["generated"])
+    assert err < (FP64_TOL if precision == "fp64" else 2e-6), err
+
+
+@pytest.mark.parametrize("case", ["third_n256", "third_n512_1yr"])
+def test_third_body_matches_reference(case):
+    from gbgpu_gb300 import GBGPUThirdBody
+    g = load_golden(case)
+    gb = GBGPUThirdBody()
+    gb.run_wave(*g["params"], g["A2"], g["varpi"], g["e2"], g["P2"], g["T2"], N=int(g["N"]),
+                T=float(g["T"]), dt=float(g["dt"]))
+    np.testing.assert_array_equal(gb.start_inds.cpu().numpy(), g["start_inds"])
+    assert np.max(rel_err(gb.XYZf.cpu().numpy(), g["XYZf"], axis=(1, 2))) < FP64_TOL
+    assert np.max(rel_err(gb.AETf.cpu().numpy(), g["AETf"], axis=(1, 2))) < FP64_TOL
+
+
+def _ll_setup(B, N, seed, f_lo=2e-3, f_hi=2.02e-3, T=4 * 31557600.0, dt=10.0, third=False):
+    from gbgpu_gb300.sensitivity import A1TDISens
+    rng = np.random.default_rng(seed)
+    p = np.array([10 ** rng.uniform(-23, -21, B), rng.uniform(f_lo, f_hi, B),
+                  10 ** rng.uniform(-18, -15, B), np.zeros(B), rng.uniform(0, 2 * np.pi, B),
+                  np.arccos(rng.uniform(-1, 1, B)), rng.uniform(0, np.pi, B),
+                  rng.uniform(0, 2 * np.pi, B), np.arcsin(rng.uniform(-1, 1, B))])
+    p[3] = 11 / 3 * p[2] ** 2 / p[1]
+    extra = None
+    if third:
+        P2 = 10 ** rng.uniform(0, np.log10(40), B)
+        extra = (10 ** rng.uniform(-2, 2, B), rng.uniform(0, 2 * np.pi, B),
+                 rng.uniform(0, 0.9, B), P2, rng.uniform(0, 1, B) * P2)
+    Nmax = int(np.max(N))
+    si = O.start_indices(p[1], Nmax, T, dt)
+    s0 = int(si.min()) - Nmax
+    L = int(si.max()) + 2 * Nmax - s0
+    f = (np.arange(L) + s0) / (int(T / dt) * dt)
+    S = A1TDISens.get_Sn(f)
+    Tu = int(T / dt) * dt
+    data = [np.sqrt(S * Tu / 4) * (rng.standard_normal(L) + 1j * rng.standard_normal(L))
+            for _ in range(2)]
+    return p, extra, data, S, s0
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_uneven_N_persistent_kernel(gbgpu, precision):
+    """Per-binary N in one launch == the oracle run one N-group at a time."""
+    B = 300
+    rng = np.random.default_rng(3)
+    Ns = 2 ** rng.integers(5, 12, B)
+    p, _, data, S, s0 = _ll_setup(B, Ns, 4)
+    gb = gbgpu()
+    gb.d_d = 0.0
+    like = gb.get_ll(p, [dev(x) for x in data], [dev(S), dev(S)], N=Ns, T=4 * 31557600.0,
+                     dt=10.0, start_freq_ind=s0, precision=precision)
+    hh = gb.h_h.cpu().numpy().real
+    ref = np.zeros(B)
+    ref_hh = np.zeros(B)
+    for N in np.unique(Ns):
+        sel = Ns == N
+        r, _, h, _ = O.get_ll(p[:, sel], data, [S, S], int(N), T=4 * 31557600.0, dt=10.0,
+                              start_freq_ind=s0, return_terms=True)
+        ref[sel] = r
+        ref_hh[sel] = h.real
+    scale = np.maximum(1.0, ref_hh)
+    tol = FP64_TOL if precision == "fp64" else MIXED_LL_TOL
+    assert np.max(np.abs(like - ref) / scale) < tol
+    assert np.max(np.abs(hh - ref_hh) / scale) < tol
+
+
+@pytest.mark.parametrize("N,precision", [(32, "fp64"), (4096, "fp64"), (8192, "mixed"),
+                                         (1024, "mixed")])
+def test_ll_extreme_N(gbgpu, N, precision):
+    B = 5
+    p, _, data, S, s0 = _ll_setup(B, N, 7, f_lo=1e-2, f_hi=1.001e-2)
+    gb = gbgpu()
+    gb.d_d = 0.0
+    like = gb.get_ll(p, [dev(x) for x in data], [dev(S), dev(S)], N=N, T=4 * 31557600.0,
+                     dt=5.0, start_freq_ind=s0, precision=precision)
+    ref, _, hh, _ = O.get_ll(p, data, [S, S], N, T=4 * 31557600.0, dt=5.0, start_freq_ind=s0,
+                             return_terms=True)
+    tol = FP64_TOL if precision == "fp64" else MIXED_LL_TOL
+    assert np.max(np.abs(like - ref) / np.maximum(1.0, hh.real)) < tol
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_third_body_ll(precision):
+    from gbgpu_gb300 import GBGPUThirdBody
+    B, N = 40, 512
+    p, extra, data, S, s0 = _ll_setup(B, N, 11, dt=5.0, third=True)
+    gb = GBGPUThirdBody()
+    gb.d_d = 0.0
+    full = np.concatenate([p, np.array(extra)])
+    like = gb.get_ll(full, [dev(x) for x in data], [dev(S), dev(S)], N=N, T=4 * 31557600.0,
+                     dt=5.0, start_freq_ind=s0, precision=precision)
+    ref, _, hh, _ = O.get_ll(p, data, [S, S], N, T=4 * 31557600.0, dt=5.0, start_freq_ind=s0,
+                             third=extra, return_terms=True)
+    tol = FP64_TOL if precision == "fp64" else MIXED_LL_TOL
+    assert np.max(np.abs(like - ref) / np.maximum(1.0, hh.real)) < tol
+
+
+def test_window_outside_data_flags_and_counts_zero(gbgpu):
+    p, _, data, S, s0 = _ll_setup(4, 128, 12)
+    gb = gbgpu()
+    gb.d_d = 0.0
+    cut = 200    # data arrays end inside the last windows
+    d = [x[:-cut] for x in data]
+    with pytest.warns(UserWarning, match="extend past"):
+        gb.get_ll(p, [dev(x) for x in d], [dev(S[:-cut])] * 2, N=128, T=4 * 31557600.0,
+                  dt=10.0, start_freq_ind=s0)
+
+
+def test_empty_batch(gbgpu):
+    gb = gbgpu()
+    gb.d_d = 0.0
+    z = np.zeros(0)
+    like = gb.get_ll(np.zeros((9, 0)), [dev(np.zeros(10, complex))] * 2, [dev(np.ones(10))] * 2,
+                     N=128, T=4 * 31557600.0, dt=10.0)
+    assert like.shape == (0,)
+    del z
+
+
+def test_inject_signal_matches_reference(gbgpu):
+    g = load_golden("misc")
+    gb = gbgpu()
+    A, E = gb.inject_signal(*[x[0] for x in g["inj_params"]], N=128, T=4 * 31557600.0, dt=10.0)
+    assert len(A) == int(g["inj_len"])
+    s = int(g["inj_start"])
+    assert np.count_nonzero(A) == int(g["inj_nnz"])
+    assert rel_err(A[s:s + 128], g["inj_A"]) < FP64_TOL
+    assert rel_err(E[s:s + 128], g["inj_E"]) < FP64_TOL
+
+
+def test_information_matrix_matches_reference(gbgpu):
+    from gbgpu_gb300.sensitivity import A1TDISens
+    g = load_golden("fisher")
+    gb = gbgpu()
+    fm = gb.information_matrix(g["params"].copy(), eps=1e-9, inds=g["inds"], N=int(g["N"]),
+                               T=float(g["T"]), dt=float(g["dt"]), psd_func=A1TDISens.get_Sn)
+    # finite differences with eps = 1e-9 amplify 1e-13 waveform differences
+    # by 1/eps, so the matrices agree to about 1e-3 relative
+    for b in range(fm.shape[0]):
+        assert rel_err(fm[b], g["fisher"][b]) < 5e-3
+
+
+def test_errors_like_the_reference(gbgpu):
+    gb = gbgpu()
+    with pytest.raises(ValueError, match="d_d"):
+        gb.get_ll(np.zeros((9, 1)), [dev(np.zeros(4, complex))] * 2, [dev(np.ones(4))] * 2, N=64)
+    gb.d_d = 0.0
+    with pytest.raises(ValueError, match="data_index"):
+        gb.get_ll(np.ones((9, 1)) * 1e-3, [dev(np.zeros(4, complex))] * 2,
+                  [dev(np.ones(4))] * 2, N=64, data_index=dev(np.zeros(1), torch.int32))
+    with pytest.raises(ValueError, match="Observation time"):
+        gb.run_wave(*np.ones((9, 1)) * 1e-3, N=64, T=1e10)
+    t = torch.zeros((2, 1, 10), dtype=torch.complex128, device="cuda")
+    with pytest.raises(ValueError, match="A and E"):
+        gb.fill_global_template(np.zeros(1, np.int32), t, np.zeros((1, 64)), np.zeros((1, 64)),
+                                np.zeros(1, np.int32))
