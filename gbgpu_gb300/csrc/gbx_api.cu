@@ -88,6 +88,7 @@ extern "C" int gbx_device_info(int *num_sms_out, int *arch)
 // ---------------------------------------------------------------- orbit table
 // double rows (3s+c)*N + n : P_s[c]/c ;  rows (9 + 3a + c)*N + n : r_a[c]
 // float  rows (3a+c)*N + n : r_a[c]    (a = 12, 23, 31)
+//        rows (9 + 3s + c)*N + n, (18 + 3s + c)*N + n : P_s[c]/c as a float pair hi, lo
 __global__ void orbit_table_kernel(double *tab, const double *pos, int N, double L)
 {
     int n = blockIdx.x * blockDim.x + threadIdx.x;
@@ -97,7 +98,13 @@ __global__ void orbit_table_kernel(double *tab, const double *pos, int N, double
     for (int s = 0; s < 3; s++)
         for (int c = 0; c < 3; c++) P[s][c] = pos[((size_t)s * N + n) * 3 + c];
     for (int s = 0; s < 3; s++)
-        for (int c = 0; c < 3; c++) tab[(size_t)(3 * s + c) * N + n] = P[s][c] / gbx::kCSI;
+        for (int c = 0; c < 3; c++) {
+            double pc = P[s][c] / gbx::kCSI;
+            float hi = (float)pc;
+            tab[(size_t)(3 * s + c) * N + n] = pc;
+            tf[(size_t)(9 + 3 * s + c) * N + n] = hi;
+            tf[(size_t)(18 + 3 * s + c) * N + n] = (float)(pc - (double)hi);
+        }
     for (int c = 0; c < 3; c++) {
         // gbgpu.py:424-427: r12 = (P2 - P1)/L, r23 = (P3 - P2)/L, r31 = -(P3 - P1)/L
         double r12 = (P[1][c] - P[0][c]) / L;
@@ -115,7 +122,7 @@ __global__ void orbit_table_kernel(double *tab, const double *pos, int N, double
 extern "C" size_t gbx_orbit_table_bytes(int N)
 {
     if (N <= 0) return 0;
-    return (size_t)N * (18 * sizeof(double) + 9 * sizeof(float));
+    return (size_t)N * (18 * sizeof(double) + 27 * sizeof(float));
 }
 
 extern "C" int gbx_orbit_table(void *table, const double *sc_pos, int N, double armlength,

@@ -42,6 +42,52 @@ template <typename V, typename S> __device__ __forceinline__ V cscale(V a, S s)
 // bit reversal of the low `bits` bits
 __device__ __forceinline__ int bitrev(int k, int bits) { return (int)(__brev((unsigned)k) >> (32 - bits)); }
 
+// ---------------------------------------------------------------- double-float
+// Unevaluated pairs hi + lo of FP32 numbers (Dekker 1971; Knuth TAOCP vol. 2,
+// 4.2.2): TwoSum and TwoProd (via FMA) are error-free, so sums and products
+// of pairs carry about 48 significant bits using FP32 instructions only.
+struct dfl {
+    float h, l;
+};
+__device__ __forceinline__ dfl df_two_sum(float a, float b)
+{
+    float s = a + b;
+    float bb = s - a;
+    float e = (a - (s - bb)) + (b - bb);
+    return {s, e};
+}
+__device__ __forceinline__ dfl df_fast(float a, float b)   // requires |a| >= |b| or a == 0
+{
+    float s = a + b;
+    return {s, b - (s - a)};
+}
+__device__ __forceinline__ dfl df_add(dfl a, dfl b)
+{
+    dfl s = df_two_sum(a.h, b.h);
+    return df_fast(s.h, s.l + (a.l + b.l));
+}
+__device__ __forceinline__ dfl df_neg(dfl a) { return {-a.h, -a.l}; }
+__device__ __forceinline__ dfl df_mul(dfl a, dfl b)
+{
+    float p = a.h * b.h;
+    float e = fmaf(a.h, b.h, -p);
+    e = fmaf(a.h, b.l, e);
+    e = fmaf(a.l, b.h, e);
+    return df_fast(p, e);
+}
+__device__ __forceinline__ dfl df_mul_f(dfl a, float b)
+{
+    float p = a.h * b;
+    float e = fmaf(a.h, b, -p);
+    e = fmaf(a.l, b, e);
+    return df_fast(p, e);
+}
+__host__ __device__ __forceinline__ dfl df_from(double x)
+{
+    float h = (float)x;
+    return {h, (float)(x - (double)h)};
+}
+
 // ---------------------------------------------------------------- status
 __device__ __forceinline__ void flag(int *status, int bit)
 {

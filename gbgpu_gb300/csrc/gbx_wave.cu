@@ -9,6 +9,8 @@
 #include <math.h>
 #include <string.h>
 
+#include <type_traits>
+
 #include "gbx_common.cuh"
 #include "gbx_internal.h"
 
@@ -48,6 +50,8 @@ struct Bin {
     float2 DPf, DCf;
     float f0f, fdotf, fddotf;
     float w0h, w0l, w1, w2;        // f(t)/fstar = (w0h + w0l) + w1 t + w2 t^2 (w0 split hi/lo)
+    dfl kd[3], omd, omdfad, phi0d, pfd;   // float-pair copies for the mixed carrier phase
+    float p3f;
     float A2f, e2f, varpif, sinvarpif;
     int start;                     // start index - start_freq_ind
     int b;                         // binary index
@@ -266,7 +270,15 @@ __device__ void setup_bin(Bin &B, const KParams &K, int b, int N, int mode)
         B.epf[c] = (float)B.ep[c];
         B.ecf[c] = (float)B.ec[c];
     }
-    for (int c = 0; c < 3; c++) B.kf[c] = (float)B.k[c];
+    for (int c = 0; c < 3; c++) {
+        B.kf[c] = (float)B.k[c];
+        B.kd[c] = df_from(B.k[c]);
+    }
+    B.omd = df_from(B.om);
+    B.omdfad = df_from(B.om_m_dfa);
+    B.phi0d = df_from(phi0);
+    B.pfd = df_from(B.pifdot);
+    B.p3f = (float)B.pi3fddot;
     B.DPf = make_float2((float)B.DP.x, (float)B.DP.y);
     B.DCf = make_float2((float)B.DC.x, (float)B.DC.y);
     B.f0f = (float)f0; B.fdotf = (float)fdot; B.fddotf = (float)fddot;
@@ -407,12 +419,18 @@ __device__ __forceinline__ void slow_fp64(const Bin &B, int n, int N, double tm,
     out[2] = cmul(fc2, Z);
 }
 
+// Mixed form: the carrier phase om k.P - argS (gbgpu.py:495-505), the delays
+// k.P/c and the delayed times are evaluated in float-pair arithmetic (about
+// 48 bits, so ~1e-12 rad at 100 rad) and reduced modulo 2 pi; everything else
+// is FP32.
 template <bool THIRD>
-__device__ __forceinline__ void slow_mixed(const Bin &B, int n, int N, double tm,
-                                           const double *__restrict__ tab, float inv_fstar,
+__device__ __forceinline__ void slow_mixed(const Bin &B, int n, int N, dfl step,
+                                           const double *__restrict__ tab,
                                            const double *psi, const float *vl, float2 out[3])
 {
     const float *tabf = reinterpret_cast<const float *>(tab + (size_t)18 * N);
+    const dfl twopi = df_from(kTwoPi);
+    const float inv2pi = (float)kInvTwoPi;
     float r[3][3];
 #pragma unroll
     for (int a = 0; a < 3; a++)
@@ -422,22 +440,31 @@ __device__ __forceinline__ void slow_mixed(const Bin &B, int n, int N, double tm
 #pragma unroll
     for (int a = 0; a < 3; a++)
         kdotr[a] = fmaf(B.kf[0], r[a][0], fmaf(B.kf[1], r[a][1], B.kf[2] * r[a][2]));
-    const double base = B.phi0 + B.om_m_dfa * tm;
+    const dfl tm = df_mul_f(step, (float)n);                 // n T/N
+    const dfl base = df_add(B.phi0d, df_mul(B.omdfad, tm));  // phi0 + (om - df) tm
 #pragma unroll
     for (int s = 0; s < 3; s++) {
-        // FP64: light-travel delay, delayed time and carrier phase
-        double kP = B.k[0] * __ldg(tab + (size_t)(3 * s) * N + n) +
-                    B.k[1] * __ldg(tab + (size_t)(3 * s + 1) * N + n) +
-                    B.k[2] * __ldg(tab + (size_t)(3 * s + 2) * N + n);
-        double xi = tm - kP;
-        double argS = fma(xi * xi, fma(B.pi3fddot, xi, B.pifdot), base);
-        if (THIRD) argS += psi[s];
-        double kp = fma(B.om, kP, -argS);
-        double red = fma(-rint(kp * kInvTwoPi), kTwoPi, kp);
-        phh[s] = (float)red;
-        phl[s] = (float)(red - (double)phh[s]);
+        // k . P_s / c
+        dfl acc = {0.0f, 0.0f};
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            dfl P = {__ldg(tabf + (size_t)(9 + 3 * s + c) * N + n),
+                     __ldg(tabf + (size_t)(18 + 3 * s + c) * N + n)};
+            acc = df_add(acc, df_mul(B.kd[c], P));
+        }
+        const dfl kP = acc;
+        const dfl xi = df_add(tm, df_neg(kP));
+        // pi fdot xi^2 + pi/3 fddot xi^3 = xi^2 (pi fdot + pi/3 fddot xi)
+        const dfl c2 = df_fast(B.pfd.h, fmaf(B.p3f, xi.h, B.pfd.l));
+        dfl argS = df_add(base, df_mul(df_mul(xi, xi), c2));
+        if (THIRD) argS = df_add(argS, df_from(psi[s]));
+        dfl kp = df_add(df_mul(B.omd, kP), df_neg(argS));
+        const float q = rintf(kp.h * inv2pi);
+        kp = df_add(kp, df_neg(df_mul_f(twopi, q)));
+        phh[s] = kp.h;
+        phl[s] = kp.l;
         // FP32: instantaneous frequency over the transfer frequency
-        float xf = (float)xi;
+        const float xf = xi.h;
         float fo = B.w0h + fmaf(fmaf(B.w2, xf, B.w1), xf, B.w0l);
         if (THIRD) fo *= 1.0f + vl[s] * (float)(1.0 / kCSI);
         fonfs[s] = fo;
@@ -456,12 +483,11 @@ __device__ __forceinline__ void slow_mixed(const Bin &B, int n, int N, double tm
 #pragma unroll
     for (int q = 0; q < 6; q++) {
         float arg = 0.5f * fonfs[sc[q]] * fmaf(sg[q], kdotr[arm[q]], 1.0f);
-        // arg + phase as an exact float sum (TwoSum) plus the FP64 remainder
-        float hi = arg + phh[sc[q]];
-        float bb = hi - arg;
-        float lo = ((arg - (hi - bb)) + (phh[sc[q]] - bb)) + phl[sc[q]];
+        // arg + phase as an exact float sum (TwoSum) plus the pair's low part
+        dfl x = df_two_sum(arg, phh[sc[q]]);
+        float lo = x.l + phl[sc[q]];
         float sn, cs;
-        sincosf(hi, &sn, &cs);
+        sincosf(x.h, &sn, &cs);
         // exp(-i(hi + lo)) ~ (cs - i sn)(1 - i lo)
         float er = fmaf(-sn, lo, cs);
         float ei = -fmaf(cs, lo, sn);
@@ -469,7 +495,7 @@ __device__ __forceinline__ void slow_mixed(const Bin &B, int n, int N, double tm
         float2 e = make_float2(amp * er, amp * ei);
         G[q] = cmul(e, A[arm[q]]);
     }
-    float tf = (float)tm;
+    float tf = tm.h;
     float omL = B.w0h + fmaf(fmaf(B.w2, tf, B.w1), tf, B.w0l);
     float so, co;
     sincosf(omL, &so, &co);
@@ -485,32 +511,95 @@ __device__ __forceinline__ void slow_mixed(const Bin &B, int n, int N, double tm
 }
 
 // ----------------------------------------------------------------------------
-// in-place radix-2 decimation-in-frequency FFT over `nsub` contiguous
-// sub-arrays of length N in shared memory; output in bit-reversed order.
+// In-place decimation-in-frequency FFT over `nsub` contiguous sub-arrays of
+// length N = 2^lg in shared memory; the output is in bit-reversed order.
+//
+// Stage `hl` (half-span h = 2^hl) maps (x_i, x_{i+h}) -> (x_i + x_{i+h},
+// (x_i - x_{i+h}) W_{2h}^{i mod h}).  Stages hl >= 5 run in register passes of
+// up to three stages (radix-8 groups of elements 2^q apart, q >= 5, so a warp
+// touches 32 consecutive addresses: no bank conflicts); the last five stages
+// (h = 16 ... 1) run inside a warp on 32 consecutive elements with shuffles.
+// One __syncthreads per pass: ceil((lg - 5)/3) + 1 barriers instead of lg.
 // ----------------------------------------------------------------------------
+template <typename R, int RB>
+__device__ __forceinline__ void fft_reg_pass(typename C2<R>::T *buf, int nsub, int lg, int hl)
+{
+    using V = typename C2<R>::T;
+    constexpr int M = 1 << RB;
+    const int q = hl - RB + 1;                 // log2 of the in-group stride
+    const int groups = nsub << (lg - RB);      // N / 2^RB groups per sub-array
+    for (int g = threadIdx.x; g < groups; g += kBlock) {
+        const int a = g >> (lg - RB);
+        const int rem = g & ((1 << (lg - RB)) - 1);
+        const int blk = rem >> q;
+        const int r = rem & ((1 << q) - 1);
+        V *base = buf + ((size_t)a << lg) + ((size_t)blk << (hl + 1)) + r;
+        V x[M];
+#pragma unroll
+        for (int m = 0; m < M; m++) x[m] = base[(size_t)m << q];
+#pragma unroll
+        for (int j = 0; j < RB; j++) {
+            const int dm = M >> (j + 1);             // register distance of the pair
+            const int hh = hl - j;                   // log2 half-span of this stage
+            const int ts = kTwN >> (hh + 1);
+#pragma unroll
+            for (int m = 0; m < M; m++) {
+                if (m & dm) continue;
+                const int rp = r + ((m & (dm - 1)) << q);
+                V u = x[m], v = x[m + dm];
+                x[m] = cadd(u, v);
+                x[m + dm] = cmul(csub(u, v), tw<R>(rp * ts));
+            }
+        }
+#pragma unroll
+        for (int m = 0; m < M; m++) base[(size_t)m << q] = x[m];
+    }
+}
+
+template <typename R>
+__device__ __forceinline__ typename C2<R>::T shfl_c(typename C2<R>::T v, int o)
+{
+    v.x = __shfl_xor_sync(0xffffffffu, v.x, o);
+    v.y = __shfl_xor_sync(0xffffffffu, v.y, o);
+    return v;
+}
+
 template <typename R>
 __device__ __forceinline__ void fft_dif(typename C2<R>::T *buf, int nsub, int lg)
 {
     using V = typename C2<R>::T;
-    const int N = 1 << lg;
-    const int half = N >> 1;
-    const int total = nsub * half;
-    for (int hl = lg - 1; hl >= 0; hl--) {
-        const int h = 1 << hl;
-        const int tstride = kTwN >> (hl + 1);   // W_{2h}^r = W_{kTwN}^{r * kTwN/(2h)}
-        for (int beta = threadIdx.x; beta < total; beta += kBlock) {
-            int a = beta >> (lg - 1);
-            int j = beta & (half - 1);
-            int g = j >> hl;
-            int r = j & (h - 1);
-            int i0 = (a << lg) + (g << (hl + 1)) + r;
-            V x0 = buf[i0], x1 = buf[i0 + h];
-            V w = tw<R>(r * tstride);
-            buf[i0] = cadd(x0, x1);
-            buf[i0 + h] = cmul(csub(x0, x1), w);
-        }
+    // register passes for the stages with half-span >= 32
+    int hl = lg - 1;
+    while (hl >= 5) {
+        const int rb = (hl - 4) >= 3 ? 3 : (hl - 4);
+        if (rb == 3) fft_reg_pass<R, 3>(buf, nsub, lg, hl);
+        else if (rb == 2) fft_reg_pass<R, 2>(buf, nsub, lg, hl);
+        else fft_reg_pass<R, 1>(buf, nsub, lg, hl);
+        hl -= rb;
         __syncthreads();
     }
+    // the last five stages inside a warp: lane l holds element 32c + l
+    const int lane = threadIdx.x & 31;
+    V w[5];
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        const int hh = 4 - k;                       // half-span 2^hh = 16 >> k
+        const int rp = lane & ((1 << hh) - 1);
+        w[k] = tw<R>(rp * (kTwN >> (hh + 1)));
+    }
+    const int chunks = (nsub << lg) >> 5;
+    for (int c = threadIdx.x >> 5; c < chunks; c += kBlock >> 5) {
+        V x = buf[(c << 5) + lane];
+#pragma unroll
+        for (int k = 0; k < 5; k++) {
+            const int o = 16 >> k;
+            V y = shfl_c<R>(x, o);
+            // lower lane keeps x + y; upper lane gets (y - x) W, y being the lower element
+            x = (lane & o) ? cmul(csub(y, x), w[k]) : cadd(x, y);
+        }
+        buf[(c << 5) + lane] = x;
+    }
+    __syncthreads();
 }
 
 __device__ __forceinline__ double warp_sum(double v)
@@ -524,7 +613,7 @@ __device__ __forceinline__ double warp_sum(double v)
 // the kernel
 // ----------------------------------------------------------------------------
 template <typename R, int MODE, bool THIRD>
-__global__ void __launch_bounds__(kBlock, 2) wave_kernel(const KParams K)
+__global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(const KParams K)
 {
     using V = typename C2<R>::T;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -538,7 +627,6 @@ __global__ void __launch_bounds__(kBlock, 2) wave_kernel(const KParams K)
     const int warp = tid >> 5, lane = tid & 31;
     const int ntiles = a.tiles ? a.ntiles : (a.num_bin + K.P - 1) / K.P;
     const double fstar = kCSI / (a.armlength * 2.0 * kPi);
-    const float inv_fstar = (float)(1.0 / fstar);
     int iter = 0;
 
     for (;;) {
@@ -585,6 +673,7 @@ __global__ void __launch_bounds__(kBlock, 2) wave_kernel(const KParams K)
 
         const int S = cnt << lg;                 // samples in this tile
         const double step = a.T / (double)N;     // tm = n T/N (gbgpu.py:269)
+        const dfl stepd = df_from(step);
 
         double *psi = nullptr;
         R *vl = nullptr;
@@ -674,7 +763,7 @@ __global__ void __launch_bounds__(kBlock, 2) wave_kernel(const KParams K)
                 slow_fp64<THIRD>(B, n, N, tm, 0.0, tab, fstar, ps, vd, reinterpret_cast<double2 *>(o));
             } else {
                 float vf[3] = {(float)vv[0], (float)vv[1], (float)vv[2]};
-                slow_mixed<THIRD>(B, n, N, tm, tab, inv_fstar, ps, vf, reinterpret_cast<float2 *>(o));
+                slow_mixed<THIRD>(B, n, N, stepd, tab, ps, vf, reinterpret_cast<float2 *>(o));
             }
 #pragma unroll
             for (int c = 0; c < 3; c++) buf[(p * 3 + c) * N + n] = o[c];
@@ -733,14 +822,28 @@ __global__ void __launch_bounds__(kBlock, 2) wave_kernel(const KParams K)
                 atomicAdd(&K.E_glob[o].y, Eh.y);
             }
         } else {  // MODE_LL
-            for (int m0 = 0; m0 < S; m0 += kBlock) {
-                const int m = m0 + tid;
-                double dr = 0.0, di = 0.0, hh = 0.0;
-                if (m < S) {
-                    const int p = m >> lg, i = m & (N - 1);
-                    const Bin &B = bins[p];
-                    const int j = B.start + i;
-                    if (B.valid && j >= 0 && j < K.L) {
+            // Threads [p*Tpb, (p+1)*Tpb) own binary p of the tile and walk its
+            // window with stride Tpb, so each warp reads a contiguous run of the
+            // data/PSD window.  Per-thread sums are FP64 (plain form) or FP32
+            // (mixed form; at most N/Tpb <= 8 terms), lanes are combined with an
+            // FP64 or float-pair shuffle tree, and the <= 16 group partials of a
+            // binary are added in FP64 by one thread.
+            const int Tpb = kBlock / maxcnt;               // N/2 for N <= 512, else 256
+            const int width = Tpb < 32 ? Tpb : 32;
+            const int p = tid / Tpb;
+            const int i0 = tid - p * Tpb;
+            typedef typename std::conditional<sizeof(R) == 8, double, float>::type Acc;
+            Acc sr = 0, si = 0, sh = 0;
+            if (p < cnt) {
+                const Bin &B = bins[p];
+                bool out = false;
+                if (B.valid) {
+                    for (int i = i0; i < N; i += Tpb) {
+                        const int j = B.start + i;
+                        if (j < 0 || j >= K.L) {
+                            out = true;
+                            continue;
+                        }
                         const int pos = bitrev((i + (N >> 1)) & (N - 1), lg);
                         V X = buf[(p * 3 + 0) * N + pos], Y = buf[(p * 3 + 1) * N + pos],
                           Z = buf[(p * 3 + 2) * N + pos];
@@ -753,9 +856,9 @@ __global__ void __launch_bounds__(kBlock, 2) wave_kernel(const KParams K)
                                                            (X.y - 2.0 * Y.y + Z.y) * is6), B.scale);
                             const double wA = 1.0 / SA, wE = 1.0 / SE;
                             // conj(d) h / S  (gbgpu_utils.cu:172-178)
-                            dr = (dA.x * hA.x + dA.y * hA.y) * wA + (dE.x * hE.x + dE.y * hE.y) * wE;
-                            di = (dA.x * hA.y - dA.y * hA.x) * wA + (dE.x * hE.y - dE.y * hE.x) * wE;
-                            hh = (hA.x * hA.x + hA.y * hA.y) * wA + (hE.x * hE.x + hE.y * hE.y) * wE;
+                            sr += (dA.x * hA.x + dA.y * hA.y) * wA + (dE.x * hE.x + dE.y * hE.y) * wE;
+                            si += (dA.x * hA.y - dA.y * hA.x) * wA + (dE.x * hE.y - dE.y * hE.x) * wE;
+                            sh += (hA.x * hA.x + hA.y * hA.y) * wA + (hE.x * hE.x + hE.y * hE.y) * wE;
                         } else {
                             float2 hA = make_float2((Z.x - X.x) * (float)is2, (Z.y - X.y) * (float)is2);
                             float2 hE = make_float2((X.x - 2.f * Y.x + Z.x) * (float)is6,
@@ -764,47 +867,65 @@ __global__ void __launch_bounds__(kBlock, 2) wave_kernel(const KParams K)
                             const float wE = 1.0f / d2f_scaled(SE, B.eS);
                             const float aR = d2f_scaled(dA.x, B.eD), aI = d2f_scaled(dA.y, B.eD);
                             const float eR = d2f_scaled(dE.x, B.eD), eI = d2f_scaled(dE.y, B.eD);
-                            float fr = fmaf(aR, hA.x, aI * hA.y) * wA + fmaf(eR, hE.x, eI * hE.y) * wE;
-                            float fi = fmaf(aR, hA.y, -aI * hA.x) * wA + fmaf(eR, hE.y, -eI * hE.x) * wE;
-                            float fh = fmaf(hA.x, hA.x, hA.y * hA.y) * wA + fmaf(hE.x, hE.x, hE.y * hE.y) * wE;
-                            dr = fr; di = fi; hh = fh;
+                            sr += fmaf(aR, hA.x, aI * hA.y) * wA + fmaf(eR, hE.x, eI * hE.y) * wE;
+                            si += fmaf(aR, hA.y, -aI * hA.x) * wA + fmaf(eR, hE.y, -eI * hE.x) * wE;
+                            sh += fmaf(hA.x, hA.x, hA.y * hA.y) * wA + fmaf(hE.x, hE.x, hE.y * hE.y) * wE;
                         }
-                    } else if (B.valid) {
-                        flag(a.status, GBX_FLAG_WINDOW);
                     }
                 }
-                dr = warp_sum(dr);
-                di = warp_sum(di);
-                hh = warp_sum(hh);
-                if (lane == 0 && m0 + (warp << 5) < S) {
-                    const int e = (m0 + (warp << 5)) >> 5;
-                    red[3 * e] = dr;
-                    red[3 * e + 1] = di;
-                    red[3 * e + 2] = hh;
+                if (out) flag(a.status, GBX_FLAG_WINDOW);
+            }
+            // lane tree within groups of `width` lanes (all lanes take part)
+            double gr, gi, gh;
+            if constexpr (sizeof(R) == 8) {
+                for (int o = width >> 1; o > 0; o >>= 1) {
+                    sr += __shfl_xor_sync(0xffffffffu, sr, o);
+                    si += __shfl_xor_sync(0xffffffffu, si, o);
+                    sh += __shfl_xor_sync(0xffffffffu, sh, o);
                 }
+                gr = sr; gi = si; gh = sh;
+            } else {
+                dfl xr = {sr, 0.f}, xi = {si, 0.f}, xh = {sh, 0.f};
+                for (int o = width >> 1; o > 0; o >>= 1) {
+                    dfl yr = {__shfl_xor_sync(0xffffffffu, xr.h, o), __shfl_xor_sync(0xffffffffu, xr.l, o)};
+                    dfl yi = {__shfl_xor_sync(0xffffffffu, xi.h, o), __shfl_xor_sync(0xffffffffu, xi.l, o)};
+                    dfl yh = {__shfl_xor_sync(0xffffffffu, xh.h, o), __shfl_xor_sync(0xffffffffu, xh.l, o)};
+                    xr = df_add(xr, yr);
+                    xi = df_add(xi, yi);
+                    xh = df_add(xh, yh);
+                }
+                gr = (double)xr.h + (double)xr.l;
+                gi = (double)xi.h + (double)xi.l;
+                gh = (double)xh.h + (double)xh.l;
+            }
+            if ((tid & (width - 1)) == 0) {
+                const int g = tid / width;
+                red[3 * g] = gr;
+                red[3 * g + 1] = gi;
+                red[3 * g + 2] = gh;
             }
             __syncthreads();
             if (tid < cnt) {
                 const Bin &B = bins[tid];
-                const int e0 = (tid << lg) >> 5, e1 = ((tid + 1) << lg) >> 5;
-                double sr = 0.0, si = 0.0, sh = 0.0;
-                for (int e = e0; e < e1; e++) {
-                    sr += red[3 * e];
-                    si += red[3 * e + 1];
-                    sh += red[3 * e + 2];
+                const int per = Tpb / width;
+                double tr = 0.0, ti = 0.0, th = 0.0;
+                for (int g = tid * per; g < (tid + 1) * per; g++) {
+                    tr += red[3 * g];
+                    ti += red[3 * g + 1];
+                    th += red[3 * g + 2];
                 }
                 const double s4 = 4.0 * K.df;
                 double2 dh, hv;
                 if constexpr (sizeof(R) == 8) {
-                    dh = make_double2(s4 * sr, s4 * si);
-                    hv = make_double2(s4 * sh, 0.0);
+                    dh = make_double2(s4 * tr, s4 * ti);
+                    hv = make_double2(s4 * th, 0.0);
                 } else {
                     // undo the power-of-two scalings and apply amp * 0.5T/N [* tdi2]
                     const double cd = s4 * ldexp(1.0, B.eS - B.eD);
                     const double ch = s4 * ldexp(1.0, B.eS) *
                                       (B.scale.x * B.scale.x + B.scale.y * B.scale.y);
-                    dh = cmul(make_double2(cd * sr, cd * si), B.scale);
-                    hv = make_double2(ch * sh, 0.0);
+                    dh = cmul(make_double2(cd * tr, cd * ti), B.scale);
+                    hv = make_double2(ch * th, 0.0);
                 }
                 if (!B.valid) {
                     dh = make_double2(0.0, 0.0);
@@ -841,6 +962,9 @@ static int launch_one(const KParams &K, int maxS, cudaStream_t st)
     if (sm > 227 * 1024) return set_error(GBX_ERR_UNSUPPORTED, "tile needs %zu B of shared memory", sm);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute");
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(carveout)");
     int per_sm = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, sm);
     if (e != cudaSuccess) return cuda_error(e, "occupancy");
