@@ -23,7 +23,7 @@ EXPORTS = (
     "gbx_version", "gbx_last_error", "gbx_device_info", "gbx_init",
     "gbx_get_ll", "gbx_get_ll_ex", "gbx_fill_global", "gbx_fill_global_ex",
     "gbx_orbit_table_bytes", "gbx_orbit_table",
-    "gbx_waveform", "gbx_waveform_ll", "gbx_waveform_fill",
+    "gbx_waveform", "gbx_waveform_ll", "gbx_waveform_fill", "gbx_wave_workspace_bytes",
 )
 
 _vp = ctypes.c_void_p
@@ -38,7 +38,7 @@ class WaveArgs(ctypes.Structure):
         ("params", _vp), ("num_bin", _i), ("nparams", _i), ("N", _i), ("precision", _i),
         ("tdi2", _i), ("start_freq_ind", _i), ("T", _d), ("armlength", _d), ("year", _d),
         ("orbit", _vp * (GBX_MAX_LOG2N + 1)), ("order", _vp), ("tiles", _vp), ("ntiles", _i),
-        ("queue", _vp), ("status", _vp),
+        ("queue", _vp), ("status", _vp), ("workspace", _vp), ("workspace_bytes", ctypes.c_size_t),
     ]
 
 
@@ -75,11 +75,13 @@ def lib():
     L.gbx_orbit_table_bytes.argtypes = [_i]
     L.gbx_orbit_table_bytes.restype = ctypes.c_size_t
     L.gbx_orbit_table.argtypes = [_vp, _vp, _i, _d, _vp]
+    L.gbx_wave_workspace_bytes.argtypes = [_i]
+    L.gbx_wave_workspace_bytes.restype = ctypes.c_size_t
     L.gbx_waveform.argtypes = [ctypes.POINTER(WaveArgs), _vp, _vp, _vp, _vp]
     L.gbx_waveform_ll.argtypes = [ctypes.POINTER(WaveArgs), ctypes.POINTER(LLArgs), _vp, _vp, _vp]
     L.gbx_waveform_fill.argtypes = [ctypes.POINTER(WaveArgs), _vp, _vp, _vp, _i, _i, _ll, _vp]
     for name in EXPORTS:
-        if name not in ("gbx_last_error", "gbx_orbit_table_bytes"):
+        if name not in ("gbx_last_error", "gbx_orbit_table_bytes", "gbx_wave_workspace_bytes"):
             getattr(L, name).restype = _i
     _lib = L
     return L

@@ -14,6 +14,8 @@
 #include "gbx_common.cuh"
 #include "gbx_internal.h"
 
+extern "C" size_t gbx_wave_workspace_bytes(int num_bin);
+
 namespace gbx {
 
 __device__ double2 g_tw_d[kTwN / 2];
@@ -37,7 +39,7 @@ template <> __device__ __forceinline__ double2 tw<double>(int m) { return g_tw_d
 // ----------------------------------------------------------------------------
 // per-binary constants (shared memory)
 // ----------------------------------------------------------------------------
-struct Bin {
+struct __align__(16) Bin {
     double f0, fdot, fddot, phi0;
     double om, om_m_dfa;           // 2 pi f0, 2 pi f0 - 2 pi q/T   (gbgpu.py:462-464)
     double pifdot, pi3fddot;       // pi fdot, pi/3 fddot           (gbgpu.py:495-500)
@@ -78,6 +80,7 @@ struct KParams {
     int num_groups;
     long long gstride;             // elements between consecutive groups of A_glob / E_glob
     int P;                         // binaries per tile in uniform mode
+    double fstar;                  // c / (2 pi L)
     int maxS;                      // largest tile (samples) the shared memory is sized for
 };
 
@@ -285,7 +288,7 @@ __device__ void setup_bin(Bin &B, const KParams &K, int b, int N, int mode)
     {
         // f/fstar with the constant term kept as an unevaluated float pair so
         // the FP32 transfer frequency carries no per-binary rounding bias
-        const double fstar = kCSI / (a.armlength * 2.0 * kPi);
+        const double fstar = K.fstar;
         double w0 = f0 / fstar;
         B.w0h = (float)w0;
         B.w0l = (float)(w0 - (double)B.w0h);
@@ -626,7 +629,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
     const int ntiles = a.tiles ? a.ntiles : (a.num_bin + K.P - 1) / K.P;
-    const double fstar = kCSI / (a.armlength * 2.0 * kPi);
+    const double fstar = K.fstar;
     int iter = 0;
 
     for (;;) {
@@ -658,7 +661,14 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
             __syncthreads();
             continue;
         }
-        if (tid < cnt) {
+        if (a.workspace) {
+            // per-binary constants were prepared by prep_kernel: copy them in
+            const int4 *src = reinterpret_cast<const int4 *>(
+                static_cast<const Bin *>(a.workspace) + first);
+            int4 *dst = reinterpret_cast<int4 *>(bins);
+            const int n16 = cnt * (int)(sizeof(Bin) / 16);
+            for (int k = tid; k < n16; k += kBlock) dst[k] = src[k];
+        } else if (tid < cnt) {
             int slot = first + tid;
             int b = a.order ? a.order[slot] : slot;
             if (b < 0 || b >= a.num_bin) {
@@ -942,6 +952,50 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
 }
 
 // ----------------------------------------------------------------------------
+// per-binary constants for every slot, computed once per launch by a fully
+// occupied grid (one thread per binary) instead of by a few lanes of each tile
+// ----------------------------------------------------------------------------
+constexpr int kPrepBlock = 128;
+
+template <int MODE>
+__global__ void __launch_bounds__(kPrepBlock) prep_kernel(const KParams K)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    Bin *sb = reinterpret_cast<Bin *>(smem);
+    const gbx_wave_args &a = K.a;
+    const int s0 = blockIdx.x * kPrepBlock;
+    const int slot = s0 + threadIdx.x;
+    if (slot < a.num_bin) {
+        int lg;
+        if (a.tiles) {
+            // tiles are sorted by first slot: binary search for the owning tile
+            int lo = 0, hi = a.ntiles - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (a.tiles[4 * mid + 1] <= slot) lo = mid; else hi = mid - 1;
+            }
+            lg = a.tiles[4 * lo];
+        } else {
+            lg = 31 - __clz(a.N);
+        }
+        const int b = a.order ? a.order[slot] : slot;
+        if (b < 0 || b >= a.num_bin || lg < 5 || lg > GBX_MAX_LOG2N) {
+            flag(a.status, GBX_FLAG_TILE);
+            memset(&sb[threadIdx.x], 0, sizeof(Bin));
+            sb[threadIdx.x].b = -1;
+        } else {
+            setup_bin(sb[threadIdx.x], K, b, 1 << lg, MODE);
+        }
+    }
+    __syncthreads();
+    const int cnt = min(kPrepBlock, a.num_bin - s0);
+    const int n16 = cnt * (int)(sizeof(Bin) / 16);
+    const int4 *src = reinterpret_cast<const int4 *>(sb);
+    int4 *dst = reinterpret_cast<int4 *>(static_cast<Bin *>(a.workspace) + s0);
+    for (int k = threadIdx.x; k < n16; k += kPrepBlock) dst[k] = src[k];
+}
+
+// ----------------------------------------------------------------------------
 // host side
 // ----------------------------------------------------------------------------
 static size_t smem_bytes(int prec, bool third, int maxS)
@@ -978,6 +1032,15 @@ static int launch_one(const KParams &K, int maxS, cudaStream_t st)
         e = cudaMemsetAsync(K.a.queue, 0, sizeof(int), st);
         if (e != cudaSuccess) return cuda_error(e, "queue reset");
     }
+    if (K.a.workspace) {
+        const size_t psm = sizeof(Bin) * kPrepBlock;
+        auto pk = prep_kernel<MODE>;
+        e = cudaFuncSetAttribute(pk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psm);
+        if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(prep)");
+        pk<<<(K.a.num_bin + kPrepBlock - 1) / kPrepBlock, kPrepBlock, psm, st>>>(K);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_error(e, "prep_kernel launch");
+    }
     kern<<<grid, kBlock, sm, st>>>(K);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_error(e, "wave_kernel launch");
@@ -1007,6 +1070,11 @@ static int check_wave(const gbx_wave_args *a, int *maxS)
         return set_error(GBX_ERR_ARG, "unknown precision %d", a->precision);
     if (!(a->T > 0.0) || !(a->armlength > 0.0)) return set_error(GBX_ERR_ARG, "T and armlength must be > 0");
     if (a->nparams == 14 && !(a->year > 0.0)) return set_error(GBX_ERR_ARG, "year must be > 0");
+    if (a->workspace) {
+        if (((uintptr_t)a->workspace & 15) != 0) return set_error(GBX_ERR_ARG, "workspace must be 16-byte aligned");
+        if (a->workspace_bytes < gbx_wave_workspace_bytes(a->num_bin))
+            return set_error(GBX_ERR_ARG, "workspace smaller than gbx_wave_workspace_bytes(num_bin)");
+    }
     const int maxlg = a->precision == GBX_FP64 ? 12 : GBX_MAX_LOG2N;
     if (a->tiles == nullptr) {
         int N = a->N;
@@ -1032,6 +1100,7 @@ static KParams base_params(const gbx_wave_args *a)
     KParams K;
     memset(&K, 0, sizeof(K));
     K.a = *a;
+    K.fstar = kCSI / (a->armlength * 2.0 * kPi);
     if (a->tiles == nullptr) {
         int P = kTileMin / a->N;
         K.P = P < 1 ? 1 : P;
@@ -1044,6 +1113,12 @@ static KParams base_params(const gbx_wave_args *a)
 }  // namespace gbx
 
 using namespace gbx;
+
+extern "C" size_t gbx_wave_workspace_bytes(int num_bin)
+{
+    if (num_bin <= 0) return 0;
+    return ((size_t)num_bin * sizeof(Bin) + 255) & ~(size_t)255;
+}
 
 int gbx_twiddle_init(cudaStream_t st)
 {

@@ -100,6 +100,7 @@ class WavePlan:
                 raise NotImplementedError(f"N={n}: the CUDA path supports powers of two >= 32")
             self.tables[n.bit_length() - 1] = owner._orbit_table(n, self.T)
         self.queue = torch.zeros(1, dtype=torch.int32, device=dev) if not self.uniform else None
+        self._ws = None
 
     def args(self, params, start_freq_ind=0, status=None):
         a = nat.WaveArgs()
@@ -120,6 +121,14 @@ class WavePlan:
         a.ntiles = self.ntiles
         a.queue = self.queue.data_ptr() if self.queue is not None else None
         a.status = status.data_ptr() if status is not None else None
+        B = params.shape[1]
+        need = nat.lib().gbx_wave_workspace_bytes(B)
+        if need:
+            if self._ws is None or self._ws.numel() * 16 < need:
+                self._ws = torch.empty((need + 15) // 16, dtype=torch.complex128,
+                                       device=self.owner.device)
+            a.workspace = self._ws.data_ptr()
+            a.workspace_bytes = self._ws.numel() * 16
         return a
 
 

@@ -151,7 +151,18 @@ typedef struct gbx_wave_args {
     int ntiles;
     int *queue;
     int *status;                 /* optional device word for GBX_FLAG_* bits */
+    void *workspace;             /* optional scratch of gbx_wave_workspace_bytes(num_bin) */
+    size_t workspace_bytes;
 } gbx_wave_args;
+
+/*
+ * Scratch for the per-binary constants of one call (16-byte aligned).  With a
+ * workspace the constants are computed by a separate fully occupied kernel
+ * before the waveform kernel; with workspace = NULL each tile computes them
+ * itself (same results, slower for large batches).  Calls that run at the
+ * same time must not share a workspace.
+ */
+size_t gbx_wave_workspace_bytes(int num_bin);
 
 /* Data side of the likelihood: (num_data, L) complex128 data, (num_psd, L) PSD. */
 typedef struct gbx_ll_args {

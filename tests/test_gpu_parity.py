@@ -304,3 +304,39 @@ def test_errors_like_the_reference(gbgpu):
     with pytest.raises(ValueError, match="A and E"):
         gb.fill_global_template(np.zeros(1, np.int32), t, np.zeros((1, 64)), np.zeros((1, 64)),
                                 np.zeros(1, np.int32))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_workspace_and_in_tile_setup_agree(gbgpu, precision):
+    """gbx_waveform_ll with a prep workspace and with workspace=NULL (per-tile
+    set-up) evaluate the same per-binary constants: results are identical."""
+    import ctypes
+    from gbgpu_gb300 import _native as nat
+    B = 257
+    rng = np.random.default_rng(21)
+    Ns = 2 ** rng.integers(5, 12, B)
+    p, _, data, S, s0 = _ll_setup(B, Ns, 22)
+    gb = gbgpu()
+    dd = [dev(x) for x in data]
+    Sd = dev(S)
+    prm = dev(p).contiguous()
+    plan = gb._plan(Ns, int(4 * 31557600.0 / 10.0) * 10.0, precision, False, 9)
+    la = nat.LLArgs()
+    la.A_data, la.E_data = dd[0].data_ptr(), dd[1].data_ptr()
+    la.A_psd = la.E_psd = Sd.data_ptr()
+    la.data_length, la.num_data, la.num_psd = len(S), 1, 1
+    la.df = 1.0 / (4 * 31557600.0)
+    outs = []
+    for use_ws in (True, False):
+        a = plan.args(prm, s0)
+        if not use_ws:
+            a.workspace = None
+            a.workspace_bytes = 0
+        d_h = torch.zeros(B, dtype=torch.complex128, device="cuda")
+        h_h = torch.zeros(B, dtype=torch.complex128, device="cuda")
+        rc = nat.lib().gbx_waveform_ll(ctypes.byref(a), ctypes.byref(la), nat.ptr(d_h),
+                                       nat.ptr(h_h), nat.stream_handle())
+        nat.check(rc, "gbx_waveform_ll")
+        outs.append((d_h.cpu().numpy(), h_h.cpu().numpy()))
+    np.testing.assert_array_equal(outs[0][0], outs[1][0])
+    np.testing.assert_array_equal(outs[0][1], outs[1][1])
