@@ -53,7 +53,8 @@ struct __align__(16) Bin {
     float f0f, fdotf, fddotf;
     float w0h, w0l, w1, w2;        // f(t)/fstar = (w0h + w0l) + w1 t + w2 t^2 (w0 split hi/lo)
     dfl kd[3], omd, omdfad, phi0d, pfd;   // float-pair copies for the mixed carrier phase
-    float p3f;
+    dfl tpfd;                      // 2 pi fdot as a float pair
+    float p3f, pfddf;              // pi/3 fddot, pi fddot
     float A2f, e2f, varpif, sinvarpif;
     int start;                     // start index - start_freq_ind
     int b;                         // binary index
@@ -81,6 +82,7 @@ struct KParams {
     long long gstride;             // elements between consecutive groups of A_glob / E_glob
     int P;                         // binaries per tile in uniform mode
     double fstar;                  // c / (2 pi L)
+    dfl stepd[GBX_MAX_LOG2N + 1];  // T / 2^k as float pairs (exact: division by a power of two)
     int maxS;                      // largest tile (samples) the shared memory is sized for
 };
 
@@ -113,6 +115,42 @@ __device__ __forceinline__ float sinc_f(float a)
         return fmaf(p, x, 1.0f);
     }
     return sinf(a) / a;
+}
+
+// sin(a)/a and cos(a) from their Taylor series in x = a^2 (truncation error
+// below 2e-10 for |a| <= 1.6); sinf/cosf beyond that.
+__device__ __forceinline__ void sinc_cos_f(float a, float &S, float &C)
+{
+    const float x = a * a;
+    if (x < 2.56f) {
+        float s = -1.0f / 1307674368000.0f;
+        s = fmaf(s, x, 1.0f / 6227020800.0f);
+        s = fmaf(s, x, -1.0f / 39916800.0f);
+        s = fmaf(s, x, 1.0f / 362880.0f);
+        s = fmaf(s, x, -1.0f / 5040.0f);
+        s = fmaf(s, x, 1.0f / 120.0f);
+        s = fmaf(s, x, -1.0f / 6.0f);
+        S = fmaf(s, x, 1.0f);
+        float c = -1.0f / 87178291200.0f;
+        c = fmaf(c, x, 1.0f / 479001600.0f);
+        c = fmaf(c, x, -1.0f / 3628800.0f);
+        c = fmaf(c, x, 1.0f / 40320.0f);
+        c = fmaf(c, x, -1.0f / 720.0f);
+        c = fmaf(c, x, 1.0f / 24.0f);
+        c = fmaf(c, x, -0.5f);
+        C = fmaf(c, x, 1.0f);
+    } else {
+        float sn, cs;
+        sincosf(a, &sn, &cs);
+        S = sn / a;
+        C = cs;
+    }
+}
+
+// 2^e as a double for -1022 <= e <= 1023, built from its bit pattern
+__device__ __forceinline__ double exp2_int(int e)
+{
+    return __longlong_as_double((long long)(1023 + e) << 52);
 }
 
 // FP64 -> FP32 with an exact power-of-two scaling, done on the integer pipe.
@@ -281,7 +319,9 @@ __device__ void setup_bin(Bin &B, const KParams &K, int b, int N, int mode)
     B.omdfad = df_from(B.om_m_dfa);
     B.phi0d = df_from(phi0);
     B.pfd = df_from(B.pifdot);
+    B.tpfd = df_from(2.0 * B.pifdot);
     B.p3f = (float)B.pi3fddot;
+    B.pfddf = (float)(kPi * fddot);
     B.DPf = make_float2((float)B.DP.x, (float)B.DP.y);
     B.DCf = make_float2((float)B.DC.x, (float)B.DC.y);
     B.f0f = (float)f0; B.fdotf = (float)fdot; B.fddotf = (float)fddot;
@@ -444,30 +484,50 @@ __device__ __forceinline__ void slow_mixed(const Bin &B, int n, int N, dfl step,
     for (int a = 0; a < 3; a++)
         kdotr[a] = fmaf(B.kf[0], r[a][0], fmaf(B.kf[1], r[a][1], B.kf[2] * r[a][2]));
     const dfl tm = df_mul_f(step, (float)n);                 // n T/N
-    const dfl base = df_add(B.phi0d, df_mul(B.omdfad, tm));  // phi0 + (om - df) tm
+    // With xi = tm - kP the carrier phase om kP - argS (gbgpu.py:495-505)
+    // expands exactly into a spacecraft-independent part and powers of kP:
+    //   om kP - phi0 - (om - df) tm - pi fdot xi^2 - pi/3 fddot xi^3
+    //   = Phi0(tm) + kP w(tm) - pi kP^2 fd(tm) + pi/3 fddot kP^3
+    // Phi0 = -phi0 - (om - df) tm - pi fdot tm^2 - pi/3 fddot tm^3,
+    // w = 2 pi (f0 + fdot tm + fddot tm^2 / 2), fd = fdot + fddot tm.
+    // Phi0 and w are float pairs evaluated once per sample; the kP^2 and kP^3
+    // terms are below 1e-8 rad and need only FP32.
+    const float tf = tm.h;
+    dfl Phi0 = df_add(df_mul(B.omdfad, tm), B.phi0d);
+    const dfl tm2 = df_mul(tm, tm);
+    Phi0 = df_add(Phi0, df_mul(tm2, df_fast(B.pfd.h, fmaf(B.p3f, tf, B.pfd.l))));
+    Phi0 = df_neg(Phi0);
+    const dfl wt = df_add(B.omd, df_add(df_mul(B.tpfd, tm), dfl{B.pfddf * tf * tf, 0.0f}));
+    const float fdt = fmaf(B.fddotf, tf, B.fdotf);
 #pragma unroll
     for (int s = 0; s < 3; s++) {
-        // k . P_s / c
-        dfl acc = {0.0f, 0.0f};
+        // k . P_s / c as a float pair: exact products, TwoSum accumulation
+        dfl P[3];
 #pragma unroll
-        for (int c = 0; c < 3; c++) {
-            dfl P = {__ldg(tabf + (size_t)(9 + 3 * s + c) * N + n),
-                     __ldg(tabf + (size_t)(18 + 3 * s + c) * N + n)};
-            acc = df_add(acc, df_mul(B.kd[c], P));
-        }
-        const dfl kP = acc;
-        const dfl xi = df_add(tm, df_neg(kP));
-        // pi fdot xi^2 + pi/3 fddot xi^3 = xi^2 (pi fdot + pi/3 fddot xi)
-        const dfl c2 = df_fast(B.pfd.h, fmaf(B.p3f, xi.h, B.pfd.l));
-        dfl argS = df_add(base, df_mul(df_mul(xi, xi), c2));
-        if (THIRD) argS = df_add(argS, df_from(psi[s]));
-        dfl kp = df_add(df_mul(B.omd, kP), df_neg(argS));
-        const float q = rintf(kp.h * inv2pi);
-        kp = df_add(kp, df_neg(df_mul_f(twopi, q)));
-        phh[s] = kp.h;
-        phl[s] = kp.l;
+        for (int c = 0; c < 3; c++)
+            P[c] = {__ldg(tabf + (size_t)(9 + 3 * s + c) * N + n),
+                    __ldg(tabf + (size_t)(18 + 3 * s + c) * N + n)};
+        float p0 = B.kd[0].h * P[0].h, p1 = B.kd[1].h * P[1].h, p2 = B.kd[2].h * P[2].h;
+        float e = fmaf(B.kd[0].h, P[0].h, -p0);
+        e += fmaf(B.kd[1].h, P[1].h, -p1);
+        e += fmaf(B.kd[2].h, P[2].h, -p2);
+#pragma unroll
+        for (int c = 0; c < 3; c++) e = fmaf(B.kd[c].h, P[c].l, fmaf(B.kd[c].l, P[c].h, e));
+        dfl s01 = df_two_sum(p0, p1);
+        dfl s012 = df_two_sum(s01.h, p2);
+        const dfl kP = df_fast(s012.h, (s01.l + s012.l) + e);
+        // phase
+        const float kPf = kP.h;
+        const float small = kPf * kPf * fmaf(kPf, (1.0f / 3.0f) * B.pfddf, -(float)kPi * fdt);
+        dfl ph = df_add(Phi0, df_mul(kP, wt));
+        ph.l += small;
+        if (THIRD) ph = df_add(ph, df_neg(df_from(psi[s])));
+        const float q = rintf(ph.h * inv2pi);
+        ph = df_add(ph, df_neg(df_mul_f(twopi, q)));
+        phh[s] = ph.h;
+        phl[s] = ph.l;
         // FP32: instantaneous frequency over the transfer frequency
-        const float xf = xi.h;
+        const float xf = tf - kPf;
         float fo = B.w0h + fmaf(fmaf(B.w2, xf, B.w1), xf, B.w0l);
         if (THIRD) fo *= 1.0f + vl[s] * (float)(1.0 / kCSI);
         fonfs[s] = fo;
@@ -479,26 +539,32 @@ __device__ __forceinline__ void slow_mixed(const Bin &B, int n, int N, dfl step,
         float cc = quad_form(B.ecf, r[a][0], r[a][1], r[a][2]);
         A[a] = make_float2(fmaf(pp, B.DPf.x, cc * B.DCf.x), fmaf(pp, B.DPf.y, cc * B.DCf.y));
     }
+    // exp(-i phase_s) per spacecraft, the pair's low part applied to first order
+    float Er[3], Ei[3];
+#pragma unroll
+    for (int s = 0; s < 3; s++) {
+        float sn, cs;
+        sincosf(phh[s], &sn, &cs);
+        Er[s] = fmaf(sn, -phl[s], cs);
+        Ei[s] = -fmaf(cs, phl[s], sn);
+    }
+    // links: G = 1/4 sinc(a) exp(-i a) exp(-i phase_s) A_arm  (gbgpu.py:509-525)
     float2 G[6];
     const int arm[6] = {0, 1, 2, 0, 1, 2};
     const int sc[6] = {0, 1, 2, 1, 2, 0};
     const float sg[6] = {1.f, 1.f, 1.f, -1.f, -1.f, -1.f};
 #pragma unroll
     for (int q = 0; q < 6; q++) {
-        float arg = 0.5f * fonfs[sc[q]] * fmaf(sg[q], kdotr[arm[q]], 1.0f);
-        // arg + phase as an exact float sum (TwoSum) plus the pair's low part
-        dfl x = df_two_sum(arg, phh[sc[q]]);
-        float lo = x.l + phl[sc[q]];
-        float sn, cs;
-        sincosf(x.h, &sn, &cs);
-        // exp(-i(hi + lo)) ~ (cs - i sn)(1 - i lo)
-        float er = fmaf(-sn, lo, cs);
-        float ei = -fmaf(cs, lo, sn);
-        float amp = 0.25f * sinc_f(arg);
-        float2 e = make_float2(amp * er, amp * ei);
+        const int s = sc[q];
+        float a = 0.5f * fonfs[s] * fmaf(sg[q], kdotr[arm[q]], 1.0f);
+        float S, C;
+        sinc_cos_f(a, S, C);
+        const float aS = a * S;          // sin(a)
+        const float t = 0.25f * S;
+        // (C - i aS)(Er + i Ei)
+        float2 e = make_float2(t * fmaf(C, Er[s], aS * Ei[s]), t * fmaf(C, Ei[s], -aS * Er[s]));
         G[q] = cmul(e, A[arm[q]]);
     }
-    float tf = tm.h;
     float omL = B.w0h + fmaf(fmaf(B.w2, tf, B.w1), tf, B.w0l);
     float so, co;
     sincosf(omL, &so, &co);
@@ -682,8 +748,8 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
         __syncthreads();
 
         const int S = cnt << lg;                 // samples in this tile
-        const double step = a.T / (double)N;     // tm = n T/N (gbgpu.py:269)
-        const dfl stepd = df_from(step);
+        const double step = a.T * exp2_int(-lg);  // tm = n T/N (gbgpu.py:269), exact
+        const dfl stepd = K.stepd[lg];
 
         double *psi = nullptr;
         R *vl = nullptr;
@@ -873,8 +939,8 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                             float2 hA = make_float2((Z.x - X.x) * (float)is2, (Z.y - X.y) * (float)is2);
                             float2 hE = make_float2((X.x - 2.f * Y.x + Z.x) * (float)is6,
                                                     (X.y - 2.f * Y.y + Z.y) * (float)is6);
-                            const float wA = 1.0f / d2f_scaled(SA, B.eS);
-                            const float wE = 1.0f / d2f_scaled(SE, B.eS);
+                            const float wA = __frcp_rn(d2f_scaled(SA, B.eS));
+                            const float wE = __frcp_rn(d2f_scaled(SE, B.eS));
                             const float aR = d2f_scaled(dA.x, B.eD), aI = d2f_scaled(dA.y, B.eD);
                             const float eR = d2f_scaled(dE.x, B.eD), eI = d2f_scaled(dE.y, B.eD);
                             sr += fmaf(aR, hA.x, aI * hA.y) * wA + fmaf(eR, hE.x, eI * hE.y) * wE;
@@ -904,9 +970,11 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                     xi = df_add(xi, yi);
                     xh = df_add(xh, yh);
                 }
-                gr = (double)xr.h + (double)xr.l;
-                gi = (double)xi.h + (double)xi.l;
-                gh = (double)xh.h + (double)xh.l;
+                if ((tid & (width - 1)) == 0) {
+                    gr = (double)xr.h + (double)xr.l;
+                    gi = (double)xi.h + (double)xi.l;
+                    gh = (double)xh.h + (double)xh.l;
+                }
             }
             if ((tid & (width - 1)) == 0) {
                 const int g = tid / width;
@@ -931,8 +999,8 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                     hv = make_double2(s4 * th, 0.0);
                 } else {
                     // undo the power-of-two scalings and apply amp * 0.5T/N [* tdi2]
-                    const double cd = s4 * ldexp(1.0, B.eS - B.eD);
-                    const double ch = s4 * ldexp(1.0, B.eS) *
+                    const double cd = s4 * exp2_int(B.eS - B.eD);
+                    const double ch = s4 * exp2_int(B.eS) *
                                       (B.scale.x * B.scale.x + B.scale.y * B.scale.y);
                     dh = cmul(make_double2(cd * tr, cd * ti), B.scale);
                     hv = make_double2(ch * th, 0.0);
@@ -1101,6 +1169,7 @@ static KParams base_params(const gbx_wave_args *a)
     memset(&K, 0, sizeof(K));
     K.a = *a;
     K.fstar = kCSI / (a->armlength * 2.0 * kPi);
+    for (int k = 0; k <= GBX_MAX_LOG2N; k++) K.stepd[k] = df_from(ldexp(a->T, -k));
     if (a->tiles == nullptr) {
         int P = kTileMin / a->N;
         K.P = P < 1 ? 1 : P;
