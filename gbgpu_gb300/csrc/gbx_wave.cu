@@ -9,6 +9,7 @@
 #include <math.h>
 #include <string.h>
 
+#include <mutex>
 #include <type_traits>
 
 #include "gbx_common.cuh"
@@ -1262,4 +1263,63 @@ extern "C" int gbx_waveform_fill(const gbx_wave_args *a, void *A_glob, void *E_g
     K.gstride = group_stride;
     K.L = data_length;
     return dispatch<MODE_FILL>(K, maxS, (cudaStream_t)stream);
+}
+
+// ----------------------------------------------------------------------------
+// Allocation-free variant of gbx_waveform_ll.
+//
+// Some callers cannot allocate device memory at all: a plug-in inside a host
+// application that owns every device allocation and only lends it pointers,
+// or an FFI caller that binds this C ABI but has no CUDA allocator of its own.
+// They cannot provide the per-binary workspace or the work-queue counter, so
+// this entry point keeps both in the file-scope array below.  Every GPU that
+// loads the library holds the array (4 MiB + 256 B) until the process exits.
+// ----------------------------------------------------------------------------
+namespace gbx {
+constexpr int kNoAllocMaxBin = GBX_NOALLOC_MAX_BINS;
+constexpr size_t kNoAllocWsBytes = (size_t)kNoAllocMaxBin * sizeof(Bin);
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocWsBytes + 256];
+
+static std::mutex g_noalloc_lock;
+static void *g_noalloc_ptr[64] = {};
+
+// The host-side name g_noalloc_scratch is only a stand-in for the device
+// array; its device address comes from cudaGetSymbolAddress, once per device,
+// with that device current.
+static int noalloc_scratch(void **out)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_error(e, "cudaGetDevice");
+    if (dev < 0 || dev >= 64) return set_error(GBX_ERR_ARG, "device %d out of range", dev);
+    std::lock_guard<std::mutex> g(g_noalloc_lock);
+    if (g_noalloc_ptr[dev] == nullptr) {
+        void *ptr = nullptr;
+        e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(scratch)");
+        g_noalloc_ptr[dev] = ptr;
+    }
+    *out = g_noalloc_ptr[dev];
+    return GBX_OK;
+}
+}  // namespace gbx
+
+extern "C" int gbx_waveform_ll_noalloc(const gbx_wave_args *a, const gbx_ll_args *l, void *d_h,
+                                       void *h_h, void *stream)
+{
+    if (!a) return set_error(GBX_ERR_ARG, "NULL wave args");
+    if (a->num_bin > kNoAllocMaxBin)
+        return set_error(GBX_ERR_ARG, "num_bin %d exceeds the %d binaries of the static scratch",
+                         a->num_bin, kNoAllocMaxBin);
+    void *scratch = nullptr;
+    int rc = noalloc_scratch(&scratch);
+    if (rc) return rc;
+    gbx_wave_args b = *a;
+    b.workspace = scratch;
+    b.workspace_bytes = kNoAllocWsBytes;
+    // the queue counter lives after the workspace; it is reset on the stream
+    // before every launch that uses it
+    b.queue = b.tiles ? reinterpret_cast<int *>(static_cast<unsigned char *>(scratch) + kNoAllocWsBytes)
+                      : nullptr;
+    return gbx_waveform_ll(&b, l, d_h, h_h, stream);
 }

@@ -205,6 +205,28 @@ int gbx_waveform_fill(const gbx_wave_args *a, void *A_glob, void *E_glob,
                       const int *group_index, int num_groups, int data_length,
                       long long group_stride, void *stream);
 
+/*
+ * gbx_waveform_ll without caller-provided scratch.  No counterpart in the
+ * reference (its kernels use no scratch).  For callers that may not allocate
+ * device memory: a plug-in inside an application that owns all device
+ * allocations, or an FFI binding with no CUDA allocator.  The per-binary
+ * workspace and the work-queue counter live in one static device array of
+ * GBX_NOALLOC_MAX_BINS * 512 + 256 bytes (4 MiB) that every GPU loading the
+ * library keeps until the process exits; a->workspace and a->queue are
+ * ignored.  Batches above GBX_NOALLOC_MAX_BINS binaries are rejected with
+ * GBX_ERR_ARG.  Nothing is allocated: no cudaMalloc/cudaFree or allocating
+ * library call.  The first call on a device looks up the array's device
+ * address (and, like every entry point, builds the FFT tables and
+ * synchronises its stream once); make that first call before any stream
+ * capture.  All calls share the array: calls whose kernels overlap on the GPU
+ * (different streams, or different host threads) race on it and must be
+ * serialised by the caller.  The counter is cleared on the stream before
+ * each launch; the workspace is fully rewritten by every call.
+ */
+#define GBX_NOALLOC_MAX_BINS 8192
+int gbx_waveform_ll_noalloc(const gbx_wave_args *a, const gbx_ll_args *l, void *d_h,
+                            void *h_h, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
