@@ -1,0 +1,622 @@
+// Gradient of the log-likelihood with respect to the nine source parameters
+// (amp, f0, fdot, fddot, phi0, iota, psi, lam, beta), fused with the
+// likelihood itself.  Included by gbx_wave.cu (same translation unit: it uses
+// the per-binary set-up, the slow part, the FFT and the twiddle tables).
+//
+// With r = d - h and w_c = the residual weights 4 df r / S mapped onto the
+// X, Y, Z channels (A = (Z - X)/sqrt2, E = (X - 2Y + Z)/sqrt6):
+//   d logL / d theta = Re sum_c sum_i conj(w_c,i) d h_c,i / d theta
+//                    = Re[scale sum_c sum_n Y_c,n d x_c,n / d theta]
+//                      + Re[(d scale / d theta) Qf],
+// where x is the slow part (the reference's XYZsl, gbgpu.py:375), h = scale
+// FFT(x) heterodyned (gbgpu.py:378-388), Y_c = DFT(conj(w_c)) (forward
+// transform of the conjugated weights, which the kernel computes in place with
+// a decimation-in-time FFT on the bit-reversed buffer), and
+// Qf = sum conj(w) X.  The slow part is recomputed in the backward pass with
+// analytic derivatives (nothing is stored between the passes).
+//
+// This file is included inside namespace gbx by gbx_wave.cu.
+
+enum { MODE_GRAD = 3 };
+
+struct __align__(16) GradExtra {
+    float u[3], v[3];              // sky basis vectors (gbgpu.py:256-258)
+    float st, ct;                  // sin / cos of the polar angle
+    double2 dDPi, dDCi, dDPp, dDCp;  // d(DP, DC)/d(iota, psi), amplitude divided out
+    double2 dlnsc_f0;              // d ln(scale) / d f0 (TDI-2 factor), 0 otherwise
+    float gf0, gf1;                // d fonfs / d kP = -(fdot + fddot xi)/fstar = gf0 + gf1 xi
+    float pad[2];
+};
+
+__device__ void setup_grad(GradExtra &X, const KParams &K, int b)
+{
+    const gbx_wave_args &a = K.a;
+    const int nb = a.num_bin;
+    const double *p = a.params;
+    double f0 = p[nb + b], fdot = p[2 * nb + b], fddot = p[3 * nb + b];
+    double iota = p[5 * nb + b], psi = p[6 * nb + b], lam = p[7 * nb + b], beta = p[8 * nb + b];
+    double theta = kPi / 2.0 - beta;
+    double st, ct, sp, cp, si, ci, s2p, c2p;
+    sincos(theta, &st, &ct);
+    sincos(lam, &sp, &cp);
+    sincos(iota, &si, &ci);
+    sincos(2.0 * psi, &s2p, &c2p);
+    X.u[0] = (float)(ct * cp); X.u[1] = (float)(ct * sp); X.u[2] = (float)(-st);
+    X.v[0] = (float)sp; X.v[1] = (float)(-cp); X.v[2] = 0.0f;
+    X.st = (float)st;
+    X.ct = (float)ct;
+    // DP = Ap c2p - i Ac s2p, DC = -Ap s2p - i Ac c2p; Ap = 1 + ci^2, Ac = -2 ci
+    const double Ap = 1.0 + ci * ci, Ac = -2.0 * ci;
+    const double dAp = -2.0 * ci * si, dAc = 2.0 * si;
+    X.dDPi = make_double2(dAp * c2p, -dAc * s2p);
+    X.dDCi = make_double2(-dAp * s2p, -dAc * c2p);
+    X.dDPp = make_double2(-2.0 * Ap * s2p, -2.0 * Ac * c2p);
+    X.dDCp = make_double2(-2.0 * Ap * c2p, 2.0 * Ac * s2p);
+    X.dlnsc_f0 = make_double2(0.0, 0.0);
+    if (a.tdi2) {
+        // factor 2i sin(2wL) exp(-2iwL), wL = 2 pi f0 L/c: d ln/d f0 = (2 cot 2wL - 2i) 2 pi L/c
+        const double c = 2.0 * kPi * (a.armlength / kCSI);
+        const double wL = c * f0;
+        X.dlnsc_f0 = make_double2(2.0 * c * cos(2.0 * wL) / sin(2.0 * wL), -2.0 * c);
+    }
+    X.gf0 = (float)(-fdot / K.fstar);
+    X.gf1 = (float)(-fddot / K.fstar);
+}
+
+// S(a) = sin(a)/a, C = cos(a) and S'(a) from their Taylor series in x = a^2
+// (|a| <= 1.6), library functions beyond.
+__device__ __forceinline__ void sinc_cos_d_f(float a, float &S, float &C, float &dS)
+{
+    const float x = a * a;
+    if (x < 2.56f) {
+        sinc_cos_f(a, S, C);
+        // S'(a) = a sum_{k>=1} (-1)^k 2k x^(k-1) / (2k+1)!
+        float d = -1.0f / 93405312000.0f;
+        d = fmaf(d, x, 1.0f / 518918400.0f);
+        d = fmaf(d, x, -1.0f / 3991680.0f);
+        d = fmaf(d, x, 1.0f / 45360.0f);
+        d = fmaf(d, x, -1.0f / 840.0f);
+        d = fmaf(d, x, 1.0f / 30.0f);
+        d = fmaf(d, x, -1.0f / 3.0f);
+        dS = a * d;
+    } else {
+        float sn, cs;
+        sincosf(a, &sn, &cs);
+        S = sn / a;
+        C = cs;
+        dS = (cs - S) / a;
+    }
+}
+
+// X = G21 - G31 + (G12 - G13) fc and cyclic (gbgpu.py:370-372); links in the
+// order 12, 23, 31, 21, 32, 13
+__device__ __forceinline__ void tdi_xyz(const float2 G[6], float2 fc, float2 out[3])
+{
+    out[0] = cadd(csub(G[3], G[2]), cmul(csub(G[0], G[5]), fc));
+    out[1] = cadd(csub(G[4], G[0]), cmul(csub(G[1], G[3]), fc));
+    out[2] = cadd(csub(G[5], G[1]), cmul(csub(G[2], G[4]), fc));
+}
+
+__device__ __forceinline__ void cmac(float &re, float &im, float2 y, float2 x)
+{
+    re = fmaf(y.x, x.x, fmaf(-y.y, x.y, re));
+    im = fmaf(y.x, x.y, fmaf(y.y, x.x, im));
+}
+
+// Backward pass at one sample: recomputes the slow part with its derivatives
+// and accumulates sum_c Y_c x'_c for x' in {x_P, x_C, dx/df0, dx/dfdot,
+// dx/dfddot, dx/dlam, dx/dbeta} (7 complex accumulators in acc[14]).
+__device__ __forceinline__ void slow_grad_mixed(const Bin &B, const GradExtra &Gx, int n, int N,
+                                                dfl step, const double *__restrict__ tab,
+                                                float ifs, float fstarf, const float2 Yc[3],
+                                                float acc[14])
+{
+    const float *tabf = reinterpret_cast<const float *>(tab + (size_t)18 * N);
+    const dfl twopi = df_from(kTwoPi);
+    const float inv2pi = (float)kInvTwoPi;
+    const float TWO_PI_F = (float)kTwoPi, PI_F = (float)kPi;
+    // arm geometry and its sky derivatives
+    float kd[3], pp[3], cc[3], dkd_l[3], dkd_b[3], dpp_l[3], dcc_l[3], dpp_b[3], dcc_b[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        float r0 = __ldg(tabf + (size_t)(3 * a) * N + n);
+        float r1 = __ldg(tabf + (size_t)(3 * a + 1) * N + n);
+        float r2 = __ldg(tabf + (size_t)(3 * a + 2) * N + n);
+        float k_ = fmaf(B.kf[0], r0, fmaf(B.kf[1], r1, B.kf[2] * r2));
+        float ru = fmaf(Gx.u[0], r0, fmaf(Gx.u[1], r1, Gx.u[2] * r2));
+        float rv = fmaf(Gx.v[0], r0, Gx.v[1] * r1);
+        kd[a] = k_;
+        pp[a] = fmaf(rv, rv, -ru * ru);              // r.e+.r = (r.v)^2 - (r.u)^2
+        cc[a] = 2.0f * ru * rv;                      // r.ex.r = 2 (r.u)(r.v)
+        // d/dlam: du = -ct v, dv = ct u - st k, dk = st v
+        // d/dbeta: du = -k, dv = 0, dk = u
+        dkd_l[a] = Gx.st * rv;
+        dkd_b[a] = ru;
+        const float dru_l = -Gx.ct * rv, drv_l = fmaf(Gx.ct, ru, -Gx.st * k_);
+        dpp_l[a] = 2.0f * fmaf(rv, drv_l, -ru * dru_l);
+        dcc_l[a] = 2.0f * fmaf(dru_l, rv, ru * drv_l);
+        dpp_b[a] = 2.0f * ru * k_;                   // -2 ru (-k)
+        dcc_b[a] = -2.0f * k_ * rv;
+    }
+    // spacecraft: carrier phase (float pairs), delays and their derivatives
+    const dfl tm = df_mul_f(step, (float)n);
+    const float tf = tm.h;
+    dfl Phi0 = df_add(df_mul(B.omdfad, tm), B.phi0d);
+    const dfl tm2 = df_mul(tm, tm);
+    Phi0 = df_neg(df_add(Phi0, df_mul(tm2, df_fast(B.pfd.h, fmaf(B.p3f, tf, B.pfd.l)))));
+    const dfl wt = df_add(B.omd, df_add(df_mul(B.tpfd, tm), dfl{B.pfddf * tf * tf, 0.0f}));
+    const float fdt = fmaf(B.fddotf, tf, B.fdotf);
+    float Er[3], Ei[3], fo[3], xi[3], dph_l[3], dph_b[3], dfo_l[3], dfo_b[3];
+#pragma unroll
+    for (int s = 0; s < 3; s++) {
+        dfl P[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+            P[c] = {__ldg(tabf + (size_t)(9 + 3 * s + c) * N + n),
+                    __ldg(tabf + (size_t)(18 + 3 * s + c) * N + n)};
+        float p0 = B.kd[0].h * P[0].h, p1 = B.kd[1].h * P[1].h, p2 = B.kd[2].h * P[2].h;
+        float e = fmaf(B.kd[0].h, P[0].h, -p0);
+        e += fmaf(B.kd[1].h, P[1].h, -p1);
+        e += fmaf(B.kd[2].h, P[2].h, -p2);
+#pragma unroll
+        for (int c = 0; c < 3; c++) e = fmaf(B.kd[c].h, P[c].l, fmaf(B.kd[c].l, P[c].h, e));
+        dfl s01 = df_two_sum(p0, p1);
+        dfl s012 = df_two_sum(s01.h, p2);
+        const dfl kP = df_fast(s012.h, (s01.l + s012.l) + e);
+        const float kPf = kP.h;
+        const float small = kPf * kPf * fmaf(kPf, (1.0f / 3.0f) * B.pfddf, -PI_F * fdt);
+        dfl ph = df_add(Phi0, df_mul(kP, wt));
+        ph.l += small;
+        const float q = rintf(ph.h * inv2pi);
+        ph = df_add(ph, df_neg(df_mul_f(twopi, q)));
+        float sn, cs;
+        sincosf(ph.h, &sn, &cs);
+        Er[s] = fmaf(sn, -ph.l, cs);
+        Ei[s] = -fmaf(cs, ph.l, sn);
+        const float x = tf - kPf;
+        xi[s] = x;
+        const float f_ = B.w0h + fmaf(fmaf(B.w2, x, B.w1), x, B.w0l);
+        fo[s] = f_;
+        // d kP / d lam = st v.P/c, d kP / d beta = u.P/c
+        const float Pv = fmaf(Gx.v[0], P[0].h, Gx.v[1] * P[1].h);
+        const float Pu = fmaf(Gx.u[0], P[0].h, fmaf(Gx.u[1], P[1].h, Gx.u[2] * P[2].h));
+        const float dkP_l = Gx.st * Pv, dkP_b = Pu;
+        // d phase / d kP = 2 pi f(xi);  d fonfs / d kP = -(fdot + fddot xi)/fstar
+        const float tpf = TWO_PI_F * f_ * fstarf;
+        dph_l[s] = tpf * dkP_l;
+        dph_b[s] = tpf * dkP_b;
+        const float gfk = fmaf(Gx.gf1, x, Gx.gf0);
+        dfo_l[s] = gfk * dkP_l;
+        dfo_b[s] = gfk * dkP_b;
+    }
+    // links: value g E_s (without A), amplitude log-derivative
+    const int arm[6] = {0, 1, 2, 0, 1, 2};
+    const int sc[6] = {0, 1, 2, 1, 2, 0};
+    const float sg[6] = {1.f, 1.f, 1.f, -1.f, -1.f, -1.f};
+    float2 gE[6], G[6];
+    float h1[6], dl[6];
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+        const int s = sc[q], a = arm[q];
+        const float hh = 0.5f * fmaf(sg[q], kd[a], 1.0f);
+        const float av = fo[s] * hh;
+        float S, C, dS;
+        sinc_cos_d_f(av, S, C, dS);
+        const float aS = av * S;
+        const float t = 0.25f * S;
+        // g = 1/4 S (C - i aS); gE = g exp(-i phase_s)
+        const float2 g = make_float2(t * C, -t * aS);
+        gE[q] = cmul(g, make_float2(Er[s], Ei[s]));
+        const float2 A = make_float2(fmaf(pp[a], B.DPf.x, cc[a] * B.DCf.x),
+                                     fmaf(pp[a], B.DPf.y, cc[a] * B.DCf.y));
+        G[q] = cmul(gE[q], A);
+        h1[q] = hh;
+        dl[q] = dS / S;
+    }
+    // TDI factors (gbgpu.py:352-362) and their frequency derivatives
+    const float omL = B.w0h + fmaf(fmaf(B.w2, tf, B.w1), tf, B.w0l);
+    float so, co;
+    sincosf(omL, &so, &co);
+    const float2 fc = make_float2(co, -so);
+    const float g4 = 4.0f * omL * so;
+    const float2 fc2 = make_float2(g4 * co, -g4 * so);
+    // d fc2 / d omL = 4 fc (sin + omL cos - i omL sin), d fc / d omL = -i fc
+    const float2 dfc2 = cmul(make_float2(4.0f * fmaf(omL, co, so), -4.0f * omL * so), fc);
+    const float2 dfc = make_float2(fc.y, -fc.x);
+    float2 Xv[3];
+    tdi_xyz(G, fc, Xv);
+    // plus / cross parts (for iota, psi)
+    {
+        float2 GP[6], X3[3];
+#pragma unroll
+        for (int q = 0; q < 6; q++) GP[q] = cscale(gE[q], pp[arm[q]]);
+        tdi_xyz(GP, fc, X3);
+#pragma unroll
+        for (int c = 0; c < 3; c++) cmac(acc[0], acc[1], Yc[c], cmul(fc2, X3[c]));
+#pragma unroll
+        for (int q = 0; q < 6; q++) GP[q] = cscale(gE[q], cc[arm[q]]);
+        tdi_xyz(GP, fc, X3);
+#pragma unroll
+        for (int c = 0; c < 3; c++) cmac(acc[2], acc[3], Yc[c], cmul(fc2, X3[c]));
+    }
+    // frequency parameters: d a = h1 dfo, d phase = -2 pi xi, -pi xi^2, -pi/3 xi^3;
+    // d fonfs = 1/fstar, xi/fstar, xi^2/(2 fstar); d omL = 1/fstar, t/fstar, t^2/(2 fstar)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        float2 dG[6], X3[3];
+#pragma unroll
+        for (int q = 0; q < 6; q++) {
+            const int s = sc[q];
+            const float x = xi[s];
+            const float dfo = j == 0 ? ifs : (j == 1 ? x * ifs : 0.5f * x * x * ifs);
+            const float dph = j == 0 ? -TWO_PI_F * x : (j == 1 ? -PI_F * x * x : -(PI_F / 3.0f) * x * x * x);
+            const float da = h1[q] * dfo;
+            // (dl da - i (da + dph)) G
+            dG[q] = cmul(make_float2(dl[q] * da, -(da + dph)), G[q]);
+        }
+        tdi_xyz(dG, fc, X3);
+        const float dom = j == 0 ? ifs : (j == 1 ? tf * ifs : 0.5f * tf * tf * ifs);
+        const float2 d12 = csub(G[0], G[5]), d23 = csub(G[1], G[3]), d31 = csub(G[2], G[4]);
+        const float2 dfcj = cscale(dfc, dom), dfc2j = cscale(dfc2, dom);
+        float2 dx;
+        dx = cadd(cmul(dfc2j, Xv[0]), cmul(fc2, cadd(X3[0], cmul(d12, dfcj))));
+        cmac(acc[4 + 2 * j], acc[5 + 2 * j], Yc[0], dx);
+        dx = cadd(cmul(dfc2j, Xv[1]), cmul(fc2, cadd(X3[1], cmul(d23, dfcj))));
+        cmac(acc[4 + 2 * j], acc[5 + 2 * j], Yc[1], dx);
+        dx = cadd(cmul(dfc2j, Xv[2]), cmul(fc2, cadd(X3[2], cmul(d31, dfcj))));
+        cmac(acc[4 + 2 * j], acc[5 + 2 * j], Yc[2], dx);
+    }
+    // sky angles
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+        float2 dG[6], X3[3];
+#pragma unroll
+        for (int q = 0; q < 6; q++) {
+            const int s = sc[q], a = arm[q];
+            const float dfo = j == 0 ? dfo_l[s] : dfo_b[s];
+            const float dph = j == 0 ? dph_l[s] : dph_b[s];
+            const float dkd = j == 0 ? dkd_l[a] : dkd_b[a];
+            const float da = fmaf(h1[q], dfo, 0.5f * fo[s] * sg[q] * dkd);
+            const float dpp = j == 0 ? dpp_l[a] : dpp_b[a];
+            const float dcc = j == 0 ? dcc_l[a] : dcc_b[a];
+            const float2 dA = make_float2(fmaf(dpp, B.DPf.x, dcc * B.DCf.x),
+                                          fmaf(dpp, B.DPf.y, dcc * B.DCf.y));
+            dG[q] = cadd(cmul(make_float2(dl[q] * da, -(da + dph)), G[q]), cmul(gE[q], dA));
+        }
+        tdi_xyz(dG, fc, X3);
+#pragma unroll
+        for (int c = 0; c < 3; c++) cmac(acc[10 + 2 * j], acc[11 + 2 * j], Yc[c], cmul(fc2, X3[c]));
+    }
+}
+
+// In-place decimation-in-time FFT on bit-reversed input (natural-order output)
+// over `nsub` sub-arrays of length N = 2^lg: the five smallest half-spans
+// inside warps with shuffles, the rest in register passes of up to three
+// stages (the mirror image of fft_dif).
+template <typename R, int RB>
+__device__ __forceinline__ void fft_dit_pass(typename C2<R>::T *buf, int nsub, int lg, int hl)
+{
+    using V = typename C2<R>::T;
+    constexpr int M = 1 << RB;
+    const int groups = nsub << (lg - RB);
+    for (int g = threadIdx.x; g < groups; g += kBlock) {
+        const int a = g >> (lg - RB);
+        const int rem = g & ((1 << (lg - RB)) - 1);
+        const int blk = rem >> hl;
+        const int r = rem & ((1 << hl) - 1);
+        V *base = buf + ((size_t)a << lg) + ((size_t)blk << (hl + RB)) + r;
+        V x[M];
+#pragma unroll
+        for (int m = 0; m < M; m++) x[m] = base[(size_t)m << hl];
+#pragma unroll
+        for (int j = 0; j < RB; j++) {
+            const int dm = 1 << j;
+            const int hh = hl + j;
+            const int ts = kTwN >> (hh + 1);
+#pragma unroll
+            for (int m = 0; m < M; m++) {
+                if (m & dm) continue;
+                const int rp = r + ((m & (dm - 1)) << hl);
+                V t = cmul(tw<R>(rp * ts), x[m + dm]);
+                V u = x[m];
+                x[m] = cadd(u, t);
+                x[m + dm] = csub(u, t);
+            }
+        }
+#pragma unroll
+        for (int m = 0; m < M; m++) base[(size_t)m << hl] = x[m];
+    }
+}
+
+template <typename R>
+__device__ __forceinline__ void fft_dit(typename C2<R>::T *buf, int nsub, int lg)
+{
+    using V = typename C2<R>::T;
+    const int lane = threadIdx.x & 31;
+    V w[5];
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        const int rp = lane & ((1 << k) - 1);
+        w[k] = tw<R>(rp * (kTwN >> (k + 1)));
+    }
+    const int chunks = (nsub << lg) >> 5;
+    for (int c = threadIdx.x >> 5; c < chunks; c += kBlock >> 5) {
+        V x = buf[(c << 5) + lane];
+#pragma unroll
+        for (int k = 0; k < 5; k++) {
+            const int o = 1 << k;
+            V y = shfl_c<R>(x, o);
+            const bool up = (lane & o) != 0;
+            V t = cmul(w[k], up ? x : y);          // W times the upper element
+            x = up ? csub(y, t) : cadd(x, t);
+        }
+        buf[(c << 5) + lane] = x;
+    }
+    __syncthreads();
+    int hl = 5;
+    while (hl < lg) {
+        const int rb = (lg - hl) >= 3 ? 3 : (lg - hl);
+        if (rb == 3) fft_dit_pass<R, 3>(buf, nsub, lg, hl);
+        else if (rb == 2) fft_dit_pass<R, 2>(buf, nsub, lg, hl);
+        else fft_dit_pass<R, 1>(buf, nsub, lg, hl);
+        hl += rb;
+        __syncthreads();
+    }
+}
+
+struct GradParams {
+    KParams K;
+    double *grad;                  // (9, num_bin) FP64, the params layout
+};
+
+constexpr int kGradAcc = 19;       // ll terms 3, Qf 2, 7 complex accumulators 14
+
+__global__ void __launch_bounds__(kBlock, 1) grad_kernel(const GradParams GP)
+{
+    using V = float2;
+    const KParams &K = GP.K;
+    extern __shared__ __align__(16) unsigned char smem[];
+    Bin *bins = reinterpret_cast<Bin *>(smem);
+    GradExtra *gxs = reinterpret_cast<GradExtra *>(smem + sizeof(Bin) * kMaxPack);
+    double *red = reinterpret_cast<double *>(smem + (sizeof(Bin) + sizeof(GradExtra)) * kMaxPack);
+    V *buf = reinterpret_cast<V *>(smem + (sizeof(Bin) + sizeof(GradExtra)) * kMaxPack +
+                                   sizeof(double) * kGradAcc * 16);
+    __shared__ int s_tile;
+
+    const gbx_wave_args &a = K.a;
+    const int tid = threadIdx.x;
+    const int ntiles = a.tiles ? a.ntiles : (a.num_bin + K.P - 1) / K.P;
+    const float ifs = (float)(1.0 / K.fstar);
+    const float fstarf = (float)K.fstar;
+    const Bin *wsb = static_cast<const Bin *>(a.workspace);
+    const GradExtra *wsg = reinterpret_cast<const GradExtra *>(wsb + a.num_bin);
+    int iter = 0;
+    for (;;) {
+        if (tid == 0) s_tile = a.queue ? atomicAdd(a.queue, 1) : (int)(blockIdx.x + iter * gridDim.x);
+        __syncthreads();
+        const int tile = s_tile;
+        iter++;
+        if (tile >= ntiles) break;
+        int lg, first, cnt;
+        if (a.tiles) {
+            lg = a.tiles[4 * tile];
+            first = a.tiles[4 * tile + 1];
+            cnt = a.tiles[4 * tile + 2];
+        } else {
+            lg = 31 - __clz(a.N);
+            first = tile * K.P;
+            cnt = min(K.P, a.num_bin - first);
+        }
+        const int N = 1 << lg;
+        const double *tab = (lg >= 5 && lg <= GBX_MAX_LOG2N)
+                                ? reinterpret_cast<const double *>(a.orbit[lg]) : nullptr;
+        const int maxcnt = max(1, kTileMin >> lg);
+        if (tab == nullptr || cnt < 1 || cnt > maxcnt || first < 0 || first + cnt > a.num_bin ||
+            (cnt << lg) > K.maxS) {
+            flag(a.status, GBX_FLAG_TILE);
+            __syncthreads();
+            continue;
+        }
+        {
+            const int4 *src = reinterpret_cast<const int4 *>(wsb + first);
+            int4 *dst = reinterpret_cast<int4 *>(bins);
+            for (int k = tid; k < cnt * (int)(sizeof(Bin) / 16); k += kBlock) dst[k] = src[k];
+            const int4 *src2 = reinterpret_cast<const int4 *>(wsg + first);
+            int4 *dst2 = reinterpret_cast<int4 *>(gxs);
+            for (int k = tid; k < cnt * (int)(sizeof(GradExtra) / 16); k += kBlock) dst2[k] = src2[k];
+        }
+        __syncthreads();
+        const int S = cnt << lg;
+        const dfl stepd = K.stepd[lg];
+
+        // forward slow part and FFT
+        for (int m = tid; m < S; m += kBlock) {
+            const int p = m >> lg, n = m & (N - 1);
+            float2 o[3];
+            slow_mixed<false>(bins[p], n, N, stepd, tab, nullptr, nullptr, o);
+#pragma unroll
+            for (int c = 0; c < 3; c++) buf[(p * 3 + c) * N + n] = o[c];
+        }
+        __syncthreads();
+        fft_dif<float>(buf, 3 * cnt, lg);
+
+        // residual weights, likelihood terms, Qf; conj(w) written in place
+        const int Tpb = kBlock / maxcnt;
+        const int width = Tpb < 32 ? Tpb : 32;
+        const int p = tid / Tpb;
+        const int i0 = tid - p * Tpb;
+        float acc[kGradAcc];
+#pragma unroll
+        for (int k = 0; k < kGradAcc; k++) acc[k] = 0.0f;
+        const float is2 = 0.70710678118654752440f, is6 = 0.40824829046386301637f;
+        if (p < cnt) {
+            const Bin &B = bins[p];
+            bool out = false;
+            // scale 2^eD as a float complex: h in the data's scaled units
+            const float2 sc = make_float2((float)(B.scale.x * exp2_int(B.eD)),
+                                          (float)(B.scale.y * exp2_int(B.eD)));
+            for (int i = i0; i < N; i += Tpb) {
+                const int j = B.start + i;
+                const int pos = bitrev((i + (N >> 1)) & (N - 1), lg);
+                V X = buf[(p * 3 + 0) * N + pos], Y = buf[(p * 3 + 1) * N + pos],
+                  Z = buf[(p * 3 + 2) * N + pos];
+                float2 wX = {0.f, 0.f}, wY = {0.f, 0.f}, wZ = {0.f, 0.f};
+                if (B.valid && j >= 0 && j < K.L) {
+                    const size_t jd = (size_t)B.di * K.L + j, jn = (size_t)B.ni * K.L + j;
+                    const double2 dA = __ldg(K.A_data + jd), dE = __ldg(K.E_data + jd);
+                    const double SA = __ldg(K.A_psd + jn), SE = __ldg(K.E_psd + jn);
+                    const float2 hA = make_float2((Z.x - X.x) * is2, (Z.y - X.y) * is2);
+                    const float2 hE = make_float2((X.x - 2.f * Y.x + Z.x) * is6,
+                                                  (X.y - 2.f * Y.y + Z.y) * is6);
+                    const float wA = __frcp_rn(d2f_scaled(SA, B.eS));
+                    const float wE = __frcp_rn(d2f_scaled(SE, B.eS));
+                    const float aR = d2f_scaled(dA.x, B.eD), aI = d2f_scaled(dA.y, B.eD);
+                    const float eR = d2f_scaled(dE.x, B.eD), eI = d2f_scaled(dE.y, B.eD);
+                    acc[0] += fmaf(aR, hA.x, aI * hA.y) * wA + fmaf(eR, hE.x, eI * hE.y) * wE;
+                    acc[1] += fmaf(aR, hA.y, -aI * hA.x) * wA + fmaf(eR, hE.y, -eI * hE.x) * wE;
+                    acc[2] += fmaf(hA.x, hA.x, hA.y * hA.y) * wA + fmaf(hE.x, hE.x, hE.y * hE.y) * wE;
+                    // r' = d' - sc h ; u = r' / S'
+                    const float2 shA = cmul(sc, hA), shE = cmul(sc, hE);
+                    const float2 uA = make_float2((aR - shA.x) * wA, (aI - shA.y) * wA);
+                    const float2 uE = make_float2((eR - shE.x) * wE, (eI - shE.y) * wE);
+                    wX = make_float2(fmaf(-uA.x, is2, uE.x * is6), fmaf(-uA.y, is2, uE.y * is6));
+                    wY = make_float2(-2.f * uE.x * is6, -2.f * uE.y * is6);
+                    wZ = make_float2(fmaf(uA.x, is2, uE.x * is6), fmaf(uA.y, is2, uE.y * is6));
+                    // Qf = sum conj(w) X
+                    acc[3] += fmaf(wX.x, X.x, fmaf(wX.y, X.y, fmaf(wY.x, Y.x, fmaf(wY.y, Y.y,
+                              fmaf(wZ.x, Z.x, wZ.y * Z.y)))));
+                    acc[4] += fmaf(wX.x, X.y, fmaf(-wX.y, X.x, fmaf(wY.x, Y.y, fmaf(-wY.y, Y.x,
+                              fmaf(wZ.x, Z.y, -wZ.y * Z.x)))));
+                } else if (B.valid) {
+                    out = true;
+                }
+                buf[(p * 3 + 0) * N + pos] = make_float2(wX.x, -wX.y);
+                buf[(p * 3 + 1) * N + pos] = make_float2(wY.x, -wY.y);
+                buf[(p * 3 + 2) * N + pos] = make_float2(wZ.x, -wZ.y);
+            }
+            if (out) flag(a.status, GBX_FLAG_WINDOW);
+        }
+        __syncthreads();
+        fft_dit<float>(buf, 3 * cnt, lg);
+
+        // backward pass: Y_c,n at natural position n
+        if (p < cnt) {
+            const Bin &B = bins[p];
+            const GradExtra &Gx = gxs[p];
+            if (B.valid) {
+                for (int n = i0; n < N; n += Tpb) {
+                    float2 Yc[3];
+#pragma unroll
+                    for (int c = 0; c < 3; c++) Yc[c] = buf[(p * 3 + c) * N + n];
+                    slow_grad_mixed(B, Gx, n, N, stepd, tab, ifs, fstarf, Yc, acc + 5);
+                }
+            }
+        }
+        // group trees (float pairs), then FP64 across groups
+        double gsum[kGradAcc];
+#pragma unroll
+        for (int k = 0; k < kGradAcc; k++) {
+            dfl x = {acc[k], 0.f};
+            for (int o = width >> 1; o > 0; o >>= 1) {
+                dfl y = {__shfl_xor_sync(0xffffffffu, x.h, o), __shfl_xor_sync(0xffffffffu, x.l, o)};
+                x = df_add(x, y);
+            }
+            gsum[k] = (double)x.h + (double)x.l;
+        }
+        if ((tid & (width - 1)) == 0) {
+            const int g = tid / width;
+#pragma unroll
+            for (int k = 0; k < kGradAcc; k++) red[kGradAcc * g + k] = gsum[k];
+        }
+        __syncthreads();
+        if (tid < cnt) {
+            const Bin &B = bins[tid];
+            const GradExtra &Gx = gxs[tid];
+            const int per = Tpb / width;
+            double t[kGradAcc];
+#pragma unroll
+            for (int k = 0; k < kGradAcc; k++) t[k] = 0.0;
+            for (int g = tid * per; g < (tid + 1) * per; g++)
+#pragma unroll
+                for (int k = 0; k < kGradAcc; k++) t[k] += red[kGradAcc * g + k];
+            const double s4 = 4.0 * K.df;
+            const double cd = s4 * exp2_int(B.eS - B.eD);
+            const double ch = s4 * exp2_int(B.eS) * (B.scale.x * B.scale.x + B.scale.y * B.scale.y);
+            const double2 dh = cmul(make_double2(cd * t[0], cd * t[1]), B.scale);
+            const double2 hv = make_double2(ch * t[2], 0.0);
+            // weights were 4 df r / S in units of 2^(eS - eD): cu converts sums of w
+            const double cu = s4 * exp2_int(B.eS - B.eD);
+            const double2 sc = B.scale;
+            const double2 Qf = make_double2(cu * t[3], cu * t[4]);
+            const double2 QP = make_double2(cu * t[5], cu * t[6]);
+            const double2 QC = make_double2(cu * t[7], cu * t[8]);
+            const double2 scQf = cmul(sc, Qf);
+            const double nb = a.num_bin;
+            double g9[9];
+            const double *pr = a.params;
+            const double amp = pr[B.b];
+            g9[0] = scQf.x / amp;                                      // amp
+            g9[1] = cmul(sc, make_double2(cu * t[9], cu * t[10])).x +   // f0
+                    cmul(Gx.dlnsc_f0, scQf).x;
+            g9[2] = cmul(sc, make_double2(cu * t[11], cu * t[12])).x;  // fdot
+            g9[3] = cmul(sc, make_double2(cu * t[13], cu * t[14])).x;  // fddot
+            g9[4] = -scQf.y;                                           // phi0: Re(i sc Qf)
+            g9[5] = cmul(sc, cadd(cmul(Gx.dDPi, QP), cmul(Gx.dDCi, QC))).x;   // iota
+            g9[6] = cmul(sc, cadd(cmul(Gx.dDPp, QP), cmul(Gx.dDCp, QC))).x;   // psi
+            g9[7] = cmul(sc, make_double2(cu * t[15], cu * t[16])).x;  // lam
+            g9[8] = cmul(sc, make_double2(cu * t[17], cu * t[18])).x;  // beta
+            if (B.b >= 0) {
+                K.d_h[B.b] = B.valid ? dh : make_double2(0.0, 0.0);
+                K.h_h[B.b] = B.valid ? hv : make_double2(0.0, 0.0);
+#pragma unroll
+                for (int k = 0; k < 9; k++)
+                    GP.grad[(size_t)k * (size_t)nb + B.b] = B.valid ? g9[k] : 0.0;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(kPrepBlock) prep_grad_kernel(const KParams K)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    Bin *sb = reinterpret_cast<Bin *>(smem);
+    GradExtra *sg = reinterpret_cast<GradExtra *>(smem + sizeof(Bin) * kPrepBlock);
+    const gbx_wave_args &a = K.a;
+    const int s0 = blockIdx.x * kPrepBlock;
+    const int slot = s0 + threadIdx.x;
+    if (slot < a.num_bin) {
+        int lg;
+        if (a.tiles) {
+            int lo = 0, hi = a.ntiles - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (a.tiles[4 * mid + 1] <= slot) lo = mid; else hi = mid - 1;
+            }
+            lg = a.tiles[4 * lo];
+        } else {
+            lg = 31 - __clz(a.N);
+        }
+        const int b = a.order ? a.order[slot] : slot;
+        if (b < 0 || b >= a.num_bin || lg < 5 || lg > GBX_MAX_LOG2N) {
+            flag(a.status, GBX_FLAG_TILE);
+            memset(&sb[threadIdx.x], 0, sizeof(Bin));
+            memset(&sg[threadIdx.x], 0, sizeof(GradExtra));
+            sb[threadIdx.x].b = -1;
+        } else {
+            setup_bin(sb[threadIdx.x], K, b, 1 << lg, MODE_LL);
+            setup_grad(sg[threadIdx.x], K, b);
+        }
+    }
+    __syncthreads();
+    const int cnt = min(kPrepBlock, a.num_bin - s0);
+    Bin *wsb = static_cast<Bin *>(a.workspace);
+    GradExtra *wsg = reinterpret_cast<GradExtra *>(wsb + a.num_bin);
+    const int4 *src = reinterpret_cast<const int4 *>(sb);
+    int4 *dst = reinterpret_cast<int4 *>(wsb + s0);
+    for (int k = threadIdx.x; k < cnt * (int)(sizeof(Bin) / 16); k += kPrepBlock) dst[k] = src[k];
+    const int4 *src2 = reinterpret_cast<const int4 *>(sg);
+    int4 *dst2 = reinterpret_cast<int4 *>(wsg + s0);
+    for (int k = threadIdx.x; k < cnt * (int)(sizeof(GradExtra) / 16); k += kPrepBlock)
+        dst2[k] = src2[k];
+}

@@ -1064,6 +1064,8 @@ __global__ void __launch_bounds__(kPrepBlock) prep_kernel(const KParams K)
     for (int k = threadIdx.x; k < n16; k += kPrepBlock) dst[k] = src[k];
 }
 
+#include "gbx_grad.cuh"
+
 // ----------------------------------------------------------------------------
 // host side
 // ----------------------------------------------------------------------------
@@ -1263,6 +1265,88 @@ extern "C" int gbx_waveform_fill(const gbx_wave_args *a, void *A_glob, void *E_g
     K.gstride = group_stride;
     K.L = data_length;
     return dispatch<MODE_FILL>(K, maxS, (cudaStream_t)stream);
+}
+
+extern "C" size_t gbx_grad_workspace_bytes(int num_bin)
+{
+    if (num_bin <= 0) return 0;
+    return ((size_t)num_bin * (sizeof(Bin) + sizeof(GradExtra)) + 255) & ~(size_t)255;
+}
+
+extern "C" int gbx_waveform_ll_grad(const gbx_wave_args *a, const gbx_ll_args *l, void *d_h,
+                                    void *h_h, double *grad, void *stream)
+{
+    int maxS = 0;
+    gbx_wave_args b = a ? *a : gbx_wave_args{};
+    if (!a) return set_error(GBX_ERR_ARG, "NULL wave args");
+    // the per-binary workspace of this entry point is larger; validate it here
+    const void *ws = b.workspace;
+    const size_t wsb = b.workspace_bytes;
+    b.workspace = nullptr;
+    int rc = check_wave(&b, &maxS);
+    if (rc) return rc;
+    if (b.precision != GBX_MIXED) return set_error(GBX_ERR_UNSUPPORTED, "gradients are computed in the mixed form only");
+    if (b.nparams != 9) return set_error(GBX_ERR_UNSUPPORTED, "gradients cover the 9-parameter circular model");
+    if (!ws || ((uintptr_t)ws & 15) != 0 || wsb < gbx_grad_workspace_bytes(b.num_bin))
+        return set_error(GBX_ERR_ARG, "gradients need a 16-byte aligned workspace of gbx_grad_workspace_bytes(num_bin)");
+    if (!l || !l->A_data || !l->E_data || !l->A_psd || !l->E_psd || !d_h || !h_h || !grad)
+        return set_error(GBX_ERR_ARG, "NULL likelihood / gradient pointer");
+    if (l->data_length <= 0 || l->num_data < 1 || l->num_psd < 1)
+        return set_error(GBX_ERR_ARG, "data_length / num_data / num_psd must be positive");
+    if (b.num_bin == 0) return GBX_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    rc = ensure_init(st);
+    if (rc) return rc;
+    b.workspace = const_cast<void *>(ws);
+    b.workspace_bytes = wsb;
+    GradParams G;
+    memset(&G, 0, sizeof(G));
+    G.K = base_params(&b);
+    KParams &K = G.K;
+    K.A_data = (const double2 *)l->A_data;
+    K.E_data = (const double2 *)l->E_data;
+    K.A_psd = l->A_psd;
+    K.E_psd = l->E_psd;
+    K.L = l->data_length;
+    K.num_data = l->num_data;
+    K.num_psd = l->num_psd;
+    K.data_index = l->data_index;
+    K.noise_index = l->noise_index;
+    K.df = l->df;
+    K.d_h = (double2 *)d_h;
+    K.h_h = (double2 *)h_h;
+    K.maxS = maxS;
+    G.grad = grad;
+    const size_t sm = (sizeof(Bin) + sizeof(GradExtra)) * kMaxPack + sizeof(double) * kGradAcc * 16 +
+                      3 * (size_t)maxS * sizeof(float2);
+    if (sm > 227 * 1024) return set_error(GBX_ERR_UNSUPPORTED, "tile needs %zu B of shared memory", sm);
+    cudaError_t e = cudaFuncSetAttribute(grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(grad)");
+    e = cudaFuncSetAttribute(grad_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(grad carveout)");
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grad_kernel, kBlock, sm);
+    if (e != cudaSuccess) return cuda_error(e, "occupancy(grad)");
+    if (per_sm < 1) per_sm = 1;
+    const int ntiles = b.tiles ? b.ntiles : (b.num_bin + K.P - 1) / K.P;
+    int grid = per_sm * num_sms();
+    if (grid > ntiles) grid = ntiles;
+    if (grid < 1) return GBX_OK;
+    if (b.queue) {
+        e = cudaMemsetAsync(b.queue, 0, sizeof(int), st);
+        if (e != cudaSuccess) return cuda_error(e, "queue reset");
+    }
+    const size_t psm = (sizeof(Bin) + sizeof(GradExtra)) * kPrepBlock;
+    e = cudaFuncSetAttribute(prep_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psm);
+    if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(prep_grad)");
+    prep_grad_kernel<<<(b.num_bin + kPrepBlock - 1) / kPrepBlock, kPrepBlock, psm, st>>>(K);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_error(e, "prep_grad_kernel launch");
+    grad_kernel<<<grid, kBlock, sm, st>>>(G);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_error(e, "grad_kernel launch");
+    return GBX_OK;
 }
 
 // ----------------------------------------------------------------------------

@@ -102,7 +102,7 @@ class WavePlan:
         self.queue = torch.zeros(1, dtype=torch.int32, device=dev) if not self.uniform else None
         self._ws = None
 
-    def args(self, params, start_freq_ind=0, status=None):
+    def args(self, params, start_freq_ind=0, status=None, grad=False):
         a = nat.WaveArgs()
         a.params = params.data_ptr()
         a.num_bin = params.shape[1]
@@ -122,7 +122,8 @@ class WavePlan:
         a.queue = self.queue.data_ptr() if self.queue is not None else None
         a.status = status.data_ptr() if status is not None else None
         B = params.shape[1]
-        need = nat.lib().gbx_wave_workspace_bytes(B)
+        need = (nat.lib().gbx_grad_workspace_bytes(B) if grad
+                else nat.lib().gbx_wave_workspace_bytes(B))
         if need:
             if self._ws is None or self._ws.numel() * 16 < need:
                 self._ws = torch.empty((need + 15) // 16, dtype=torch.complex128,
@@ -511,6 +512,76 @@ class GBGPUBase(abc.ABC):
         out = like.cpu().numpy()
         self._check_status()
         return out
+
+    def get_ll_grad(self, params, data, psd, start_freq_ind=0, data_index=None,
+                    noise_index=None, **kwargs):
+        """Log-likelihood and its gradient in one fused launch (mixed form).
+
+        Returns ``(like, grad)``: NumPy ``(B,)`` and ``(9, B)`` with
+        ``grad[k, b] = d like[b] / d params[k, b]`` for amp, f0, fdot, fddot,
+        phi0, iota, psi, lam, beta.  No counterpart in the reference (its
+        derivatives are finite differences, gbgpu.py:957-1138).  Set
+        ``return_tensors=True`` to get device tensors instead.
+        """
+        like, grad = self._ll_grad_tensors(params, data, psd, start_freq_ind, data_index,
+                                           noise_index, **kwargs)
+        if kwargs.get("return_tensors"):
+            return like, grad
+        return like.cpu().numpy(), grad.cpu().numpy()
+
+    def _ll_grad_tensors(self, params, data, psd, start_freq_ind=0, data_index=None,
+                         noise_index=None, **kwargs):
+        if self.d_d is None:
+            raise ValueError("self.d_d attribute must be set before computing log-Likelihood.")
+        kwargs.pop("return_tensors", None)
+        kwargs.pop("precision", None)
+        N = kwargs.pop("N", None)
+        T = kwargs.pop("T", 4 * YRSID_SI)
+        dt = kwargs.pop("dt", 10.0)
+        oversample = kwargs.pop("oversample", 1)
+        tdi2 = kwargs.pop("tdi2", False)
+        if kwargs:
+            raise TypeError(f"unexpected keyword arguments {list(kwargs)}")
+        if self.NPARAMS != 9:
+            raise NotImplementedError("gradients cover the 9-parameter circular model")
+        T = int(T / dt) * dt
+        self._check_T(T)
+        prm = _to_device(params, torch.float64, self.device).detach().contiguous()
+        if prm.ndim != 2 or prm.shape[0] != 9:
+            raise ValueError("params must be (9, B)")
+        if N is None:
+            N = self._resolve_N(N, prm[0], prm[1], T, (), oversample)
+        elif np.ndim(N) != 0:
+            N = np.asarray(_to_host(N), dtype=np.int64).reshape(-1)
+        else:
+            N = int(N)
+        B = prm.shape[1]
+        self.num_bin, self.N, self.df = B, N, 1 / T
+        dd, pp, L, di, ni = self._prepare_data(data, psd, data_index, noise_index, B)
+        d_h = torch.empty(B, dtype=torch.complex128, device=self.device)
+        h_h = torch.empty(B, dtype=torch.complex128, device=self.device)
+        grad = torch.zeros((9, B), dtype=torch.float64, device=self.device)
+        if B:
+            plan = self._plan(N, T, "mixed", tdi2, 9)
+            self._status.zero_()
+            a = plan.args(prm, start_freq_ind, self._status, grad=True)
+            la = nat.LLArgs()
+            la.A_data, la.E_data = dd[0].data_ptr(), dd[1].data_ptr()
+            la.A_psd, la.E_psd = pp[0].data_ptr(), pp[1].data_ptr()
+            la.data_length = int(L)
+            la.num_data = int(dd[0].numel() // L)
+            la.num_psd = int(pp[0].numel() // L)
+            la.data_index = di.data_ptr()
+            la.noise_index = ni.data_ptr()
+            la.df = 1.0 / T
+            rc = nat.lib().gbx_waveform_ll_grad(ctypes.byref(a), ctypes.byref(la), nat.ptr(d_h),
+                                                nat.ptr(h_h), nat.ptr(grad), nat.stream_handle())
+            nat.check(rc, "gbx_waveform_ll_grad")
+        self._lazy = (prm, N, T, tdi2)
+        self.d_h, self.h_h = d_h, h_h
+        d_d = torch.as_tensor(self.d_d, device=self.device)
+        like = -0.5 * (d_d + h_h.real - 2 * d_h.real)
+        return like, grad
 
     # --------------------------------------------------------- global fill
     def fill_global_template(self, group_index, templates, A, E, start_inds, N=None,

@@ -206,6 +206,19 @@ int gbx_waveform_fill(const gbx_wave_args *a, void *A_glob, void *E_glob,
                       long long group_stride, void *stream);
 
 /*
+ * Fused waveform + likelihood + gradient (no counterpart in the reference,
+ * which has only finite-difference Fisher matrices, gbgpu/gbgpu.py:957-1138).
+ * Computes d_h, h_h as gbx_waveform_ll and grad[k*num_bin + b] =
+ * d logL_b / d params[k, b] for the nine parameters (amp, f0, fdot, fddot,
+ * phi0, iota, psi, lam, beta) of logL = -1/2 (<d|d> + <h|h> - 2 Re<d|h>).
+ * Mixed form and the 9-parameter circular model only.  The workspace is
+ * required and must hold gbx_grad_workspace_bytes(num_bin) bytes.
+ */
+size_t gbx_grad_workspace_bytes(int num_bin);
+int gbx_waveform_ll_grad(const gbx_wave_args *a, const gbx_ll_args *l, void *d_h, void *h_h,
+                         double *grad, void *stream);
+
+/*
  * gbx_waveform_ll without caller-provided scratch.  No counterpart in the
  * reference (its kernels use no scratch).  For callers that may not allocate
  * device memory: a plug-in inside an application that owns all device
