@@ -246,6 +246,66 @@ def sparse_accuracy(gb, p, Ns, Sd, seed, count=2000):
     return (d / torch.clamp(out["fp64"][1], min=1.0)).max().item()
 
 
+def config3(gb, data, Sd, seed, steps):
+    """BASELINE config 3 shape: 50,000 binaries, N = 256, TDI-2, config-0
+    parameter distributions, on the same 4-yr data grid.  Times the FP64 and
+    mixed fused likelihood and the likelihood + gradient kernel."""
+    import ctypes
+    import torch
+    from gbgpu_gb300 import _native as nat
+    rng = np.random.default_rng(seed + 3)
+    B = 50_000
+    f0 = rng.uniform(1e-3, 5e-3, B)
+    fdot = 10 ** rng.uniform(-18, -15, B)
+    p = np.array([10 ** rng.uniform(-23, -21, B), f0, fdot, 11.0 / 3.0 * fdot ** 2 / f0,
+                  rng.uniform(0, 2 * np.pi, B), np.arccos(rng.uniform(-1, 1, B)),
+                  rng.uniform(0, np.pi, B), rng.uniform(0, 2 * np.pi, B),
+                  np.arcsin(rng.uniform(-1, 1, B))])
+    prm = torch.as_tensor(p, device="cuda").contiguous()
+    Tu = int(T_OBS / DT) * DT
+    L = data[0].shape[0]
+    zeros = torch.zeros(B, dtype=torch.int32, device="cuda")
+    la = nat.LLArgs()
+    la.A_data, la.E_data = data[0].data_ptr(), data[1].data_ptr()
+    la.A_psd = la.E_psd = Sd.data_ptr()
+    la.data_length, la.num_data, la.num_psd = L, 1, 1
+    la.data_index = la.noise_index = zeros.data_ptr()
+    la.df = 1.0 / Tu
+    d_h = torch.empty(B, dtype=torch.complex128, device="cuda")
+    h_h = torch.empty(B, dtype=torch.complex128, device="cuda")
+    g = torch.empty((9, B), dtype=torch.float64, device="cuda")
+    lib = nat.lib()
+    sh = nat.stream_handle()
+    out = {"workload": "50,000 binaries, N=256, tdi2=True, T=4x31557600 s",
+           "steps": steps}
+    for name, prec in (("fp64", "fp64"), ("mixed", "mixed"), ("grad", "mixed")):
+        plan = gb._plan(256, Tu, prec, True, 9)
+        a = plan.args(prm, grad=(name == "grad"))
+
+        def run():
+            if name == "grad":
+                rc = lib.gbx_waveform_ll_grad(ctypes.byref(a), ctypes.byref(la), nat.ptr(d_h),
+                                              nat.ptr(h_h), nat.ptr(g), sh)
+            else:
+                rc = lib.gbx_waveform_ll(ctypes.byref(a), ctypes.byref(la), nat.ptr(d_h),
+                                         nat.ptr(h_h), sh)
+            nat.check(rc, name)
+        for _ in range(2):
+            run()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            run()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        out[f"{name}_binaries_per_s"] = B / (ms / 1e3)
+    out["grad_over_forward"] = out["grad_binaries_per_s"] / out["mixed_binaries_per_s"]
+    out["mixed_over_fp64"] = out["mixed_binaries_per_s"] / out["fp64_binaries_per_s"]
+    return out
+
+
 def run_gpu(args, rank, world):
     import torch
     import torch.distributed as dist
@@ -278,9 +338,19 @@ def run_gpu(args, rank, world):
     stream = torch.cuda.current_stream()
     sh = nat.stream_handle(stream)
 
+    grad_out = torch.empty((9, B), dtype=torch.float64, device="cuda")
+    gplan = gb._plan(Ns, int(T_OBS / DT) * DT, "mixed", False, 9)
+    wargs["grad"] = gplan.args(params_d, grad=True)
+
     def step(prec):
-        rc = lib.gbx_waveform_ll(ctypes.byref(wargs[prec]), ctypes.byref(la),
-                                 ctypes.c_void_p(d_h.data_ptr()), ctypes.c_void_p(h_h.data_ptr()), sh)
+        if prec == "grad":
+            rc = lib.gbx_waveform_ll_grad(ctypes.byref(wargs["grad"]), ctypes.byref(la),
+                                          ctypes.c_void_p(d_h.data_ptr()),
+                                          ctypes.c_void_p(h_h.data_ptr()),
+                                          ctypes.c_void_p(grad_out.data_ptr()), sh)
+        else:
+            rc = lib.gbx_waveform_ll(ctypes.byref(wargs[prec]), ctypes.byref(la),
+                                     ctypes.c_void_p(d_h.data_ptr()), ctypes.c_void_p(h_h.data_ptr()), sh)
         if rc:
             nat.check(rc, "gbx_waveform_ll")
 
@@ -330,6 +400,8 @@ def run_gpu(args, rank, world):
     with ClockSampler(torch.cuda.current_device()) as clk:
         ms_mixed, wall_mixed = timed("mixed", args.steps, args.warmup)
     ms_fp64, _ = timed("fp64", max(1, min(args.steps, 3)), 1)
+    ms_grad, _ = timed("grad", max(1, min(args.steps, 10)), 1)
+    cfg3 = config3(gb, data, Sd, args.seed + rank, max(1, min(args.steps, 10)))
 
     # e2e through the public API: host params -> device, like -> host
     p_pin = torch.from_numpy(np.ascontiguousarray(p)).pin_memory()
@@ -382,7 +454,10 @@ def run_gpu(args, rank, world):
             "note": "vs the FP64 form of the same kernel (itself within 1e-10 of the "
                     "reference); crowded = the 200k-source data, sparse = 2000 "
                     "non-overlapping sources + noise"},
-        "grads_per_s": None,
+        "grads_per_s": B / (ms_grad / 1e3),
+        "grads_note": "binaries/s of the fused likelihood + 9-parameter gradient kernel "
+                      "(mixed form) on the same 200k-binary batch",
+        "config3": cfg3,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "note": f"peak {peak_src}; the kernel is FP64-pipe bound (carrier phase), "

@@ -106,82 +106,66 @@ __device__ __forceinline__ void cmac(float &re, float &im, float2 y, float2 x)
 // Backward pass at one sample: recomputes the slow part with its derivatives
 // and accumulates sum_c Y_c x'_c for x' in {x_P, x_C, dx/df0, dx/dfdot,
 // dx/dfddot, dx/dlam, dx/dbeta} (7 complex accumulators in acc[14]).
+//
+// Reverse mode through the TDI combination: x_c = sum_q M_cq(omL) G_q with
+// M in {0, +-fc2, +-fc2 fc} (gbgpu.py:370-375), so sum_c Y_c dx_c =
+// sum_q Z_q dG_q + dOmL sum_q Zd_q G_q with the link adjoints
+// Z_q = sum_c Y_c M_cq and Zd_q = sum_c Y_c dM_cq/domL.  Each parameter then
+// costs one complex multiply-add per link.
 __device__ __forceinline__ void slow_grad_mixed(const Bin &B, const GradExtra &Gx, int n, int N,
                                                 dfl step, const double *__restrict__ tab,
                                                 float ifs, float fstarf, const float2 Yc[3],
-                                                float acc[14])
+                                                const float2 Es[3], float acc[14])
 {
     const float *tabf = reinterpret_cast<const float *>(tab + (size_t)18 * N);
-    const dfl twopi = df_from(kTwoPi);
-    const float inv2pi = (float)kInvTwoPi;
     const float TWO_PI_F = (float)kTwoPi, PI_F = (float)kPi;
-    // arm geometry and its sky derivatives
-    float kd[3], pp[3], cc[3], dkd_l[3], dkd_b[3], dpp_l[3], dcc_l[3], dpp_b[3], dcc_b[3];
+    // arm geometry: k.r, u.r, v.r
+    float kd[3], ru[3], rv[3];
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         float r0 = __ldg(tabf + (size_t)(3 * a) * N + n);
         float r1 = __ldg(tabf + (size_t)(3 * a + 1) * N + n);
         float r2 = __ldg(tabf + (size_t)(3 * a + 2) * N + n);
-        float k_ = fmaf(B.kf[0], r0, fmaf(B.kf[1], r1, B.kf[2] * r2));
-        float ru = fmaf(Gx.u[0], r0, fmaf(Gx.u[1], r1, Gx.u[2] * r2));
-        float rv = fmaf(Gx.v[0], r0, Gx.v[1] * r1);
-        kd[a] = k_;
-        pp[a] = fmaf(rv, rv, -ru * ru);              // r.e+.r = (r.v)^2 - (r.u)^2
-        cc[a] = 2.0f * ru * rv;                      // r.ex.r = 2 (r.u)(r.v)
-        // d/dlam: du = -ct v, dv = ct u - st k, dk = st v
-        // d/dbeta: du = -k, dv = 0, dk = u
-        dkd_l[a] = Gx.st * rv;
-        dkd_b[a] = ru;
-        const float dru_l = -Gx.ct * rv, drv_l = fmaf(Gx.ct, ru, -Gx.st * k_);
-        dpp_l[a] = 2.0f * fmaf(rv, drv_l, -ru * dru_l);
-        dcc_l[a] = 2.0f * fmaf(dru_l, rv, ru * drv_l);
-        dpp_b[a] = 2.0f * ru * k_;                   // -2 ru (-k)
-        dcc_b[a] = -2.0f * k_ * rv;
+        kd[a] = fmaf(B.kf[0], r0, fmaf(B.kf[1], r1, B.kf[2] * r2));
+        ru[a] = fmaf(Gx.u[0], r0, fmaf(Gx.u[1], r1, Gx.u[2] * r2));
+        rv[a] = fmaf(Gx.v[0], r0, Gx.v[1] * r1);
     }
-    // spacecraft: carrier phase (float pairs), delays and their derivatives
+    // TDI factors and the link adjoints
     const dfl tm = df_mul_f(step, (float)n);
     const float tf = tm.h;
-    dfl Phi0 = df_add(df_mul(B.omdfad, tm), B.phi0d);
-    const dfl tm2 = df_mul(tm, tm);
-    Phi0 = df_neg(df_add(Phi0, df_mul(tm2, df_fast(B.pfd.h, fmaf(B.p3f, tf, B.pfd.l)))));
-    const dfl wt = df_add(B.omd, df_add(df_mul(B.tpfd, tm), dfl{B.pfddf * tf * tf, 0.0f}));
-    const float fdt = fmaf(B.fddotf, tf, B.fdotf);
+    const float omL = B.w0h + fmaf(fmaf(B.w2, tf, B.w1), tf, B.w0l);
+    float so, co;
+    sincosf(omL, &so, &co);
+    const float2 fc = make_float2(co, -so);
+    const float g4 = 4.0f * omL * so;
+    const float2 fa = make_float2(g4 * co, -g4 * so);              // fc2
+    const float2 fb = cmul(fa, fc);                                 // fc2 fc
+    // d fc2 / d omL = 4 fc (sin + omL cos - i omL sin), d fc / d omL = -i fc
+    const float2 da = cmul(make_float2(4.0f * fmaf(omL, co, so), -4.0f * omL * so), fc);
+    const float2 db = cadd(cmul(da, fc), cmul(fa, make_float2(fc.y, -fc.x)));
+    const float2 YA0 = cmul(Yc[0], fa), YA1 = cmul(Yc[1], fa), YA2 = cmul(Yc[2], fa);
+    const float2 YB0 = cmul(Yc[0], fb), YB1 = cmul(Yc[1], fb), YB2 = cmul(Yc[2], fb);
+    const float2 YdA0 = cmul(Yc[0], da), YdA1 = cmul(Yc[1], da), YdA2 = cmul(Yc[2], da);
+    const float2 YdB0 = cmul(Yc[0], db), YdB1 = cmul(Yc[1], db), YdB2 = cmul(Yc[2], db);
+    // spacecraft: exp(-i phase) from the forward pass, FP32 delays and derivatives
     float Er[3], Ei[3], fo[3], xi[3], dph_l[3], dph_b[3], dfo_l[3], dfo_b[3];
 #pragma unroll
     for (int s = 0; s < 3; s++) {
-        dfl P[3];
-#pragma unroll
-        for (int c = 0; c < 3; c++)
-            P[c] = {__ldg(tabf + (size_t)(9 + 3 * s + c) * N + n),
-                    __ldg(tabf + (size_t)(18 + 3 * s + c) * N + n)};
-        float p0 = B.kd[0].h * P[0].h, p1 = B.kd[1].h * P[1].h, p2 = B.kd[2].h * P[2].h;
-        float e = fmaf(B.kd[0].h, P[0].h, -p0);
-        e += fmaf(B.kd[1].h, P[1].h, -p1);
-        e += fmaf(B.kd[2].h, P[2].h, -p2);
-#pragma unroll
-        for (int c = 0; c < 3; c++) e = fmaf(B.kd[c].h, P[c].l, fmaf(B.kd[c].l, P[c].h, e));
-        dfl s01 = df_two_sum(p0, p1);
-        dfl s012 = df_two_sum(s01.h, p2);
-        const dfl kP = df_fast(s012.h, (s01.l + s012.l) + e);
-        const float kPf = kP.h;
-        const float small = kPf * kPf * fmaf(kPf, (1.0f / 3.0f) * B.pfddf, -PI_F * fdt);
-        dfl ph = df_add(Phi0, df_mul(kP, wt));
-        ph.l += small;
-        const float q = rintf(ph.h * inv2pi);
-        ph = df_add(ph, df_neg(df_mul_f(twopi, q)));
-        float sn, cs;
-        sincosf(ph.h, &sn, &cs);
-        Er[s] = fmaf(sn, -ph.l, cs);
-        Ei[s] = -fmaf(cs, ph.l, sn);
+        float P0 = __ldg(tabf + (size_t)(9 + 3 * s) * N + n);
+        float P1 = __ldg(tabf + (size_t)(9 + 3 * s + 1) * N + n);
+        float P2 = __ldg(tabf + (size_t)(9 + 3 * s + 2) * N + n);
+        Er[s] = Es[s].x;
+        Ei[s] = Es[s].y;
+        const float kPf = fmaf(B.kf[0], P0, fmaf(B.kf[1], P1, B.kf[2] * P2));
         const float x = tf - kPf;
         xi[s] = x;
         const float f_ = B.w0h + fmaf(fmaf(B.w2, x, B.w1), x, B.w0l);
         fo[s] = f_;
-        // d kP / d lam = st v.P/c, d kP / d beta = u.P/c
-        const float Pv = fmaf(Gx.v[0], P[0].h, Gx.v[1] * P[1].h);
-        const float Pu = fmaf(Gx.u[0], P[0].h, fmaf(Gx.u[1], P[1].h, Gx.u[2] * P[2].h));
+        // d kP / d lam = st v.P/c, d kP / d beta = u.P/c;
+        // d phase / d kP = 2 pi f(xi); d fonfs / d kP = -(fdot + fddot xi)/fstar
+        const float Pv = fmaf(Gx.v[0], P0, Gx.v[1] * P1);
+        const float Pu = fmaf(Gx.u[0], P0, fmaf(Gx.u[1], P1, Gx.u[2] * P2));
         const float dkP_l = Gx.st * Pv, dkP_b = Pu;
-        // d phase / d kP = 2 pi f(xi);  d fonfs / d kP = -(fdot + fddot xi)/fstar
         const float tpf = TWO_PI_F * f_ * fstarf;
         dph_l[s] = tpf * dkP_l;
         dph_b[s] = tpf * dkP_b;
@@ -189,103 +173,77 @@ __device__ __forceinline__ void slow_grad_mixed(const Bin &B, const GradExtra &G
         dfo_l[s] = gfk * dkP_l;
         dfo_b[s] = gfk * dkP_b;
     }
-    // links: value g E_s (without A), amplitude log-derivative
+    const float dom0 = ifs, dom1 = tf * ifs, dom2 = 0.5f * tf * tf * ifs;
+    // links 12, 23, 31, 21, 32, 13: arm, spacecraft, sign of k.r
     const int arm[6] = {0, 1, 2, 0, 1, 2};
     const int sc[6] = {0, 1, 2, 1, 2, 0};
     const float sg[6] = {1.f, 1.f, 1.f, -1.f, -1.f, -1.f};
-    float2 gE[6], G[6];
-    float h1[6], dl[6];
 #pragma unroll
     for (int q = 0; q < 6; q++) {
         const int s = sc[q], a = arm[q];
+        // link adjoints (X = fa (G21 - G31) + fb (G12 - G13) and cyclic)
+        float2 Z, Zd;
+        switch (q) {
+        case 0: Z = csub(YB0, YA1); Zd = csub(YdB0, YdA1); break;   // G12
+        case 1: Z = csub(YB1, YA2); Zd = csub(YdB1, YdA2); break;   // G23
+        case 2: Z = csub(YB2, YA0); Zd = csub(YdB2, YdA0); break;   // G31
+        case 3: Z = csub(YA0, YB1); Zd = csub(YdA0, YdB1); break;   // G21
+        case 4: Z = csub(YA1, YB2); Zd = csub(YdA1, YdB2); break;   // G32
+        default: Z = csub(YA2, YB0); Zd = csub(YdA2, YdB0); break;  // G13
+        }
         const float hh = 0.5f * fmaf(sg[q], kd[a], 1.0f);
         const float av = fo[s] * hh;
         float S, C, dS;
         sinc_cos_d_f(av, S, C, dS);
-        const float aS = av * S;
         const float t = 0.25f * S;
-        // g = 1/4 S (C - i aS); gE = g exp(-i phase_s)
-        const float2 g = make_float2(t * C, -t * aS);
-        gE[q] = cmul(g, make_float2(Er[s], Ei[s]));
-        const float2 A = make_float2(fmaf(pp[a], B.DPf.x, cc[a] * B.DCf.x),
-                                     fmaf(pp[a], B.DPf.y, cc[a] * B.DCf.y));
-        G[q] = cmul(gE[q], A);
-        h1[q] = hh;
-        dl[q] = dS / S;
-    }
-    // TDI factors (gbgpu.py:352-362) and their frequency derivatives
-    const float omL = B.w0h + fmaf(fmaf(B.w2, tf, B.w1), tf, B.w0l);
-    float so, co;
-    sincosf(omL, &so, &co);
-    const float2 fc = make_float2(co, -so);
-    const float g4 = 4.0f * omL * so;
-    const float2 fc2 = make_float2(g4 * co, -g4 * so);
-    // d fc2 / d omL = 4 fc (sin + omL cos - i omL sin), d fc / d omL = -i fc
-    const float2 dfc2 = cmul(make_float2(4.0f * fmaf(omL, co, so), -4.0f * omL * so), fc);
-    const float2 dfc = make_float2(fc.y, -fc.x);
-    float2 Xv[3];
-    tdi_xyz(G, fc, Xv);
-    // plus / cross parts (for iota, psi)
-    {
-        float2 GP[6], X3[3];
-#pragma unroll
-        for (int q = 0; q < 6; q++) GP[q] = cscale(gE[q], pp[arm[q]]);
-        tdi_xyz(GP, fc, X3);
-#pragma unroll
-        for (int c = 0; c < 3; c++) cmac(acc[0], acc[1], Yc[c], cmul(fc2, X3[c]));
-#pragma unroll
-        for (int q = 0; q < 6; q++) GP[q] = cscale(gE[q], cc[arm[q]]);
-        tdi_xyz(GP, fc, X3);
-#pragma unroll
-        for (int c = 0; c < 3; c++) cmac(acc[2], acc[3], Yc[c], cmul(fc2, X3[c]));
-    }
-    // frequency parameters: d a = h1 dfo, d phase = -2 pi xi, -pi xi^2, -pi/3 xi^3;
-    // d fonfs = 1/fstar, xi/fstar, xi^2/(2 fstar); d omL = 1/fstar, t/fstar, t^2/(2 fstar)
-#pragma unroll
-    for (int j = 0; j < 3; j++) {
-        float2 dG[6], X3[3];
-#pragma unroll
-        for (int q = 0; q < 6; q++) {
-            const int s = sc[q];
+        const float2 gE = cmul(make_float2(t * C, -t * av * S), make_float2(Er[s], Ei[s]));
+        const float pp = fmaf(rv[a], rv[a], -ru[a] * ru[a]);      // r.e+.r
+        const float cc = 2.0f * ru[a] * rv[a];                       // r.ex.r
+        const float2 A = make_float2(fmaf(pp, B.DPf.x, cc * B.DCf.x), fmaf(pp, B.DPf.y, cc * B.DCf.y));
+        const float2 G = cmul(gE, A);
+        const float2 ZgE = cmul(Z, gE);
+        const float2 ZG = cmul(Z, G);
+        const float2 ZdG = cmul(Zd, G);
+        const float dl = dS / S;
+        // plus / cross parts
+        acc[0] = fmaf(pp, ZgE.x, acc[0]);
+        acc[1] = fmaf(pp, ZgE.y, acc[1]);
+        acc[2] = fmaf(cc, ZgE.x, acc[2]);
+        acc[3] = fmaf(cc, ZgE.y, acc[3]);
+        // (dl da - i (da + dph)) ZG + dOmL ZdG for the frequency parameters
+        {
             const float x = xi[s];
-            const float dfo = j == 0 ? ifs : (j == 1 ? x * ifs : 0.5f * x * x * ifs);
-            const float dph = j == 0 ? -TWO_PI_F * x : (j == 1 ? -PI_F * x * x : -(PI_F / 3.0f) * x * x * x);
-            const float da = h1[q] * dfo;
-            // (dl da - i (da + dph)) G
-            dG[q] = cmul(make_float2(dl[q] * da, -(da + dph)), G[q]);
+            const float d0 = hh * ifs, d1 = hh * x * ifs, d2 = 0.5f * hh * x * x * ifs;
+            const float p0 = -TWO_PI_F * x, p1 = -PI_F * x * x, p2 = -(PI_F / 3.0f) * x * x * x;
+            float al, be;
+            al = dl * d0; be = d0 + p0;
+            acc[4] = fmaf(al, ZG.x, fmaf(be, ZG.y, fmaf(dom0, ZdG.x, acc[4])));
+            acc[5] = fmaf(al, ZG.y, fmaf(-be, ZG.x, fmaf(dom0, ZdG.y, acc[5])));
+            al = dl * d1; be = d1 + p1;
+            acc[6] = fmaf(al, ZG.x, fmaf(be, ZG.y, fmaf(dom1, ZdG.x, acc[6])));
+            acc[7] = fmaf(al, ZG.y, fmaf(-be, ZG.x, fmaf(dom1, ZdG.y, acc[7])));
+            al = dl * d2; be = d2 + p2;
+            acc[8] = fmaf(al, ZG.x, fmaf(be, ZG.y, fmaf(dom2, ZdG.x, acc[8])));
+            acc[9] = fmaf(al, ZG.y, fmaf(-be, ZG.x, fmaf(dom2, ZdG.y, acc[9])));
         }
-        tdi_xyz(dG, fc, X3);
-        const float dom = j == 0 ? ifs : (j == 1 ? tf * ifs : 0.5f * tf * tf * ifs);
-        const float2 d12 = csub(G[0], G[5]), d23 = csub(G[1], G[3]), d31 = csub(G[2], G[4]);
-        const float2 dfcj = cscale(dfc, dom), dfc2j = cscale(dfc2, dom);
-        float2 dx;
-        dx = cadd(cmul(dfc2j, Xv[0]), cmul(fc2, cadd(X3[0], cmul(d12, dfcj))));
-        cmac(acc[4 + 2 * j], acc[5 + 2 * j], Yc[0], dx);
-        dx = cadd(cmul(dfc2j, Xv[1]), cmul(fc2, cadd(X3[1], cmul(d23, dfcj))));
-        cmac(acc[4 + 2 * j], acc[5 + 2 * j], Yc[1], dx);
-        dx = cadd(cmul(dfc2j, Xv[2]), cmul(fc2, cadd(X3[2], cmul(d31, dfcj))));
-        cmac(acc[4 + 2 * j], acc[5 + 2 * j], Yc[2], dx);
-    }
-    // sky angles
-#pragma unroll
-    for (int j = 0; j < 2; j++) {
-        float2 dG[6], X3[3];
-#pragma unroll
-        for (int q = 0; q < 6; q++) {
-            const int s = sc[q], a = arm[q];
-            const float dfo = j == 0 ? dfo_l[s] : dfo_b[s];
-            const float dph = j == 0 ? dph_l[s] : dph_b[s];
-            const float dkd = j == 0 ? dkd_l[a] : dkd_b[a];
-            const float da = fmaf(h1[q], dfo, 0.5f * fo[s] * sg[q] * dkd);
-            const float dpp = j == 0 ? dpp_l[a] : dpp_b[a];
-            const float dcc = j == 0 ? dcc_l[a] : dcc_b[a];
-            const float2 dA = make_float2(fmaf(dpp, B.DPf.x, dcc * B.DCf.x),
-                                          fmaf(dpp, B.DPf.y, dcc * B.DCf.y));
-            dG[q] = cadd(cmul(make_float2(dl[q] * da, -(da + dph)), G[q]), cmul(gE[q], dA));
+        // sky angles: d/dlam (du = -ct v, dv = ct u - st k, dk = st v),
+        //             d/dbeta (du = -k, dv = 0, dk = u)
+        {
+            const float2 ZgDP = cmul(ZgE, B.DPf), ZgDC = cmul(ZgE, B.DCf);
+            const float dru_l = -Gx.ct * rv[a], drv_l = fmaf(Gx.ct, ru[a], -Gx.st * kd[a]);
+            const float dpp_l = 2.0f * fmaf(rv[a], drv_l, -ru[a] * dru_l);
+            const float dcc_l = 2.0f * fmaf(dru_l, rv[a], ru[a] * drv_l);
+            const float dpp_b = 2.0f * ru[a] * kd[a];
+            const float dcc_b = -2.0f * kd[a] * rv[a];
+            const float dd_l = fmaf(hh, dfo_l[s], 0.5f * fo[s] * sg[q] * Gx.st * rv[a]);
+            const float dd_b = fmaf(hh, dfo_b[s], 0.5f * fo[s] * sg[q] * ru[a]);
+            float al = dl * dd_l, be = dd_l + dph_l[s];
+            acc[10] = fmaf(al, ZG.x, fmaf(be, ZG.y, fmaf(dpp_l, ZgDP.x, fmaf(dcc_l, ZgDC.x, acc[10]))));
+            acc[11] = fmaf(al, ZG.y, fmaf(-be, ZG.x, fmaf(dpp_l, ZgDP.y, fmaf(dcc_l, ZgDC.y, acc[11]))));
+            al = dl * dd_b; be = dd_b + dph_b[s];
+            acc[12] = fmaf(al, ZG.x, fmaf(be, ZG.y, fmaf(dpp_b, ZgDP.x, fmaf(dcc_b, ZgDC.x, acc[12]))));
+            acc[13] = fmaf(al, ZG.y, fmaf(-be, ZG.x, fmaf(dpp_b, ZgDP.y, fmaf(dcc_b, ZgDC.y, acc[13]))));
         }
-        tdi_xyz(dG, fc, X3);
-#pragma unroll
-        for (int c = 0; c < 3; c++) cmac(acc[10 + 2 * j], acc[11 + 2 * j], Yc[c], cmul(fc2, X3[c]));
     }
 }
 
@@ -371,7 +329,7 @@ struct GradParams {
 
 constexpr int kGradAcc = 19;       // ll terms 3, Qf 2, 7 complex accumulators 14
 
-__global__ void __launch_bounds__(kBlock, 1) grad_kernel(const GradParams GP)
+__global__ void __launch_bounds__(kBlock, 2) grad_kernel(const GradParams GP)
 {
     using V = float2;
     const KParams &K = GP.K;
@@ -381,6 +339,7 @@ __global__ void __launch_bounds__(kBlock, 1) grad_kernel(const GradParams GP)
     double *red = reinterpret_cast<double *>(smem + (sizeof(Bin) + sizeof(GradExtra)) * kMaxPack);
     V *buf = reinterpret_cast<V *>(smem + (sizeof(Bin) + sizeof(GradExtra)) * kMaxPack +
                                    sizeof(double) * kGradAcc * 16);
+    V *es = buf + 3 * (size_t)K.maxS;             // exp(-i phase_s) per sample, from the forward pass
     __shared__ int s_tile;
 
     const gbx_wave_args &a = K.a;
@@ -433,7 +392,8 @@ __global__ void __launch_bounds__(kBlock, 1) grad_kernel(const GradParams GP)
         for (int m = tid; m < S; m += kBlock) {
             const int p = m >> lg, n = m & (N - 1);
             float2 o[3];
-            slow_mixed<false>(bins[p], n, N, stepd, tab, nullptr, nullptr, o);
+            slow_mixed<false, true>(bins[p], n, N, stepd, tab, nullptr, nullptr, o,
+                                    es + 3 * (size_t)m);
 #pragma unroll
             for (int c = 0; c < 3; c++) buf[(p * 3 + c) * N + n] = o[c];
         }
@@ -505,10 +465,13 @@ __global__ void __launch_bounds__(kBlock, 1) grad_kernel(const GradParams GP)
             const GradExtra &Gx = gxs[p];
             if (B.valid) {
                 for (int n = i0; n < N; n += Tpb) {
-                    float2 Yc[3];
+                    float2 Yc[3], Es[3];
 #pragma unroll
-                    for (int c = 0; c < 3; c++) Yc[c] = buf[(p * 3 + c) * N + n];
-                    slow_grad_mixed(B, Gx, n, N, stepd, tab, ifs, fstarf, Yc, acc + 5);
+                    for (int c = 0; c < 3; c++) {
+                        Yc[c] = buf[(p * 3 + c) * N + n];
+                        Es[c] = es[3 * ((size_t)(p << lg) + n) + c];
+                    }
+                    slow_grad_mixed(B, Gx, n, N, stepd, tab, ifs, fstarf, Yc, Es, acc + 5);
                 }
             }
         }

@@ -467,10 +467,11 @@ __device__ __forceinline__ void slow_fp64(const Bin &B, int n, int N, double tm,
 // k.P/c and the delayed times are evaluated in float-pair arithmetic (about
 // 48 bits, so ~1e-12 rad at 100 rad) and reduced modulo 2 pi; everything else
 // is FP32.
-template <bool THIRD>
+template <bool THIRD, bool STORE_E = false>
 __device__ __forceinline__ void slow_mixed(const Bin &B, int n, int N, dfl step,
                                            const double *__restrict__ tab,
-                                           const double *psi, const float *vl, float2 out[3])
+                                           const double *psi, const float *vl, float2 out[3],
+                                           float2 *Eout = nullptr)
 {
     const float *tabf = reinterpret_cast<const float *>(tab + (size_t)18 * N);
     const dfl twopi = df_from(kTwoPi);
@@ -548,6 +549,7 @@ __device__ __forceinline__ void slow_mixed(const Bin &B, int n, int N, dfl step,
         sincosf(phh[s], &sn, &cs);
         Er[s] = fmaf(sn, -phl[s], cs);
         Ei[s] = -fmaf(cs, phl[s], sn);
+        if (STORE_E) Eout[s] = make_float2(Er[s], Ei[s]);
     }
     // links: G = 1/4 sinc(a) exp(-i a) exp(-i phase_s) A_arm  (gbgpu.py:509-525)
     float2 G[6];
@@ -1318,7 +1320,7 @@ extern "C" int gbx_waveform_ll_grad(const gbx_wave_args *a, const gbx_ll_args *l
     K.maxS = maxS;
     G.grad = grad;
     const size_t sm = (sizeof(Bin) + sizeof(GradExtra)) * kMaxPack + sizeof(double) * kGradAcc * 16 +
-                      3 * (size_t)maxS * sizeof(float2);
+                      6 * (size_t)maxS * sizeof(float2);
     if (sm > 227 * 1024) return set_error(GBX_ERR_UNSUPPORTED, "tile needs %zu B of shared memory", sm);
     cudaError_t e = cudaFuncSetAttribute(grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(grad)");
