@@ -25,6 +25,7 @@ EXPORTS = (
     "gbx_orbit_table_bytes", "gbx_orbit_table",
     "gbx_waveform", "gbx_waveform_ll", "gbx_waveform_fill", "gbx_wave_workspace_bytes",
     "gbx_waveform_ll_noalloc", "gbx_waveform_ll_grad", "gbx_grad_workspace_bytes",
+    "gbx_swap_ll",
 )
 
 _vp = ctypes.c_void_p
@@ -86,6 +87,7 @@ def lib():
                                        _vp, _vp, _vp, _vp]
     L.gbx_grad_workspace_bytes.argtypes = [_i]
     L.gbx_grad_workspace_bytes.restype = ctypes.c_size_t
+    L.gbx_swap_ll.argtypes = [ctypes.POINTER(WaveArgs), ctypes.POINTER(LLArgs), _vp, _vp]
     L.gbx_waveform_fill.argtypes = [ctypes.POINTER(WaveArgs), _vp, _vp, _vp, _i, _i, _ll, _vp]
     for name in EXPORTS:
         if name not in ("gbx_last_error", "gbx_orbit_table_bytes", "gbx_wave_workspace_bytes",

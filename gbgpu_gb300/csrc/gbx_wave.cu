@@ -73,6 +73,7 @@ struct KParams {
     const int *data_index, *noise_index;
     double df;
     double2 *d_h, *h_h;
+    double *dlogl;                 // swap: one log-likelihood change per (old, new) pair
     // waveform outputs
     double2 *XYZ, *AET;
     int *start_out;
@@ -87,7 +88,14 @@ struct KParams {
     int maxS;                      // largest tile (samples) the shared memory is sized for
 };
 
-enum { MODE_WAVE = 0, MODE_LL = 1, MODE_FILL = 2 };
+enum { MODE_WAVE = 0, MODE_LL = 1, MODE_FILL = 2, MODE_SWAP = 4 };
+
+// doubles of the per-tile reduction scratch: 3 per 32-sample chunk, and at
+// least 8 per lane group (16 groups) for the swap epilogue
+__host__ __device__ __forceinline__ int red_doubles(int maxS)
+{
+    return 3 * (maxS >> 5) > 128 ? 3 * (maxS >> 5) : 128;
+}
 
 __device__ __forceinline__ double quad_form(const double *e, double x, double y, double z)
 {
@@ -367,7 +375,7 @@ __device__ void setup_bin(Bin &B, const KParams &K, int b, int N, int mode)
     }
     B.di = B.ni = B.gi = 0;
     B.eS = B.eD = 0;
-    if (mode == MODE_LL) {
+    if (mode == MODE_LL || mode == MODE_SWAP) {
         int di = K.data_index ? K.data_index[b] : 0;
         int ni = K.noise_index ? K.noise_index[b] : 0;
         if (di < 0 || di >= K.num_data || ni < 0 || ni >= K.num_psd) {
@@ -690,8 +698,8 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
     using V = typename C2<R>::T;
     extern __shared__ __align__(16) unsigned char smem[];
     Bin *bins = reinterpret_cast<Bin *>(smem);
-    double *red = reinterpret_cast<double *>(smem + sizeof(Bin) * kMaxPack);  // [maxS/32][3]
-    V *buf = reinterpret_cast<V *>(smem + sizeof(Bin) * kMaxPack + sizeof(double) * 3 * (K.maxS >> 5));
+    double *red = reinterpret_cast<double *>(smem + sizeof(Bin) * kMaxPack);
+    V *buf = reinterpret_cast<V *>(smem + sizeof(Bin) * kMaxPack + sizeof(double) * red_doubles(K.maxS));
     __shared__ int s_tile;
 
     const gbx_wave_args &a = K.a;
@@ -723,7 +731,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
         const int N = 1 << lg;
         const double *tab = (lg >= 5 && lg <= GBX_MAX_LOG2N)
                                 ? reinterpret_cast<const double *>(a.orbit[lg]) : nullptr;
-        const int maxcnt = max(1, kTileMin >> lg);
+        const int maxcnt = max(MODE == MODE_SWAP ? 2 : 1, kTileMin >> lg);
         if (tab == nullptr || cnt < 1 || cnt > maxcnt || first < 0 || first + cnt > a.num_bin ||
             (cnt << lg) > K.maxS || (sizeof(R) == 8 && lg > 12)) {
             flag(a.status, GBX_FLAG_TILE);
@@ -881,6 +889,120 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                                                     (Xd.y + Yd.y + Zd.y) / r3);
                 }
                 if (i == 0 && K.start_out) K.start_out[B.b] = B.start;
+            }
+        } else if (MODE == MODE_SWAP) {
+            // binaries 2j (current source) and 2j+1 (proposal) of the tile form a
+            // pair; threads [j*Tp2, (j+1)*Tp2) walk both windows.  With r the
+            // residual row and Dh = h_new - h_old:
+            //   dlogL = Re<r|Dh> - 1/2 <Dh|Dh>
+            //         = Re<r|h_new> - Re<r|h_old> - (<h_new|h_new> + <h_old|h_old>)/2
+            //           + Re<h_old|h_new>   (cross term on the windows' overlap)
+            const int Tp2 = 2 * (kBlock / maxcnt);
+            const int width = Tp2 < 32 ? Tp2 : 32;
+            const int pr = tid / Tp2;
+            const int i0 = tid - pr * Tp2;
+            typedef typename std::conditional<sizeof(R) == 8, double, float>::type Acc;
+            Acc acc8[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // Crn (2), Cro (2), Hn, Ho, Cx (2)
+            if (2 * pr + 1 < cnt) {
+                const Bin &Bo = bins[2 * pr], &Bn = bins[2 * pr + 1];
+                const int po = 2 * pr, pn = 2 * pr + 1;
+                if (Bo.valid && Bn.valid) {
+                    bool out = false;
+                    for (int e = i0; e < 2 * N; e += Tp2) {
+                        const bool isnew = e < N;
+                        const int i = isnew ? e : e - N;
+                        const Bin &Bw = isnew ? Bn : Bo;
+                        const int pw = isnew ? pn : po;
+                        const int j = Bw.start + i;
+                        if (j < 0 || j >= K.L) {
+                            out = true;
+                            continue;
+                        }
+                        const int pos = bitrev((i + (N >> 1)) & (N - 1), lg);
+                        V X = buf[(pw * 3 + 0) * N + pos], Y = buf[(pw * 3 + 1) * N + pos],
+                          Z = buf[(pw * 3 + 2) * N + pos];
+                        const size_t jd = (size_t)Bn.di * K.L + j, jn = (size_t)Bn.ni * K.L + j;
+                        const double2 dA = __ldg(K.A_data + jd), dE = __ldg(K.E_data + jd);
+                        const double SA = __ldg(K.A_psd + jn), SE = __ldg(K.E_psd + jn);
+                        Acc wA, wE, aR, aI, eR, eI;
+                        if constexpr (sizeof(R) == 8) {
+                            wA = 1.0 / SA; wE = 1.0 / SE;
+                            aR = dA.x; aI = dA.y; eR = dE.x; eI = dE.y;
+                        } else {
+                            wA = __frcp_rn(d2f_scaled(SA, Bn.eS));
+                            wE = __frcp_rn(d2f_scaled(SE, Bn.eS));
+                            aR = d2f_scaled(dA.x, Bn.eD); aI = d2f_scaled(dA.y, Bn.eD);
+                            eR = d2f_scaled(dE.x, Bn.eD); eI = d2f_scaled(dE.y, Bn.eD);
+                        }
+                        const Acc hAr = (Z.x - X.x) * (Acc)is2, hAi = (Z.y - X.y) * (Acc)is2;
+                        const Acc hEr = (X.x - 2 * Y.x + Z.x) * (Acc)is6, hEi = (X.y - 2 * Y.y + Z.y) * (Acc)is6;
+                        // conj(r) h / S
+                        const Acc cr = (aR * hAr + aI * hAi) * wA + (eR * hEr + eI * hEi) * wE;
+                        const Acc ci = (aR * hAi - aI * hAr) * wA + (eR * hEi - eI * hEr) * wE;
+                        const Acc hh2 = (hAr * hAr + hAi * hAi) * wA + (hEr * hEr + hEi * hEi) * wE;
+                        if (isnew) {
+                            acc8[0] += cr; acc8[1] += ci; acc8[4] += hh2;
+                            const int k = j - Bo.start;
+                            if (k >= 0 && k < N) {
+                                const int pk = bitrev((k + (N >> 1)) & (N - 1), lg);
+                                V Xo = buf[(po * 3 + 0) * N + pk], Yo = buf[(po * 3 + 1) * N + pk],
+                                  Zo = buf[(po * 3 + 2) * N + pk];
+                                const Acc oAr = (Zo.x - Xo.x) * (Acc)is2, oAi = (Zo.y - Xo.y) * (Acc)is2;
+                                const Acc oEr = (Xo.x - 2 * Yo.x + Zo.x) * (Acc)is6,
+                                          oEi = (Xo.y - 2 * Yo.y + Zo.y) * (Acc)is6;
+                                // conj(h_old) h_new / S
+                                acc8[6] += (oAr * hAr + oAi * hAi) * wA + (oEr * hEr + oEi * hEi) * wE;
+                                acc8[7] += (oAr * hAi - oAi * hAr) * wA + (oEr * hEi - oEi * hEr) * wE;
+                            }
+                        } else {
+                            acc8[2] += cr; acc8[3] += ci; acc8[5] += hh2;
+                        }
+                    }
+                    if (out) flag(a.status, GBX_FLAG_WINDOW);
+                }
+            }
+            double gs[8];
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                if constexpr (sizeof(R) == 8) {
+                    double x = acc8[k];
+                    for (int o = width >> 1; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+                    gs[k] = x;
+                } else {
+                    dfl x = {acc8[k], 0.f};
+                    for (int o = width >> 1; o > 0; o >>= 1) {
+                        dfl y = {__shfl_xor_sync(0xffffffffu, x.h, o), __shfl_xor_sync(0xffffffffu, x.l, o)};
+                        x = df_add(x, y);
+                    }
+                    gs[k] = (double)x.h + (double)x.l;
+                }
+            }
+            if ((tid & (width - 1)) == 0) {
+                const int g = tid / width;
+#pragma unroll
+                for (int k = 0; k < 8; k++) red[8 * g + k] = gs[k];
+            }
+            __syncthreads();
+            if (2 * tid + 1 < cnt) {
+                const Bin &Bo = bins[2 * tid], &Bn = bins[2 * tid + 1];
+                const int per = Tp2 / width;
+                double t[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                for (int g = tid * per; g < (tid + 1) * per; g++)
+#pragma unroll
+                    for (int k = 0; k < 8; k++) t[k] += red[8 * g + k];
+                double cdh = 4.0 * K.df, chh = 4.0 * K.df;
+                if constexpr (sizeof(R) == 4) {
+                    cdh *= exp2_int(Bn.eS - Bn.eD);
+                    chh *= exp2_int(Bn.eS);
+                }
+                const double2 so = Bo.scale, sn = Bn.scale;
+                const double rn = cmul(sn, make_double2(t[0], t[1])).x * cdh;
+                const double ro = cmul(so, make_double2(t[2], t[3])).x * cdh;
+                const double hn = (sn.x * sn.x + sn.y * sn.y) * t[4] * chh;
+                const double ho = (so.x * so.x + so.y * so.y) * t[5] * chh;
+                const double cx = cmul(make_double2(so.x, -so.y), cmul(sn, make_double2(t[6], t[7]))).x * chh;
+                const bool ok = Bo.valid && Bn.valid && Bo.b >= 0 && Bn.b >= 0;
+                if (Bn.b >= 0) K.dlogl[Bn.b >> 1] = ok ? (rn - ro - 0.5 * (hn + ho) + cx) : 0.0;
             }
         } else if (MODE == MODE_FILL) {
             for (int m = tid; m < S; m += kBlock) {
@@ -1073,7 +1195,7 @@ __global__ void __launch_bounds__(kPrepBlock) prep_kernel(const KParams K)
 // ----------------------------------------------------------------------------
 static size_t smem_bytes(int prec, bool third, int maxS)
 {
-    size_t head = sizeof(Bin) * kMaxPack + sizeof(double) * 3 * (size_t)(maxS >> 5);
+    size_t head = sizeof(Bin) * kMaxPack + sizeof(double) * (size_t)red_doubles(maxS);
     size_t rc = prec == GBX_FP64 ? sizeof(double2) : sizeof(float2);
     size_t r = prec == GBX_FP64 ? sizeof(double) : sizeof(float);
     size_t s = head + 3 * (size_t)maxS * rc;
@@ -1267,6 +1389,37 @@ extern "C" int gbx_waveform_fill(const gbx_wave_args *a, void *A_glob, void *E_g
     K.gstride = group_stride;
     K.L = data_length;
     return dispatch<MODE_FILL>(K, maxS, (cudaStream_t)stream);
+}
+
+extern "C" int gbx_swap_ll(const gbx_wave_args *a, const gbx_ll_args *l, double *dlogl,
+                           void *stream)
+{
+    int maxS = 0;
+    int rc = check_wave(a, &maxS);
+    if (rc) return rc;
+    if (a->tiles || a->order) return set_error(GBX_ERR_ARG, "gbx_swap_ll takes a uniform N and no order");
+    if (a->num_bin % 2) return set_error(GBX_ERR_ARG, "num_bin must be even: (old, new) pairs");
+    if (!l || !l->A_data || !l->E_data || !l->A_psd || !l->E_psd || !dlogl)
+        return set_error(GBX_ERR_ARG, "NULL likelihood pointer");
+    if (l->data_length <= 0 || l->num_data < 1 || l->num_psd < 1)
+        return set_error(GBX_ERR_ARG, "data_length / num_data / num_psd must be positive");
+    rc = ensure_init((cudaStream_t)stream);
+    if (rc) return rc;
+    KParams K = base_params(a);
+    K.P = kTileMin / a->N < 2 ? 2 : kTileMin / a->N;
+    maxS = K.P * a->N;
+    K.A_data = (const double2 *)l->A_data;
+    K.E_data = (const double2 *)l->E_data;
+    K.A_psd = l->A_psd;
+    K.E_psd = l->E_psd;
+    K.L = l->data_length;
+    K.num_data = l->num_data;
+    K.num_psd = l->num_psd;
+    K.data_index = l->data_index;
+    K.noise_index = l->noise_index;
+    K.df = l->df;
+    K.dlogl = dlogl;
+    return dispatch<MODE_SWAP>(K, maxS, (cudaStream_t)stream);
 }
 
 extern "C" size_t gbx_grad_workspace_bytes(int num_bin)

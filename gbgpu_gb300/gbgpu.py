@@ -583,6 +583,69 @@ class GBGPUBase(abc.ABC):
         like = -0.5 * (d_d + h_h.real - 2 * d_h.real)
         return like, grad
 
+    def swap_likelihood(self, params_old, params_new, data, psd, start_freq_ind=0,
+                        data_index=None, noise_index=None, return_tensor=False, **kwargs):
+        """Change of log-likelihood when source ``params_old[:, j]`` is replaced by
+        ``params_new[:, j]`` (no counterpart in this version of the reference).
+
+        ``data`` holds residuals r = d - (current sum of sources), one row per
+        walker selected by ``data_index``; with Dh = h_new - h_old,
+        ``dlogL_j = Re<r|Dh> - <Dh|Dh>/2`` over the union of both windows, in
+        the inner product of the reference's likelihood.  Keywords as in
+        ``get_ll`` (N must be a single power of two; ``precision``).
+        """
+        precision = kwargs.pop("precision", self.precision)
+        N = kwargs.pop("N", None)
+        T = kwargs.pop("T", 4 * YRSID_SI)
+        dt = kwargs.pop("dt", 10.0)
+        oversample = kwargs.pop("oversample", 1)
+        tdi2 = kwargs.pop("tdi2", False)
+        if kwargs:
+            raise TypeError(f"unexpected keyword arguments {list(kwargs)}")
+        T = int(T / dt) * dt
+        self._check_T(T)
+        po = _to_device(params_old, torch.float64, self.device)
+        pn = _to_device(params_new, torch.float64, self.device)
+        if po.shape != pn.shape or po.ndim != 2 or po.shape[0] != self.NPARAMS:
+            raise ValueError(f"params_old / params_new must both be ({self.NPARAMS}, B)")
+        B = po.shape[1]
+        if N is None:
+            N = max(self._resolve_N(None, po[0], po[1], T, [po[i] for i in range(9, self.NPARAMS)],
+                                    oversample),
+                    self._resolve_N(None, pn[0], pn[1], T, [pn[i] for i in range(9, self.NPARAMS)],
+                                    oversample))
+        if np.ndim(N) != 0:
+            raise NotImplementedError("swap_likelihood takes one N per call")
+        N = int(N)
+        prm = torch.stack([po, pn], dim=2).reshape(self.NPARAMS, 2 * B).contiguous()
+        di = None if data_index is None else _to_device(data_index, torch.int32, self.device)
+        ni = None if noise_index is None else _to_device(noise_index, torch.int32, self.device)
+        di2 = None if di is None else di.repeat_interleave(2).contiguous()
+        ni2 = None if ni is None else ni.repeat_interleave(2).contiguous()
+        dd, pp, L, di2, ni2 = self._prepare_data(data, psd, di2, ni2, 2 * B)
+        out = torch.empty(B, dtype=torch.float64, device=self.device)
+        if B:
+            plan = self._plan(N, T, precision, tdi2, self.NPARAMS)
+            self._status.zero_()
+            a = plan.args(prm, start_freq_ind, self._status)
+            la = nat.LLArgs()
+            la.A_data, la.E_data = dd[0].data_ptr(), dd[1].data_ptr()
+            la.A_psd, la.E_psd = pp[0].data_ptr(), pp[1].data_ptr()
+            la.data_length = int(L)
+            la.num_data = int(dd[0].numel() // L)
+            la.num_psd = int(pp[0].numel() // L)
+            la.data_index = di2.data_ptr()
+            la.noise_index = ni2.data_ptr()
+            la.df = 1.0 / T
+            rc = nat.lib().gbx_swap_ll(ctypes.byref(a), ctypes.byref(la), nat.ptr(out),
+                                       nat.stream_handle())
+            nat.check(rc, "gbx_swap_ll")
+        if return_tensor:
+            return out
+        res = out.cpu().numpy()
+        self._check_status()
+        return res
+
     # --------------------------------------------------------- global fill
     def fill_global_template(self, group_index, templates, A, E, start_inds, N=None,
                              start_freq_ind=0):

@@ -206,6 +206,19 @@ int gbx_waveform_fill(const gbx_wave_args *a, void *A_glob, void *E_glob,
                       long long group_stride, void *stream);
 
 /*
+ * Swap log-likelihood (no counterpart in this version of the reference; the
+ * build's own definition): for each pair j, binaries 2j (the current source)
+ * and 2j+1 (the proposal) of the batch, with r the residual row chosen by
+ * data_index[2j+1] (d minus the walker's current sum of sources) and
+ * Dh = h_new - h_old,
+ *   dlogl[j] = Re<r|Dh> - 1/2 <Dh|Dh>
+ * with <a|b> = 4 df sum_{A,E} conj(a) b / S over the union of both windows
+ * (the inner product of gbgpu/cutils/gbgpu_utils.cu:172-183).  Uniform N,
+ * num_bin even; both precisions; circular or third-body parameters.
+ */
+int gbx_swap_ll(const gbx_wave_args *a, const gbx_ll_args *l, double *dlogl, void *stream);
+
+/*
  * Fused waveform + likelihood + gradient (no counterpart in the reference,
  * which has only finite-difference Fisher matrices, gbgpu/gbgpu.py:957-1138).
  * Computes d_h, h_h as gbx_waveform_ll and grad[k*num_bin + b] =
