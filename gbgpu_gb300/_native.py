@@ -25,7 +25,7 @@ EXPORTS = (
     "gbx_orbit_table_bytes", "gbx_orbit_table",
     "gbx_waveform", "gbx_waveform_ll", "gbx_waveform_fill", "gbx_wave_workspace_bytes",
     "gbx_waveform_ll_noalloc", "gbx_waveform_ll_grad", "gbx_grad_workspace_bytes",
-    "gbx_swap_ll",
+    "gbx_swap_ll", "gbx_fill_global_det",
 )
 
 _vp = ctypes.c_void_p
@@ -74,6 +74,7 @@ def lib():
     L.gbx_get_ll_ex.argtypes = [_vp] * 8 + [_d, _vp, _i, _i, _vp, _vp, _i, _ll, _ll, _vp, _vp]
     L.gbx_fill_global.argtypes = [_vp] * 5 + [_i, _i, _vp, _i, _vp, _vp]
     L.gbx_fill_global_ex.argtypes = [_vp] * 5 + [_i, _i, _vp, _i, _i, _ll, _ll, _ll, _vp, _vp]
+    L.gbx_fill_global_det.argtypes = [_vp] * 5 + [_i, _i, _vp, _vp, _i, _i, _ll, _ll, _ll, _vp]
     L.gbx_orbit_table_bytes.argtypes = [_i]
     L.gbx_orbit_table_bytes.restype = ctypes.c_size_t
     L.gbx_orbit_table.argtypes = [_vp, _vp, _i, _d, _vp]

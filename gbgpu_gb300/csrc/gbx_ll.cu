@@ -83,6 +83,74 @@ __global__ void __launch_bounds__(256) fill_global_kernel(
     }
 }
 
+// Deterministic fill: one CTA per (chunk of kDetChunk output bins, group).
+// Binaries of a group are visited in the order given by `order` (sorted by
+// start index), so every output bin is the same sum in the same order on
+// every run; every bin of channels A/E is written (zero where no window
+// reaches), which is the reference's overwrite semantics (gbgpu.py:796-837).
+constexpr int kDetChunk = 1024;
+constexpr int kDetThreads = 256;
+
+__global__ void __launch_bounds__(kDetThreads) fill_det_kernel(
+    double2 *__restrict__ A_g, double2 *__restrict__ E_g, const double2 *__restrict__ A_t,
+    const double2 *__restrict__ E_t, const int *__restrict__ start_ind, int M,
+    const int *__restrict__ order, const int *__restrict__ group_first, int L, long long gstride,
+    long long tsi, long long tsb)
+{
+    __shared__ int s_lo, s_hi;
+    const int g = blockIdx.y;
+    const int c0 = blockIdx.x * kDetChunk;
+    if (threadIdx.x == 0) {
+        // binaries whose window [s, s + M) meets [c0, c0 + kDetChunk): s in [c0 - M + 1, c0 + kDetChunk)
+        const int b0 = group_first[g], b1 = group_first[g + 1];
+        int lo = b0, hi = b1;
+        const long long want_lo = (long long)c0 - M + 1;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if ((long long)start_ind[order[mid]] < want_lo) lo = mid + 1; else hi = mid;
+        }
+        s_lo = lo;
+        int lo2 = lo, hi2 = b1;
+        const long long want_hi = (long long)c0 + kDetChunk;
+        while (lo2 < hi2) {
+            const int mid = (lo2 + hi2) >> 1;
+            if ((long long)start_ind[order[mid]] < want_hi) lo2 = mid + 1; else hi2 = mid;
+        }
+        s_hi = lo2;
+    }
+    __syncthreads();
+    constexpr int PER = kDetChunk / kDetThreads;
+    double2 a[PER], e[PER];
+#pragma unroll
+    for (int k = 0; k < PER; k++) {
+        a[k] = make_double2(0.0, 0.0);
+        e[k] = make_double2(0.0, 0.0);
+    }
+    for (int q = s_lo; q < s_hi; q++) {
+        const int b = order[q];
+        const int s = start_ind[b];
+#pragma unroll
+        for (int k = 0; k < PER; k++) {
+            const int j = c0 + threadIdx.x + k * kDetThreads;
+            const int i = j - s;
+            if (i >= 0 && i < M) {
+                const double2 x = __ldg(A_t + i * tsi + b * tsb);
+                const double2 y = __ldg(E_t + i * tsi + b * tsb);
+                a[k].x += x.x; a[k].y += x.y;
+                e[k].x += y.x; e[k].y += y.y;
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < PER; k++) {
+        const int j = c0 + threadIdx.x + k * kDetThreads;
+        if (j < L) {
+            A_g[(size_t)g * gstride + j] = a[k];
+            E_g[(size_t)g * gstride + j] = e[k];
+        }
+    }
+}
+
 static int grid_for(int num_bin)
 {
     int blocks = (num_bin + 7) / 8;
@@ -157,4 +225,30 @@ extern "C" int gbx_fill_global(void *A_glob, void *E_glob, const void *A_templat
     return gbx_fill_global_ex(A_glob, E_glob, A_template, E_template, start_ind, M, num_bin,
                               group_index, data_length, 0, (long long)data_length,
                               (long long)num_bin, 1LL, status, stream);
+}
+
+extern "C" int gbx_fill_global_det(void *A_glob, void *E_glob, const void *A_template,
+                                   const void *E_template, const int *start_ind, int M,
+                                   int num_bin, const int *order, const int *group_first,
+                                   int num_groups, int data_length, long long group_stride,
+                                   long long t_stride_i, long long t_stride_b, void *stream)
+{
+    if (num_bin < 0 || M < 0 || data_length < 0 || num_groups < 0)
+        return set_error(GBX_ERR_ARG, "negative size");
+    if (num_groups == 0 || data_length == 0) return GBX_OK;
+    if (!A_glob || !E_glob || !group_first || (num_bin > 0 && (!A_template || !E_template ||
+                                                                !start_ind || !order)))
+        return set_error(GBX_ERR_ARG, "NULL pointer");
+    if (group_stride < data_length) return set_error(GBX_ERR_ARG, "group_stride < data_length");
+    if (num_groups > 65535) return set_error(GBX_ERR_UNSUPPORTED, "at most 65535 groups");
+    int rc = ensure_init((cudaStream_t)stream);
+    if (rc) return rc;
+    dim3 grid((data_length + kDetChunk - 1) / kDetChunk, num_groups);
+    fill_det_kernel<<<grid, kDetThreads, 0, (cudaStream_t)stream>>>(
+        (double2 *)A_glob, (double2 *)E_glob, (const double2 *)A_template,
+        (const double2 *)E_template, start_ind, M, order, group_first, data_length, group_stride,
+        t_stride_i, t_stride_b);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_error(e, "fill_det launch");
+    return GBX_OK;
 }

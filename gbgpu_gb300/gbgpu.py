@@ -648,12 +648,18 @@ class GBGPUBase(abc.ABC):
 
     # --------------------------------------------------------- global fill
     def fill_global_template(self, group_index, templates, A, E, start_inds, N=None,
-                             start_freq_ind=0):
+                             start_freq_ind=0, mode="atomic"):
         """Sum waveforms into templates[g, 0:2] (gbgpu.py:737-837), in place.
 
         Channels 0 and 1 of ``templates`` are overwritten with the new sums,
-        as in the reference; other channels are untouched.
+        as in the reference; other channels are untouched.  ``mode="atomic"``
+        adds with FP64 atomics (summation order varies between runs, as on the
+        reference's GPU backend); ``mode="deterministic"`` sorts the binaries
+        by (group, start) and gathers every output bin in that order, giving
+        identical bits on every run.
         """
+        if mode not in ("atomic", "deterministic"):
+            raise ValueError("mode must be 'atomic' or 'deterministic'")
         total_groups, nchannels, data_length = templates.shape
         num_bin = len(group_index)
         if nchannels < 2:
@@ -683,6 +689,10 @@ class GBGPUBase(abc.ABC):
                                  "also needs to be provided.")
             A, E = A.contiguous(), E.contiguous()
             tsi, tsb = num_bin, 1
+        if mode == "deterministic":
+            self._fill_det(work, gi, si, A, E, int(N), int(tsi), int(tsb))
+            self._finish_fill(templates, tt, work, host_out)
+            return
         work[:, 0:2].zero_()
         self._status.zero_()
         if num_bin:
@@ -695,6 +705,25 @@ class GBGPUBase(abc.ABC):
                 ctypes.c_void_p(self._status.data_ptr()), nat.stream_handle())
             nat.check(rc, "gbx_fill_global_ex")
         self._finish_fill(templates, tt, work, host_out)
+
+    def _fill_det(self, work, gi, si, A, E, N, tsi, tsb):
+        """Sorted gather into channels 0/1 of ``work`` (G, nch, L), in place."""
+        G, nch, L = work.shape
+        B = gi.shape[0]
+        if B and (int(gi.min()) < 0 or int(gi.max()) >= G):
+            raise ValueError("group_index out of range")
+        key = (gi.to(torch.int64) << 32) | (si.to(torch.int64) + (1 << 31))
+        order = torch.argsort(key, stable=True).to(torch.int32).contiguous()
+        first = torch.zeros(G + 1, dtype=torch.int32, device=self.device)
+        if B:
+            first[1:] = torch.cumsum(torch.bincount(gi.to(torch.int64), minlength=G), 0).to(torch.int32)
+        rc = nat.lib().gbx_fill_global_det(
+            ctypes.c_void_p(work[0, 0].data_ptr()), ctypes.c_void_p(work[0, 1].data_ptr()),
+            ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(E.data_ptr()),
+            ctypes.c_void_p(si.data_ptr()), int(N), int(B), ctypes.c_void_p(order.data_ptr()),
+            ctypes.c_void_p(first.data_ptr()), int(G), int(L), int(nch * L), int(tsi), int(tsb),
+            nat.stream_handle())
+        nat.check(rc, "gbx_fill_global_det")
 
     def _finish_fill(self, templates, tt, work, host_out):
         if work is not tt:
@@ -713,6 +742,9 @@ class GBGPUBase(abc.ABC):
         ``params`` is (B, nparams), transposed relative to ``get_ll``.
         """
         precision = kwargs.pop("precision", self.precision)
+        fill_mode = kwargs.pop("fill_mode", "atomic")
+        if fill_mode not in ("atomic", "deterministic"):
+            raise ValueError("fill_mode must be 'atomic' or 'deterministic'")
         N = kwargs.pop("N", None)
         T = kwargs.pop("T", 4 * YRSID_SI)
         dt = kwargs.pop("dt", 10.0)
@@ -734,6 +766,22 @@ class GBGPUBase(abc.ABC):
         tt = _to_device(templates, torch.complex128, self.device)
         work = tt if tt.is_contiguous() else tt.contiguous()
         gi = _to_device(group_index, torch.int32, self.device).contiguous()
+        if fill_mode == "deterministic":
+            # waveform windows first (A/E/T, (B, 3, N)), then the sorted gather
+            if np.ndim(N) != 0:
+                raise NotImplementedError("deterministic fill takes one N per call")
+            AET = torch.empty((B, 3, int(N)), dtype=torch.complex128, device=self.device)
+            start = torch.empty(B, dtype=torch.int32, device=self.device)
+            if B:
+                plan = self._plan(N, T, precision, tdi2, prm.shape[0])
+                a = plan.args(prm, start_freq_ind, self._status)
+                rc = nat.lib().gbx_waveform(ctypes.byref(a), None, nat.ptr(AET), nat.ptr(start),
+                                            nat.stream_handle())
+                nat.check(rc, "gbx_waveform")
+            self._fill_det(work, gi, start, AET[:, 0], AET[:, 1], int(N), 1, 3 * int(N))
+            self._lazy = (prm, N, T, tdi2)
+            self._finish_fill(templates, tt, work, host_out)
+            return
         work[:, 0:2].zero_()
         self._status.zero_()
         if B:

@@ -109,6 +109,22 @@ int gbx_fill_global_ex(void *A_glob, void *E_glob, const void *A_template,
                        int *status, void *stream);
 
 /*
+ * Deterministic form of gbx_fill_global_ex (no counterpart in the reference,
+ * whose GPU fill order depends on atomic scheduling).  `order` lists the
+ * binaries sorted by (group, start index) and group_first[g] ..
+ * group_first[g+1] is group g's slice of it (num_groups + 1 entries).  Every
+ * bin of channels A/E of every group is written -- the sum of the windows that
+ * reach it, added in `order`, or zero -- so repeated calls give identical
+ * bits and the reference's overwrite semantics hold without zeroing first.
+ * Group indices themselves are implied by group_first.
+ */
+int gbx_fill_global_det(void *A_glob, void *E_glob, const void *A_template,
+                        const void *E_template, const int *start_ind, int M, int num_bin,
+                        const int *order, const int *group_first, int num_groups,
+                        int data_length, long long group_stride, long long t_stride_i,
+                        long long t_stride_b, void *stream);
+
+/*
  * Orbit table for one N.  `sc_pos` is the (3, N, 3) FP64 array of spacecraft
  * positions [m] at tm_n = n T/N for spacecraft 1, 2, 3 -- exactly what the
  * reference obtains from orbits.get_pos (gbgpu/gbgpu.py:390-397).  The table
