@@ -306,6 +306,115 @@ def config3(gb, data, Sd, seed, steps):
     return out
 
 
+def config2(gb, seed, B=1_000_000, G=256, N=256, steps=3):
+    """BASELINE config 2: 1e6 binaries, f0 density f^(-11/3) on [1e-4, 1e-2] Hz,
+    amp ~ f0^(2/3) with log-normal scatter (sigma 0.3), N = 256, group index
+    uniform over 256 walkers, templates (256, 2, 12,623,041) complex128
+    (103.4 GB).  Times the fused FP64 atomic fill and the deterministic fill
+    (waveforms, sort by (group, start), ordered gather); the zeroing of the
+    templates that the atomic mode needs is timed separately."""
+    import torch
+    rng = np.random.default_rng(seed + 2)
+    lo, hi = 1e-4, 1e-2
+    u = rng.uniform(0, 1, B)
+    f0 = (lo ** (-8 / 3) - u * (lo ** (-8 / 3) - hi ** (-8 / 3))) ** (-3 / 8)
+    fdot = 10 ** rng.uniform(-18, -15, B)
+    amp = 1e-22 * (f0 / 1e-3) ** (2 / 3) * np.exp(0.3 * rng.standard_normal(B))
+    p = np.array([amp, f0, fdot, 11.0 / 3.0 * fdot ** 2 / f0, rng.uniform(0, 2 * np.pi, B),
+                  np.arccos(rng.uniform(-1, 1, B)), rng.uniform(0, np.pi, B),
+                  rng.uniform(0, 2 * np.pi, B), np.arcsin(rng.uniform(-1, 1, B))])
+    gi = torch.as_tensor(rng.integers(0, G, B).astype(np.int32), device="cuda")
+    pT = torch.as_tensor(p.T.copy(), device="cuda")
+    L = int(int(T_OBS / DT) / 2) + 1
+    out = {"workload": f"{B} binaries (f^-11/3 on 1e-4..1e-2 Hz), N={N}, {G} groups x 2 x {L} "
+                       "complex128 templates", "steps": steps}
+    try:
+        tmpl = torch.empty((G, 2, L), dtype=torch.complex128, device="cuda")
+    except RuntimeError as e:
+        out["unavailable"] = f"template allocation failed: {e}"[:200]
+        return out
+    out["template_GB"] = tmpl.numel() * 16 / 1e9
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+
+    def timeit(fn):
+        fn()
+        torch.cuda.synchronize()
+        ev[0].record()
+        for _ in range(steps):
+            fn()
+        ev[1].record()
+        torch.cuda.synchronize()
+        return ev[0].elapsed_time(ev[1]) / steps
+
+    ms_zero = timeit(lambda: tmpl.zero_())
+    for mode in ("atomic", "deterministic"):
+        ms = timeit(lambda: gb.generate_global_template(pT, gi, tmpl, N=N, T=T_OBS, dt=DT,
+                                                        precision="fp64", fill_mode=mode))
+        out[f"{mode}_ms"] = ms
+        out[f"{mode}_binaries_per_s"] = B / (ms / 1e3)
+    out["zeroing_ms"] = ms_zero
+    out["note"] = ("atomic_ms includes the zeroing of channels 0/1 (the reference's "
+                   "overwrite semantics); deterministic writes every bin itself")
+    del tmpl
+    torch.cuda.empty_cache()
+    return out
+
+
+def config4(seed, W=4096, K=500, N=512, steps=100, replays=3):
+    """BASELINE config 4: GBGPUThirdBody, 4,096 walkers x 500 sources, N = 512,
+    T = 4 yr, dt = 5 s; every walker proposes a swap of one source per step
+    (swap likelihood in the mixed form, Metropolis accept, residual update);
+    100 steps are captured as one CUDA graph and replayed.  Sources sit in a
+    ~2.5e-4 Hz band (34,000 bins) of seeded noise.  Reports swaps/s."""
+    import torch
+    from gbgpu_gb300 import GBGPUThirdBody
+    from gbgpu_gb300.mcmc import SwapSampler, random_proposals, log_uniforms
+    from gbgpu_gb300.sensitivity import A1TDISens
+    rng = np.random.default_rng(seed + 4)
+    Tu = int(T_OBS / DT) * DT
+    s0 = int(2e-3 * Tu)
+    Lb = 34_000
+    f0 = (s0 + 1024 + rng.uniform(0, Lb - 2048, (W, K))) / Tu
+    fdot = 10 ** rng.uniform(-18, -16, (W, K))
+    P2 = 10 ** rng.uniform(0, np.log10(40), (W, K))
+    p = np.stack([10 ** rng.uniform(-23, -21, (W, K)), f0, fdot, 11 / 3 * fdot ** 2 / f0,
+                  rng.uniform(0, 2 * np.pi, (W, K)), np.arccos(rng.uniform(-1, 1, (W, K))),
+                  rng.uniform(0, np.pi, (W, K)), rng.uniform(0, 2 * np.pi, (W, K)),
+                  np.arcsin(rng.uniform(-1, 1, (W, K))), 10 ** rng.uniform(-2, 2, (W, K)),
+                  rng.uniform(0, 2 * np.pi, (W, K)), rng.uniform(0, 0.9, (W, K)), P2,
+                  rng.uniform(0, 1, (W, K)) * P2])
+    S = A1TDISens.get_Sn((np.arange(Lb) + s0) / Tu)
+    Sd = torch.as_tensor(S, device="cuda")
+    g = torch.Generator(device="cuda").manual_seed(seed + 44)
+    sig = torch.sqrt(Sd * (Tu / 4.0))
+    data = [torch.complex(torch.randn(Lb, generator=g, device="cuda", dtype=torch.float64) * sig,
+                          torch.randn(Lb, generator=g, device="cuda", dtype=torch.float64) * sig)
+            for _ in range(2)]
+    gb = GBGPUThirdBody(precision="mixed")
+    smp = SwapSampler(gb, torch.as_tensor(p, device="cuda"), data, [Sd, Sd], N=N, T=T_OBS,
+                      dt=DT, start_freq_ind=s0)
+    scale = torch.tensor([0.05, 2e-9, 0, 0, 0.2, 0.1, 0.1, 0.02, 0.02, 0.05, 0.1, 0.02, 0.01, 0.01],
+                         dtype=torch.float64, device="cuda")
+    ks = [int(x) for x in rng.integers(0, K, steps)]
+    props = torch.stack([random_proposals(smp.params[:, :, k], scale, g) for k in ks])
+    props[:, 11].clamp_(0.0, 0.9)
+    lus = log_uniforms(W, steps, g, "cuda")
+    smp.capture(ks, props, lus)
+    smp.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(replays):
+        smp.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / replays
+    return {"workload": f"GBGPUThirdBody, {W} walkers x {K} sources, N={N}, dt=5 s; "
+                        f"{steps} swap steps per CUDA graph", "graph_ms": ms,
+            "swaps_per_s": W * steps / (ms / 1e3),
+            "acceptance": float(smp.accepted.sum().item()) / (W * steps * (replays + 1))}
+
+
 def run_gpu(args, rank, world):
     import torch
     import torch.distributed as dist
@@ -402,6 +511,11 @@ def run_gpu(args, rank, world):
     ms_fp64, _ = timed("fp64", max(1, min(args.steps, 3)), 1)
     ms_grad, _ = timed("grad", max(1, min(args.steps, 10)), 1)
     cfg3 = config3(gb, data, Sd, args.seed + rank, max(1, min(args.steps, 10)))
+    cfg2 = cfg4 = None
+    if not args.no_fill_bench:
+        cfg2 = config2(gb, args.seed + rank)
+    if not args.no_mcmc_bench:
+        cfg4 = config4(args.seed + rank)
 
     # e2e through the public API: host params -> device, like -> host
     p_pin = torch.from_numpy(np.ascontiguousarray(p)).pin_memory()
@@ -458,6 +572,8 @@ def run_gpu(args, rank, world):
         "grads_note": "binaries/s of the fused likelihood + 9-parameter gradient kernel "
                       "(mixed form) on the same 200k-binary batch",
         "config3": cfg3,
+        "config2": cfg2,
+        "config4": cfg4,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "note": f"peak {peak_src}; the kernel is FP64-pipe bound (carrier phase), "
@@ -538,6 +654,8 @@ def main():
     ap.add_argument("--seed", type=int, default=2026)
     ap.add_argument("--cpu-workers", type=int, default=os.cpu_count() or 1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fill-bench", action="store_true")
+    ap.add_argument("--no-mcmc-bench", action="store_true")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

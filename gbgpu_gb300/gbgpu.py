@@ -796,6 +796,49 @@ class GBGPUBase(abc.ABC):
         self._lazy = (prm, N, T, tdi2)
         self._finish_fill(templates, tt, work, host_out)
 
+    def add_to_templates(self, params, group_index, templates, start_freq_ind=0, **kwargs):
+        """Add waveforms into templates without zeroing them first (no
+        counterpart in the reference, whose fill always overwrites).
+
+        ``params`` is (nparams, B) on the device; ``templates`` is either a
+        contiguous (G, nch, L) complex128 CUDA tensor (channels 0 and 1 are
+        A and E) or a pair ``(A, E)`` of contiguous (G, L) tensors; they are
+        updated in place with FP64 atomics.  Nothing here synchronises or
+        copies from the host once the plan for (N, T, precision) exists, so the
+        call can be captured in a CUDA graph.
+        """
+        precision = kwargs.pop("precision", self.precision)
+        N = int(kwargs.pop("N"))
+        T = kwargs.pop("T", 4 * YRSID_SI)
+        dt = kwargs.pop("dt", 10.0)
+        tdi2 = kwargs.pop("tdi2", False)
+        if kwargs:
+            raise TypeError(f"unexpected keyword arguments {list(kwargs)}")
+        T = int(T / dt) * dt
+        if isinstance(templates, (tuple, list)):
+            tA, tE = templates
+            if not (tA.is_cuda and tE.is_cuda and tA.is_contiguous() and tE.is_contiguous()
+                    and tA.shape == tE.shape and tA.ndim == 2):
+                raise TypeError("(A, E) templates must be contiguous (G, L) CUDA tensors")
+            G, L = tA.shape
+            pA, pE, gstride = tA.data_ptr(), tE.data_ptr(), L
+        else:
+            if not (isinstance(templates, torch.Tensor) and templates.is_cuda
+                    and templates.is_contiguous()):
+                raise TypeError("templates must be a contiguous CUDA tensor")
+            G, nch, L = templates.shape
+            pA, pE, gstride = templates[0, 0].data_ptr(), templates[0, 1].data_ptr(), nch * L
+        B = params.shape[1]
+        if B == 0:
+            return
+        plan = self._plan(N, T, precision, tdi2, params.shape[0])
+        a = plan.args(params, start_freq_ind, self._status)
+        rc = nat.lib().gbx_waveform_fill(
+            ctypes.byref(a), ctypes.c_void_p(pA), ctypes.c_void_p(pE),
+            ctypes.c_void_p(group_index.data_ptr()), int(G), int(L), int(gstride),
+            nat.stream_handle())
+        nat.check(rc, "gbx_waveform_fill")
+
     # ------------------------------------------------------------- injection
     def inject_signal(self, *args, fmax=None, T=4.0 * YRSID_SI, dt=10.0, **kwargs):
         """Binary 0 placed on a 0..fmax grid, as NumPy (A, E) (gbgpu.py:880-946)."""

@@ -1,0 +1,117 @@
+"""Ensemble swap sampler on the GPU: the caller of the swap likelihood.
+
+Each of W walkers holds K sources and a residual r_w = d - sum_k h(theta_wk)
+restricted to a frequency band.  One proposal step replaces, in every walker,
+source k_s by a proposed one, computes dlogL with the swap kernel, accepts
+with probability min(1, exp(dlogL)) and updates the residual of accepted
+walkers by adding h_old - h_new (a template fill with amplitudes +-amp, exact
+because h is linear in amp).  All proposals and uniform draws are prepared on
+the device beforehand, so a block of steps is captured and replayed as one
+CUDA graph.  Sources in a walker are assumed not to change the N that the
+batch is evaluated with.
+"""
+
+import math
+
+import torch
+
+
+class SwapSampler:
+    def __init__(self, gb, params, data, psd, N, T, dt, start_freq_ind, tdi2=False,
+                 precision="mixed"):
+        """``params``: (nparams, W, K) FP64 CUDA tensor of the current sources;
+        ``data``: [A, E] (Lb,) complex128 band of the data; ``psd``: [A, E] (Lb,)."""
+        self.gb = gb
+        self.params = params.contiguous()
+        self.nparams, self.W, self.K = params.shape
+        self.kw = dict(N=N, T=T, dt=dt, tdi2=tdi2, precision=precision)
+        self.s0 = int(start_freq_ind)
+        self.psd = [p.contiguous() for p in psd]
+        Lb = data[0].shape[0]
+        dev = params.device
+        # residuals as (channel, walker, bin): each channel is a contiguous
+        # (W, Lb) array whose rows the likelihood selects with data_index
+        self.res = torch.empty((2, self.W, Lb), dtype=torch.complex128, device=dev)
+        self.res[0] = data[0]
+        self.res[1] = data[1]
+        # r_w = d - sum_k h(theta_wk): add every source with amplitude -amp
+        allp = self.params.reshape(self.nparams, self.W * self.K).clone()
+        allp[0] = -allp[0]
+        gw = torch.arange(self.W, device=dev, dtype=torch.int32).repeat_interleave(self.K)
+        gb.add_to_templates(allp.contiguous(), gw, (self.res[0], self.res[1]),
+                            start_freq_ind=self.s0, **self.kw)
+        self.walkers = torch.arange(self.W, device=dev, dtype=torch.int32)
+        self.accepted = torch.zeros(self.W, dtype=torch.int64, device=dev)
+        self.graph = None
+
+    def step(self, k, proposal, log_u):
+        """One Metropolis swap step for source ``k`` of every walker.
+
+        ``proposal``: (nparams, W) proposed sources; ``log_u``: (W,) log uniforms.
+        Returns dlogL (W,).
+        """
+        old = self.params[:, :, k].contiguous()
+        dl = self.gb.swap_likelihood(old, proposal, [self.res[0], self.res[1]], self.psd,
+                                     data_index=self.walkers, start_freq_ind=self.s0,
+                                     return_tensor=True, **self.kw)
+        acc = log_u < dl
+        accf = acc.to(torch.float64)
+        # residual += h_old - h_new for accepted walkers (amplitudes zeroed otherwise)
+        upd = torch.cat([old, proposal], dim=1).clone()
+        upd[0, :self.W] = old[0] * accf
+        upd[0, self.W:] = -proposal[0] * accf
+        groups = torch.cat([self.walkers, self.walkers])
+        self.gb.add_to_templates(upd.contiguous(), groups, (self.res[0], self.res[1]),
+                                 start_freq_ind=self.s0, **self.kw)
+        self.params[:, :, k] = torch.where(acc[None, :], proposal, old)
+        self.accepted += acc
+        return dl
+
+    def capture(self, ks, proposals, log_us):
+        """Capture len(ks) steps (proposals (S, nparams, W), log_us (S, W)) as one graph."""
+        self.ks = list(ks)
+        self.proposals = proposals
+        self.log_us = log_us
+        # warm-up outside capture: builds plans, workspaces and cached kernels
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            self._snapshot = (self.params.clone(), self.res.clone(), self.accepted.clone())
+            self.step(self.ks[0], self.proposals[0], self.log_us[0])
+            self.params.copy_(self._snapshot[0])
+            self.res.copy_(self._snapshot[1])
+            self.accepted.copy_(self._snapshot[2])
+        torch.cuda.current_stream().wait_stream(s)
+        torch.cuda.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.dls = [self.step(k, self.proposals[i], self.log_us[i])
+                        for i, k in enumerate(self.ks)]
+        return self.graph
+
+    def replay(self):
+        self.graph.replay()
+
+    def log_likelihood(self):
+        """-1/2 <r_w|r_w> of every walker's residual (the band's contribution)."""
+        Tu = int(self.kw["T"] / self.kw["dt"]) * self.kw["dt"]
+        w = 4.0 / Tu
+        out = torch.zeros(self.W, dtype=torch.float64, device=self.res.device)
+        for ch in range(2):
+            out += w * (self.res[ch].abs() ** 2 / self.psd[ch][None, :]).sum(1)
+        return -0.5 * out
+
+
+def random_proposals(params_k, scale, gen):
+    """Gaussian moves of (nparams, W) sources: relative for amp, absolute otherwise."""
+    p = params_k.clone()
+    z = torch.randn(p.shape, generator=gen, device=p.device, dtype=p.dtype)
+    p[0] = p[0] * (1 + scale[0] * z[0])
+    for i in range(1, p.shape[0]):
+        p[i] = p[i] + scale[i] * z[i]
+    return p
+
+
+def log_uniforms(W, steps, gen, device):
+    u = torch.rand((steps, W), generator=gen, device=device, dtype=torch.float64)
+    return torch.log(u.clamp_min(math.ldexp(1.0, -60)))
