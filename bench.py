@@ -133,7 +133,10 @@ def _cpu_task(args):
     return _t.perf_counter() - t0, p.shape[1]
 
 
-def cpu_baseline(p, Ns, dA, dE, S, workers, per_class=(256, 256, 128, 64, 32, 24)):
+CPU_SAMPLE = (25600, 25600, 12800, 6400, 3200, 2400)   # ~15 s of CPU work in total
+
+
+def cpu_baseline(p, Ns, dA, dE, S, workers, per_class=CPU_SAMPLE, pool=None):
     """Times the oracle port on a bounded sample of every N class with a spawn
     pool of ``workers`` processes and extrapolates to the workload's N mix."""
     import multiprocessing as mp
@@ -152,12 +155,18 @@ def cpu_baseline(p, Ns, dA, dE, S, workers, per_class=(256, 256, 128, 64, 32, 24
             si = O.start_indices(p[1, sel], n, T_OBS, DT)
             a, b = int(si.min()) - 1, int(si.max()) + n + 1
             tasks.append((p[:, sel].copy(), n, dA[a:b].copy(), dE[a:b].copy(), S[a:b].copy(), a))
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(workers) as pool:
+    own = pool is None
+    if own:
+        pool = mp.get_context("spawn").Pool(workers)
         pool.map(_cpu_warm, range(workers), chunksize=1)     # imports done before timing
+    try:
         t0 = time.perf_counter()
         res = pool.map(_cpu_task, tasks, chunksize=1)
         wall = time.perf_counter() - t0
+    finally:
+        if own:
+            pool.close()
+            pool.join()
     busy = {}
     for (task, (dt_, nb)) in zip(tasks, res):
         busy[task[1]] = busy.get(task[1], 0.0) + dt_
@@ -347,14 +356,16 @@ def config2(gb, seed, B=1_000_000, G=256, N=256, steps=3):
         return ev[0].elapsed_time(ev[1]) / steps
 
     ms_zero = timeit(lambda: tmpl.zero_())
-    for mode in ("atomic", "deterministic"):
-        ms = timeit(lambda: gb.generate_global_template(pT, gi, tmpl, N=N, T=T_OBS, dt=DT,
-                                                        precision="fp64", fill_mode=mode))
-        out[f"{mode}_ms"] = ms
-        out[f"{mode}_binaries_per_s"] = B / (ms / 1e3)
+    for prec in ("fp64", "mixed"):
+        for mode in ("atomic", "deterministic"):
+            ms = timeit(lambda: gb.generate_global_template(pT, gi, tmpl, N=N, T=T_OBS, dt=DT,
+                                                            precision=prec, fill_mode=mode))
+            out[f"{prec}_{mode}_ms"] = ms
+            out[f"{prec}_{mode}_binaries_per_s"] = B / (ms / 1e3)
     out["zeroing_ms"] = ms_zero
-    out["note"] = ("atomic_ms includes the zeroing of channels 0/1 (the reference's "
-                   "overwrite semantics); deterministic writes every bin itself")
+    out["note"] = ("templates accumulate in FP64 in every variant; fp64/mixed is the waveform "
+                   "precision.  atomic includes zeroing channels 0/1 (the reference's overwrite "
+                   "semantics); deterministic writes every bin itself")
     del tmpl
     torch.cuda.empty_cache()
     return out
@@ -624,13 +635,26 @@ def run_reference(args):
     sig[0] = 0.0
     dA = (rng.standard_normal(L) + 1j * rng.standard_normal(L)) * sig
     dE = (rng.standard_normal(L) + 1j * rng.standard_normal(L)) * sig
+    import multiprocessing as mp
     workers = os.cpu_count() or 1
     vals = []
     base = None
-    for _ in range(max(1, args.steps)):
-        base = cpu_baseline(p, Ns, dA, dE, S, workers=workers,
-                            per_class=(64, 64, 32, 16, 8, 8))
-        vals.append(base["value"])
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import fastgb_oracle as O
+    O._lib()
+    pool = mp.get_context("spawn").Pool(workers)
+    try:
+        pool.map(_cpu_warm, range(workers), chunksize=1)
+        for _ in range(max(1, args.warmup)):
+            cpu_baseline(p, Ns, dA, dE, S, workers=workers, per_class=(256, 256, 128, 64, 32, 24),
+                         pool=pool)
+        for _ in range(max(1, args.steps)):
+            base = cpu_baseline(p, Ns, dA, dE, S, workers=workers,
+                                per_class=(2560, 2560, 1280, 640, 320, 240), pool=pool)
+            vals.append(base["value"])
+    finally:
+        pool.close()
+        pool.join()
     v = float(np.median(vals))
     base["value"] = v
     return {"metric": METRIC, "value": v, "unit": "binaries/s", "n_gpus": 1,
