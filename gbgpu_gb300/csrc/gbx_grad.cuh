@@ -262,10 +262,11 @@ __device__ __forceinline__ void fft_dit_pass(typename C2<R>::T *buf, int nsub, i
         const int rem = g & ((1 << (lg - RB)) - 1);
         const int blk = rem >> hl;
         const int r = rem & ((1 << hl) - 1);
-        V *base = buf + ((size_t)a << lg) + ((size_t)blk << (hl + RB)) + r;
+        V *sub = buf + ((size_t)a << lg);
+        const int p0 = (blk << (hl + RB)) + r;
         V x[M];
 #pragma unroll
-        for (int m = 0; m < M; m++) x[m] = base[(size_t)m << hl];
+        for (int m = 0; m < M; m++) x[m] = sub[swz(p0 + (m << hl), lg)];
 #pragma unroll
         for (int j = 0; j < RB; j++) {
             const int dm = 1 << j;
@@ -282,7 +283,7 @@ __device__ __forceinline__ void fft_dit_pass(typename C2<R>::T *buf, int nsub, i
             }
         }
 #pragma unroll
-        for (int m = 0; m < M; m++) base[(size_t)m << hl] = x[m];
+        for (int m = 0; m < M; m++) sub[swz(p0 + (m << hl), lg)] = x[m];
     }
 }
 
@@ -299,7 +300,9 @@ __device__ __forceinline__ void fft_dit(typename C2<R>::T *buf, int nsub, int lg
     }
     const int chunks = (nsub << lg) >> 5;
     for (int c = threadIdx.x >> 5; c < chunks; c += kBlock >> 5) {
-        V x = buf[(c << 5) + lane];
+        const int e = (c << 5) + lane;
+        const int idx = ((e >> lg) << lg) + swz(e & ((1 << lg) - 1), lg);
+        V x = buf[idx];
 #pragma unroll
         for (int k = 0; k < 5; k++) {
             const int o = 1 << k;
@@ -308,7 +311,7 @@ __device__ __forceinline__ void fft_dit(typename C2<R>::T *buf, int nsub, int lg
             V t = cmul(w[k], up ? x : y);          // W times the upper element
             x = up ? csub(y, t) : cadd(x, t);
         }
-        buf[(c << 5) + lane] = x;
+        buf[idx] = x;
     }
     __syncthreads();
     int hl = 5;
@@ -395,7 +398,7 @@ __global__ void __launch_bounds__(kBlock, 2) grad_kernel(const GradParams GP)
             slow_mixed<false, true>(bins[p], n, N, stepd, tab, nullptr, nullptr, o,
                                     es + 3 * (size_t)m);
 #pragma unroll
-            for (int c = 0; c < 3; c++) buf[(p * 3 + c) * N + n] = o[c];
+            for (int c = 0; c < 3; c++) buf[(p * 3 + c) * N + swz(n, lg)] = o[c];
         }
         __syncthreads();
         fft_dif<float>(buf, 3 * cnt, lg);
@@ -418,8 +421,9 @@ __global__ void __launch_bounds__(kBlock, 2) grad_kernel(const GradParams GP)
             for (int i = i0; i < N; i += Tpb) {
                 const int j = B.start + i;
                 const int pos = bitrev((i + (N >> 1)) & (N - 1), lg);
-                V X = buf[(p * 3 + 0) * N + pos], Y = buf[(p * 3 + 1) * N + pos],
-                  Z = buf[(p * 3 + 2) * N + pos];
+                const int sp = swz(pos, lg);
+                V X = buf[(p * 3 + 0) * N + sp], Y = buf[(p * 3 + 1) * N + sp],
+                  Z = buf[(p * 3 + 2) * N + sp];
                 float2 wX = {0.f, 0.f}, wY = {0.f, 0.f}, wZ = {0.f, 0.f};
                 if (B.valid && j >= 0 && j < K.L) {
                     const size_t jd = (size_t)B.di * K.L + j, jn = (size_t)B.ni * K.L + j;
@@ -450,9 +454,9 @@ __global__ void __launch_bounds__(kBlock, 2) grad_kernel(const GradParams GP)
                 } else if (B.valid) {
                     out = true;
                 }
-                buf[(p * 3 + 0) * N + pos] = make_float2(wX.x, -wX.y);
-                buf[(p * 3 + 1) * N + pos] = make_float2(wY.x, -wY.y);
-                buf[(p * 3 + 2) * N + pos] = make_float2(wZ.x, -wZ.y);
+                buf[(p * 3 + 0) * N + sp] = make_float2(wX.x, -wX.y);
+                buf[(p * 3 + 1) * N + sp] = make_float2(wY.x, -wY.y);
+                buf[(p * 3 + 2) * N + sp] = make_float2(wZ.x, -wZ.y);
             }
             if (out) flag(a.status, GBX_FLAG_WINDOW);
         }
@@ -468,7 +472,7 @@ __global__ void __launch_bounds__(kBlock, 2) grad_kernel(const GradParams GP)
                     float2 Yc[3], Es[3];
 #pragma unroll
                     for (int c = 0; c < 3; c++) {
-                        Yc[c] = buf[(p * 3 + c) * N + n];
+                        Yc[c] = buf[(p * 3 + c) * N + swz(n, lg)];
                         Es[c] = es[3 * ((size_t)(p << lg) + n) + c];
                     }
                     slow_grad_mixed(B, Gx, n, N, stepd, tab, ifs, fstarf, Yc, Es, acc + 5);

@@ -156,6 +156,17 @@ __device__ __forceinline__ void sinc_cos_f(float a, float &S, float &C)
     }
 }
 
+// Shared-memory position swizzle for one length-2^lg sub-array: the low k
+// bits are XOR-ed with the top k bits (k = 4 for lg >= 8).  Bit-reversed reads
+// (the FFT output order) then spread over the banks instead of hitting one;
+// runs of consecutive positions stay conflict-free.  A bijection, applied to
+// every access of the sub-array.
+__device__ __forceinline__ int swz(int pos, int lg)
+{
+    const int k = lg >= 8 ? 4 : (lg >> 1);
+    return pos ^ ((pos >> (lg - k)) & ((1 << k) - 1));
+}
+
 // 2^e as a double for -1022 <= e <= 1023, built from its bit pattern
 __device__ __forceinline__ double exp2_int(int e)
 {
@@ -613,10 +624,11 @@ __device__ __forceinline__ void fft_reg_pass(typename C2<R>::T *buf, int nsub, i
         const int rem = g & ((1 << (lg - RB)) - 1);
         const int blk = rem >> q;
         const int r = rem & ((1 << q) - 1);
-        V *base = buf + ((size_t)a << lg) + ((size_t)blk << (hl + 1)) + r;
+        V *sub = buf + ((size_t)a << lg);
+        const int p0 = (blk << (hl + 1)) + r;
         V x[M];
 #pragma unroll
-        for (int m = 0; m < M; m++) x[m] = base[(size_t)m << q];
+        for (int m = 0; m < M; m++) x[m] = sub[swz(p0 + (m << q), lg)];
 #pragma unroll
         for (int j = 0; j < RB; j++) {
             const int dm = M >> (j + 1);             // register distance of the pair
@@ -632,7 +644,7 @@ __device__ __forceinline__ void fft_reg_pass(typename C2<R>::T *buf, int nsub, i
             }
         }
 #pragma unroll
-        for (int m = 0; m < M; m++) base[(size_t)m << q] = x[m];
+        for (int m = 0; m < M; m++) sub[swz(p0 + (m << q), lg)] = x[m];
     }
 }
 
@@ -669,7 +681,9 @@ __device__ __forceinline__ void fft_dif(typename C2<R>::T *buf, int nsub, int lg
     }
     const int chunks = (nsub << lg) >> 5;
     for (int c = threadIdx.x >> 5; c < chunks; c += kBlock >> 5) {
-        V x = buf[(c << 5) + lane];
+        const int e = (c << 5) + lane;
+        const int idx = ((e >> lg) << lg) + swz(e & ((1 << lg) - 1), lg);
+        V x = buf[idx];
 #pragma unroll
         for (int k = 0; k < 5; k++) {
             const int o = 16 >> k;
@@ -677,7 +691,7 @@ __device__ __forceinline__ void fft_dif(typename C2<R>::T *buf, int nsub, int lg
             // lower lane keeps x + y; upper lane gets (y - x) W, y being the lower element
             x = (lane & o) ? cmul(csub(y, x), w[k]) : cadd(x, y);
         }
-        buf[(c << 5) + lane] = x;
+        buf[idx] = x;
     }
     __syncthreads();
 }
@@ -853,7 +867,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                 slow_mixed<THIRD>(B, n, N, stepd, tab, ps, vf, reinterpret_cast<float2 *>(o));
             }
 #pragma unroll
-            for (int c = 0; c < 3; c++) buf[(p * 3 + c) * N + n] = o[c];
+            for (int c = 0; c < 3; c++) buf[(p * 3 + c) * N + swz(n, lg)] = o[c];
         }
         __syncthreads();
 
@@ -867,8 +881,8 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                 const Bin &B = bins[p];
                 if (B.b < 0) continue;
                 const int pos = bitrev((i + (N >> 1)) & (N - 1), lg);   // fftshift
-                V X = buf[(p * 3 + 0) * N + pos], Y = buf[(p * 3 + 1) * N + pos],
-                  Z = buf[(p * 3 + 2) * N + pos];
+                V X = buf[(p * 3 + 0) * N + swz(pos, lg)], Y = buf[(p * 3 + 1) * N + swz(pos, lg)],
+                  Z = buf[(p * 3 + 2) * N + swz(pos, lg)];
                 double2 Xd = cmul(make_double2((double)X.x, (double)X.y), B.scale);
                 double2 Yd = cmul(make_double2((double)Y.x, (double)Y.y), B.scale);
                 double2 Zd = cmul(make_double2((double)Z.x, (double)Z.y), B.scale);
@@ -919,8 +933,8 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                             continue;
                         }
                         const int pos = bitrev((i + (N >> 1)) & (N - 1), lg);
-                        V X = buf[(pw * 3 + 0) * N + pos], Y = buf[(pw * 3 + 1) * N + pos],
-                          Z = buf[(pw * 3 + 2) * N + pos];
+                        V X = buf[(pw * 3 + 0) * N + swz(pos, lg)], Y = buf[(pw * 3 + 1) * N + swz(pos, lg)],
+                          Z = buf[(pw * 3 + 2) * N + swz(pos, lg)];
                         const size_t jd = (size_t)Bn.di * K.L + j, jn = (size_t)Bn.ni * K.L + j;
                         const double2 dA = __ldg(K.A_data + jd), dE = __ldg(K.E_data + jd);
                         const double SA = __ldg(K.A_psd + jn), SE = __ldg(K.E_psd + jn);
@@ -945,8 +959,8 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                             const int k = j - Bo.start;
                             if (k >= 0 && k < N) {
                                 const int pk = bitrev((k + (N >> 1)) & (N - 1), lg);
-                                V Xo = buf[(po * 3 + 0) * N + pk], Yo = buf[(po * 3 + 1) * N + pk],
-                                  Zo = buf[(po * 3 + 2) * N + pk];
+                                V Xo = buf[(po * 3 + 0) * N + swz(pk, lg)], Yo = buf[(po * 3 + 1) * N + swz(pk, lg)],
+                                  Zo = buf[(po * 3 + 2) * N + swz(pk, lg)];
                                 const Acc oAr = (Zo.x - Xo.x) * (Acc)is2, oAi = (Zo.y - Xo.y) * (Acc)is2;
                                 const Acc oEr = (Xo.x - 2 * Yo.x + Zo.x) * (Acc)is6,
                                           oEi = (Xo.y - 2 * Yo.y + Zo.y) * (Acc)is6;
@@ -1011,8 +1025,8 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                 const int j = B.start + i;
                 if (!B.valid || j < 0 || j >= K.L) continue;
                 const int pos = bitrev((i + (N >> 1)) & (N - 1), lg);
-                V X = buf[(p * 3 + 0) * N + pos], Y = buf[(p * 3 + 1) * N + pos],
-                  Z = buf[(p * 3 + 2) * N + pos];
+                V X = buf[(p * 3 + 0) * N + swz(pos, lg)], Y = buf[(p * 3 + 1) * N + swz(pos, lg)],
+                  Z = buf[(p * 3 + 2) * N + swz(pos, lg)];
                 double2 Ah = cmul(make_double2((double)((Z.x - X.x) * is2), (double)((Z.y - X.y) * is2)), B.scale);
                 double2 Eh = cmul(make_double2((double)((X.x - 2 * Y.x + Z.x) * is6),
                                                (double)((X.y - 2 * Y.y + Z.y) * is6)), B.scale);
@@ -1046,8 +1060,8 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                             continue;
                         }
                         const int pos = bitrev((i + (N >> 1)) & (N - 1), lg);
-                        V X = buf[(p * 3 + 0) * N + pos], Y = buf[(p * 3 + 1) * N + pos],
-                          Z = buf[(p * 3 + 2) * N + pos];
+                        V X = buf[(p * 3 + 0) * N + swz(pos, lg)], Y = buf[(p * 3 + 1) * N + swz(pos, lg)],
+                          Z = buf[(p * 3 + 2) * N + swz(pos, lg)];
                         const size_t jd = (size_t)B.di * K.L + j, jn = (size_t)B.ni * K.L + j;
                         const double2 dA = __ldg(K.A_data + jd), dE = __ldg(K.E_data + jd);
                         const double SA = __ldg(K.A_psd + jn), SE = __ldg(K.E_psd + jn);
