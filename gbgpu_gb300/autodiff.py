@@ -1,9 +1,10 @@
 """torch.autograd binding of the fused likelihood-and-gradient kernel.
 
 ``log_likelihood(gb, params, data, psd, **kw)`` returns logL (B,) as a torch
-tensor that is differentiable with respect to ``params`` (9, B): the forward
-launch computes logL and its gradient together (``gbx_waveform_ll_grad``), the
-backward multiplies the stored gradient by the incoming one.
+tensor that is differentiable with respect to ``params`` (9, B), or (14, B)
+for ``GBGPUThirdBody``: the forward launch computes logL and its gradient
+together (``gbx_waveform_ll_grad``), the backward multiplies the stored
+gradient by the incoming one.
 """
 
 import torch
@@ -23,5 +24,5 @@ class _LogLikelihood(torch.autograd.Function):
 
 
 def log_likelihood(gb, params, data, psd, **kwargs):
-    """Differentiable logL of each binary; ``params`` is a (9, B) FP64 CUDA tensor."""
+    """Differentiable logL of each binary; ``params`` is a (gb.NPARAMS, B) FP64 CUDA tensor."""
     return _LogLikelihood.apply(params, gb, data, psd, kwargs)

@@ -25,7 +25,7 @@ struct __align__(16) GradExtra {
     double2 dDPi, dDCi, dDPp, dDCp;  // d(DP, DC)/d(iota, psi), amplitude divided out
     double2 dlnsc_f0;              // d ln(scale) / d f0 (TDI-2 factor), 0 otherwise
     float gf0, gf1;                // d fonfs / d kP = -(fdot + fddot xi)/fstar = gf0 + gf1 xi
-    float pad[2];
+    float cosvarpi, P2yr;          // third body: cos varpi, period in years
 };
 
 __device__ void setup_grad(GradExtra &X, const KParams &K, int b)
@@ -61,6 +61,12 @@ __device__ void setup_grad(GradExtra &X, const KParams &K, int b)
     }
     X.gf0 = (float)(-fdot / K.fstar);
     X.gf1 = (float)(-fddot / K.fstar);
+    X.cosvarpi = 0.0f;
+    X.P2yr = 1.0f;
+    if (a.nparams >= 14) {
+        X.cosvarpi = (float)cos(p[10 * nb + b]);
+        X.P2yr = (float)p[12 * nb + b];
+    }
 }
 
 // S(a) = sin(a)/a, C = cos(a) and S'(a) from their Taylor series in x = a^2
@@ -112,10 +118,20 @@ __device__ __forceinline__ void cmac(float &re, float &im, float2 y, float2 x)
 // sum_q Z_q dG_q + dOmL sum_q Zd_q G_q with the link adjoints
 // Z_q = sum_c Y_c M_cq and Zd_q = sum_c Y_c dM_cq/domL.  Each parameter then
 // costs one complex multiply-add per link.
+//
+// Third body (THIRD): fonfs carries the factor (1 + v_LOS/c) (vls: v_LOS of
+// the three spacecraft at this sample), which scales its f0/fdot/fddot and
+// k.P derivatives; the derivatives through v_LOS and the cumulative Doppler
+// phase are left to the third-body pass, which needs per spacecraft
+//   cph[s] = sum over the two links at s of Z dG/dphase   (= -i Z G),
+//   cfo[s] = sum over the two links at s of Z dG/dfonfs  (= (S'/S - i) hh Z G).
+template <bool THIRD>
 __device__ __forceinline__ void slow_grad_mixed(const Bin &B, const GradExtra &Gx, int n, int N,
                                                 dfl step, const double *__restrict__ tab,
                                                 float ifs, float fstarf, const float2 Yc[3],
-                                                const float2 Es[3], float acc[14])
+                                                const float2 Es[3], float acc[14],
+                                                const float *vls = nullptr, float2 *cph = nullptr,
+                                                float2 *cfo = nullptr)
 {
     const float *tabf = reinterpret_cast<const float *>(tab + (size_t)18 * N);
     const float TWO_PI_F = (float)kTwoPi, PI_F = (float)kPi;
@@ -148,7 +164,7 @@ __device__ __forceinline__ void slow_grad_mixed(const Bin &B, const GradExtra &G
     const float2 YdA0 = cmul(Yc[0], da), YdA1 = cmul(Yc[1], da), YdA2 = cmul(Yc[2], da);
     const float2 YdB0 = cmul(Yc[0], db), YdB1 = cmul(Yc[1], db), YdB2 = cmul(Yc[2], db);
     // spacecraft: exp(-i phase) from the forward pass, FP32 delays and derivatives
-    float Er[3], Ei[3], fo[3], xi[3], dph_l[3], dph_b[3], dfo_l[3], dfo_b[3];
+    float Er[3], Ei[3], fo[3], xi[3], dph_l[3], dph_b[3], dfo_l[3], dfo_b[3], dop[3];
 #pragma unroll
     for (int s = 0; s < 3; s++) {
         float P0 = __ldg(tabf + (size_t)(9 + 3 * s) * N + n);
@@ -160,7 +176,8 @@ __device__ __forceinline__ void slow_grad_mixed(const Bin &B, const GradExtra &G
         const float x = tf - kPf;
         xi[s] = x;
         const float f_ = B.w0h + fmaf(fmaf(B.w2, x, B.w1), x, B.w0l);
-        fo[s] = f_;
+        dop[s] = THIRD ? 1.0f + vls[s] * (float)(1.0 / kCSI) : 1.0f;
+        fo[s] = THIRD ? f_ * dop[s] : f_;
         // d kP / d lam = st v.P/c, d kP / d beta = u.P/c;
         // d phase / d kP = 2 pi f(xi); d fonfs / d kP = -(fdot + fddot xi)/fstar
         const float Pv = fmaf(Gx.v[0], P0, Gx.v[1] * P1);
@@ -169,7 +186,7 @@ __device__ __forceinline__ void slow_grad_mixed(const Bin &B, const GradExtra &G
         const float tpf = TWO_PI_F * f_ * fstarf;
         dph_l[s] = tpf * dkP_l;
         dph_b[s] = tpf * dkP_b;
-        const float gfk = fmaf(Gx.gf1, x, Gx.gf0);
+        const float gfk = THIRD ? fmaf(Gx.gf1, x, Gx.gf0) * dop[s] : fmaf(Gx.gf1, x, Gx.gf0);
         dfo_l[s] = gfk * dkP_l;
         dfo_b[s] = gfk * dkP_b;
     }
@@ -178,6 +195,8 @@ __device__ __forceinline__ void slow_grad_mixed(const Bin &B, const GradExtra &G
     const int arm[6] = {0, 1, 2, 0, 1, 2};
     const int sc[6] = {0, 1, 2, 1, 2, 0};
     const float sg[6] = {1.f, 1.f, 1.f, -1.f, -1.f, -1.f};
+    float2 zg[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    float2 zgd[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
 #pragma unroll
     for (int q = 0; q < 6; q++) {
         const int s = sc[q], a = arm[q];
@@ -205,6 +224,10 @@ __device__ __forceinline__ void slow_grad_mixed(const Bin &B, const GradExtra &G
         const float2 ZG = cmul(Z, G);
         const float2 ZdG = cmul(Zd, G);
         const float dl = dS / S;
+        if (THIRD) {
+            zg[s] = cadd(zg[s], ZG);
+            zgd[s] = cadd(zgd[s], make_float2(hh * fmaf(dl, ZG.x, ZG.y), hh * fmaf(dl, ZG.y, -ZG.x)));
+        }
         // plus / cross parts
         acc[0] = fmaf(pp, ZgE.x, acc[0]);
         acc[1] = fmaf(pp, ZgE.y, acc[1]);
@@ -213,7 +236,8 @@ __device__ __forceinline__ void slow_grad_mixed(const Bin &B, const GradExtra &G
         // (dl da - i (da + dph)) ZG + dOmL ZdG for the frequency parameters
         {
             const float x = xi[s];
-            const float d0 = hh * ifs, d1 = hh * x * ifs, d2 = 0.5f * hh * x * x * ifs;
+            const float hd = THIRD ? hh * dop[s] : hh;
+            const float d0 = hd * ifs, d1 = hd * x * ifs, d2 = 0.5f * hd * x * x * ifs;
             const float p0 = -TWO_PI_F * x, p1 = -PI_F * x * x, p2 = -(PI_F / 3.0f) * x * x * x;
             float al, be;
             al = dl * d0; be = d0 + p0;
@@ -243,6 +267,100 @@ __device__ __forceinline__ void slow_grad_mixed(const Bin &B, const GradExtra &G
             al = dl * dd_b; be = dd_b + dph_b[s];
             acc[12] = fmaf(al, ZG.x, fmaf(be, ZG.y, fmaf(dpp_b, ZgDP.x, fmaf(dcc_b, ZgDC.x, acc[12]))));
             acc[13] = fmaf(al, ZG.y, fmaf(-be, ZG.x, fmaf(dpp_b, ZgDP.y, fmaf(dcc_b, ZgDC.y, acc[13]))));
+        }
+    }
+    if (THIRD) {
+#pragma unroll
+        for (int s = 0; s < 3; s++) {
+            cph[s] = make_float2(zg[s].y, -zg[s].x);
+            cfo[s] = zgd[s];
+        }
+    }
+}
+
+// Adjoint of the third body's cumulative Doppler phase and of v_LOS at
+// sample k (all three spacecraft).  With psi_n = (pi/c) sum_{m=1..n}
+// dxi_m (g_{m-1} + g_m), g = v_LOS f_GW, dxi_m = xi_m - xi_{m-1}, and
+// R_k = sum_{n>=k} cph_n (the suffix sums), the phase enters as -psi, so
+//   sum_n cph_n d(-psi_n) = -(pi/c) sum_k [W_k dg_k + H_k dxi_k],
+//   W_k = R_k dxi_k + R_{k+1} dxi_{k+1},  H_k = R_k (g_{k-1} + g_k) - R_{k+1} (g_k + g_{k+1})
+// (terms outside 1 <= m <= N-1 dropped).  v_LOS also scales fonfs by
+// (1 + v/c): sum cfo_k fo_base/c dv_k.  Accumulates into the f0, fdot,
+// fddot, lam, beta slots (acc[4..13] of the 7-accumulator block) and the
+// five third-body slots t5[10] (A2, varpi, e2, P2, T2).
+__device__ __forceinline__ void third_grad_sample(const Bin &B, const GradExtra &Gx, int k, int N,
+                                                  int lg, double step, const double *__restrict__ tab,
+                                                  float ifs, const float2 *Rrow0, const float *grow0,
+                                                  const float2 cfo[3], float acc[14], float t5[10])
+{
+    const float *tabf = reinterpret_cast<const float *>(tab + (size_t)18 * N);
+    const double tmk = (double)k * step;
+    const float cpsi = -(float)(kPi / kCSI);
+    const float ic = (float)(1.0 / kCSI);
+#pragma unroll
+    for (int s = 0; s < 3; s++) {
+        const float2 *Rrow = Rrow0 + (size_t)s * N;
+        const float *grow = grow0 + (size_t)s * N;
+        const double *t0 = tab + (size_t)(3 * s) * N;
+        const double kPk = B.k[0] * __ldg(t0 + k) + B.k[1] * __ldg(t0 + N + k) +
+                           B.k[2] * __ldg(t0 + 2 * N + k);
+        const double xi = tmk - kPk;
+        float dv[6];
+        const float v = vlos_grad_mixed(xi, B, Gx.cosvarpi, Gx.P2yr, dv);
+        const float xf = (float)xi;
+        const float fgw = fmaf(fmaf(0.5f * B.fddotf, xf, B.fdotf), xf, B.f0f);
+        const float fgwd = fmaf(B.fddotf, xf, B.fdotf);
+        const float gk = grow[k];
+        float2 W = {0.f, 0.f}, H = {0.f, 0.f};
+        if (k >= 1) {
+            const double kPm = B.k[0] * __ldg(t0 + k - 1) + B.k[1] * __ldg(t0 + N + k - 1) +
+                               B.k[2] * __ldg(t0 + 2 * N + k - 1);
+            const float dxi = (float)(step - (kPk - kPm));
+            const float2 R = Rrow[swz(k, lg)];
+            const float gs = grow[k - 1] + gk;
+            W = make_float2(R.x * dxi, R.y * dxi);
+            H = make_float2(R.x * gs, R.y * gs);
+        }
+        if (k <= N - 2) {
+            const double kPp = B.k[0] * __ldg(t0 + k + 1) + B.k[1] * __ldg(t0 + N + k + 1) +
+                               B.k[2] * __ldg(t0 + 2 * N + k + 1);
+            const float dxi = (float)(step - (kPp - kPk));
+            const float2 R = Rrow[swz(k + 1, lg)];
+            const float gs = gk + grow[k + 1];
+            W = make_float2(fmaf(R.x, dxi, W.x), fmaf(R.y, dxi, W.y));
+            H = make_float2(fmaf(-R.x, gs, H.x), fmaf(-R.y, gs, H.y));
+        }
+        // f0, fdot, fddot: dg = v {1, xi, xi^2/2}
+        const float wv = cpsi * v;
+        const float w1 = wv * xf, w2 = 0.5f * wv * xf * xf;
+        acc[4] = fmaf(wv, W.x, acc[4]);
+        acc[5] = fmaf(wv, W.y, acc[5]);
+        acc[6] = fmaf(w1, W.x, acc[6]);
+        acc[7] = fmaf(w1, W.y, acc[7]);
+        acc[8] = fmaf(w2, W.x, acc[8]);
+        acc[9] = fmaf(w2, W.y, acc[9]);
+        // sky angles: dxi = -dkP, dg = g' dxi, dv = v' dxi
+        const float cv = fgw * ifs * ic;                 // d fonfs / d v = fo_base / c
+        const float gd = fmaf(dv[5], fgw, v * fgwd);
+        const float q5 = cv * dv[5];
+        const float2 Q = make_float2(-cpsi * fmaf(W.x, gd, H.x) - q5 * cfo[s].x,
+                                     -cpsi * fmaf(W.y, gd, H.y) - q5 * cfo[s].y);
+        const float P0 = __ldg(tabf + (size_t)(9 + 3 * s) * N + k);
+        const float P1 = __ldg(tabf + (size_t)(9 + 3 * s + 1) * N + k);
+        const float P2 = __ldg(tabf + (size_t)(9 + 3 * s + 2) * N + k);
+        const float dkP_l = Gx.st * fmaf(Gx.v[0], P0, Gx.v[1] * P1);
+        const float dkP_b = fmaf(Gx.u[0], P0, fmaf(Gx.u[1], P1, Gx.u[2] * P2));
+        acc[10] = fmaf(Q.x, dkP_l, acc[10]);
+        acc[11] = fmaf(Q.y, dkP_l, acc[11]);
+        acc[12] = fmaf(Q.x, dkP_b, acc[12]);
+        acc[13] = fmaf(Q.y, dkP_b, acc[13]);
+        // third-body parameters: dg = f_GW dv, d fonfs = fo_base/c dv
+        const float wf = cpsi * fgw;
+        const float2 Tc = make_float2(fmaf(wf, W.x, cv * cfo[s].x), fmaf(wf, W.y, cv * cfo[s].y));
+#pragma unroll
+        for (int j = 0; j < 5; j++) {
+            t5[2 * j] = fmaf(Tc.x, dv[j], t5[2 * j]);
+            t5[2 * j + 1] = fmaf(Tc.y, dv[j], t5[2 * j + 1]);
         }
     }
 }
@@ -327,14 +445,25 @@ __device__ __forceinline__ void fft_dit(typename C2<R>::T *buf, int nsub, int lg
 
 struct GradParams {
     KParams K;
-    double *grad;                  // (9, num_bin) FP64, the params layout
+    double *grad;                  // (nparams, num_bin) FP64, the params layout
 };
 
-constexpr int kGradAcc = 19;       // ll terms 3, Qf 2, 7 complex accumulators 14
+// accumulators per thread: ll terms 3, Qf 2, 7 complex (P, C, f0, fdot, fddot,
+// lam, beta) 14; the third body adds 5 complex (A2, varpi, e2, P2, T2)
+template <bool THIRD> __host__ __device__ constexpr int grad_acc() { return THIRD ? 29 : 19; }
 
-__global__ void __launch_bounds__(kBlock, 2) grad_kernel(const GradParams GP)
+// shared memory of a grad_kernel tile of maxS samples
+__host__ __device__ constexpr size_t grad_smem_bytes(bool third, int maxS)
+{
+    return (sizeof(Bin) + sizeof(GradExtra)) * kMaxPack + sizeof(double) * (third ? 29 : 19) * 16 +
+           (size_t)maxS * (6 * sizeof(float2) + (third ? 3 * (sizeof(double) + 2 * sizeof(float)) : 0));
+}
+
+template <bool THIRD>
+__global__ void __launch_bounds__(kBlock, THIRD ? 1 : 2) grad_kernel(const GradParams GP)
 {
     using V = float2;
+    constexpr int kGradAcc = grad_acc<THIRD>();
     const KParams &K = GP.K;
     extern __shared__ __align__(16) unsigned char smem[];
     Bin *bins = reinterpret_cast<Bin *>(smem);
@@ -343,6 +472,10 @@ __global__ void __launch_bounds__(kBlock, 2) grad_kernel(const GradParams GP)
     V *buf = reinterpret_cast<V *>(smem + (sizeof(Bin) + sizeof(GradExtra)) * kMaxPack +
                                    sizeof(double) * kGradAcc * 16);
     V *es = buf + 3 * (size_t)K.maxS;             // exp(-i phase_s) per sample, from the forward pass
+    // third body: cumulative phase, v_LOS and g = v_LOS f_GW per (sample, spacecraft)
+    double *psi = reinterpret_cast<double *>(es + 3 * (size_t)K.maxS);
+    float *vl = reinterpret_cast<float *>(psi + 3 * (size_t)K.maxS);
+    float *gq = vl + 3 * (size_t)K.maxS;
     __shared__ int s_tile;
 
     const gbx_wave_args &a = K.a;
@@ -390,13 +523,23 @@ __global__ void __launch_bounds__(kBlock, 2) grad_kernel(const GradParams GP)
         __syncthreads();
         const int S = cnt << lg;
         const dfl stepd = K.stepd[lg];
+        const double step = a.T * exp2_int(-lg);
+        if (THIRD) third_prepass<float>(bins, tab, cnt, lg, step, psi, vl, reinterpret_cast<double *>(buf), gq);
 
         // forward slow part and FFT
         for (int m = tid; m < S; m += kBlock) {
             const int p = m >> lg, n = m & (N - 1);
             float2 o[3];
-            slow_mixed<false, true>(bins[p], n, N, stepd, tab, nullptr, nullptr, o,
-                                    es + 3 * (size_t)m);
+            double ps[3] = {0.0, 0.0, 0.0};
+            float vv[3] = {0.f, 0.f, 0.f};
+            if (THIRD) {
+#pragma unroll
+                for (int s = 0; s < 3; s++) {
+                    ps[s] = psi[(p * 3 + s) * N + n];
+                    vv[s] = vl[(p * 3 + s) * N + n];
+                }
+            }
+            slow_mixed<THIRD, true>(bins[p], n, N, stepd, tab, ps, vv, o, es + 3 * (size_t)m);
 #pragma unroll
             for (int c = 0; c < 3; c++) buf[(p * 3 + c) * N + swz(n, lg)] = o[c];
         }
@@ -470,12 +613,63 @@ __global__ void __launch_bounds__(kBlock, 2) grad_kernel(const GradParams GP)
             if (B.valid) {
                 for (int n = i0; n < N; n += Tpb) {
                     float2 Yc[3], Es[3];
+                    float2 *ep = es + 3 * ((size_t)(p << lg) + n);
 #pragma unroll
                     for (int c = 0; c < 3; c++) {
                         Yc[c] = buf[(p * 3 + c) * N + swz(n, lg)];
-                        Es[c] = es[3 * ((size_t)(p << lg) + n) + c];
+                        Es[c] = ep[c];
                     }
-                    slow_grad_mixed(B, Gx, n, N, stepd, tab, ifs, fstarf, Yc, Es, acc + 5);
+                    if (THIRD) {
+                        // cph replaces Y and cfo replaces exp(-i phase) in this thread's own slots
+                        float vv[3];
+                        float2 cph[3], cfo[3];
+#pragma unroll
+                        for (int s = 0; s < 3; s++) vv[s] = vl[(p * 3 + s) * N + n];
+                        slow_grad_mixed<true>(B, Gx, n, N, stepd, tab, ifs, fstarf, Yc, Es, acc + 5,
+                                              vv, cph, cfo);
+#pragma unroll
+                        for (int s = 0; s < 3; s++) {
+                            buf[(p * 3 + s) * N + swz(n, lg)] = cph[s];
+                            ep[s] = cfo[s];
+                        }
+                    } else {
+                        slow_grad_mixed<false>(B, Gx, n, N, stepd, tab, ifs, fstarf, Yc, Es, acc + 5);
+                    }
+                }
+            }
+        }
+        if (THIRD) {
+            __syncthreads();
+            // suffix sums R_k = sum_{n >= k} cph_n along every (binary, spacecraft) row
+            const int warp = tid >> 5, lane = tid & 31;
+            const int chunk = N >> 5;
+            for (int row = warp; row < 3 * cnt; row += kBlock / 32) {
+                V *rp = buf + (size_t)row * N;
+                const int c0 = lane * chunk;
+                float2 t = {0.f, 0.f};
+                for (int c = 0; c < chunk; c++) t = cadd(t, rp[swz(c0 + c, lg)]);
+                float2 incl = t;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    float2 y = make_float2(__shfl_down_sync(0xffffffffu, incl.x, o),
+                                           __shfl_down_sync(0xffffffffu, incl.y, o));
+                    if (lane + o < 32) incl = cadd(incl, y);
+                }
+                float2 run = csub(incl, t);
+                for (int c = chunk - 1; c >= 0; c--) {
+                    run = cadd(run, rp[swz(c0 + c, lg)]);
+                    rp[swz(c0 + c, lg)] = run;
+                }
+            }
+            __syncthreads();
+            if (p < cnt && bins[p].valid) {
+                const Bin &B = bins[p];
+                const GradExtra &Gx = gxs[p];
+                for (int k = i0; k < N; k += Tpb) {
+                    const float2 *cf = es + 3 * ((size_t)(p << lg) + k);
+                    const float2 cfo[3] = {cf[0], cf[1], cf[2]};
+                    third_grad_sample(B, Gx, k, N, lg, step, tab, ifs, buf + (size_t)(p * 3) * N,
+                                      gq + (size_t)(p * 3) * N, cfo, acc + 5, acc + 19);
                 }
             }
         }
@@ -538,6 +732,13 @@ __global__ void __launch_bounds__(kBlock, 2) grad_kernel(const GradParams GP)
 #pragma unroll
                 for (int k = 0; k < 9; k++)
                     GP.grad[(size_t)k * (size_t)nb + B.b] = B.valid ? g9[k] : 0.0;
+                if (THIRD) {
+#pragma unroll
+                    for (int j = 0; j < 5; j++) {
+                        const double gj = cmul(sc, make_double2(cu * t[19 + 2 * j], cu * t[20 + 2 * j])).x;
+                        GP.grad[(size_t)(9 + j) * (size_t)nb + B.b] = B.valid ? gj : 0.0;
+                    }
+                }
             }
         }
         __syncthreads();

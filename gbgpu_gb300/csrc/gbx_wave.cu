@@ -64,6 +64,8 @@ struct __align__(16) Bin {
     int valid;
 };
 
+static_assert(sizeof(Bin) == 512, "Bin is copied as 32 int4 per binary");
+
 struct KParams {
     gbx_wave_args a;
     // likelihood
@@ -246,7 +248,8 @@ __device__ double vlos_fp64(double t, const Bin &B)
 // Same model with the Kepler solve in FP32.  The mean anomaly and its 2 pi
 // reductions stay in FP64; since only sin/cos of the anomaly are used, the
 // un-reduction is applied modulo 2 pi, which keeps |u| <= pi in FP32.
-__device__ float vlos_mixed(double t, const Bin &B)
+// Returns the eccentric anomaly u (mod 2 pi) at mean anomaly n2 (t - T2).
+__device__ __forceinline__ float kepler_u_mixed(double t, const Bin &B)
 {
     double ld = B.n2 * (t - B.T2);
     bool neg = ld < 0.0;
@@ -279,6 +282,13 @@ __device__ float vlos_mixed(double t, const Bin &B)
     float u = u0 + u4;
     if (overpi) u = -u;
     if (neg) u = -u;
+    return u;
+}
+
+__device__ float vlos_mixed(double t, const Bin &B)
+{
+    float u = kepler_u_mixed(t, B);
+    const float e = B.e2f;
     if (e > 1e-6f) {
         float bt = (1.0f - sqrtf(1.0f - e * e)) / e;
         float su, cu;
@@ -286,6 +296,46 @@ __device__ float vlos_mixed(double t, const Bin &B)
         u += 2.0f * atan2f(bt * su, 1.0f - bt * cu);
     }
     return B.A2f * (sinf(u + B.varpif) + e * B.sinvarpif);
+}
+
+// v_LOS (as vlos_mixed) and its derivatives dv[0..4] = d/d(A2, varpi, e2,
+// P2 [yr], T2 [yr]), dv[5] = d/dt.  With c = 1 - e cos u and M = n2 (t - T2):
+// du/dM = 1/c, du/de = sin u / c (Kepler), and for the true anomaly
+// dphi/du = sqrt(1-e^2)/c, dphi/de|u = sin u / (sqrt(1-e^2) c); below
+// e = 1e-6 the model takes phi = u (gbgpu/thirdbody.py:339-350).
+// n2 = 2 pi / (P2 yr) and T2 [s] = T2 yr give dM/dP2 = -M/P2 and
+// dM/dT2 = -n2 yr = -2 pi / P2.
+__device__ float vlos_grad_mixed(double t, const Bin &B, float cosvarpi, float P2yr, float dv[6])
+{
+    const float u = kepler_u_mixed(t, B);
+    const float e = B.e2f;
+    float su, cu;
+    sincosf(u, &su, &cu);
+    const float c = 1.0f - e * cu;
+    const float ic = 1.0f / c;
+    float phi = u, dphi_dM, dphi_de;
+    if (e > 1e-6f) {
+        const float sq = sqrtf(1.0f - e * e);
+        const float bt = (1.0f - sq) / e;
+        phi += 2.0f * atan2f(bt * su, 1.0f - bt * cu);
+        dphi_dM = sq * ic * ic;
+        dphi_de = su * ic * (sq * ic + 1.0f / sq);
+    } else {
+        dphi_dM = ic;
+        dphi_de = su * ic;
+    }
+    float sp, cp;
+    sincosf(phi + B.varpif, &sp, &cp);
+    const float A = B.A2f;
+    dv[0] = sp + e * B.sinvarpif;
+    dv[1] = A * fmaf(e, cosvarpi, cp);
+    dv[2] = A * fmaf(cp, dphi_de, B.sinvarpif);
+    const float dvdM = A * cp * dphi_dM;
+    const float iP2 = 1.0f / P2yr;
+    dv[3] = dvdM * (float)(B.n2 * (t - B.T2)) * -iP2;
+    dv[4] = dvdM * (float)(-kTwoPi) * iP2;
+    dv[5] = dvdM * (float)B.n2;
+    return A * dv[0];
 }
 
 // ----------------------------------------------------------------------------
@@ -706,6 +756,80 @@ __device__ __forceinline__ double warp_sum(double v)
 // ----------------------------------------------------------------------------
 // the kernel
 // ----------------------------------------------------------------------------
+// Third-body pre-passes (gbgpu/thirdbody.py:155-226) for a tile of cnt
+// binaries with N = 2^lg samples:
+//   A) v_LOS at every (sample, spacecraft) -> vl, and g = v_LOS f_GW;
+//   B) trapezoid increments (xi_n - xi_{n-1}) (g_{n-1} + g_n) pi / c -> inc;
+//   C) their inclusive prefix sum along n -> psi (the phase added to argS).
+// inc is scratch of 3 cnt N doubles; gout, when given, receives g in FP32.
+// Called by every thread of the block (contains barriers).
+template <typename R>
+__device__ __forceinline__ void third_prepass(const Bin *bins, const double *__restrict__ tab,
+                                              int cnt, int lg, double step, double *psi, R *vl,
+                                              double *inc, float *gout)
+{
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int N = 1 << lg, S = cnt << lg;
+    for (int m = tid; m < S; m += kBlock) {
+        const int p = m >> lg, n = m & (N - 1);
+        const Bin &B = bins[p];
+        const double tm = (double)n * step;
+#pragma unroll
+        for (int s = 0; s < 3; s++) {
+            double kP = B.k[0] * __ldg(tab + (size_t)(3 * s) * N + n) +
+                        B.k[1] * __ldg(tab + (size_t)(3 * s + 1) * N + n) +
+                        B.k[2] * __ldg(tab + (size_t)(3 * s + 2) * N + n);
+            double xi = tm - kP;
+            double v = (sizeof(R) == 8) ? vlos_fp64(xi, B) : (double)vlos_mixed(xi, B);
+            double fgw = B.f0 + B.fdot * xi + 0.5 * B.fddot * xi * xi;
+            psi[(p * 3 + s) * N + n] = v * fgw;
+            vl[(p * 3 + s) * N + n] = (R)v;
+            if (gout) gout[(p * 3 + s) * N + n] = (float)(v * fgw);
+        }
+    }
+    __syncthreads();
+    for (int m = tid; m < S; m += kBlock) {
+        const int p = m >> lg, n = m & (N - 1);
+        const Bin &B = bins[p];
+#pragma unroll
+        for (int s = 0; s < 3; s++) {
+            double v = 0.0;
+            if (n > 0) {
+                double d = step;
+#pragma unroll
+                for (int c = 0; c < 3; c++)
+                    d -= B.k[c] * (__ldg(tab + (size_t)(3 * s + c) * N + n) -
+                                   __ldg(tab + (size_t)(3 * s + c) * N + n - 1));
+                // xi_n - xi_{n-1} = step - (kP_n - kP_{n-1})
+                v = d * (psi[(p * 3 + s) * N + n - 1] + psi[(p * 3 + s) * N + n]) / 2.0 *
+                    kPi * 2.0 / kCSI;
+            }
+            inc[(p * 3 + s) * N + n] = v;
+        }
+    }
+    __syncthreads();
+    // warp per (binary, spacecraft) row
+    const int chunk = N >> 5;
+    for (int row = warp; row < 3 * cnt; row += kBlock / 32) {
+        const double *src = inc + (size_t)row * N + lane * chunk;
+        double *dst = psi + (size_t)row * N + lane * chunk;
+        double t = 0.0;
+        for (int c = 0; c < chunk; c++) t += src[c];
+        double incl = t;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            double y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        double run = incl - t;
+        for (int c = 0; c < chunk; c++) {
+            run += src[c];
+            dst[c] = run;
+        }
+    }
+    __syncthreads();
+}
+
 template <typename R, int MODE, bool THIRD>
 __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(const KParams K)
 {
@@ -718,7 +842,6 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
 
     const gbx_wave_args &a = K.a;
     const int tid = threadIdx.x;
-    const int warp = tid >> 5, lane = tid & 31;
     const int ntiles = a.tiles ? a.ntiles : (a.num_bin + K.P - 1) / K.P;
     const double fstar = K.fstar;
     int iter = 0;
@@ -779,69 +902,10 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
         double *psi = nullptr;
         R *vl = nullptr;
         if (THIRD) {
-            // third-body pre-passes (gbgpu/thirdbody.py:155-226):
-            // A) v_LOS and g = v_LOS f_GW at every (sample, spacecraft)
             psi = reinterpret_cast<double *>(buf + 3 * (size_t)maxcnt * N);
             vl = reinterpret_cast<R *>(psi + 3 * (size_t)maxcnt * N);
-            double *inc = reinterpret_cast<double *>(buf);
-            for (int m = tid; m < S; m += kBlock) {
-                const int p = m >> lg, n = m & (N - 1);
-                const Bin &B = bins[p];
-                const double tm = (double)n * step;
-#pragma unroll
-                for (int s = 0; s < 3; s++) {
-                    double kP = B.k[0] * __ldg(tab + (size_t)(3 * s) * N + n) +
-                                B.k[1] * __ldg(tab + (size_t)(3 * s + 1) * N + n) +
-                                B.k[2] * __ldg(tab + (size_t)(3 * s + 2) * N + n);
-                    double xi = tm - kP;
-                    double v = (sizeof(R) == 8) ? vlos_fp64(xi, B) : (double)vlos_mixed(xi, B);
-                    double fgw = B.f0 + B.fdot * xi + 0.5 * B.fddot * xi * xi;
-                    psi[(p * 3 + s) * N + n] = v * fgw;
-                    vl[(p * 3 + s) * N + n] = (R)v;
-                }
-            }
-            __syncthreads();
-            // B) trapezoid increments (xi_n - xi_{n-1}) (g_{n-1} + g_n) pi / c
-            for (int m = tid; m < S; m += kBlock) {
-                const int p = m >> lg, n = m & (N - 1);
-                const Bin &B = bins[p];
-#pragma unroll
-                for (int s = 0; s < 3; s++) {
-                    double v = 0.0;
-                    if (n > 0) {
-                        double d = step;
-#pragma unroll
-                        for (int c = 0; c < 3; c++)
-                            d -= B.k[c] * (__ldg(tab + (size_t)(3 * s + c) * N + n) -
-                                           __ldg(tab + (size_t)(3 * s + c) * N + n - 1));
-                        // xi_n - xi_{n-1} = step - (kP_n - kP_{n-1})
-                        v = d * (psi[(p * 3 + s) * N + n - 1] + psi[(p * 3 + s) * N + n]) / 2.0 *
-                            kPi * 2.0 / kCSI;
-                    }
-                    inc[(p * 3 + s) * N + n] = v;
-                }
-            }
-            __syncthreads();
-            // C) inclusive prefix sum along n for every (binary, spacecraft): warp per row
-            const int chunk = N >> 5;
-            for (int row = warp; row < 3 * cnt; row += kBlock / 32) {
-                const double *src = inc + (size_t)row * N + lane * chunk;
-                double *dst = psi + (size_t)row * N + lane * chunk;
-                double t = 0.0;
-                for (int c = 0; c < chunk; c++) t += src[c];
-                double incl = t;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    double y = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (lane >= o) incl += y;
-                }
-                double run = incl - t;
-                for (int c = 0; c < chunk; c++) {
-                    run += src[c];
-                    dst[c] = run;
-                }
-            }
-            __syncthreads();
+            third_prepass<R>(bins, tab, cnt, lg, step, psi, vl, reinterpret_cast<double *>(buf),
+                             nullptr);
         }
 
         // slow part -> buf[(p*3 + channel)*N + n]
@@ -1455,7 +1519,8 @@ extern "C" int gbx_waveform_ll_grad(const gbx_wave_args *a, const gbx_ll_args *l
     int rc = check_wave(&b, &maxS);
     if (rc) return rc;
     if (b.precision != GBX_MIXED) return set_error(GBX_ERR_UNSUPPORTED, "gradients are computed in the mixed form only");
-    if (b.nparams != 9) return set_error(GBX_ERR_UNSUPPORTED, "gradients cover the 9-parameter circular model");
+    if (b.nparams != 9 && b.nparams != 14)
+        return set_error(GBX_ERR_UNSUPPORTED, "gradients cover the 9-parameter model and the 14-parameter third-body model");
     if (!ws || ((uintptr_t)ws & 15) != 0 || wsb < gbx_grad_workspace_bytes(b.num_bin))
         return set_error(GBX_ERR_ARG, "gradients need a 16-byte aligned workspace of gbx_grad_workspace_bytes(num_bin)");
     if (!l || !l->A_data || !l->E_data || !l->A_psd || !l->E_psd || !d_h || !h_h || !grad)
@@ -1486,16 +1551,17 @@ extern "C" int gbx_waveform_ll_grad(const gbx_wave_args *a, const gbx_ll_args *l
     K.h_h = (double2 *)h_h;
     K.maxS = maxS;
     G.grad = grad;
-    const size_t sm = (sizeof(Bin) + sizeof(GradExtra)) * kMaxPack + sizeof(double) * kGradAcc * 16 +
-                      6 * (size_t)maxS * sizeof(float2);
+    const bool third = b.nparams == 14;
+    auto kern = third ? grad_kernel<true> : grad_kernel<false>;
+    const size_t sm = grad_smem_bytes(third, maxS);
     if (sm > 227 * 1024) return set_error(GBX_ERR_UNSUPPORTED, "tile needs %zu B of shared memory", sm);
-    cudaError_t e = cudaFuncSetAttribute(grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(grad)");
-    e = cudaFuncSetAttribute(grad_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                              cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(grad carveout)");
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grad_kernel, kBlock, sm);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, sm);
     if (e != cudaSuccess) return cuda_error(e, "occupancy(grad)");
     if (per_sm < 1) per_sm = 1;
     const int ntiles = b.tiles ? b.ntiles : (b.num_bin + K.P - 1) / K.P;
@@ -1512,7 +1578,7 @@ extern "C" int gbx_waveform_ll_grad(const gbx_wave_args *a, const gbx_ll_args *l
     prep_grad_kernel<<<(b.num_bin + kPrepBlock - 1) / kPrepBlock, kPrepBlock, psm, st>>>(K);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_error(e, "prep_grad_kernel launch");
-    grad_kernel<<<grid, kBlock, sm, st>>>(G);
+    kern<<<grid, kBlock, sm, st>>>(G);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_error(e, "grad_kernel launch");
     return GBX_OK;

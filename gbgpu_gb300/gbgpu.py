@@ -517,11 +517,12 @@ class GBGPUBase(abc.ABC):
                     noise_index=None, **kwargs):
         """Log-likelihood and its gradient in one fused launch (mixed form).
 
-        Returns ``(like, grad)``: NumPy ``(B,)`` and ``(9, B)`` with
+        Returns ``(like, grad)``: NumPy ``(B,)`` and ``(NPARAMS, B)`` with
         ``grad[k, b] = d like[b] / d params[k, b]`` for amp, f0, fdot, fddot,
-        phi0, iota, psi, lam, beta.  No counterpart in the reference (its
-        derivatives are finite differences, gbgpu.py:957-1138).  Set
-        ``return_tensors=True`` to get device tensors instead.
+        phi0, iota, psi, lam, beta (and, for GBGPUThirdBody, A2, varpi, e2,
+        P2, T2).  No counterpart in the reference (its derivatives are finite
+        differences, gbgpu.py:957-1138).  Set ``return_tensors=True`` to get
+        device tensors instead.
         """
         like, grad = self._ll_grad_tensors(params, data, psd, start_freq_ind, data_index,
                                            noise_index, **kwargs)
@@ -542,15 +543,17 @@ class GBGPUBase(abc.ABC):
         tdi2 = kwargs.pop("tdi2", False)
         if kwargs:
             raise TypeError(f"unexpected keyword arguments {list(kwargs)}")
-        if self.NPARAMS != 9:
-            raise NotImplementedError("gradients cover the 9-parameter circular model")
         T = int(T / dt) * dt
         self._check_T(T)
         prm = _to_device(params, torch.float64, self.device).detach().contiguous()
-        if prm.ndim != 2 or prm.shape[0] != 9:
-            raise ValueError("params must be (9, B)")
+        npar = self.NPARAMS
+        if prm.ndim != 2 or prm.shape[0] != npar:
+            raise ValueError(f"params must be ({npar}, B)")
+        extra = [prm[i] for i in range(9, npar)]
+        if extra:
+            self.prepare_additional_args(*extra)
         if N is None:
-            N = self._resolve_N(N, prm[0], prm[1], T, (), oversample)
+            N = self._resolve_N(N, prm[0], prm[1], T, extra, oversample)
         elif np.ndim(N) != 0:
             N = np.asarray(_to_host(N), dtype=np.int64).reshape(-1)
         else:
@@ -560,9 +563,9 @@ class GBGPUBase(abc.ABC):
         dd, pp, L, di, ni = self._prepare_data(data, psd, data_index, noise_index, B)
         d_h = torch.empty(B, dtype=torch.complex128, device=self.device)
         h_h = torch.empty(B, dtype=torch.complex128, device=self.device)
-        grad = torch.zeros((9, B), dtype=torch.float64, device=self.device)
+        grad = torch.zeros((npar, B), dtype=torch.float64, device=self.device)
         if B:
-            plan = self._plan(N, T, "mixed", tdi2, 9)
+            plan = self._plan(N, T, "mixed", tdi2, npar)
             self._status.zero_()
             a = plan.args(prm, start_freq_ind, self._status, grad=True)
             la = nat.LLArgs()

@@ -1,13 +1,15 @@
-"""Gradient kernel (gbx_waveform_ll_grad) against FP64 finite differences.
+"""Gradient kernel (gbx_waveform_ll_grad) against FP64 references.
 
-The reference has no gradients; the check is the five-point central
-difference (relative step 1e-7 -- for fddot a step moving its phase term by
-1e-4 rad -- with the stencil of the reference's
-information_matrix, gbgpu.py:1108-1110) of the plain FP64 fused likelihood,
-which itself matches the reference's likelihood to 1e-10.  Tolerance:
-|g - g_fd| <= 2e-3 |g_fd| + 2e-3 rms_b(g_fd) per parameter, covering the mixed
-form's ~1e-6 relative template error amplified by cancellation in the
-residual and the stencil's truncation error.
+The reference has no gradients; the checks are (1) the forward-mode FP64
+gradient of the torch restatement (oracle/fastgb_torch.py, torch.func.jvp)
+and (2) the five-point central difference (relative step 1e-7 -- for fddot a
+step moving its phase term by 1e-4 rad -- with the stencil of the
+reference's information_matrix, gbgpu.py:1108-1110) of the plain FP64 fused
+likelihood, which itself matches the reference's likelihood to 1e-10.
+Tolerance: |g - g_ref| <= 2e-3 |g_ref| + 2e-3 rms_b(g_ref) per parameter,
+covering the mixed form's ~1e-6 relative template error amplified by
+cancellation in the residual and the stencil's truncation error.  The
+third-body model (14 parameters) is checked the same way.
 """
 
 import numpy as np
@@ -21,8 +23,8 @@ pytestmark = pytest.mark.gpu
 T_OBS = 4 * 31557600.0
 
 
-def _case(B, N, seed, dt=10.0, tdi2=False):
-    from gbgpu_gb300 import GBGPU
+def _case(B, N, seed, dt=10.0, tdi2=False, third=False):
+    from gbgpu_gb300 import GBGPU, GBGPUThirdBody
     from gbgpu_gb300.sensitivity import A1TDISens
     rng = np.random.default_rng(seed)
     T = int(T_OBS / dt) * dt
@@ -32,11 +34,17 @@ def _case(B, N, seed, dt=10.0, tdi2=False):
                       np.arccos(rng.uniform(-0.9, 0.9, B)), rng.uniform(0.3, 2.8, B),
                       rng.uniform(0.5, 5.5, B), np.arcsin(rng.uniform(-0.9, 0.9, B))])
     truth[3] = 11 / 3 * truth[2] ** 2 / truth[1]
+    if third:
+        # A2 [m/s], varpi, e2, P2 [yr], T2 [yr]: a Doppler phase of O(1) rad
+        P2 = 10 ** rng.uniform(0.3, 1.0, B)
+        truth = np.concatenate([truth, np.array([10 ** rng.uniform(0.5, 1.5, B),
+                                                 rng.uniform(0.3, 6.0, B), rng.uniform(0.1, 0.8, B),
+                                                 P2, rng.uniform(0.1, 0.9, B) * P2])])
     si = O.start_indices(truth[1], N, T, dt)
     s0 = int(si.min()) - N
     L = int(si.max()) + 2 * N - s0
     S = A1TDISens.get_Sn((np.arange(L) + s0) / T)
-    gb = GBGPU(precision="fp64")
+    gb = GBGPUThirdBody(precision="fp64") if third else GBGPU(precision="fp64")
     tmpl = torch.zeros((1, 2, L), dtype=torch.complex128, device="cuda")
     gb.generate_global_template(truth.T, np.zeros(B, np.int32), tmpl, N=N, T=T_OBS, dt=dt,
                                 tdi2=tdi2, start_freq_ind=s0)
@@ -50,12 +58,18 @@ def _case(B, N, seed, dt=10.0, tdi2=False):
     ev[2] *= 1 + rng.uniform(-0.05, 0.05, B)
     for k in (4, 5, 6, 7, 8):
         ev[k] += rng.uniform(-0.02, 0.02, B)
+    if third:
+        ev[9] *= 1 + rng.uniform(-0.05, 0.05, B)
+        ev[10] += rng.uniform(-0.05, 0.05, B)
+        ev[11] += rng.uniform(-0.02, 0.02, B)
+        ev[12] *= 1 + rng.uniform(-0.02, 0.02, B)
+        ev[13] += rng.uniform(-0.02, 0.02, B)
     return gb, ev, data, torch.as_tensor(S, device="cuda"), s0, dt
 
 
 def _fd(gb, p, data, Sd, s0, N, dt, tdi2):
     out = np.zeros_like(p)
-    for k in range(9):
+    for k in range(p.shape[0]):
         h = 1e-7 * np.maximum(np.abs(p[k]), 1.0 if k >= 4 else 0.0)
         if k == 3:
             # a relative step of fddot (~1e-31) moves logL by ~1e-11, at FP64
@@ -111,3 +125,44 @@ def test_gradient_uneven_N_and_autograd():
     np.testing.assert_allclose(pt.grad.cpu().numpy(), grad * w.cpu().numpy()[None, :],
                                rtol=1e-12, atol=0)
     np.testing.assert_allclose(ll.detach().cpu().numpy(), like, rtol=1e-12, atol=1e-9)
+
+
+NAMES14 = ["amp", "f0", "fdot", "fddot", "phi0", "iota", "psi", "lam", "beta",
+           "A2", "varpi", "e2", "P2", "T2"]
+
+
+def _check(grad, ref, tol=2e-3):
+    for k in range(ref.shape[0]):
+        rms = np.sqrt(np.mean(ref[k] ** 2))
+        err = np.abs(grad[k] - ref[k])
+        bad = err > tol * np.abs(ref[k]) + tol * rms
+        assert not np.any(bad), (NAMES14[k], np.max(err / (np.abs(ref[k]) + rms)))
+
+
+def _forward_mode(p, data, Sd, s0, N, dt, tdi2):
+    import fastgb_torch as FT
+    d = [x.cpu().numpy() for x in data]
+    S = Sd.cpu().numpy()
+    third = p[9:] if p.shape[0] > 9 else None
+    return FT.forward_gradient(p[:9], d, [S, S], N, T_OBS, dt, tdi2=tdi2, third=third,
+                               start_freq_ind=s0)
+
+
+@pytest.mark.parametrize("N,tdi2", [(256, True), (512, False)])
+def test_gradient_matches_forward_mode(N, tdi2):
+    gb, p, data, Sd, s0, dt = _case(16, N, 90 + N, tdi2=tdi2)
+    gb.d_d = 0.0
+    _, grad = gb.get_ll_grad(p, data, [Sd, Sd], N=N, T=T_OBS, dt=dt, tdi2=tdi2, start_freq_ind=s0)
+    _check(grad, _forward_mode(p, data, Sd, s0, N, dt, tdi2))
+
+
+@pytest.mark.parametrize("N", [256, 512])
+def test_third_body_gradient(N):
+    gb, p, data, Sd, s0, dt = _case(16, N, 120 + N, dt=5.0, third=True)
+    gb.d_d = 0.0
+    like, grad = gb.get_ll_grad(p, data, [Sd, Sd], N=N, T=T_OBS, dt=dt, start_freq_ind=s0)
+    assert grad.shape == (14, 16)
+    _check(grad, _forward_mode(p, data, Sd, s0, N, dt, False))
+    _check(grad, _fd(gb, p, data, Sd, s0, N, dt, False))
+    like_m = gb.get_ll(p, data, [Sd, Sd], N=N, T=T_OBS, dt=dt, start_freq_ind=s0, precision="mixed")
+    np.testing.assert_allclose(like, like_m, rtol=1e-12, atol=1e-9)
