@@ -455,7 +455,7 @@ template <bool THIRD> __host__ __device__ constexpr int grad_acc() { return THIR
 // shared memory of a grad_kernel tile of maxS samples
 __host__ __device__ constexpr size_t grad_smem_bytes(bool third, int maxS)
 {
-    return (sizeof(Bin) + sizeof(GradExtra)) * kMaxPack + sizeof(double) * (third ? 29 : 19) * 16 +
+    return (sizeof(Bin) + sizeof(GradExtra)) * kMaxPack + sizeof(double) * (third ? 29 : 19) * 32 +
            (size_t)maxS * (6 * sizeof(float2) + (third ? 3 * (sizeof(double) + 2 * sizeof(float)) : 0));
 }
 
@@ -469,8 +469,9 @@ __global__ void __launch_bounds__(kBlock, THIRD ? 1 : 2) grad_kernel(const GradP
     Bin *bins = reinterpret_cast<Bin *>(smem);
     GradExtra *gxs = reinterpret_cast<GradExtra *>(smem + sizeof(Bin) * kMaxPack);
     double *red = reinterpret_cast<double *>(smem + (sizeof(Bin) + sizeof(GradExtra)) * kMaxPack);
+    // red: group partial sums (float pairs) and per-binary FP64 sums, 16 x kGradAcc each
     V *buf = reinterpret_cast<V *>(smem + (sizeof(Bin) + sizeof(GradExtra)) * kMaxPack +
-                                   sizeof(double) * kGradAcc * 16);
+                                   sizeof(double) * kGradAcc * 32);
     V *es = buf + 3 * (size_t)K.maxS;             // exp(-i phase_s) per sample, from the forward pass
     // third body: cumulative phase, v_LOS and g = v_LOS f_GW per (sample, spacecraft)
     double *psi = reinterpret_cast<double *>(es + 3 * (size_t)K.maxS);
@@ -559,8 +560,7 @@ __global__ void __launch_bounds__(kBlock, THIRD ? 1 : 2) grad_kernel(const GradP
             const Bin &B = bins[p];
             bool out = false;
             // scale 2^eD as a float complex: h in the data's scaled units
-            const float2 sc = make_float2((float)(B.scale.x * exp2_int(B.eD)),
-                                          (float)(B.scale.y * exp2_int(B.eD)));
+            const float2 sc = make_float2(d2f_scaled(B.scale.x, B.eD), d2f_scaled(B.scale.y, B.eD));
             for (int i = i0; i < N; i += Tpb) {
                 const int j = B.start + i;
                 const int pos = bitrev((i + (N >> 1)) & (N - 1), lg);
@@ -673,72 +673,79 @@ __global__ void __launch_bounds__(kBlock, THIRD ? 1 : 2) grad_kernel(const GradP
                 }
             }
         }
-        // group trees (float pairs), then FP64 across groups
-        double gsum[kGradAcc];
-#pragma unroll
-        for (int k = 0; k < kGradAcc; k++) {
-            dfl x = {acc[k], 0.f};
-            for (int o = width >> 1; o > 0; o >>= 1) {
-                dfl y = {__shfl_xor_sync(0xffffffffu, x.h, o), __shfl_xor_sync(0xffffffffu, x.l, o)};
-                x = df_add(x, y);
-            }
-            gsum[k] = (double)x.h + (double)x.l;
-        }
-        if ((tid & (width - 1)) == 0) {
+        // Reduction: float-pair trees within groups of `width` lanes; group
+        // leaders store the pairs; then one thread per (binary, accumulator)
+        // adds its groups and converts to FP64 once, and one thread per
+        // (binary, output) forms the result.  Spreading the FP64 work over
+        // lanes keeps it off the critical path (the FP64 pipe issues a warp
+        // instruction per 64 cycles per SM sub-partition, whatever the mask).
+        float2 *red2 = reinterpret_cast<float2 *>(red);
+        double *tsum = red + kGradAcc * 16;
+        {
+            const bool leader = (tid & (width - 1)) == 0;
             const int g = tid / width;
 #pragma unroll
-            for (int k = 0; k < kGradAcc; k++) red[kGradAcc * g + k] = gsum[k];
+            for (int k = 0; k < kGradAcc; k++) {
+                dfl x = {acc[k], 0.f};
+                for (int o = width >> 1; o > 0; o >>= 1) {
+                    dfl y = {__shfl_xor_sync(0xffffffffu, x.h, o), __shfl_xor_sync(0xffffffffu, x.l, o)};
+                    x = df_add(x, y);
+                }
+                if (leader) red2[kGradAcc * g + k] = make_float2(x.h, x.l);
+            }
         }
         __syncthreads();
-        if (tid < cnt) {
-            const Bin &B = bins[tid];
-            const GradExtra &Gx = gxs[tid];
+        {
             const int per = Tpb / width;
-            double t[kGradAcc];
-#pragma unroll
-            for (int k = 0; k < kGradAcc; k++) t[k] = 0.0;
-            for (int g = tid * per; g < (tid + 1) * per; g++)
-#pragma unroll
-                for (int k = 0; k < kGradAcc; k++) t[k] += red[kGradAcc * g + k];
-            const double s4 = 4.0 * K.df;
-            const double cd = s4 * exp2_int(B.eS - B.eD);
-            const double ch = s4 * exp2_int(B.eS) * (B.scale.x * B.scale.x + B.scale.y * B.scale.y);
-            const double2 dh = cmul(make_double2(cd * t[0], cd * t[1]), B.scale);
-            const double2 hv = make_double2(ch * t[2], 0.0);
-            // weights were 4 df r / S in units of 2^(eS - eD): cu converts sums of w
-            const double cu = s4 * exp2_int(B.eS - B.eD);
-            const double2 sc = B.scale;
-            const double2 Qf = make_double2(cu * t[3], cu * t[4]);
-            const double2 QP = make_double2(cu * t[5], cu * t[6]);
-            const double2 QC = make_double2(cu * t[7], cu * t[8]);
-            const double2 scQf = cmul(sc, Qf);
-            const double nb = a.num_bin;
-            double g9[9];
-            const double *pr = a.params;
-            const double amp = pr[B.b];
-            g9[0] = scQf.x / amp;                                      // amp
-            g9[1] = cmul(sc, make_double2(cu * t[9], cu * t[10])).x +   // f0
-                    cmul(Gx.dlnsc_f0, scQf).x;
-            g9[2] = cmul(sc, make_double2(cu * t[11], cu * t[12])).x;  // fdot
-            g9[3] = cmul(sc, make_double2(cu * t[13], cu * t[14])).x;  // fddot
-            g9[4] = -scQf.y;                                           // phi0: Re(i sc Qf)
-            g9[5] = cmul(sc, cadd(cmul(Gx.dDPi, QP), cmul(Gx.dDCi, QC))).x;   // iota
-            g9[6] = cmul(sc, cadd(cmul(Gx.dDPp, QP), cmul(Gx.dDCp, QC))).x;   // psi
-            g9[7] = cmul(sc, make_double2(cu * t[15], cu * t[16])).x;  // lam
-            g9[8] = cmul(sc, make_double2(cu * t[17], cu * t[18])).x;  // beta
-            if (B.b >= 0) {
-                K.d_h[B.b] = B.valid ? dh : make_double2(0.0, 0.0);
-                K.h_h[B.b] = B.valid ? hv : make_double2(0.0, 0.0);
-#pragma unroll
-                for (int k = 0; k < 9; k++)
-                    GP.grad[(size_t)k * (size_t)nb + B.b] = B.valid ? g9[k] : 0.0;
-                if (THIRD) {
-#pragma unroll
-                    for (int j = 0; j < 5; j++) {
-                        const double gj = cmul(sc, make_double2(cu * t[19 + 2 * j], cu * t[20 + 2 * j])).x;
-                        GP.grad[(size_t)(9 + j) * (size_t)nb + B.b] = B.valid ? gj : 0.0;
-                    }
+            for (int t = tid; t < cnt * kGradAcc; t += kBlock) {
+                const int q = t / kGradAcc, k = t - q * kGradAcc;
+                dfl x = {0.f, 0.f};
+                for (int g = q * per; g < (q + 1) * per; g++) {
+                    const float2 y = red2[kGradAcc * g + k];
+                    x = df_add(x, dfl{y.x, y.y});
                 }
+                tsum[t] = (double)x.h + (double)x.l;
+            }
+        }
+        __syncthreads();
+        {
+            constexpr int kOut = (THIRD ? 14 : 9) + 1;   // gradient rows + (d_h, h_h)
+            for (int t = tid; t < cnt * kOut; t += kBlock) {
+                const int q = t / kOut, j = t - q * kOut;
+                const Bin &B = bins[q];
+                if (B.b < 0) continue;
+                const GradExtra &Gx = gxs[q];
+                const double *ts = tsum + q * kGradAcc;
+                const double s4 = 4.0 * K.df;
+                // weights were 4 df r / S in units of 2^(eS - eD): cu converts sums of w
+                const double cu = s4 * exp2_int(B.eS - B.eD);
+                const double2 sc = B.scale;
+                const double nb = a.num_bin;
+                if (j == kOut - 1) {
+                    const double ch = s4 * exp2_int(B.eS) * (sc.x * sc.x + sc.y * sc.y);
+                    const double2 dh = cmul(make_double2(cu * ts[0], cu * ts[1]), sc);
+                    K.d_h[B.b] = B.valid ? dh : make_double2(0.0, 0.0);
+                    K.h_h[B.b] = B.valid ? make_double2(ch * ts[2], 0.0) : make_double2(0.0, 0.0);
+                    continue;
+                }
+                double g;
+                if (j == 0 || j == 1 || j == 4) {
+                    const double2 scQf = cmul(sc, make_double2(cu * ts[3], cu * ts[4]));
+                    if (j == 0) g = scQf.x / a.params[B.b];                       // amp
+                    else if (j == 4) g = -scQf.y;                                  // phi0: Re(i sc Qf)
+                    else g = cmul(sc, make_double2(cu * ts[9], cu * ts[10])).x +   // f0
+                             cmul(Gx.dlnsc_f0, scQf).x;
+                } else if (j == 5 || j == 6) {                                     // iota, psi
+                    const double2 QP = make_double2(cu * ts[5], cu * ts[6]);
+                    const double2 QC = make_double2(cu * ts[7], cu * ts[8]);
+                    const double2 dP = j == 5 ? Gx.dDPi : Gx.dDPp, dC = j == 5 ? Gx.dDCi : Gx.dDCp;
+                    g = cmul(sc, cadd(cmul(dP, QP), cmul(dC, QC))).x;
+                } else {
+                    // fdot 11, fddot 13, lam 15, beta 17; third body 19 + 2 (j - 9)
+                    const int k = j == 2 ? 11 : j == 3 ? 13 : j == 7 ? 15 : j == 8 ? 17 : 19 + 2 * (j - 9);
+                    g = cmul(sc, make_double2(cu * ts[k], cu * ts[k + 1])).x;
+                }
+                GP.grad[(size_t)j * (size_t)nb + B.b] = B.valid ? g : 0.0;
             }
         }
         __syncthreads();

@@ -1155,7 +1155,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                 if (out) flag(a.status, GBX_FLAG_WINDOW);
             }
             // lane tree within groups of `width` lanes (all lanes take part)
-            double gr, gi, gh;
+            double gr = 0.0, gi = 0.0, gh = 0.0;
             if constexpr (sizeof(R) == 8) {
                 for (int o = width >> 1; o > 0; o >>= 1) {
                     sr += __shfl_xor_sync(0xffffffffu, sr, o);
@@ -1173,28 +1173,48 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                     xi = df_add(xi, yi);
                     xh = df_add(xh, yh);
                 }
+                // leaders keep the float pairs; the FP64 conversion happens
+                // once per (binary, term) below, spread over lanes
                 if ((tid & (width - 1)) == 0) {
-                    gr = (double)xr.h + (double)xr.l;
-                    gi = (double)xi.h + (double)xi.l;
-                    gh = (double)xh.h + (double)xh.l;
+                    float2 *red2 = reinterpret_cast<float2 *>(red);
+                    const int g = tid / width;
+                    red2[3 * g] = make_float2(xr.h, xr.l);
+                    red2[3 * g + 1] = make_float2(xi.h, xi.l);
+                    red2[3 * g + 2] = make_float2(xh.h, xh.l);
                 }
             }
-            if ((tid & (width - 1)) == 0) {
+            if (sizeof(R) == 8 && (tid & (width - 1)) == 0) {
                 const int g = tid / width;
                 red[3 * g] = gr;
                 red[3 * g + 1] = gi;
                 red[3 * g + 2] = gh;
             }
             __syncthreads();
+            // per (binary, term) sums over the binary's groups -> tsum (FP64)
+            double *tsum = red + 64;
+            {
+                const int per = Tpb / width;
+                for (int t = tid; t < 3 * cnt; t += kBlock) {
+                    const int q = t / 3, c = t - 3 * q;
+                    if constexpr (sizeof(R) == 8) {
+                        double x = 0.0;
+                        for (int g = q * per; g < (q + 1) * per; g++) x += red[3 * g + c];
+                        tsum[t] = x;
+                    } else {
+                        const float2 *red2 = reinterpret_cast<const float2 *>(red);
+                        dfl x = {0.f, 0.f};
+                        for (int g = q * per; g < (q + 1) * per; g++) {
+                            const float2 y = red2[3 * g + c];
+                            x = df_add(x, dfl{y.x, y.y});
+                        }
+                        tsum[t] = (double)x.h + (double)x.l;
+                    }
+                }
+            }
+            __syncthreads();
             if (tid < cnt) {
                 const Bin &B = bins[tid];
-                const int per = Tpb / width;
-                double tr = 0.0, ti = 0.0, th = 0.0;
-                for (int g = tid * per; g < (tid + 1) * per; g++) {
-                    tr += red[3 * g];
-                    ti += red[3 * g + 1];
-                    th += red[3 * g + 2];
-                }
+                const double tr = tsum[3 * tid], ti = tsum[3 * tid + 1], th = tsum[3 * tid + 2];
                 const double s4 = 4.0 * K.df;
                 double2 dh, hv;
                 if constexpr (sizeof(R) == 8) {
