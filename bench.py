@@ -287,11 +287,16 @@ def config3(gb, data, Sd, seed, steps):
     sh = nat.stream_handle()
     out = {"workload": "50,000 binaries, N=256, tdi2=True, T=4x31557600 s",
            "steps": steps}
+    shapes = {}
     for name, prec in (("fp64", "fp64"), ("mixed", "mixed"), ("grad", "mixed")):
-        plan = gb._plan(256, Tu, prec, True, 9)
-        a = plan.args(prm, grad=(name == "grad"))
+        box = {}
+
+        def set_shape(tile, bps):
+            plan = gb._plan(256, Tu, prec, True, 9, tile, bps)
+            box["a"] = plan.args(prm, grad=(name == "grad"))
 
         def run():
+            a = box["a"]
             if name == "grad":
                 rc = lib.gbx_waveform_ll_grad(ctypes.byref(a), ctypes.byref(la), nat.ptr(d_h),
                                               nat.ptr(h_h), nat.ptr(g), sh)
@@ -299,6 +304,18 @@ def config3(gb, data, Sd, seed, steps):
                 rc = lib.gbx_waveform_ll(ctypes.byref(a), ctypes.byref(la), nat.ptr(d_h),
                                          nat.ptr(h_h), sh)
             nat.check(rc, name)
+
+        shape = (0, 0)
+        if gb.autotune:
+            from gbgpu_gb300.autotune import default_tuner, workload_key
+
+            def trial(tile, bps):
+                set_shape(tile, bps)
+                run()
+            shape = default_tuner().tune(
+                workload_key("grad" if name == "grad" else "ll", 256, B, prec, True, 9), trial)
+        shapes[name] = {"tile": int(shape[0]), "blocks_per_sm": int(shape[1])}
+        set_shape(*shape)
         for _ in range(2):
             run()
         torch.cuda.synchronize()
@@ -310,6 +327,7 @@ def config3(gb, data, Sd, seed, steps):
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / steps
         out[f"{name}_binaries_per_s"] = B / (ms / 1e3)
+    out["launch_shapes"] = shapes
     out["grad_over_forward"] = out["grad_binaries_per_s"] / out["mixed_binaries_per_s"]
     out["mixed_over_fp64"] = out["mixed_binaries_per_s"] / out["fp64_binaries_per_s"]
     return out
@@ -436,14 +454,13 @@ def run_gpu(args, rank, world):
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
     B = args.binaries
     p, Ns = draw_workload(B, args.seed + rank)
-    gb = GBGPU(precision="mixed")
+    gb = GBGPU(precision="mixed", autotune=not args.no_autotune)
     data, Sd, d_d, S_host = make_data(gb, p, Ns, args.seed + rank)
     gb.d_d = d_d
     L = data[0].shape[0]
 
     params_d = torch.as_tensor(p, device="cuda").contiguous()
-    plans = {prec: gb._plan(Ns, int(T_OBS / DT) * DT, prec, False, 9)
-             for prec in ("mixed", "fp64")}
+    Tu_ = int(T_OBS / DT) * DT
     d_h = torch.empty(B, dtype=torch.complex128, device="cuda")
     h_h = torch.empty(B, dtype=torch.complex128, device="cuda")
     zeros = torch.zeros(B, dtype=torch.int32, device="cuda")
@@ -453,14 +470,18 @@ def run_gpu(args, rank, world):
     la.data_length, la.num_data, la.num_psd = L, 1, 1
     la.data_index = la.noise_index = zeros.data_ptr()
     la.df = 1.0 / (int(T_OBS / DT) * DT)
-    wargs = {k: v.args(params_d) for k, v in plans.items()}
     lib = nat.lib()
     stream = torch.cuda.current_stream()
     sh = nat.stream_handle(stream)
-
     grad_out = torch.empty((9, B), dtype=torch.float64, device="cuda")
-    gplan = gb._plan(Ns, int(T_OBS / DT) * DT, "mixed", False, 9)
-    wargs["grad"] = gplan.args(params_d, grad=True)
+
+    def set_shape(prec, tile, bps):
+        plan = gb._plan(Ns, Tu_, "mixed" if prec == "grad" else prec, False, 9, tile, bps)
+        wargs[prec] = plan.args(params_d, grad=(prec == "grad"))
+
+    wargs = {}
+    for prec in ("mixed", "fp64", "grad"):
+        set_shape(prec, 0, 0)
 
     def step(prec):
         if prec == "grad":
@@ -494,6 +515,23 @@ def run_gpu(args, rank, world):
         t_wall = time.perf_counter() - t_wall
         ms = [a.elapsed_time(b) for a, b in ev]
         return float(np.mean(ms)), t_wall
+
+    # launch shapes: picked by the autotuner on this batch (same keys as the
+    # class API, so the e2e calls below reuse them), else the defaults
+    shapes = {}
+    if not args.no_autotune:
+        from gbgpu_gb300.autotune import default_tuner, workload_key
+
+        for prec in ("mixed", "fp64", "grad"):
+            kind = "grad" if prec == "grad" else "ll"
+            pr = "mixed" if prec == "grad" else prec
+
+            def run(tile, bps, prec=prec):
+                set_shape(prec, tile, bps)
+                step(prec)
+            shapes[prec] = default_tuner().tune(workload_key(kind, Ns, B, pr, False, 9), run)
+            set_shape(prec, *shapes[prec])
+    torch.cuda.synchronize()
 
     # accuracy of the mixed form on the full batch against the FP64 form
     step("fp64")
@@ -582,6 +620,8 @@ def run_gpu(args, rank, world):
         "grads_per_s": B / (ms_grad / 1e3),
         "grads_note": "binaries/s of the fused likelihood + 9-parameter gradient kernel "
                       "(mixed form) on the same 200k-binary batch",
+        "launch_shapes": {k: {"tile": int(v[0]), "blocks_per_sm": int(v[1])}
+                          for k, v in shapes.items()} or "defaults (tile 512, full occupancy)",
         "config3": cfg3,
         "config2": cfg2,
         "config4": cfg4,
@@ -680,6 +720,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fill-bench", action="store_true")
     ap.add_argument("--no-mcmc-bench", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="use the kernels' default launch shape instead of the autotuner's")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

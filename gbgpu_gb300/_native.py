@@ -41,6 +41,7 @@ class WaveArgs(ctypes.Structure):
         ("tdi2", _i), ("start_freq_ind", _i), ("T", _d), ("armlength", _d), ("year", _d),
         ("orbit", _vp * (GBX_MAX_LOG2N + 1)), ("order", _vp), ("tiles", _vp), ("ntiles", _i),
         ("queue", _vp), ("status", _vp), ("workspace", _vp), ("workspace_bytes", ctypes.c_size_t),
+        ("tile", _i), ("blocks_per_sm", _i),
     ]
 
 

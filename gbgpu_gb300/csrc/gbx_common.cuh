@@ -9,8 +9,16 @@
 namespace gbx {
 
 constexpr int kBlock = 256;        // threads per CTA for the waveform family
-constexpr int kTileMin = 512;      // minimum samples per tile (P = kTileMin / N binaries)
-constexpr int kMaxPack = 16;       // kTileMin / 32
+constexpr int kTileMin = 512;      // default samples per tile (P = kTileMin / N binaries)
+constexpr int kMaxPack = 16;       // most binaries in one tile
+
+// binaries of N = 2^lg packed in one tile of `tile` samples (tile 0 = kTileMin)
+__host__ __device__ __forceinline__ int tile_pack(int tile, int lg, int minp)
+{
+    int p = (tile ? tile : kTileMin) >> lg;
+    p = p < minp ? minp : p;
+    return p > kMaxPack ? kMaxPack : p;
+}
 constexpr int kTwN = 8192;         // twiddle table period (largest supported N)
 constexpr double kPi = 3.141592653589793238462643383279502884;
 constexpr double kTwoPi = 6.283185307179586476925286766559005768;

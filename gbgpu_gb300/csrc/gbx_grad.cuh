@@ -506,7 +506,7 @@ __global__ void __launch_bounds__(kBlock, THIRD ? 1 : 2) grad_kernel(const GradP
         const int N = 1 << lg;
         const double *tab = (lg >= 5 && lg <= GBX_MAX_LOG2N)
                                 ? reinterpret_cast<const double *>(a.orbit[lg]) : nullptr;
-        const int maxcnt = max(1, kTileMin >> lg);
+        const int maxcnt = tile_pack(a.tile, lg, 1);
         if (tab == nullptr || cnt < 1 || cnt > maxcnt || first < 0 || first + cnt > a.num_bin ||
             (cnt << lg) > K.maxS) {
             flag(a.status, GBX_FLAG_TILE);

@@ -868,7 +868,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
         const int N = 1 << lg;
         const double *tab = (lg >= 5 && lg <= GBX_MAX_LOG2N)
                                 ? reinterpret_cast<const double *>(a.orbit[lg]) : nullptr;
-        const int maxcnt = max(MODE == MODE_SWAP ? 2 : 1, kTileMin >> lg);
+        const int maxcnt = tile_pack(a.tile, lg, MODE == MODE_SWAP ? 2 : 1);
         if (tab == nullptr || cnt < 1 || cnt > maxcnt || first < 0 || first + cnt > a.num_bin ||
             (cnt << lg) > K.maxS || (sizeof(R) == 8 && lg > 12)) {
             flag(a.status, GBX_FLAG_TILE);
@@ -1315,6 +1315,7 @@ static int launch_one(const KParams &K, int maxS, cudaStream_t st)
     int per_sm = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, sm);
     if (e != cudaSuccess) return cuda_error(e, "occupancy");
+    if (K.a.blocks_per_sm > 0 && per_sm > K.a.blocks_per_sm) per_sm = K.a.blocks_per_sm;
     if (per_sm < 1) per_sm = 1;
     int nsm = num_sms();
     int ntiles = K.a.tiles ? K.a.ntiles : (K.a.num_bin + K.P - 1) / K.P;
@@ -1368,6 +1369,9 @@ static int check_wave(const gbx_wave_args *a, int *maxS)
         if (a->workspace_bytes < gbx_wave_workspace_bytes(a->num_bin))
             return set_error(GBX_ERR_ARG, "workspace smaller than gbx_wave_workspace_bytes(num_bin)");
     }
+    if (a->tile != 0 && (a->tile < 64 || a->tile > 4096 || (a->tile & (a->tile - 1)) != 0))
+        return set_error(GBX_ERR_ARG, "tile=%d: need 0 or a power of two in [64, 4096]", a->tile);
+    if (a->blocks_per_sm < 0) return set_error(GBX_ERR_ARG, "blocks_per_sm < 0");
     const int maxlg = a->precision == GBX_FP64 ? 12 : GBX_MAX_LOG2N;
     if (a->tiles == nullptr) {
         int N = a->N;
@@ -1375,15 +1379,15 @@ static int check_wave(const gbx_wave_args *a, int *maxS)
         int lg = 31 - __builtin_clz((unsigned)N);
         if (lg > maxlg) return set_error(GBX_ERR_UNSUPPORTED, "N=%d above the limit of this precision", N);
         if (!a->orbit[lg]) return set_error(GBX_ERR_ARG, "no orbit table for N=%d", N);
-        *maxS = N > kTileMin ? N : kTileMin;
+        *maxS = tile_pack(a->tile, lg, 1) * N;
     } else {
         if (a->ntiles < 0) return set_error(GBX_ERR_ARG, "ntiles < 0");
-        // the largest N with a table bounds the tile size
+        // the N with a table bound the tile size
         int mx = 0;
         for (int k = 5; k <= maxlg; k++)
-            if (a->orbit[k]) mx = k;
+            if (a->orbit[k]) mx = max(mx, tile_pack(a->tile, k, 1) << k);
         if (mx == 0) return set_error(GBX_ERR_ARG, "no orbit tables");
-        *maxS = (1 << mx) > kTileMin ? (1 << mx) : kTileMin;
+        *maxS = mx;
     }
     return GBX_OK;
 }
@@ -1395,12 +1399,7 @@ static KParams base_params(const gbx_wave_args *a)
     K.a = *a;
     K.fstar = kCSI / (a->armlength * 2.0 * kPi);
     for (int k = 0; k <= GBX_MAX_LOG2N; k++) K.stepd[k] = df_from(ldexp(a->T, -k));
-    if (a->tiles == nullptr) {
-        int P = kTileMin / a->N;
-        K.P = P < 1 ? 1 : P;
-    } else {
-        K.P = 1;
-    }
+    K.P = a->tiles == nullptr ? tile_pack(a->tile, 31 - __builtin_clz((unsigned)a->N), 1) : 1;
     return K;
 }
 
@@ -1504,7 +1503,7 @@ extern "C" int gbx_swap_ll(const gbx_wave_args *a, const gbx_ll_args *l, double 
     rc = ensure_init((cudaStream_t)stream);
     if (rc) return rc;
     KParams K = base_params(a);
-    K.P = kTileMin / a->N < 2 ? 2 : kTileMin / a->N;
+    K.P = tile_pack(a->tile, 31 - __builtin_clz((unsigned)a->N), 2);
     maxS = K.P * a->N;
     K.A_data = (const double2 *)l->A_data;
     K.E_data = (const double2 *)l->E_data;
@@ -1583,6 +1582,7 @@ extern "C" int gbx_waveform_ll_grad(const gbx_wave_args *a, const gbx_ll_args *l
     int per_sm = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, sm);
     if (e != cudaSuccess) return cuda_error(e, "occupancy(grad)");
+    if (b.blocks_per_sm > 0 && per_sm > b.blocks_per_sm) per_sm = b.blocks_per_sm;
     if (per_sm < 1) per_sm = 1;
     const int ntiles = b.tiles ? b.ntiles : (b.num_bin + K.P - 1) / K.P;
     int grid = per_sm * num_sms();

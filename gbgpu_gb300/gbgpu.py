@@ -15,6 +15,7 @@ through device memory, and the waveform attributes (``XYZf``, ``AETf``,
 import abc
 import ctypes
 import hashlib
+import os
 import warnings
 
 import numpy as np
@@ -27,7 +28,9 @@ from .orbits import EqualArmlengthOrbits, Orbits
 from .utility import get_N
 
 _PRECISIONS = {"fp64": nat.GBX_FP64, "mixed": nat.GBX_MIXED}
-_TILE_MIN = 512
+_TILE_MIN = 512       # default samples per tile of the fused kernels
+_MAX_PACK = 16        # most binaries in one tile
+_PLAN_CACHE = 64      # WavePlans kept per GBGPU object
 
 
 def _is_pow2(n):
@@ -46,9 +49,10 @@ def _to_host(x):
     return np.asarray(x)
 
 
-def plan_tiles(N_per_bin):
+def plan_tiles(N_per_bin, tile=0):
     """Tile list for a batch of uneven N: binaries sorted by decreasing N,
-    packed max(1, 512/N) per tile.  Returns (order int32, tiles int32 (t, 4))."""
+    packed clamp(tile/N, 1, 16) per tile (tile 0 = 512 samples, the kernels'
+    default).  Returns (order int32, tiles int32 (t, 4))."""
     Ns = np.asarray(N_per_bin, dtype=np.int64).reshape(-1)
     if Ns.size and (np.any(Ns < 32) or np.any(Ns & (Ns - 1))):
         raise NotImplementedError("per-binary N must be powers of two >= 32")
@@ -58,7 +62,7 @@ def plan_tiles(N_per_bin):
     pos = 0
     for N in sorted(set(Ns.tolist()), reverse=True):
         cnt = int(np.count_nonzero(sortedN == N))
-        P = max(1, _TILE_MIN // N)
+        P = min(_MAX_PACK, max(1, (tile or _TILE_MIN) // N))
         first = pos + np.arange(0, cnt, P)
         count = np.minimum(P, pos + cnt - first)
         lg = int(N).bit_length() - 1
@@ -71,12 +75,14 @@ def plan_tiles(N_per_bin):
 class WavePlan:
     """Device-resident description of a batch (orbit tables, tiles, queue)."""
 
-    def __init__(self, owner, N, T, precision, tdi2=False, nparams=9):
+    def __init__(self, owner, N, T, precision, tdi2=False, nparams=9, tile=0, blocks_per_sm=0):
         self.owner = owner
         self.T = float(T)
         self.precision = precision
         self.tdi2 = bool(tdi2)
         self.nparams = nparams
+        self.tile = int(tile)
+        self.blocks_per_sm = int(blocks_per_sm)
         dev = owner.device
         if np.ndim(N) == 0:
             self.uniform = True
@@ -88,7 +94,7 @@ class WavePlan:
             self.uniform = False
             self.N = 0
             Ns_arr = np.asarray(N, dtype=np.int64).reshape(-1)
-            order, tiles = plan_tiles(Ns_arr)
+            order, tiles = plan_tiles(Ns_arr, self.tile)
             Ns = sorted(set(Ns_arr.tolist()))
             self.order = torch.as_tensor(order, device=dev)
             self.tiles = torch.as_tensor(tiles.reshape(-1), device=dev)
@@ -103,7 +109,11 @@ class WavePlan:
         self._ws = None
 
     def args(self, params, start_freq_ind=0, status=None, grad=False):
+        """gbx_wave_args for this plan.  The struct holds references to the
+        plan and to ``params`` so that the device buffers it points to (tile
+        list, queue, workspace, orbit tables) live as long as it does."""
         a = nat.WaveArgs()
+        a._keep = (self, params, status)
         a.params = params.data_ptr()
         a.num_bin = params.shape[1]
         a.nparams = params.shape[0]
@@ -121,6 +131,8 @@ class WavePlan:
         a.ntiles = self.ntiles
         a.queue = self.queue.data_ptr() if self.queue is not None else None
         a.status = status.data_ptr() if status is not None else None
+        a.tile = self.tile
+        a.blocks_per_sm = self.blocks_per_sm
         B = params.shape[1]
         need = (nat.lib().gbx_grad_workspace_bytes(B) if grad
                 else nat.lib().gbx_wave_workspace_bytes(B))
@@ -142,12 +154,20 @@ class GBGPUBase(abc.ABC):
         force_backend: accepted for API compatibility; only the GPU exists.
         precision: ``"fp64"`` (plain form) or ``"mixed"`` (FP64 phase, FP32
             slow part and FFT) for the fused likelihood / fill kernels.
+        autotune: pick the fused kernels' launch shape (samples per tile,
+            blocks per SM) by timing candidates on the first batch of each
+            workload (cached per device); default from ``GBX_AUTOTUNE=1``.
     """
 
     NPARAMS = 9
 
-    def __init__(self, orbits: Orbits = None, force_backend=None, precision="fp64", device=None):
+    def __init__(self, orbits: Orbits = None, force_backend=None, precision="fp64", device=None,
+                 autotune=None):
         self._backend = get_backend(force_backend)
+        # launch shapes picked by timing (gbgpu_gb300.autotune); default from
+        # the environment variable GBX_AUTOTUNE=1, else the kernels' defaults
+        self.autotune = (os.environ.get("GBX_AUTOTUNE", "0") == "1") if autotune is None \
+            else bool(autotune)
         self.device = torch.device(device) if device is not None else torch.device(
             "cuda", torch.cuda.current_device())
         if precision not in _PRECISIONS:
@@ -226,21 +246,24 @@ class GBGPUBase(abc.ABC):
                 f"Observation time ({T}) is larger than length of time in orbital information "
                 f"({np.max(self.orbits.t_base)})")
 
-    def _plan(self, N, T, precision, tdi2, nparams):
+    def _plan(self, N, T, precision, tdi2, nparams, tile=0, blocks_per_sm=0):
         """WavePlan cache: tile schedules and orbit tables are built once per
-        distinct (N or N-array contents, T, precision, tdi2, nparams)."""
+        distinct (N or N-array contents, T, precision, tdi2, nparams, launch
+        shape)."""
         if np.ndim(N) == 0:
-            key = (int(N), float(T), precision, bool(tdi2), nparams)
+            key = (int(N), float(T), precision, bool(tdi2), nparams, tile, blocks_per_sm)
         else:
             arr = np.ascontiguousarray(N, dtype=np.int64)
             key = (hashlib.blake2b(arr.view(np.uint8), digest_size=16).digest(), arr.shape[0],
-                   float(T), precision, bool(tdi2), nparams)
-        plan = self._plans.get(key)
+                   float(T), precision, bool(tdi2), nparams, tile, blocks_per_sm)
+        plan = self._plans.pop(key, None)
         if plan is None:
-            if len(self._plans) > 32:
-                self._plans.clear()
-            plan = WavePlan(self, N, T, precision, tdi2, nparams)
-            self._plans[key] = plan
+            # least recently used plans go first; a plan stays alive while any
+            # gbx_wave_args built from it does (WavePlan.args keeps a reference)
+            while len(self._plans) >= _PLAN_CACHE:
+                self._plans.pop(next(iter(self._plans)))
+            plan = WavePlan(self, N, T, precision, tdi2, nparams, tile, blocks_per_sm)
+        self._plans[key] = plan
         return plan
 
     def _params(self, base, add_args):
@@ -417,17 +440,18 @@ class GBGPUBase(abc.ABC):
         noise_index = _to_device(noise_index, torch.int32, self.device).contiguous()
         return dd, pp, data_length, data_index, noise_index
 
-    def _fused_ll(self, params, N, T, tdi2, dd, pp, data_length, data_index, noise_index,
-                  start_freq_ind, precision):
-        B = params.shape[1]
-        d_h = torch.empty(B, dtype=torch.complex128, device=self.device)
-        h_h = torch.empty(B, dtype=torch.complex128, device=self.device)
-        if B == 0:
-            return d_h, h_h
-        plan = self._plan(N, T, precision, tdi2, params.shape[0])
-        self._status.zero_()
-        a = plan.args(params, start_freq_ind, self._status)
+    def _launch_shape(self, kind, N, B, precision, tdi2, nparams, run):
+        """(tile, blocks_per_sm) for this workload: the autotuner's choice when
+        autotuning is on (timing ``run`` on the first call), else defaults."""
+        if not self.autotune:
+            return 0, 0
+        from .autotune import default_tuner, workload_key
+        return default_tuner().tune(workload_key(kind, N, B, precision, tdi2, nparams), run)
+
+    @staticmethod
+    def _ll_args(dd, pp, data_length, data_index, noise_index, T):
         la = nat.LLArgs()
+        la._keep = (dd, pp, data_index, noise_index)     # the struct holds raw pointers
         la.A_data, la.E_data = dd[0].data_ptr(), dd[1].data_ptr()
         la.A_psd, la.E_psd = pp[0].data_ptr(), pp[1].data_ptr()
         la.data_length = int(data_length)
@@ -436,9 +460,28 @@ class GBGPUBase(abc.ABC):
         la.data_index = data_index.data_ptr()
         la.noise_index = noise_index.data_ptr()
         la.df = 1.0 / T
-        rc = nat.lib().gbx_waveform_ll(ctypes.byref(a), ctypes.byref(la), nat.ptr(d_h),
-                                       nat.ptr(h_h), nat.stream_handle())
-        nat.check(rc, "gbx_waveform_ll")
+        return la
+
+    def _fused_ll(self, params, N, T, tdi2, dd, pp, data_length, data_index, noise_index,
+                  start_freq_ind, precision):
+        B = params.shape[1]
+        d_h = torch.empty(B, dtype=torch.complex128, device=self.device)
+        h_h = torch.empty(B, dtype=torch.complex128, device=self.device)
+        if B == 0:
+            return d_h, h_h
+        la = self._ll_args(dd, pp, data_length, data_index, noise_index, T)
+        nparams = params.shape[0]
+
+        def run(tile, bps):
+            plan = self._plan(N, T, precision, tdi2, nparams, tile, bps)
+            a = plan.args(params, start_freq_ind, self._status)
+            rc = nat.lib().gbx_waveform_ll(ctypes.byref(a), ctypes.byref(la), nat.ptr(d_h),
+                                           nat.ptr(h_h), nat.stream_handle())
+            nat.check(rc, "gbx_waveform_ll")
+
+        shape = self._launch_shape("ll", N, B, precision, tdi2, nparams, run)
+        self._status.zero_()
+        run(*shape)
         return d_h, h_h
 
     def _check_status(self):
@@ -565,21 +608,19 @@ class GBGPUBase(abc.ABC):
         h_h = torch.empty(B, dtype=torch.complex128, device=self.device)
         grad = torch.zeros((npar, B), dtype=torch.float64, device=self.device)
         if B:
-            plan = self._plan(N, T, "mixed", tdi2, npar)
+            la = self._ll_args(dd, pp, L, di, ni, T)
+
+            def run(tile, bps):
+                plan = self._plan(N, T, "mixed", tdi2, npar, tile, bps)
+                a = plan.args(prm, start_freq_ind, self._status, grad=True)
+                rc = nat.lib().gbx_waveform_ll_grad(ctypes.byref(a), ctypes.byref(la),
+                                                    nat.ptr(d_h), nat.ptr(h_h), nat.ptr(grad),
+                                                    nat.stream_handle())
+                nat.check(rc, "gbx_waveform_ll_grad")
+
+            shape = self._launch_shape("grad", N, B, "mixed", tdi2, npar, run)
             self._status.zero_()
-            a = plan.args(prm, start_freq_ind, self._status, grad=True)
-            la = nat.LLArgs()
-            la.A_data, la.E_data = dd[0].data_ptr(), dd[1].data_ptr()
-            la.A_psd, la.E_psd = pp[0].data_ptr(), pp[1].data_ptr()
-            la.data_length = int(L)
-            la.num_data = int(dd[0].numel() // L)
-            la.num_psd = int(pp[0].numel() // L)
-            la.data_index = di.data_ptr()
-            la.noise_index = ni.data_ptr()
-            la.df = 1.0 / T
-            rc = nat.lib().gbx_waveform_ll_grad(ctypes.byref(a), ctypes.byref(la), nat.ptr(d_h),
-                                                nat.ptr(h_h), nat.ptr(grad), nat.stream_handle())
-            nat.check(rc, "gbx_waveform_ll_grad")
+            run(*shape)
         self._lazy = (prm, N, T, tdi2)
         self.d_h, self.h_h = d_h, h_h
         d_d = torch.as_tensor(self.d_d, device=self.device)

@@ -87,6 +87,9 @@ class SwapSampler:
         with torch.cuda.graph(self.graph):
             self.dls = [self.step(k, self.proposals[i], self.log_us[i])
                         for i, k in enumerate(self.ks)]
+        # the graph holds raw pointers into the plans' tile lists, queues and
+        # workspaces: keep those plans alive for as long as the graph
+        self._graph_plans = list(self.gb._plans.values())
         return self.graph
 
     def replay(self):

@@ -169,6 +169,14 @@ typedef struct gbx_wave_args {
     int *status;                 /* optional device word for GBX_FLAG_* bits */
     void *workspace;             /* optional scratch of gbx_wave_workspace_bytes(num_bin) */
     size_t workspace_bytes;
+    /* Launch shape (0 = defaults).  tile: samples per tile, a power of two
+     * in [64, 4096]; a tile holds clamp(tile / N, 1, 16) binaries of one N
+     * (at least 2 for gbx_swap_ll) and the likelihood epilogue gives each
+     * binary 256 / that many threads.  Default 512.  blocks_per_sm: resident
+     * persistent blocks per SM, capped by occupancy; default as many as fit.
+     * Tile lists passed in `tiles` must be packed with the same tile. */
+    int tile;
+    int blocks_per_sm;
 } gbx_wave_args;
 
 /*

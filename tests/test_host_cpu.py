@@ -29,26 +29,26 @@ def test_library_exports_every_declared_symbol():
 
 
 def test_struct_mirrors_match_c_layout(tmp_path):
+    """Every field offset and the size of the ctypes mirrors equal the C ones."""
     from gbgpu_gb300 import _native
+    structs = {"gbx_wave_args": _native.WaveArgs, "gbx_ll_args": _native.LLArgs}
+    lines = []
+    for cname, py in structs.items():
+        lines.append(f'  printf("%zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'  printf("%zu\\n", offsetof({cname}, {fname}));')
     src = tmp_path / "layout.c"
-    src.write_text(r'''
-#include <stdio.h>
-#include <stddef.h>
-#include "gbgpu_gb300.h"
-int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(gbx_wave_args),
-         offsetof(gbx_wave_args, T), offsetof(gbx_wave_args, orbit),
-         offsetof(gbx_wave_args, ntiles), offsetof(gbx_wave_args, status),
-         sizeof(gbx_ll_args), offsetof(gbx_ll_args, data_index), offsetof(gbx_ll_args, df));
-  return 0; }''')
+    src.write_text("#include <stdio.h>\n#include <stddef.h>\n#include \"gbgpu_gb300.h\"\n"
+                   "int main(void) {\n" + "\n".join(lines) + "\n  return 0; }\n")
     exe = tmp_path / "layout"
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
                    check=True)
     got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True,
                                           check=True).stdout.split()]
-    W, Lg = _native.WaveArgs, _native.LLArgs
-    want = [ctypes.sizeof(W), W.T.offset, W.orbit.offset, W.ntiles.offset, W.status.offset,
-            ctypes.sizeof(Lg), Lg.data_index.offset, Lg.df.offset]
+    want = []
+    for py in structs.values():
+        want.append(ctypes.sizeof(py))
+        want += [getattr(py, fname).offset for fname, _ in py._fields_]
     assert got == want
 
 
@@ -104,12 +104,13 @@ def test_orbits_identical_to_oracle():
         np.testing.assert_array_equal(a.get_pos(t, np.full(257, s)), b.get_pos(t, np.full(257, s)))
 
 
-@pytest.mark.parametrize("seed", [0, 1, 2])
-def test_plan_tiles_cover_every_binary_once(seed):
+@pytest.mark.parametrize("seed,tile", [(0, 0), (1, 0), (2, 0), (3, 64), (4, 256), (5, 2048),
+                                       (6, 4096)])
+def test_plan_tiles_cover_every_binary_once(seed, tile):
     from gbgpu_gb300.gbgpu import plan_tiles
     rng = np.random.default_rng(seed)
     Ns = 2 ** rng.integers(5, 13, 1000)
-    order, tiles = plan_tiles(Ns)
+    order, tiles = plan_tiles(Ns, tile)
     assert sorted(order.tolist()) == list(range(1000))
     seen = np.zeros(1000, int)
     prevN = 1 << 20
@@ -117,7 +118,7 @@ def test_plan_tiles_cover_every_binary_once(seed):
         N = 1 << lg
         assert N <= prevN                       # decreasing N (load balance)
         prevN = N
-        assert 1 <= cnt <= max(1, 512 // N)
+        assert 1 <= cnt <= min(16, max(1, (tile or 512) // N))
         for s in range(first, first + cnt):
             assert Ns[order[s]] == N
             seen[order[s]] += 1
@@ -129,3 +130,15 @@ def test_plan_tiles_rejects_non_power_of_two():
     with pytest.raises(NotImplementedError):
         plan_tiles([64, 96])
     assert plan_tiles([])[1].shape == (0, 4)
+
+
+def test_autotune_workload_keys():
+    from gbgpu_gb300.autotune import workload_key
+    k1 = workload_key("ll", 256, 50000, "mixed", True, 9)
+    assert k1 == "ll|256:65536|mixed|tdi2=1|np=9"
+    Ns = np.array([64] * 1000 + [2048] * 30)
+    k2 = workload_key("grad", Ns, Ns.size, "mixed", False, 14)
+    assert k2 == "grad|64:1024,2048:32|mixed|tdi2=0|np=14"
+    # batches of similar size and the same N mix share a key
+    assert workload_key("ll", np.array([64] * 1100 + [2048] * 29), 1129, "mixed", False, 14) \
+        == k2.replace("grad", "ll")
