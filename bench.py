@@ -320,10 +320,12 @@ def config3(gb, data, Sd, seed, steps):
             run()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.nvtx.range_push(f"config3_{name}")
         e0.record()
         for _ in range(steps):
             run()
         e1.record()
+        torch.cuda.nvtx.range_pop()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / steps
         out[f"{name}_binaries_per_s"] = B / (ms / 1e3)
@@ -363,21 +365,24 @@ def config2(gb, seed, B=1_000_000, G=256, N=256, steps=3):
     out["template_GB"] = tmpl.numel() * 16 / 1e9
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
 
-    def timeit(fn):
+    def timeit(fn, name):
         fn()
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push(name)
         ev[0].record()
         for _ in range(steps):
             fn()
         ev[1].record()
+        torch.cuda.nvtx.range_pop()
         torch.cuda.synchronize()
         return ev[0].elapsed_time(ev[1]) / steps
 
-    ms_zero = timeit(lambda: tmpl.zero_())
+    ms_zero = timeit(lambda: tmpl.zero_(), "config2_zero")
     for prec in ("fp64", "mixed"):
         for mode in ("atomic", "deterministic"):
             ms = timeit(lambda: gb.generate_global_template(pT, gi, tmpl, N=N, T=T_OBS, dt=DT,
-                                                            precision=prec, fill_mode=mode))
+                                                            precision=prec, fill_mode=mode),
+                        f"config2_{prec}_{mode}")
             out[f"{prec}_{mode}_ms"] = ms
             out[f"{prec}_{mode}_binaries_per_s"] = B / (ms / 1e3)
     out["zeroing_ms"] = ms_zero
@@ -432,10 +437,12 @@ def config4(seed, W=4096, K=500, N=512, steps=100, replays=3):
     smp.replay()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("config4_graph")
     e0.record()
     for _ in range(replays):
         smp.replay()
     e1.record()
+    torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / replays
     return {"workload": f"GBGPUThirdBody, {W} walkers x {K} sources, N={N}, dt=5 s; "
@@ -506,11 +513,13 @@ def run_gpu(args, rank, world):
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
               for _ in range(K)]
         t_wall = time.perf_counter()
+        torch.cuda.nvtx.range_push(f"config1_{prec}")   # ncu --nvtx-include config1_<prec>/
         for a, b in ev:
             flush.zero_()                     # evict L2 between timed steps
             a.record(stream)
             step(prec)
             b.record(stream)
+        torch.cuda.nvtx.range_pop()
         torch.cuda.synchronize()
         t_wall = time.perf_counter() - t_wall
         ms = [a.elapsed_time(b) for a, b in ev]

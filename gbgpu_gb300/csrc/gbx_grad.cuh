@@ -453,10 +453,12 @@ struct GradParams {
 template <bool THIRD> __host__ __device__ constexpr int grad_acc() { return THIRD ? 29 : 19; }
 
 // shared memory of a grad_kernel tile of maxS samples
+// (buf: A and E per sample, 2 float2; es: 3 float2; third body: psi 3
+// doubles, v_LOS and g 3 floats each)
 __host__ __device__ constexpr size_t grad_smem_bytes(bool third, int maxS)
 {
     return (sizeof(Bin) + sizeof(GradExtra)) * kMaxPack + sizeof(double) * (third ? 29 : 19) * 32 +
-           (size_t)maxS * (6 * sizeof(float2) + (third ? 3 * (sizeof(double) + 2 * sizeof(float)) : 0));
+           (size_t)maxS * (5 * sizeof(float2) + (third ? 3 * (sizeof(double) + 2 * sizeof(float)) : 0));
 }
 
 template <bool THIRD>
@@ -464,6 +466,7 @@ __global__ void __launch_bounds__(kBlock, THIRD ? 1 : 2) grad_kernel(const GradP
 {
     using V = float2;
     constexpr int kGradAcc = grad_acc<THIRD>();
+    const float is2 = 0.70710678118654752440f, is6 = 0.40824829046386301637f;
     const KParams &K = GP.K;
     extern __shared__ __align__(16) unsigned char smem[];
     Bin *bins = reinterpret_cast<Bin *>(smem);
@@ -472,9 +475,14 @@ __global__ void __launch_bounds__(kBlock, THIRD ? 1 : 2) grad_kernel(const GradP
     // red: group partial sums (float pairs) and per-binary FP64 sums, 16 x kGradAcc each
     V *buf = reinterpret_cast<V *>(smem + (sizeof(Bin) + sizeof(GradExtra)) * kMaxPack +
                                    sizeof(double) * kGradAcc * 32);
-    V *es = buf + 3 * (size_t)K.maxS;             // exp(-i phase_s) per sample, from the forward pass
-    // third body: cumulative phase, v_LOS and g = v_LOS f_GW per (sample, spacecraft)
+    // buf: the A and E channels (forward transform, then the adjoint's);
+    // es: exp(-i phase_s) per sample from the forward pass, directly after buf
+    // (the third-body pre-passes use buf and es together as FP64 scratch)
+    V *es = buf + 2 * (size_t)K.maxS;
+    // third body: cumulative phase (forward; reused for the phase adjoints cph
+    // in the backward pass), v_LOS and g = v_LOS f_GW per (sample, spacecraft)
     double *psi = reinterpret_cast<double *>(es + 3 * (size_t)K.maxS);
+    float2 *cphs = reinterpret_cast<float2 *>(psi);
     float *vl = reinterpret_cast<float *>(psi + 3 * (size_t)K.maxS);
     float *gq = vl + 3 * (size_t)K.maxS;
     __shared__ int s_tile;
@@ -541,11 +549,13 @@ __global__ void __launch_bounds__(kBlock, THIRD ? 1 : 2) grad_kernel(const GradP
                 }
             }
             slow_mixed<THIRD, true>(bins[p], n, N, stepd, tab, ps, vv, o, es + 3 * (size_t)m);
-#pragma unroll
-            for (int c = 0; c < 3; c++) buf[(p * 3 + c) * N + swz(n, lg)] = o[c];
+            // A and E before the (linear) transform
+            buf[(p * 2 + 0) * N + swz(n, lg)] = {(o[2].x - o[0].x) * is2, (o[2].y - o[0].y) * is2};
+            buf[(p * 2 + 1) * N + swz(n, lg)] = {(o[0].x - 2.f * o[1].x + o[2].x) * is6,
+                                                 (o[0].y - 2.f * o[1].y + o[2].y) * is6};
         }
         __syncthreads();
-        fft_dif<float>(buf, 3 * cnt, lg);
+        fft_dif<float>(buf, 2 * cnt, lg);
 
         // residual weights, likelihood terms, Qf; conj(w) written in place
         const int Tpb = kBlock / maxcnt;
@@ -555,7 +565,6 @@ __global__ void __launch_bounds__(kBlock, THIRD ? 1 : 2) grad_kernel(const GradP
         float acc[kGradAcc];
 #pragma unroll
         for (int k = 0; k < kGradAcc; k++) acc[k] = 0.0f;
-        const float is2 = 0.70710678118654752440f, is6 = 0.40824829046386301637f;
         if (p < cnt) {
             const Bin &B = bins[p];
             bool out = false;
@@ -565,16 +574,12 @@ __global__ void __launch_bounds__(kBlock, THIRD ? 1 : 2) grad_kernel(const GradP
                 const int j = B.start + i;
                 const int pos = bitrev((i + (N >> 1)) & (N - 1), lg);
                 const int sp = swz(pos, lg);
-                V X = buf[(p * 3 + 0) * N + sp], Y = buf[(p * 3 + 1) * N + sp],
-                  Z = buf[(p * 3 + 2) * N + sp];
-                float2 wX = {0.f, 0.f}, wY = {0.f, 0.f}, wZ = {0.f, 0.f};
+                const V hA = buf[(p * 2 + 0) * N + sp], hE = buf[(p * 2 + 1) * N + sp];
+                float2 uA = {0.f, 0.f}, uE = {0.f, 0.f};
                 if (B.valid && j >= 0 && j < K.L) {
                     const size_t jd = (size_t)B.di * K.L + j, jn = (size_t)B.ni * K.L + j;
                     const double2 dA = __ldg(K.A_data + jd), dE = __ldg(K.E_data + jd);
                     const double SA = __ldg(K.A_psd + jn), SE = __ldg(K.E_psd + jn);
-                    const float2 hA = make_float2((Z.x - X.x) * is2, (Z.y - X.y) * is2);
-                    const float2 hE = make_float2((X.x - 2.f * Y.x + Z.x) * is6,
-                                                  (X.y - 2.f * Y.y + Z.y) * is6);
                     const float wA = __frcp_rn(d2f_scaled(SA, B.eS));
                     const float wE = __frcp_rn(d2f_scaled(SE, B.eS));
                     const float aR = d2f_scaled(dA.x, B.eD), aI = d2f_scaled(dA.y, B.eD);
@@ -584,27 +589,22 @@ __global__ void __launch_bounds__(kBlock, THIRD ? 1 : 2) grad_kernel(const GradP
                     acc[2] += fmaf(hA.x, hA.x, hA.y * hA.y) * wA + fmaf(hE.x, hE.x, hE.y * hE.y) * wE;
                     // r' = d' - sc h ; u = r' / S'
                     const float2 shA = cmul(sc, hA), shE = cmul(sc, hE);
-                    const float2 uA = make_float2((aR - shA.x) * wA, (aI - shA.y) * wA);
-                    const float2 uE = make_float2((eR - shE.x) * wE, (eI - shE.y) * wE);
-                    wX = make_float2(fmaf(-uA.x, is2, uE.x * is6), fmaf(-uA.y, is2, uE.y * is6));
-                    wY = make_float2(-2.f * uE.x * is6, -2.f * uE.y * is6);
-                    wZ = make_float2(fmaf(uA.x, is2, uE.x * is6), fmaf(uA.y, is2, uE.y * is6));
-                    // Qf = sum conj(w) X
-                    acc[3] += fmaf(wX.x, X.x, fmaf(wX.y, X.y, fmaf(wY.x, Y.x, fmaf(wY.y, Y.y,
-                              fmaf(wZ.x, Z.x, wZ.y * Z.y)))));
-                    acc[4] += fmaf(wX.x, X.y, fmaf(-wX.y, X.x, fmaf(wY.x, Y.y, fmaf(-wY.y, Y.x,
-                              fmaf(wZ.x, Z.y, -wZ.y * Z.x)))));
+                    uA = make_float2((aR - shA.x) * wA, (aI - shA.y) * wA);
+                    uE = make_float2((eR - shE.x) * wE, (eI - shE.y) * wE);
+                    // Qf = sum_c conj(w_c) x_c = conj(uA) hA + conj(uE) hE (the
+                    // X, Y, Z weights are the A, E ones mapped back)
+                    acc[3] += fmaf(uA.x, hA.x, fmaf(uA.y, hA.y, fmaf(uE.x, hE.x, uE.y * hE.y)));
+                    acc[4] += fmaf(uA.x, hA.y, fmaf(-uA.y, hA.x, fmaf(uE.x, hE.y, -uE.y * hE.x)));
                 } else if (B.valid) {
                     out = true;
                 }
-                buf[(p * 3 + 0) * N + sp] = make_float2(wX.x, -wX.y);
-                buf[(p * 3 + 1) * N + sp] = make_float2(wY.x, -wY.y);
-                buf[(p * 3 + 2) * N + sp] = make_float2(wZ.x, -wZ.y);
+                buf[(p * 2 + 0) * N + sp] = make_float2(uA.x, -uA.y);
+                buf[(p * 2 + 1) * N + sp] = make_float2(uE.x, -uE.y);
             }
             if (out) flag(a.status, GBX_FLAG_WINDOW);
         }
         __syncthreads();
-        fft_dit<float>(buf, 3 * cnt, lg);
+        fft_dit<float>(buf, 2 * cnt, lg);
 
         // backward pass: Y_c,n at natural position n
         if (p < cnt) {
@@ -614,13 +614,16 @@ __global__ void __launch_bounds__(kBlock, THIRD ? 1 : 2) grad_kernel(const GradP
                 for (int n = i0; n < N; n += Tpb) {
                     float2 Yc[3], Es[3];
                     float2 *ep = es + 3 * ((size_t)(p << lg) + n);
+                    // Y_X, Y_Y, Y_Z from the transformed A, E weights
+                    const V YA = buf[(p * 2 + 0) * N + swz(n, lg)], YE = buf[(p * 2 + 1) * N + swz(n, lg)];
+                    Yc[0] = make_float2(fmaf(-YA.x, is2, YE.x * is6), fmaf(-YA.y, is2, YE.y * is6));
+                    Yc[1] = make_float2(-2.f * YE.x * is6, -2.f * YE.y * is6);
+                    Yc[2] = make_float2(fmaf(YA.x, is2, YE.x * is6), fmaf(YA.y, is2, YE.y * is6));
 #pragma unroll
-                    for (int c = 0; c < 3; c++) {
-                        Yc[c] = buf[(p * 3 + c) * N + swz(n, lg)];
-                        Es[c] = ep[c];
-                    }
+                    for (int c = 0; c < 3; c++) Es[c] = ep[c];
                     if (THIRD) {
-                        // cph replaces Y and cfo replaces exp(-i phase) in this thread's own slots
+                        // cph goes to the (now free) psi rows, cfo replaces exp(-i phase)
+                        // in this thread's own slots
                         float vv[3];
                         float2 cph[3], cfo[3];
 #pragma unroll
@@ -629,7 +632,7 @@ __global__ void __launch_bounds__(kBlock, THIRD ? 1 : 2) grad_kernel(const GradP
                                               vv, cph, cfo);
 #pragma unroll
                         for (int s = 0; s < 3; s++) {
-                            buf[(p * 3 + s) * N + swz(n, lg)] = cph[s];
+                            cphs[(p * 3 + s) * N + swz(n, lg)] = cph[s];
                             ep[s] = cfo[s];
                         }
                     } else {
@@ -644,7 +647,7 @@ __global__ void __launch_bounds__(kBlock, THIRD ? 1 : 2) grad_kernel(const GradP
             const int warp = tid >> 5, lane = tid & 31;
             const int chunk = N >> 5;
             for (int row = warp; row < 3 * cnt; row += kBlock / 32) {
-                V *rp = buf + (size_t)row * N;
+                V *rp = cphs + (size_t)row * N;
                 const int c0 = lane * chunk;
                 float2 t = {0.f, 0.f};
                 for (int c = 0; c < chunk; c++) t = cadd(t, rp[swz(c0 + c, lg)]);
@@ -668,7 +671,7 @@ __global__ void __launch_bounds__(kBlock, THIRD ? 1 : 2) grad_kernel(const GradP
                 for (int k = i0; k < N; k += Tpb) {
                     const float2 *cf = es + 3 * ((size_t)(p << lg) + k);
                     const float2 cfo[3] = {cf[0], cf[1], cf[2]};
-                    third_grad_sample(B, Gx, k, N, lg, step, tab, ifs, buf + (size_t)(p * 3) * N,
+                    third_grad_sample(B, Gx, k, N, lg, step, tab, ifs, cphs + (size_t)(p * 3) * N,
                                       gq + (size_t)(p * 3) * N, cfo, acc + 5, acc + 19);
                 }
             }

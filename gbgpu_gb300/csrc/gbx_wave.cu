@@ -834,6 +834,9 @@ template <typename R, int MODE, bool THIRD>
 __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(const KParams K)
 {
     using V = typename C2<R>::T;
+    // transformed channels: X, Y, Z for the waveform outputs; A, E otherwise
+    constexpr int NCH = MODE == MODE_WAVE ? 3 : 2;
+    const R is2 = (R)0.70710678118654752440, is6 = (R)0.40824829046386301637;
     extern __shared__ __align__(16) unsigned char smem[];
     Bin *bins = reinterpret_cast<Bin *>(smem);
     double *red = reinterpret_cast<double *>(smem + sizeof(Bin) * kMaxPack);
@@ -930,15 +933,22 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                 float vf[3] = {(float)vv[0], (float)vv[1], (float)vv[2]};
                 slow_mixed<THIRD>(B, n, N, stepd, tab, ps, vf, reinterpret_cast<float2 *>(o));
             }
+            if constexpr (NCH == 3) {
 #pragma unroll
-            for (int c = 0; c < 3; c++) buf[(p * 3 + c) * N + swz(n, lg)] = o[c];
+                for (int c = 0; c < 3; c++) buf[(p * 3 + c) * N + swz(n, lg)] = o[c];
+            } else {
+                // A = (Z - X)/sqrt2, E = (X - 2Y + Z)/sqrt6 (utility.py:24-38) formed
+                // before the transform: the FFT is linear, so two transforms suffice
+                buf[(p * 2 + 0) * N + swz(n, lg)] = {(o[2].x - o[0].x) * is2, (o[2].y - o[0].y) * is2};
+                buf[(p * 2 + 1) * N + swz(n, lg)] = {(o[0].x - 2 * o[1].x + o[2].x) * is6,
+                                                     (o[0].y - 2 * o[1].y + o[2].y) * is6};
+            }
         }
         __syncthreads();
 
-        fft_dif<R>(buf, 3 * cnt, lg);
+        fft_dif<R>(buf, NCH * cnt, lg);
 
         // ------------------------------------------------------------ epilogue
-        const R is2 = (R)0.70710678118654752440, is6 = (R)0.40824829046386301637;
         if (MODE == MODE_WAVE) {
             for (int m = tid; m < S; m += kBlock) {
                 const int p = m >> lg, i = m & (N - 1);
@@ -997,8 +1007,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                             continue;
                         }
                         const int pos = bitrev((i + (N >> 1)) & (N - 1), lg);
-                        V X = buf[(pw * 3 + 0) * N + swz(pos, lg)], Y = buf[(pw * 3 + 1) * N + swz(pos, lg)],
-                          Z = buf[(pw * 3 + 2) * N + swz(pos, lg)];
+                        const V hA = buf[(pw * 2 + 0) * N + swz(pos, lg)], hE = buf[(pw * 2 + 1) * N + swz(pos, lg)];
                         const size_t jd = (size_t)Bn.di * K.L + j, jn = (size_t)Bn.ni * K.L + j;
                         const double2 dA = __ldg(K.A_data + jd), dE = __ldg(K.E_data + jd);
                         const double SA = __ldg(K.A_psd + jn), SE = __ldg(K.E_psd + jn);
@@ -1012,8 +1021,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                             aR = d2f_scaled(dA.x, Bn.eD); aI = d2f_scaled(dA.y, Bn.eD);
                             eR = d2f_scaled(dE.x, Bn.eD); eI = d2f_scaled(dE.y, Bn.eD);
                         }
-                        const Acc hAr = (Z.x - X.x) * (Acc)is2, hAi = (Z.y - X.y) * (Acc)is2;
-                        const Acc hEr = (X.x - 2 * Y.x + Z.x) * (Acc)is6, hEi = (X.y - 2 * Y.y + Z.y) * (Acc)is6;
+                        const Acc hAr = hA.x, hAi = hA.y, hEr = hE.x, hEi = hE.y;
                         // conj(r) h / S
                         const Acc cr = (aR * hAr + aI * hAi) * wA + (eR * hEr + eI * hEi) * wE;
                         const Acc ci = (aR * hAi - aI * hAr) * wA + (eR * hEi - eI * hEr) * wE;
@@ -1023,11 +1031,9 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                             const int k = j - Bo.start;
                             if (k >= 0 && k < N) {
                                 const int pk = bitrev((k + (N >> 1)) & (N - 1), lg);
-                                V Xo = buf[(po * 3 + 0) * N + swz(pk, lg)], Yo = buf[(po * 3 + 1) * N + swz(pk, lg)],
-                                  Zo = buf[(po * 3 + 2) * N + swz(pk, lg)];
-                                const Acc oAr = (Zo.x - Xo.x) * (Acc)is2, oAi = (Zo.y - Xo.y) * (Acc)is2;
-                                const Acc oEr = (Xo.x - 2 * Yo.x + Zo.x) * (Acc)is6,
-                                          oEi = (Xo.y - 2 * Yo.y + Zo.y) * (Acc)is6;
+                                const V oA = buf[(po * 2 + 0) * N + swz(pk, lg)],
+                                        oE = buf[(po * 2 + 1) * N + swz(pk, lg)];
+                                const Acc oAr = oA.x, oAi = oA.y, oEr = oE.x, oEi = oE.y;
                                 // conj(h_old) h_new / S
                                 acc8[6] += (oAr * hAr + oAi * hAi) * wA + (oEr * hEr + oEi * hEi) * wE;
                                 acc8[7] += (oAr * hAi - oAi * hAr) * wA + (oEr * hEi - oEi * hEr) * wE;
@@ -1039,26 +1045,25 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                     if (out) flag(a.status, GBX_FLAG_WINDOW);
                 }
             }
-            double gs[8];
-#pragma unroll
-            for (int k = 0; k < 8; k++) {
-                if constexpr (sizeof(R) == 8) {
-                    double x = acc8[k];
-                    for (int o = width >> 1; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-                    gs[k] = x;
-                } else {
-                    dfl x = {acc8[k], 0.f};
-                    for (int o = width >> 1; o > 0; o >>= 1) {
-                        dfl y = {__shfl_xor_sync(0xffffffffu, x.h, o), __shfl_xor_sync(0xffffffffu, x.l, o)};
-                        x = df_add(x, y);
-                    }
-                    gs[k] = (double)x.h + (double)x.l;
-                }
-            }
-            if ((tid & (width - 1)) == 0) {
+            {
+                // group trees; only the group leaders convert to FP64
+                const bool leader = (tid & (width - 1)) == 0;
                 const int g = tid / width;
 #pragma unroll
-                for (int k = 0; k < 8; k++) red[8 * g + k] = gs[k];
+                for (int k = 0; k < 8; k++) {
+                    if constexpr (sizeof(R) == 8) {
+                        double x = acc8[k];
+                        for (int o = width >> 1; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+                        if (leader) red[8 * g + k] = x;
+                    } else {
+                        dfl x = {acc8[k], 0.f};
+                        for (int o = width >> 1; o > 0; o >>= 1) {
+                            dfl y = {__shfl_xor_sync(0xffffffffu, x.h, o), __shfl_xor_sync(0xffffffffu, x.l, o)};
+                            x = df_add(x, y);
+                        }
+                        if (leader) red[8 * g + k] = (double)x.h + (double)x.l;
+                    }
+                }
             }
             __syncthreads();
             if (2 * tid + 1 < cnt) {
@@ -1089,11 +1094,9 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                 const int j = B.start + i;
                 if (!B.valid || j < 0 || j >= K.L) continue;
                 const int pos = bitrev((i + (N >> 1)) & (N - 1), lg);
-                V X = buf[(p * 3 + 0) * N + swz(pos, lg)], Y = buf[(p * 3 + 1) * N + swz(pos, lg)],
-                  Z = buf[(p * 3 + 2) * N + swz(pos, lg)];
-                double2 Ah = cmul(make_double2((double)((Z.x - X.x) * is2), (double)((Z.y - X.y) * is2)), B.scale);
-                double2 Eh = cmul(make_double2((double)((X.x - 2 * Y.x + Z.x) * is6),
-                                               (double)((X.y - 2 * Y.y + Z.y) * is6)), B.scale);
+                const V hA = buf[(p * 2 + 0) * N + swz(pos, lg)], hE = buf[(p * 2 + 1) * N + swz(pos, lg)];
+                double2 Ah = cmul(make_double2((double)hA.x, (double)hA.y), B.scale);
+                double2 Eh = cmul(make_double2((double)hE.x, (double)hE.y), B.scale);
                 const size_t o = (size_t)B.gi * K.gstride + j;
                 atomicAdd(&K.A_glob[o].x, Ah.x);
                 atomicAdd(&K.A_glob[o].y, Ah.y);
@@ -1124,24 +1127,20 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                             continue;
                         }
                         const int pos = bitrev((i + (N >> 1)) & (N - 1), lg);
-                        V X = buf[(p * 3 + 0) * N + swz(pos, lg)], Y = buf[(p * 3 + 1) * N + swz(pos, lg)],
-                          Z = buf[(p * 3 + 2) * N + swz(pos, lg)];
+                        const V tA = buf[(p * 2 + 0) * N + swz(pos, lg)], tE = buf[(p * 2 + 1) * N + swz(pos, lg)];
                         const size_t jd = (size_t)B.di * K.L + j, jn = (size_t)B.ni * K.L + j;
                         const double2 dA = __ldg(K.A_data + jd), dE = __ldg(K.E_data + jd);
                         const double SA = __ldg(K.A_psd + jn), SE = __ldg(K.E_psd + jn);
                         if constexpr (sizeof(R) == 8) {
-                            double2 hA = cmul(make_double2((Z.x - X.x) * is2, (Z.y - X.y) * is2), B.scale);
-                            double2 hE = cmul(make_double2((X.x - 2.0 * Y.x + Z.x) * is6,
-                                                           (X.y - 2.0 * Y.y + Z.y) * is6), B.scale);
+                            double2 hA = cmul(make_double2(tA.x, tA.y), B.scale);
+                            double2 hE = cmul(make_double2(tE.x, tE.y), B.scale);
                             const double wA = 1.0 / SA, wE = 1.0 / SE;
                             // conj(d) h / S  (gbgpu_utils.cu:172-178)
                             sr += (dA.x * hA.x + dA.y * hA.y) * wA + (dE.x * hE.x + dE.y * hE.y) * wE;
                             si += (dA.x * hA.y - dA.y * hA.x) * wA + (dE.x * hE.y - dE.y * hE.x) * wE;
                             sh += (hA.x * hA.x + hA.y * hA.y) * wA + (hE.x * hE.x + hE.y * hE.y) * wE;
                         } else {
-                            float2 hA = make_float2((Z.x - X.x) * (float)is2, (Z.y - X.y) * (float)is2);
-                            float2 hE = make_float2((X.x - 2.f * Y.x + Z.x) * (float)is6,
-                                                    (X.y - 2.f * Y.y + Z.y) * (float)is6);
+                            const float2 hA = tA, hE = tE;
                             const float wA = __frcp_rn(d2f_scaled(SA, B.eS));
                             const float wE = __frcp_rn(d2f_scaled(SE, B.eS));
                             const float aR = d2f_scaled(dA.x, B.eD), aI = d2f_scaled(dA.y, B.eD);
@@ -1291,12 +1290,15 @@ __global__ void __launch_bounds__(kPrepBlock) prep_kernel(const KParams K)
 // ----------------------------------------------------------------------------
 // host side
 // ----------------------------------------------------------------------------
-static size_t smem_bytes(int prec, bool third, int maxS)
+// nch transformed channels per binary (3 for the waveform outputs, 2 = A, E
+// otherwise); the third-body pre-passes use three slots per sample of buf as
+// FP64 scratch and keep psi and v_LOS after them
+static size_t smem_bytes(int prec, bool third, int maxS, int nch)
 {
     size_t head = sizeof(Bin) * kMaxPack + sizeof(double) * (size_t)red_doubles(maxS);
     size_t rc = prec == GBX_FP64 ? sizeof(double2) : sizeof(float2);
     size_t r = prec == GBX_FP64 ? sizeof(double) : sizeof(float);
-    size_t s = head + 3 * (size_t)maxS * rc;
+    size_t s = head + (third ? 3 : nch) * (size_t)maxS * rc;
     if (third) s += 3 * (size_t)maxS * (sizeof(double) + r);
     return s;
 }
@@ -1305,7 +1307,7 @@ template <typename R, int MODE, bool THIRD>
 static int launch_one(const KParams &K, int maxS, cudaStream_t st)
 {
     auto kern = wave_kernel<R, MODE, THIRD>;
-    size_t sm = smem_bytes(sizeof(R) == 8 ? GBX_FP64 : GBX_MIXED, THIRD, maxS);
+    size_t sm = smem_bytes(sizeof(R) == 8 ? GBX_FP64 : GBX_MIXED, THIRD, maxS, MODE == MODE_WAVE ? 3 : 2);
     if (sm > 227 * 1024) return set_error(GBX_ERR_UNSUPPORTED, "tile needs %zu B of shared memory", sm);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute");
