@@ -974,6 +974,79 @@ class GBGPUBase(abc.ABC):
             return info.cpu().numpy()
         return info
 
+    def fisher_matrices(self, params, N, T=4 * YRSID_SI, dt=10.0, tdi2=False, inds=None,
+                        psd_func=None, psd_kwargs={}, return_gpu=False):
+        """Per-binary Fisher matrices F_ij = <dh/dtheta_i | dh/dtheta_j> (A and E)
+        for a whole batch, by five-point FP64 central differences of the
+        batched waveform in absolute parameter steps.
+
+        Unlike ``information_matrix`` (the reference's, gbgpu.py:957-1138: steps
+        relative to each parameter, and every binary of a call must share one
+        start bin), binaries may sit anywhere: each derivative is taken on the
+        binary's own window; the f0 stencil stays inside the binary's carrier
+        bin rint(f0 T) (shortened near a bin edge), and a step that still moves
+        the window is aligned before differencing.  ``params`` is (nparams, B); ``inds``
+        selects the parameters (default all 9 / 14).  Steps: amp 1e-6 amp;
+        f0 1e-4/T; fdot 1e-4/T^2; fddot 1e-4/T^3 (phase-equivalent); angles
+        1e-6 rad; third body: A2, P2 relative 1e-6, varpi, e2, T2 1e-6.  Returns (B, n, n)
+        NumPy (or a CUDA tensor with ``return_gpu``).
+        """
+        if psd_func is None:
+            from .sensitivity import A1TDISens
+            psd_func = A1TDISens.get_Sn
+        prm = _to_device(params, torch.float64, self.device).contiguous()
+        npar, B = prm.shape
+        if npar != self.NPARAMS:
+            raise ValueError(f"params must be ({self.NPARAMS}, B)")
+        inds = list(range(npar)) if inds is None else [int(i) for i in inds]
+        Tu = int(T / dt) * dt
+        N = int(N)
+        absolute = {1: 1e-4 / Tu, 2: 1e-4 / Tu ** 2, 3: 1e-4 / Tu ** 3, 4: 1e-6, 5: 1e-6,
+                    6: 1e-6, 7: 1e-6, 8: 1e-6, 10: 1e-6, 11: 1e-6, 13: 1e-6}
+
+        def wave(p):
+            self.run_wave(*p, N=N, T=T, dt=dt, tdi2=tdi2)
+            return torch.stack([self.A, self.E], 1), self.start_inds.clone()
+
+        h0, s0 = wave(prm)
+        n = len(inds)
+        dh = torch.zeros((B, n, 2, N), dtype=torch.complex128, device=self.device)
+        cols = torch.arange(N, device=self.device)
+
+        def aligned(h, s):
+            # the window starting at bin s on the grid of the centre window s0:
+            # out[i] = h[i - (s - s0)] where that index exists, else 0
+            src = cols[None, :] - (s - s0)[:, None]
+            ok = (src >= 0) & (src < N)
+            idx = src.clamp(0, N - 1)[:, None, :].expand(-1, 2, -1)
+            return torch.where(ok[:, None, :], torch.gather(h, 2, idx), torch.zeros_like(h))
+
+        for i, ind in enumerate(inds):
+            step = prm[ind].abs() * 1e-6 if ind in (0, 9, 12) else \
+                torch.full((B,), absolute[ind], dtype=torch.float64, device=self.device)
+            if ind == 1:
+                # keep the stencil inside the carrier bin rint(f0 T): the
+                # heterodyned model is not exactly invariant under a change of q
+                frac = prm[1] * Tu - torch.round(prm[1] * Tu)
+                room = (0.5 - frac.abs()) / Tu
+                step = torch.minimum(step, torch.clamp(room / 2.5, min=1e-7 / Tu))
+            step = torch.where(step > 0, step, torch.full_like(step, 1e-12))
+            hs = []
+            for m in (2, 1, -1, -2):
+                q = prm.clone()
+                q[ind] = q[ind] + m * step
+                h, si = wave(q)
+                hs.append(aligned(h, si))
+            dh[:, i] = (-hs[0] + 8 * hs[1] - 8 * hs[2] + hs[3]) / (12 * step)[:, None, None]
+        self.run_wave(*prm, N=N, T=T, dt=dt, tdi2=tdi2)
+        freqs = self.freqs
+        psd = torch.as_tensor(np.asarray(psd_func(_to_host(freqs), **psd_kwargs)),
+                              device=self.device, dtype=torch.float64)
+        w = 4.0 / Tu / psd                                          # (B, N)
+        F = torch.einsum("bicn,bjcn->bij", dh.conj() * w[:, None, None, :], dh).real
+        F = 0.5 * (F + F.transpose(1, 2))
+        return F if return_gpu else F.cpu().numpy()
+
     # ----------------------------------------------------------------- hooks
     @abc.abstractmethod
     def add_to_argS(self, argS, f0, fdot, fddot, xi, *args):

@@ -118,3 +118,130 @@ def random_proposals(params_k, scale, gen):
 def log_uniforms(W, steps, gen, device):
     u = torch.rand((steps, W), generator=gen, device=device, dtype=torch.float64)
     return torch.log(u.clamp_min(math.ldexp(1.0, -60)))
+
+
+class HMCSampler:
+    """Hamiltonian Monte Carlo over the source parameters of a batch of
+    independent binaries, driven by the fused likelihood + gradient kernel.
+
+    Every binary is its own chain with target logL (the mixed fused
+    likelihood, the one the gradient belongs to).  The free parameters
+    (default amp, f0, fdot, phi0, iota, psi, lam, beta; fddot is held fixed)
+    move in whitened coordinates x = theta / scale with unit mass, so
+    ``scales`` (e.g. Fisher-diagonal standard deviations) set the metric.  A
+    transition is ``n_leapfrog`` leapfrog steps (one kernel launch each: the
+    gradient at the end of a step is the one the next step starts with)
+    followed by a Metropolis test on H = -logL + |p|^2 / 2.  Momenta and
+    uniform draws are prepared on the device beforehand, so any number of
+    transitions is captured and replayed as one CUDA graph.  The reference
+    has no counterpart (its derivatives are finite differences).
+    """
+
+    FREE = (0, 1, 2, 4, 5, 6, 7, 8)
+
+    def __init__(self, gb, params, data, psd, N, T, dt, scales, step_size, n_leapfrog,
+                 start_freq_ind=0, tdi2=False, data_index=None, noise_index=None, free=FREE):
+        import ctypes
+        from . import _native as nat
+        self._nat, self._ctypes = nat, ctypes
+        self.gb = gb
+        dev = gb.device
+        self.params = params.to(device=dev, dtype=torch.float64).clone().contiguous()
+        npar, B = self.params.shape
+        if npar != gb.NPARAMS:
+            raise ValueError(f"params must be ({gb.NPARAMS}, B)")
+        if gb.d_d is None:
+            raise ValueError("set gb.d_d before sampling")
+        self.B = B
+        self.free = torch.as_tensor(list(free), device=dev, dtype=torch.long)
+        nf = len(free)
+        s = torch.as_tensor(scales, device=dev, dtype=torch.float64)
+        self.scale = (s[:, None].expand(nf, B) if s.ndim == 1 else s).contiguous()
+        self.eps = float(step_size)
+        self.n_leapfrog = int(n_leapfrog)
+        Tu = int(T / dt) * dt
+        dd, pp, L, di, ni = gb._prepare_data(data, psd, data_index, noise_index, B)
+        self.la = gb._ll_args(dd, pp, L, di, ni, Tu)
+        self.d_h = torch.zeros(B, dtype=torch.complex128, device=dev)
+        self.h_h = torch.zeros(B, dtype=torch.complex128, device=dev)
+        self.grad = torch.zeros((npar, B), dtype=torch.float64, device=dev)
+        self.d_d = torch.as_tensor(gb.d_d, dtype=torch.float64, device=dev)
+        self._lib = nat.lib()
+
+        def bind(tile, bps):
+            plan = gb._plan(N, Tu, "mixed", tdi2, npar, tile, bps)
+            self.args = plan.args(self.params, start_freq_ind, gb._status, grad=True)
+
+        def run(tile, bps):
+            bind(tile, bps)
+            self._evaluate()
+        self.args = None
+        bind(*gb._launch_shape("grad", N, B, "mixed", tdi2, npar, run))
+        # state at the current point
+        self._evaluate()
+        self.logL = self._like().clone()
+        self.g = self.grad[self.free].clone()
+        self.accepted = torch.zeros(B, dtype=torch.int64, device=dev)
+        self.dH = torch.zeros(B, dtype=torch.float64, device=dev)
+        self.graph = None
+
+    def _evaluate(self):
+        nat, ct = self._nat, self._ctypes
+        rc = self._lib.gbx_waveform_ll_grad(ct.byref(self.args), ct.byref(self.la),
+                                            nat.ptr(self.d_h), nat.ptr(self.h_h),
+                                            nat.ptr(self.grad), nat.stream_handle())
+        nat.check(rc, "gbx_waveform_ll_grad")
+
+    def _like(self):
+        return -0.5 * (self.d_d + self.h_h.real - 2.0 * self.d_h.real)
+
+    def leapfrog(self, p, g):
+        """``n_leapfrog`` leapfrog steps from the current parameters (moved in
+        place) with whitened momenta ``p`` and free-parameter gradient ``g``
+        there.  Returns (p, g, logL) at the end point."""
+        f, s, eps = self.free, self.scale, self.eps
+        for _ in range(self.n_leapfrog):
+            p = p + (0.5 * eps) * (g * s)
+            self.params[f] = self.params[f] + eps * (s * p)
+            self._evaluate()
+            g = self.grad[f]
+            p = p + (0.5 * eps) * (g * s)
+        return p, g, self._like()
+
+    def transition(self, mom, log_u):
+        """One HMC transition of every chain: ``mom`` (nfree, B) standard normal
+        momenta, ``log_u`` (B,) log uniforms.  Returns the accept mask."""
+        f = self.free
+        q0 = self.params[f].clone()
+        H0 = -self.logL + 0.5 * (mom * mom).sum(0)
+        p, g, like = self.leapfrog(mom.clone(), self.g)
+        dH = (-like + 0.5 * (p * p).sum(0)) - H0
+        acc = (log_u < -dH) & torch.isfinite(dH)
+        self.params[f] = torch.where(acc[None, :], self.params[f], q0)
+        self.logL.copy_(torch.where(acc, like, self.logL))
+        self.g.copy_(torch.where(acc[None, :], g, self.g))
+        self.accepted += acc
+        self.dH.copy_(dH)
+        return acc
+
+    def capture(self, moms, log_us):
+        """Capture len(moms) transitions (moms (S, nfree, B), log_us (S, B)) as one graph."""
+        self.moms, self.log_us = moms, log_us
+        snap = (self.params.clone(), self.logL.clone(), self.g.clone(), self.accepted.clone())
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):                 # warm-up outside capture
+            self.transition(moms[0], log_us[0])
+        torch.cuda.current_stream().wait_stream(s)
+        torch.cuda.synchronize()
+        for dst, src in zip((self.params, self.logL, self.g, self.accepted), snap):
+            dst.copy_(src)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            for i in range(moms.shape[0]):
+                self.transition(moms[i], log_us[i])
+        self._graph_keep = (self.args, self.la)
+        return self.graph
+
+    def replay(self):
+        self.graph.replay()

@@ -1,0 +1,75 @@
+"""Batched per-binary Fisher matrices (GBGPUBase.fisher_matrices).
+
+Checked against the exact FP64 Fisher matrix of the torch restatement
+(oracle/fastgb_torch.py): J_i = dh/dtheta_i by forward mode, F_ij = 4/T
+sum Re conj(J_i) J_j / S over the A, E windows.  Includes binaries whose f0
+sits next to a bin boundary (the difference stencil moves their window) and
+the third-body model.
+"""
+
+import numpy as np
+import pytest
+
+import fastgb_oracle as O
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+T_OBS = 4 * 31557600.0
+DT = 10.0
+
+
+def _exact_fisher(p, th, N):
+    import fastgb_torch as FT
+    from gbgpu_gb300.sensitivity import A1TDISens
+    Tu = int(T_OBS / DT) * DT
+    pt = torch.as_tensor(p)
+    tt = None if th is None else torch.as_tensor(th)
+    rows = p.shape[0] + (0 if th is None else th.shape[0])
+    J = []
+    for k in range(rows):
+        dp = torch.zeros_like(pt)
+        dt_ = None if tt is None else torch.zeros_like(tt)
+        if k < p.shape[0]:
+            dp[k] = 1.0
+        else:
+            dt_[k - p.shape[0]] = 1.0
+        if tt is None:
+            _, j = torch.func.jvp(lambda x: FT.waveform_aet(x, N, T_OBS, DT), (pt,), (dp,))
+        else:
+            _, j = torch.func.jvp(lambda x, y: FT.waveform_aet(x, N, T_OBS, DT, third=y),
+                                  (pt, tt), (dp, dt_))
+        J.append(j.numpy())
+    J = np.stack(J, 1)                                   # (B, n, 2, N)
+    start = O.start_indices(p[1], N, T_OBS, DT)
+    S = A1TDISens.get_Sn((start[:, None] + np.arange(N)[None, :]) / Tu)
+    return 4.0 / Tu * np.einsum("bicn,bjcn->bij", np.conj(J) / S[:, None, None, :], J).real
+
+
+@pytest.mark.parametrize("third", [False, True])
+def test_fisher_matrices_match_exact_forward_mode(third):
+    from gbgpu_gb300 import GBGPU, GBGPUThirdBody
+    rng = np.random.default_rng(9)
+    B, N = 12, 256
+    Tu = int(T_OBS / DT) * DT
+    q = np.rint(rng.uniform(2e-3, 4e-3, B) * Tu)
+    frac = rng.uniform(-0.3, 0.3, B)
+    frac[:3] = [0.49995, -0.49995, 0.4999]                 # stencil crosses a bin edge
+    f0 = (q + frac) / Tu
+    fdot = 10 ** rng.uniform(-17, -16, B)
+    p = np.array([10 ** rng.uniform(-22.3, -21.7, B), f0, fdot, 11 / 3 * fdot ** 2 / f0,
+                  rng.uniform(0.5, 5.5, B), np.arccos(rng.uniform(-0.9, 0.9, B)),
+                  rng.uniform(0.3, 2.8, B), rng.uniform(0.5, 5.5, B),
+                  np.arcsin(rng.uniform(-0.9, 0.9, B))])
+    th = None
+    if third:
+        P2 = 10 ** rng.uniform(0.3, 1.0, B)
+        th = np.array([10 ** rng.uniform(0.5, 1.5, B), rng.uniform(0.3, 6.0, B),
+                       rng.uniform(0.1, 0.8, B), P2, rng.uniform(0.1, 0.9, B) * P2])
+    gb = GBGPUThirdBody() if third else GBGPU()
+    full = p if th is None else np.concatenate([p, th])
+    F = gb.fisher_matrices(full, N=N, T=T_OBS, dt=DT)
+    ref = _exact_fisher(p, th, N)
+    d = np.sqrt(np.einsum("bii->bi", ref))
+    err = np.abs(F - ref) / (d[:, :, None] * d[:, None, :])
+    assert np.max(err) < 1e-5, np.unravel_index(np.argmax(err), err.shape)
