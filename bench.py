@@ -332,6 +332,77 @@ def config3(gb, data, Sd, seed, steps):
     out["launch_shapes"] = shapes
     out["grad_over_forward"] = out["grad_binaries_per_s"] / out["mixed_binaries_per_s"]
     out["mixed_over_fp64"] = out["mixed_binaries_per_s"] / out["fp64_binaries_per_s"]
+    out["fisher"] = config3_fisher(gb, p, Tu)
+    out["hmc"] = config3_hmc(gb, p, data, Sd, seed)
+    return out
+
+
+FREE8 = (0, 1, 2, 4, 5, 6, 7, 8)      # amp, f0, fdot, phi0, iota, psi, lam, beta (fddot fixed)
+
+
+def config3_fisher(gb, p, Tu):
+    """Per-binary 8x8 Fisher matrices of the 50k config-3 binaries (FP64
+    five-point differences of the batched waveform, TDI-2)."""
+    import torch
+    B = p.shape[1]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    torch.cuda.nvtx.range_push("config3_fisher")
+    F = gb.fisher_matrices(p, N=256, T=T_OBS, dt=DT, tdi2=True, inds=FREE8, return_gpu=True)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    dt_s = time.perf_counter() - t0
+    ok = bool(torch.isfinite(F).all().item())
+    return {"binaries": B, "params": len(FREE8), "seconds": dt_s, "binaries_per_s": B / dt_s,
+            "finite": ok, "note": "5-point FP64 differences: 32 batched FP64 waveform launches "
+                                  "+ one inner-product einsum"}
+
+
+def config3_hmc(gb, p, data, Sd, seed, B=4096, transitions=100, n_leapfrog=10, step=0.2):
+    """1,000-step HMC leapfrog chains for 4,096 binaries in one CUDA graph: the
+    4,096 loudest config-3 binaries, injected into a copy of the data; mass
+    metric from their Fisher diagonals; every leapfrog step is one fused
+    likelihood + gradient launch."""
+    import torch
+    from gbgpu_gb300.mcmc import HMCSampler
+    sel = np.argsort(-p[0])[:B]
+    q = np.ascontiguousarray(p[:, sel])
+    dA, dE = data[0].clone(), data[1].clone()
+    gb.add_to_templates(torch.as_tensor(q, device="cuda"), torch.zeros(B, dtype=torch.int32,
+                                                                    device="cuda"),
+                        (dA[None], dE[None]), N=256, T=T_OBS, dt=DT, tdi2=True, precision="fp64")
+    F = gb.fisher_matrices(q, N=256, T=T_OBS, dt=DT, tdi2=True, inds=FREE8, return_gpu=True)
+    sig = 1.0 / torch.sqrt(torch.diagonal(F, dim1=1, dim2=2)).T.contiguous()
+    d_d = gb.d_d
+    gb.d_d = 0.0
+    smp = HMCSampler(gb, torch.as_tensor(q, device="cuda"), [dA, dE], [Sd, Sd], N=256, T=T_OBS,
+                     dt=DT, scales=sig, step_size=step, n_leapfrog=n_leapfrog, tdi2=True,
+                     free=FREE8)
+    gb.d_d = d_d
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed + 33)
+    moms = torch.randn((transitions, len(FREE8), B), generator=g, device="cuda",
+                       dtype=torch.float64)
+    lus = torch.log(torch.rand((transitions, B), generator=g, device="cuda",
+                               dtype=torch.float64).clamp_min(1e-300))
+    smp.capture(moms, lus)
+    smp.accepted.zero_()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("config3_hmc")
+    e0.record()
+    smp.replay()
+    e1.record()
+    torch.cuda.nvtx.range_pop()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    steps = transitions * n_leapfrog
+    return {"binaries": B, "leapfrog_steps": steps, "transitions": transitions,
+            "step_size": step, "graph_ms": ms,
+            "binary_leapfrog_steps_per_s": B * steps / (ms / 1e3),
+            "acceptance": float(smp.accepted.sum().item()) / (B * transitions),
+            "note": "whitened coordinates (Fisher-diagonal sigmas); one fused likelihood + "
+                    "gradient launch per leapfrog step, all captured in one CUDA graph"}
     return out
 
 

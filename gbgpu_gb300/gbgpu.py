@@ -14,7 +14,6 @@ through device memory, and the waveform attributes (``XYZf``, ``AETf``,
 
 import abc
 import ctypes
-import hashlib
 import os
 import warnings
 
@@ -37,10 +36,32 @@ def _is_pow2(n):
     return n >= 1 and (n & (n - 1)) == 0
 
 
-def _to_device(x, dtype, device):
+def _to_device(x, dtype, device, non_blocking=False):
+    """``non_blocking`` queues a copy from pinned host memory on the current
+    stream; only for callers that read their results back before returning."""
     if isinstance(x, torch.Tensor):
-        return x.to(device=device, dtype=dtype)
+        nb = non_blocking and x.device.type == "cpu" and x.is_pinned() and x.dtype == dtype
+        return x.to(device=device, dtype=dtype, non_blocking=nb)
     return torch.as_tensor(np.asarray(x), dtype=dtype, device=device)
+
+
+_KEY_MULT = np.zeros((2, 0), dtype=np.uint64)
+
+
+def _array_key(arr):
+    """128-bit content key of an int64 array: two dot products with fixed
+    random odd 64-bit multipliers, wrapping mod 2^64 (one vectorised pass; a
+    cryptographic hash of a 200k-entry N array cost milliseconds per call)."""
+    global _KEY_MULT
+    n = arr.shape[0]
+    if _KEY_MULT.shape[1] < n:
+        rng = np.random.default_rng(0x5EED)
+        m = max(n, 2 * _KEY_MULT.shape[1], 1024)
+        _KEY_MULT = rng.integers(0, 2 ** 63, size=(2, m), dtype=np.uint64) * np.uint64(2) + \
+            np.uint64(1)
+    v = arr.view(np.uint64)
+    with np.errstate(over="ignore"):
+        return (int(np.dot(v, _KEY_MULT[0, :n])), int(np.dot(v, _KEY_MULT[1, :n])))
 
 
 def _to_host(x):
@@ -176,6 +197,7 @@ class GBGPUBase(abc.ABC):
         self.d_d = None
         self._tables = {}
         self._plans = {}
+        self._shapes = {}
         self._status = torch.zeros(1, dtype=torch.int32, device=self.device)
         self._lazy = None
         self._XYZf = self._AETf = self._start_inds = None
@@ -254,8 +276,8 @@ class GBGPUBase(abc.ABC):
             key = (int(N), float(T), precision, bool(tdi2), nparams, tile, blocks_per_sm)
         else:
             arr = np.ascontiguousarray(N, dtype=np.int64)
-            key = (hashlib.blake2b(arr.view(np.uint8), digest_size=16).digest(), arr.shape[0],
-                   float(T), precision, bool(tdi2), nparams, tile, blocks_per_sm)
+            key = (_array_key(arr), arr.shape[0], float(T), precision, bool(tdi2), nparams, tile,
+                   blocks_per_sm)
         plan = self._plans.pop(key, None)
         if plan is None:
             # least recently used plans go first; a plan stays alive while any
@@ -445,8 +467,14 @@ class GBGPUBase(abc.ABC):
         autotuning is on (timing ``run`` on the first call), else defaults."""
         if not self.autotune:
             return 0, 0
-        from .autotune import default_tuner, workload_key
-        return default_tuner().tune(workload_key(kind, N, B, precision, tdi2, nparams), run)
+        nkey = int(N) if np.ndim(N) == 0 else _array_key(np.ascontiguousarray(N, dtype=np.int64))
+        ck = (kind, nkey, int(B), precision, bool(tdi2), int(nparams))
+        shape = self._shapes.get(ck)
+        if shape is None:
+            from .autotune import default_tuner, workload_key
+            shape = default_tuner().tune(workload_key(kind, N, B, precision, tdi2, nparams), run)
+            self._shapes[ck] = shape
+        return shape
 
     @staticmethod
     def _ll_args(dd, pp, data_length, data_index, noise_index, T):
@@ -521,7 +549,8 @@ class GBGPUBase(abc.ABC):
         self._check_T(T)
         if isinstance(params, (np.ndarray, torch.Tensor)) and params.ndim == 2 and \
                 params.shape[0] == self.NPARAMS:
-            prm = _to_device(params, torch.float64, self.device).contiguous()
+            # get_ll reads the likelihood back before returning
+            prm = _to_device(params, torch.float64, self.device, non_blocking=True).contiguous()
             base = [params[0], params[1]]
             extra = [params[i] for i in range(9, self.NPARAMS)]
             if extra:
@@ -1038,11 +1067,14 @@ class GBGPUBase(abc.ABC):
                 h, si = wave(q)
                 hs.append(aligned(h, si))
             dh[:, i] = (-hs[0] + 8 * hs[1] - 8 * hs[2] + hs[3]) / (12 * step)[:, None, None]
-        self.run_wave(*prm, N=N, T=T, dt=dt, tdi2=tdi2)
-        freqs = self.freqs
-        psd = torch.as_tensor(np.asarray(psd_func(_to_host(freqs), **psd_kwargs)),
-                              device=self.device, dtype=torch.float64)
-        w = 4.0 / Tu / psd                                          # (B, N)
+        # the PSD on the union of the windows' bins (one host evaluation per
+        # distinct bin), gathered per binary on the device
+        lo = int(s0.min().item())
+        hi = int(s0.max().item()) + N
+        grid = np.asarray(psd_func((lo + np.arange(hi - lo)) / Tu, **psd_kwargs), dtype=np.float64)
+        grid = torch.as_tensor(grid, device=self.device)
+        psd = grid[(s0 - lo)[:, None] + cols[None, :]]             # (B, N)
+        w = 4.0 / Tu / psd
         F = torch.einsum("bicn,bjcn->bij", dh.conj() * w[:, None, None, :], dh).real
         F = 0.5 * (F + F.transpose(1, 2))
         return F if return_gpu else F.cpu().numpy()
