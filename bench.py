@@ -666,7 +666,7 @@ def run_gpu(args, rank, world):
     ab = alg_bytes(Ns)
     achieved = ab / (ms_mixed / 1e3) / 1e9
     peak, peak_src = hbm_peak()
-    traffic = profiled_traffic()
+    traffic = profiled("dram_bytes_per_launch")
     out = {
         "metric": METRIC,
         "value": value,
@@ -707,8 +707,13 @@ def run_gpu(args, rank, world):
         "config4": cfg4,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
-                     "note": f"peak {peak_src}; the kernel is FP64-pipe bound (carrier phase), "
-                             "so the HBM fraction is low by design"},
+                     "issue_active_frac": profiled("issue_active_frac"),
+                     "note": f"peak {peak_src}; achieved = algorithmic bytes (48 N + 104 per "
+                             "binary) / the timed step (prep_kernel + wave_kernel); traffic = "
+                             "ncu DRAM bytes of one full-size wave_kernel launch (windows overlap "
+                             "in L2).  The kernel is instruction-issue bound on the FP32/ALU "
+                             "pipes (issue_active_frac from ncu), so the HBM fraction is low "
+                             "by construction"},
         "e2e": {"value": world * B / e2e_max, "unit": "binaries/s",
                 "h2d_bytes_per_step": int(p.nbytes), "d2h_bytes_per_step": int(B * 8)},
         "clocks": clk.summary(),
@@ -728,12 +733,14 @@ def hbm_peak():
         return 6800.0, "of fallback (6.8 TB/s)"
 
 
-def profiled_traffic():
-    """DRAM bytes per launch of the fused kernel from the committed ncu summary."""
+def profiled(key):
+    """A figure of the committed ncu summary of the fused kernel (a line
+    ``key: value``): ``dram_bytes_per_launch`` (dram__bytes_read.sum +
+    dram__bytes_write.sum of one full-size launch) or ``issue_active_frac``."""
     path = os.path.join(ROOT, "profiles", "wave_ll_mixed_config1.txt")
     try:
         for line in open(path):
-            if line.startswith("dram_bytes_per_launch:"):
+            if line.startswith(key + ":"):
                 return float(line.split(":")[1])
     except OSError:
         pass
