@@ -247,9 +247,10 @@ int gbx_swap_ll(const gbx_wave_args *a, const gbx_ll_args *l, double *dlogl, voi
  * which has only finite-difference Fisher matrices, gbgpu/gbgpu.py:957-1138).
  * Computes d_h, h_h as gbx_waveform_ll and grad[k*num_bin + b] =
  * d logL_b / d params[k, b] for the nine parameters (amp, f0, fdot, fddot,
- * phi0, iota, psi, lam, beta) of logL = -1/2 (<d|d> + <h|h> - 2 Re<d|h>).
- * Mixed form and the 9-parameter circular model only.  The workspace is
- * required and must hold gbx_grad_workspace_bytes(num_bin) bytes.
+ * phi0, iota, psi, lam, beta) of logL = -1/2 (<d|d> + <h|h> - 2 Re<d|h>),
+ * and with nparams = 14 also for the third body's (A2, varpi, e2, P2, T2).
+ * Mixed form only (N <= 2048 for the third body).  The workspace is required
+ * and must hold gbx_grad_workspace_bytes(num_bin) bytes.
  */
 size_t gbx_grad_workspace_bytes(int num_bin);
 int gbx_waveform_ll_grad(const gbx_wave_args *a, const gbx_ll_args *l, void *d_h, void *h_h,
