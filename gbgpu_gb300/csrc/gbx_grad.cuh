@@ -87,7 +87,7 @@ __device__ __forceinline__ void sinc_cos_d_f(float a, float &S, float &C, float 
         dS = a * d;
     } else {
         float sn, cs;
-        sincosf(a, &sn, &cs);
+        sincos_mod(a, sn, cs);
         S = sn / a;
         C = cs;
         dS = (cs - S) / a;
@@ -151,7 +151,7 @@ __device__ __forceinline__ void slow_grad_mixed(const Bin &B, const GradExtra &G
     const float tf = tm.h;
     const float omL = B.w0h + fmaf(fmaf(B.w2, tf, B.w1), tf, B.w0l);
     float so, co;
-    sincosf(omL, &so, &co);
+    sincos_mod(omL, so, co);
     const float2 fc = make_float2(co, -so);
     const float g4 = 4.0f * omL * so;
     const float2 fa = make_float2(g4 * co, -g4 * so);              // fc2

@@ -49,7 +49,7 @@ struct __align__(16) Bin {
     double2 DP, DC;                // polarisation factors divided by amp
     double2 scale;                 // amp * 0.5 T / N [* tdi2 factor]
     double A2, varpi, e2, n2, T2;  // third body (n2, T2 in SI)
-    float kf[3], epf[6], ecf[6];
+    float kf[3], uf[3], vf[3];      // k, u, v in FP32 (mixed form; r.e+.r = (r.v)^2 - (r.u)^2)
     float2 DPf, DCf;
     float f0f, fdotf, fddotf;
     float w0h, w0l, w1, w2;        // f(t)/fstar = (w0h + w0l) + w1 t + w2 t^2 (w0 split hi/lo)
@@ -64,7 +64,7 @@ struct __align__(16) Bin {
     int valid;
 };
 
-static_assert(sizeof(Bin) == 512, "Bin is copied as 32 int4 per binary");
+static_assert(sizeof(Bin) % 16 == 0, "Bin is copied as int4 vectors");
 
 struct KParams {
     gbx_wave_args a;
@@ -104,12 +104,6 @@ __device__ __forceinline__ double quad_form(const double *e, double x, double y,
     return e[0] * x * x + e[1] * y * y + e[2] * z * z +
            2.0 * (e[3] * x * y + e[4] * x * z + e[5] * y * z);
 }
-__device__ __forceinline__ float quad_form(const float *e, float x, float y, float z)
-{
-    float xx = x * x, yy = y * y, zz = z * z, xy = x * y, xz = x * z, yz = y * z;
-    return fmaf(e[0], xx, fmaf(e[1], yy, fmaf(e[2], zz, 2.0f * fmaf(e[3], xy, fmaf(e[4], xz, e[5] * yz)))));
-}
-
 // sin(a)/a from its Taylor series (error < 1e-11 for |a| <= 1.6), falls back
 // to sinf(a)/a for larger arguments.
 __device__ __forceinline__ float sinc_f(float a)
@@ -128,12 +122,50 @@ __device__ __forceinline__ float sinc_f(float a)
     return sinf(a) / a;
 }
 
-// sin(a)/a and cos(a) from their Taylor series in x = a^2 (truncation error
-// below 2e-10 for |a| <= 1.6); sinf/cosf beyond that.
+// sin(x) and cos(x) for moderate |x| (the carrier phase reduced to [-pi, pi],
+// omega L, link arguments: |x| < 8).  Cody-Waite reduction r = x - k pi/2
+// with pi/2 split into two floats (Cody & Waite, "Software Manual for the
+// Elementary Functions", 1980), then the Taylor series of sin and cos on
+// |r| <= pi/4 (truncation below 2e-9 and 2e-10), then the quadrant k mod 4.
+__device__ __forceinline__ void sincos_mod(float x, float &s, float &c)
+{
+    constexpr float kTwoOverPi = 0.636619772367581343f;
+    constexpr float kPio2Hi = 1.57079637050628662f;       // float(pi/2)
+    constexpr float kPio2Lo = -4.37113900018624283e-8f;   // pi/2 - float(pi/2)
+    const float k = rintf(x * kTwoOverPi);
+    const float r = fmaf(-k, kPio2Lo, fmaf(-k, kPio2Hi, x));
+    const float r2 = r * r;
+    float ps = fmaf(r2, 1.0f / 362880.0f, -1.0f / 5040.0f);
+    ps = fmaf(r2, ps, 1.0f / 120.0f);
+    ps = fmaf(r2, ps, -1.0f / 6.0f);
+    const float sr = fmaf(r * r2, ps, r);
+    float pc = fmaf(r2, -1.0f / 3628800.0f, 1.0f / 40320.0f);
+    pc = fmaf(r2, pc, -1.0f / 720.0f);
+    pc = fmaf(r2, pc, 1.0f / 24.0f);
+    pc = fmaf(r2, pc, -0.5f);
+    const float cr = fmaf(r2, pc, 1.0f);
+    const int q = (int)k;
+    const float a = (q & 1) ? cr : sr, b = (q & 1) ? sr : cr;
+    s = (q & 2) ? -a : a;
+    c = ((q + 1) & 2) ? -b : b;
+}
+
+// sin(a)/a and cos(a) from their Taylor series in x = a^2: 4 and 5 terms for
+// |a| < 0.5 (truncation below 3e-8 and 3e-10, relative), 8 terms up to
+// |a| = 1.6 (below 2e-10); sincos_mod beyond that.
 __device__ __forceinline__ void sinc_cos_f(float a, float &S, float &C)
 {
     const float x = a * a;
-    if (x < 2.56f) {
+    if (x < 0.25f) {
+        float s = fmaf(x, -1.0f / 5040.0f, 1.0f / 120.0f);
+        s = fmaf(s, x, -1.0f / 6.0f);
+        S = fmaf(s, x, 1.0f);
+        float c = fmaf(x, -1.0f / 3628800.0f, 1.0f / 40320.0f);
+        c = fmaf(c, x, -1.0f / 720.0f);
+        c = fmaf(c, x, 1.0f / 24.0f);
+        c = fmaf(c, x, -0.5f);
+        C = fmaf(c, x, 1.0f);
+    } else if (x < 2.56f) {
         float s = -1.0f / 1307674368000.0f;
         s = fmaf(s, x, 1.0f / 6227020800.0f);
         s = fmaf(s, x, -1.0f / 39916800.0f);
@@ -152,7 +184,7 @@ __device__ __forceinline__ void sinc_cos_f(float a, float &S, float &C)
         C = fmaf(c, x, 1.0f);
     } else {
         float sn, cs;
-        sincosf(a, &sn, &cs);
+        sincos_mod(a, sn, cs);
         S = sn / a;
         C = cs;
     }
@@ -378,11 +410,11 @@ __device__ void setup_bin(Bin &B, const KParams &K, int b, int N, int mode)
     for (int c = 0; c < 6; c++) {
         B.ep[c] = v[ia[c]] * v[ib[c]] - u[ia[c]] * u[ib[c]];
         B.ec[c] = u[ia[c]] * v[ib[c]] + v[ia[c]] * u[ib[c]];
-        B.epf[c] = (float)B.ep[c];
-        B.ecf[c] = (float)B.ec[c];
     }
     for (int c = 0; c < 3; c++) {
         B.kf[c] = (float)B.k[c];
+        B.uf[c] = (float)u[c];
+        B.vf[c] = (float)v[c];
         B.kd[c] = df_from(B.k[c]);
     }
     B.omd = df_from(B.om);
@@ -606,8 +638,11 @@ __device__ __forceinline__ void slow_mixed(const Bin &B, int n, int N, dfl step,
     float2 A[3];
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        float pp = quad_form(B.epf, r[a][0], r[a][1], r[a][2]);
-        float cc = quad_form(B.ecf, r[a][0], r[a][1], r[a][2]);
+        // r.e+.r = (r.v)^2 - (r.u)^2, r.ex.r = 2 (r.u)(r.v)  (v has no z component)
+        const float ru = fmaf(B.uf[0], r[a][0], fmaf(B.uf[1], r[a][1], B.uf[2] * r[a][2]));
+        const float rv = fmaf(B.vf[0], r[a][0], B.vf[1] * r[a][1]);
+        const float pp = fmaf(rv, rv, -ru * ru);
+        const float cc = 2.0f * ru * rv;
         A[a] = make_float2(fmaf(pp, B.DPf.x, cc * B.DCf.x), fmaf(pp, B.DPf.y, cc * B.DCf.y));
     }
     // exp(-i phase_s) per spacecraft, the pair's low part applied to first order
@@ -615,7 +650,7 @@ __device__ __forceinline__ void slow_mixed(const Bin &B, int n, int N, dfl step,
 #pragma unroll
     for (int s = 0; s < 3; s++) {
         float sn, cs;
-        sincosf(phh[s], &sn, &cs);
+        sincos_mod(phh[s], sn, cs);
         Er[s] = fmaf(sn, -phl[s], cs);
         Ei[s] = -fmaf(cs, phl[s], sn);
         if (STORE_E) Eout[s] = make_float2(Er[s], Ei[s]);
@@ -639,7 +674,7 @@ __device__ __forceinline__ void slow_mixed(const Bin &B, int n, int N, dfl step,
     }
     float omL = B.w0h + fmaf(fmaf(B.w2, tf, B.w1), tf, B.w0l);
     float so, co;
-    sincosf(omL, &so, &co);
+    sincos_mod(omL, so, co);
     float2 fc = make_float2(co, -so);
     float g4 = 4.0f * omL * so;
     float2 fc2 = make_float2(g4 * co, -g4 * so);
@@ -1607,6 +1642,32 @@ extern "C" int gbx_waveform_ll_grad(const gbx_wave_args *a, const gbx_ll_args *l
 }
 
 // ----------------------------------------------------------------------------
+// Diagnostic entry point for the FP32 math helpers
+// ----------------------------------------------------------------------------
+namespace gbx {
+__global__ void math_selftest_kernel(const float *x, float *out, int n, int which)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float a, b;
+    if (which == 0) sincos_mod(x[i], a, b);
+    else sinc_cos_f(x[i], a, b);
+    out[2 * i] = a;
+    out[2 * i + 1] = b;
+}
+}  // namespace gbx
+
+extern "C" int gbx_math_selftest(const float *x, float *out, int n, int which, void *stream)
+{
+    if (n < 0 || (n > 0 && (!x || !out)) || (which != 0 && which != 1))
+        return set_error(GBX_ERR_ARG, "math selftest: bad arguments");
+    if (n == 0) return GBX_OK;
+    gbx::math_selftest_kernel<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(x, out, n, which);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GBX_OK : cuda_error(e, "math_selftest_kernel launch");
+}
+
+// ----------------------------------------------------------------------------
 // Allocation-free variant of gbx_waveform_ll.
 //
 // Some callers cannot allocate device memory at all: a plug-in inside a host
@@ -1618,7 +1679,9 @@ extern "C" int gbx_waveform_ll_grad(const gbx_wave_args *a, const gbx_ll_args *l
 // ----------------------------------------------------------------------------
 namespace gbx {
 constexpr int kNoAllocMaxBin = GBX_NOALLOC_MAX_BINS;
-constexpr size_t kNoAllocWsBytes = (size_t)kNoAllocMaxBin * sizeof(Bin);
+// 512 bytes per binary: the published size (4 MiB + 256 B) stays fixed while Bin fits
+static_assert(sizeof(Bin) <= 512, "the allocation-free scratch holds 512 bytes per binary");
+constexpr size_t kNoAllocWsBytes = (size_t)kNoAllocMaxBin * 512;
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocWsBytes + 256];
 
 static std::mutex g_noalloc_lock;

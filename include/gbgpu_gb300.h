@@ -278,6 +278,15 @@ int gbx_waveform_ll_grad(const gbx_wave_args *a, const gbx_ll_args *l, void *d_h
 int gbx_waveform_ll_noalloc(const gbx_wave_args *a, const gbx_ll_args *l, void *d_h,
                             void *h_h, void *stream);
 
+/*
+ * Diagnostic: evaluates one of the kernels' own FP32 math helpers on n device
+ * inputs x (no counterpart in the reference).  which = 0: out[2i], out[2i+1]
+ * = sin(x[i]), cos(x[i]) by the helper the mixed kernels use for reduced
+ * phases and omega L; which = 1: sin(a)/a and cos(a) of the link transfer
+ * functions.  For tests of those helpers against FP64.
+ */
+int gbx_math_selftest(const float *x, float *out, int n, int which, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
