@@ -492,6 +492,7 @@ __global__ void __launch_bounds__(kBlock, THIRD ? 1 : 2) grad_kernel(const GradP
     const int ntiles = a.tiles ? a.ntiles : (a.num_bin + K.P - 1) / K.P;
     const float ifs = (float)(1.0 / K.fstar);
     const float fstarf = (float)K.fstar;
+    const float Loc = (float)(1.0 / (kTwoPi * K.fstar));    // L / c
     const Bin *wsb = static_cast<const Bin *>(a.workspace);
     const GradExtra *wsg = reinterpret_cast<const GradExtra *>(wsb + a.num_bin);
     int iter = 0;
@@ -548,7 +549,7 @@ __global__ void __launch_bounds__(kBlock, THIRD ? 1 : 2) grad_kernel(const GradP
                     vv[s] = vl[(p * 3 + s) * N + n];
                 }
             }
-            slow_mixed<THIRD, true>(bins[p], n, N, stepd, tab, ps, vv, o, es + 3 * (size_t)m);
+            slow_mixed<THIRD, true>(bins[p], n, N, stepd, Loc, tab, ps, vv, o, es + 3 * (size_t)m);
             // A and E before the (linear) transform
             buf[(p * 2 + 0) * N + swz(n, lg)] = {(o[2].x - o[0].x) * is2, (o[2].y - o[0].y) * is2};
             buf[(p * 2 + 1) * N + swz(n, lg)] = {(o[0].x - 2.f * o[1].x + o[2].x) * is6,

@@ -569,7 +569,7 @@ __device__ __forceinline__ void slow_fp64(const Bin &B, int n, int N, double tm,
 // 48 bits, so ~1e-12 rad at 100 rad) and reduced modulo 2 pi; everything else
 // is FP32.
 template <bool THIRD, bool STORE_E = false>
-__device__ __forceinline__ void slow_mixed(const Bin &B, int n, int N, dfl step,
+__device__ __forceinline__ void slow_mixed(const Bin &B, int n, int N, dfl step, float Loc,
                                            const double *__restrict__ tab,
                                            const double *psi, const float *vl, float2 out[3],
                                            float2 *Eout = nullptr)
@@ -602,31 +602,45 @@ __device__ __forceinline__ void slow_mixed(const Bin &B, int n, int N, dfl step,
     Phi0 = df_neg(Phi0);
     const dfl wt = df_add(B.omd, df_add(df_mul(B.tpfd, tm), dfl{B.pfddf * tf * tf, 0.0f}));
     const float fdt = fmaf(B.fddotf, tf, B.fdotf);
+    // spacecraft 1: k . P_1 / c as a float pair (exact products, TwoSum accumulation)
+    dfl P[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+        P[c] = {__ldg(tabf + (size_t)(9 + c) * N + n), __ldg(tabf + (size_t)(18 + c) * N + n)};
+    float p0 = B.kd[0].h * P[0].h, p1 = B.kd[1].h * P[1].h, p2 = B.kd[2].h * P[2].h;
+    float e = fmaf(B.kd[0].h, P[0].h, -p0);
+    e += fmaf(B.kd[1].h, P[1].h, -p1);
+    e += fmaf(B.kd[2].h, P[2].h, -p2);
+#pragma unroll
+    for (int c = 0; c < 3; c++) e = fmaf(B.kd[c].h, P[c].l, fmaf(B.kd[c].l, P[c].h, e));
+    const dfl s01 = df_two_sum(p0, p1);
+    const dfl s012 = df_two_sum(s01.h, p2);
+    const dfl kP0 = df_fast(s012.h, (s01.l + s012.l) + e);
+    // its phase, reduced mod 2 pi
+    dfl ph0 = df_add(Phi0, df_mul(kP0, wt));
+    if (!THIRD) {
+        const float q = rintf(ph0.h * inv2pi);
+        ph0 = df_add(ph0, df_neg(df_mul_f(twopi, q)));
+    }
+    // spacecraft 2 and 3 differ by k.(P_s - P_1)/c = (L/c) k.r (r_12 and -r_31,
+    // |.| <= L/c = 8.3 s): the carrier phase moves by that times w (<= 1.3 rad
+    // below 25 mHz), added in FP32 to the float pair of spacecraft 1
+    const float dk[3] = {0.0f, Loc * kdotr[0], -Loc * kdotr[2]};
 #pragma unroll
     for (int s = 0; s < 3; s++) {
-        // k . P_s / c as a float pair: exact products, TwoSum accumulation
-        dfl P[3];
-#pragma unroll
-        for (int c = 0; c < 3; c++)
-            P[c] = {__ldg(tabf + (size_t)(9 + 3 * s + c) * N + n),
-                    __ldg(tabf + (size_t)(18 + 3 * s + c) * N + n)};
-        float p0 = B.kd[0].h * P[0].h, p1 = B.kd[1].h * P[1].h, p2 = B.kd[2].h * P[2].h;
-        float e = fmaf(B.kd[0].h, P[0].h, -p0);
-        e += fmaf(B.kd[1].h, P[1].h, -p1);
-        e += fmaf(B.kd[2].h, P[2].h, -p2);
-#pragma unroll
-        for (int c = 0; c < 3; c++) e = fmaf(B.kd[c].h, P[c].l, fmaf(B.kd[c].l, P[c].h, e));
-        dfl s01 = df_two_sum(p0, p1);
-        dfl s012 = df_two_sum(s01.h, p2);
-        const dfl kP = df_fast(s012.h, (s01.l + s012.l) + e);
-        // phase
-        const float kPf = kP.h;
+        const float kPf = kP0.h + dk[s];
         const float small = kPf * kPf * fmaf(kPf, (1.0f / 3.0f) * B.pfddf, -(float)kPi * fdt);
-        dfl ph = df_add(Phi0, df_mul(kP, wt));
+        dfl ph = ph0;
+        if (s > 0) {
+            const dfl d = df_two_sum(ph0.h, dk[s] * wt.h);
+            ph = dfl{d.h, d.l + ph0.l};
+        }
         ph.l += small;
-        if (THIRD) ph = df_add(ph, df_neg(df_from(psi[s])));
-        const float q = rintf(ph.h * inv2pi);
-        ph = df_add(ph, df_neg(df_mul_f(twopi, q)));
+        if (THIRD) {
+            ph = df_add(ph, df_neg(df_from(psi[s])));
+            const float q = rintf(ph.h * inv2pi);
+            ph = df_add(ph, df_neg(df_mul_f(twopi, q)));
+        }
         phh[s] = ph.h;
         phl[s] = ph.l;
         // FP32: instantaneous frequency over the transfer frequency
@@ -882,6 +896,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
     const int tid = threadIdx.x;
     const int ntiles = a.tiles ? a.ntiles : (a.num_bin + K.P - 1) / K.P;
     const double fstar = K.fstar;
+    const float Loc = (float)(1.0 / (kTwoPi * fstar));         // L / c
     int iter = 0;
 
     for (;;) {
@@ -966,7 +981,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                 slow_fp64<THIRD>(B, n, N, tm, 0.0, tab, fstar, ps, vd, reinterpret_cast<double2 *>(o));
             } else {
                 float vf[3] = {(float)vv[0], (float)vv[1], (float)vv[2]};
-                slow_mixed<THIRD>(B, n, N, stepd, tab, ps, vf, reinterpret_cast<float2 *>(o));
+                slow_mixed<THIRD>(B, n, N, stepd, Loc, tab, ps, vf, reinterpret_cast<float2 *>(o));
             }
             if constexpr (NCH == 3) {
 #pragma unroll
