@@ -330,6 +330,29 @@ __device__ float vlos_mixed(double t, const Bin &B)
     return B.A2f * (sinf(u + B.varpif) + e * B.sinvarpif);
 }
 
+// v_LOS (as vlos_mixed) and its time derivative dv/dt = A2 cos(phi + varpi)
+// dphi/dM n2, with dphi/dM = sqrt(1 - e^2) / (1 - e cos u)^2 (1 / (1 - e cos u)
+// below e = 1e-6, where the model takes phi = u).
+__device__ float vlos_dt_mixed(double t, const Bin &B, float &dvdt)
+{
+    const float u = kepler_u_mixed(t, B);
+    const float e = B.e2f;
+    float su, cu;
+    sincosf(u, &su, &cu);
+    const float ic = 1.0f / (1.0f - e * cu);
+    float phi = u, dphi_dM = ic;
+    if (e > 1e-6f) {
+        const float sq = sqrtf(1.0f - e * e);
+        const float bt = (1.0f - sq) / e;
+        phi += 2.0f * atan2f(bt * su, 1.0f - bt * cu);
+        dphi_dM = sq * ic * ic;
+    }
+    float sp, cp;
+    sincosf(phi + B.varpif, &sp, &cp);
+    dvdt = B.A2f * cp * dphi_dM * (float)B.n2;
+    return B.A2f * (sp + e * B.sinvarpif);
+}
+
 // v_LOS (as vlos_mixed) and its derivatives dv[0..4] = d/d(A2, varpi, e2,
 // P2 [yr], T2 [yr]), dv[5] = d/dt.  With c = 1 - e cos u and M = n2 (t - T2):
 // du/dM = 1/c, du/de = sin u / c (Kepler), and for the true anomaly
@@ -492,6 +515,8 @@ __device__ void setup_bin(Bin &B, const KParams &K, int b, int N, int mode)
             gi = 0;
         }
         B.gi = gi;
+        // a zero amplitude adds nothing (the samplers zero rejected proposals)
+        if (amp == 0.0) B.valid = 0;
     }
 }
 
@@ -823,13 +848,36 @@ __device__ __forceinline__ void third_prepass(const Bin *bins, const double *__r
         const int p = m >> lg, n = m & (N - 1);
         const Bin &B = bins[p];
         const double tm = (double)n * step;
+        if (!B.valid) {                       // outputs unused: no Kepler solves
+#pragma unroll
+            for (int s = 0; s < 3; s++) {
+                psi[(p * 3 + s) * N + n] = 0.0;
+                vl[(p * 3 + s) * N + n] = (R)0;
+                if (gout) gout[(p * 3 + s) * N + n] = 0.0f;
+            }
+            continue;
+        }
+        // mixed form: one Kepler solve per sample (spacecraft 1), the other two
+        // spacecraft's delayed times are within L/c = 8.3 s of it, so v_LOS
+        // there is v + (dv/dt) dxi (second-order error < 3e-9 v for P2 >= 1 yr)
+        double xi0 = 0.0;
+        float v0 = 0.0f, dv0 = 0.0f;
 #pragma unroll
         for (int s = 0; s < 3; s++) {
             double kP = B.k[0] * __ldg(tab + (size_t)(3 * s) * N + n) +
                         B.k[1] * __ldg(tab + (size_t)(3 * s + 1) * N + n) +
                         B.k[2] * __ldg(tab + (size_t)(3 * s + 2) * N + n);
             double xi = tm - kP;
-            double v = (sizeof(R) == 8) ? vlos_fp64(xi, B) : (double)vlos_mixed(xi, B);
+            double v;
+            if constexpr (sizeof(R) == 8) {
+                v = vlos_fp64(xi, B);
+            } else {
+                if (s == 0) {
+                    xi0 = xi;
+                    v0 = vlos_dt_mixed(xi, B, dv0);
+                }
+                v = (double)fmaf(dv0, (float)(xi - xi0), v0);
+            }
             double fgw = B.f0 + B.fdot * xi + 0.5 * B.fddot * xi * xi;
             psi[(p * 3 + s) * N + n] = v * fgw;
             vl[(p * 3 + s) * N + n] = (R)v;
@@ -976,7 +1024,11 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                 }
             }
             V o[3];
-            if constexpr (sizeof(R) == 8) {
+            if (!B.valid) {
+                // nothing of this binary reaches the outputs (bad index, or a
+                // zero-amplitude fill): skip the slow part
+                o[0] = o[1] = o[2] = V{0, 0};
+            } else if constexpr (sizeof(R) == 8) {
                 double vd[3] = {(double)vv[0], (double)vv[1], (double)vv[2]};
                 slow_fp64<THIRD>(B, n, N, tm, 0.0, tab, fstar, ps, vd, reinterpret_cast<double2 *>(o));
             } else {
