@@ -116,15 +116,24 @@ __device__ __forceinline__ void cmac(float &re, float &im, float2 y, float2 x)
 // Reverse mode through the TDI combination: x_c = sum_q M_cq(omL) G_q with
 // M in {0, +-fc2, +-fc2 fc} (gbgpu.py:370-375), so sum_c Y_c dx_c =
 // sum_q Z_q dG_q + dOmL sum_q Zd_q G_q with the link adjoints
-// Z_q = sum_c Y_c M_cq and Zd_q = sum_c Y_c dM_cq/domL.  Each parameter then
-// costs one complex multiply-add per link.
+// Z_q = sum_c Y_c M_cq and Zd_q = sum_c Y_c dM_cq/domL.
+//
+// A link q (spacecraft s, arm a) is G = 1/4 sinc(a_q) e^{-i a_q} E_s A_a with
+// a_q = fonfs_s hh_q, E_s = exp(-i phase_s), A_a = pp_a DP + cc_a DC.  Every
+// parameter enters through fonfs_s, phase_s (per spacecraft), k.r_a, pp_a,
+// cc_a (per arm) or omL, so the links are summed first into
+//   U_s = sum_{q at s} hh_q (S'/S - i) Z_q G_q     (d/d fonfs_s)
+//   V_s = -i sum_{q at s} Z_q G_q                   (d/d phase_s)
+//   R_a = sum_{q on a} fonfs_s sg_q / 2 (S'/S - i) Z_q G_q   (d/d k.r_a)
+//   Q_a = sum_{q on a} Z_q G_q / A_a               (d/d pp_a, cc_a: Q_a DP, Q_a DC)
+//   W   = sum_q Zd_q G_q                            (d/d omL)
+// and each parameter costs a few multiply-adds per spacecraft or arm.
 //
 // Third body (THIRD): fonfs carries the factor (1 + v_LOS/c) (vls: v_LOS of
 // the three spacecraft at this sample), which scales its f0/fdot/fddot and
 // k.P derivatives; the derivatives through v_LOS and the cumulative Doppler
-// phase are left to the third-body pass, which needs per spacecraft
-//   cph[s] = sum over the two links at s of Z dG/dphase   (= -i Z G),
-//   cfo[s] = sum over the two links at s of Z dG/dfonfs  (= (S'/S - i) hh Z G).
+// phase are left to the third-body pass, which takes cph[s] = V_s and
+// cfo[s] = U_s.
 template <bool THIRD>
 __device__ __forceinline__ void slow_grad_mixed(const Bin &B, const GradExtra &Gx, int n, int N,
                                                 dfl step, const double *__restrict__ tab,
@@ -135,7 +144,7 @@ __device__ __forceinline__ void slow_grad_mixed(const Bin &B, const GradExtra &G
 {
     const float *tabf = reinterpret_cast<const float *>(tab + (size_t)18 * N);
     const float TWO_PI_F = (float)kTwoPi, PI_F = (float)kPi;
-    // arm geometry: k.r, u.r, v.r
+    // arm geometry: k.r, u.r, v.r, and the polarisation projections
     float kd[3], ru[3], rv[3];
 #pragma unroll
     for (int a = 0; a < 3; a++) {
@@ -163,40 +172,34 @@ __device__ __forceinline__ void slow_grad_mixed(const Bin &B, const GradExtra &G
     const float2 YB0 = cmul(Yc[0], fb), YB1 = cmul(Yc[1], fb), YB2 = cmul(Yc[2], fb);
     const float2 YdA0 = cmul(Yc[0], da), YdA1 = cmul(Yc[1], da), YdA2 = cmul(Yc[2], da);
     const float2 YdB0 = cmul(Yc[0], db), YdB1 = cmul(Yc[1], db), YdB2 = cmul(Yc[2], db);
-    // spacecraft: exp(-i phase) from the forward pass, FP32 delays and derivatives
-    float Er[3], Ei[3], fo[3], xi[3], dph_l[3], dph_b[3], dfo_l[3], dfo_b[3], dop[3];
+    // spacecraft: delayed times and fonfs (FP32)
+    float fo[3], xi[3], dop[3];
 #pragma unroll
     for (int s = 0; s < 3; s++) {
-        float P0 = __ldg(tabf + (size_t)(9 + 3 * s) * N + n);
-        float P1 = __ldg(tabf + (size_t)(9 + 3 * s + 1) * N + n);
-        float P2 = __ldg(tabf + (size_t)(9 + 3 * s + 2) * N + n);
-        Er[s] = Es[s].x;
-        Ei[s] = Es[s].y;
+        const float P0 = __ldg(tabf + (size_t)(9 + 3 * s) * N + n);
+        const float P1 = __ldg(tabf + (size_t)(9 + 3 * s + 1) * N + n);
+        const float P2 = __ldg(tabf + (size_t)(9 + 3 * s + 2) * N + n);
         const float kPf = fmaf(B.kf[0], P0, fmaf(B.kf[1], P1, B.kf[2] * P2));
         const float x = tf - kPf;
         xi[s] = x;
         const float f_ = B.w0h + fmaf(fmaf(B.w2, x, B.w1), x, B.w0l);
         dop[s] = THIRD ? 1.0f + vls[s] * (float)(1.0 / kCSI) : 1.0f;
         fo[s] = THIRD ? f_ * dop[s] : f_;
-        // d kP / d lam = st v.P/c, d kP / d beta = u.P/c;
-        // d phase / d kP = 2 pi f(xi); d fonfs / d kP = -(fdot + fddot xi)/fstar
-        const float Pv = fmaf(Gx.v[0], P0, Gx.v[1] * P1);
-        const float Pu = fmaf(Gx.u[0], P0, fmaf(Gx.u[1], P1, Gx.u[2] * P2));
-        const float dkP_l = Gx.st * Pv, dkP_b = Pu;
-        const float tpf = TWO_PI_F * f_ * fstarf;
-        dph_l[s] = tpf * dkP_l;
-        dph_b[s] = tpf * dkP_b;
-        const float gfk = THIRD ? fmaf(Gx.gf1, x, Gx.gf0) * dop[s] : fmaf(Gx.gf1, x, Gx.gf0);
-        dfo_l[s] = gfk * dkP_l;
-        dfo_b[s] = gfk * dkP_b;
     }
-    const float dom0 = ifs, dom1 = tf * ifs, dom2 = 0.5f * tf * tf * ifs;
+    float2 A[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const float pp = fmaf(rv[a], rv[a], -ru[a] * ru[a]);      // r.e+.r
+        const float cc = 2.0f * ru[a] * rv[a];                       // r.ex.r
+        A[a] = make_float2(fmaf(pp, B.DPf.x, cc * B.DCf.x), fmaf(pp, B.DPf.y, cc * B.DCf.y));
+    }
     // links 12, 23, 31, 21, 32, 13: arm, spacecraft, sign of k.r
     const int arm[6] = {0, 1, 2, 0, 1, 2};
     const int sc[6] = {0, 1, 2, 1, 2, 0};
     const float sg[6] = {1.f, 1.f, 1.f, -1.f, -1.f, -1.f};
-    float2 zg[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-    float2 zgd[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    float2 U[3], V[3], R[3], Q[3], W = {0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < 3; k++) U[k] = V[k] = R[k] = Q[k] = make_float2(0.f, 0.f);
 #pragma unroll
     for (int q = 0; q < 6; q++) {
         const int s = sc[q], a = arm[q];
@@ -215,65 +218,93 @@ __device__ __forceinline__ void slow_grad_mixed(const Bin &B, const GradExtra &G
         float S, C, dS;
         sinc_cos_d_f(av, S, C, dS);
         const float t = 0.25f * S;
-        const float2 gE = cmul(make_float2(t * C, -t * av * S), make_float2(Er[s], Ei[s]));
-        const float pp = fmaf(rv[a], rv[a], -ru[a] * ru[a]);      // r.e+.r
-        const float cc = 2.0f * ru[a] * rv[a];                       // r.ex.r
-        const float2 A = make_float2(fmaf(pp, B.DPf.x, cc * B.DCf.x), fmaf(pp, B.DPf.y, cc * B.DCf.y));
-        const float2 G = cmul(gE, A);
+        const float2 gE = cmul(make_float2(t * C, -t * av * S), Es[s]);
         const float2 ZgE = cmul(Z, gE);
-        const float2 ZG = cmul(Z, G);
-        const float2 ZdG = cmul(Zd, G);
+        const float2 ZG = cmul(ZgE, A[a]);
+        const float2 G = cmul(gE, A[a]);
+        W = cadd(W, cmul(Zd, G));
+        Q[a] = cadd(Q[a], ZgE);
         const float dl = dS / S;
-        if (THIRD) {
-            zg[s] = cadd(zg[s], ZG);
-            zgd[s] = cadd(zgd[s], make_float2(hh * fmaf(dl, ZG.x, ZG.y), hh * fmaf(dl, ZG.y, -ZG.x)));
-        }
-        // plus / cross parts
-        acc[0] = fmaf(pp, ZgE.x, acc[0]);
-        acc[1] = fmaf(pp, ZgE.y, acc[1]);
-        acc[2] = fmaf(cc, ZgE.x, acc[2]);
-        acc[3] = fmaf(cc, ZgE.y, acc[3]);
-        // (dl da - i (da + dph)) ZG + dOmL ZdG for the frequency parameters
-        {
+        const float2 w = make_float2(fmaf(dl, ZG.x, ZG.y), fmaf(dl, ZG.y, -ZG.x));   // (S'/S - i) Z G
+        U[s] = make_float2(fmaf(hh, w.x, U[s].x), fmaf(hh, w.y, U[s].y));
+        V[s] = make_float2(V[s].x + ZG.y, V[s].y - ZG.x);
+        const float hf = 0.5f * sg[q] * fo[s];
+        R[a] = make_float2(fmaf(hf, w.x, R[a].x), fmaf(hf, w.y, R[a].y));
+    }
+    // plus / cross parts: sum_a (pp_a, cc_a) Q_a
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const float pp = fmaf(rv[a], rv[a], -ru[a] * ru[a]);
+        const float cc = 2.0f * ru[a] * rv[a];
+        acc[0] = fmaf(pp, Q[a].x, acc[0]);
+        acc[1] = fmaf(pp, Q[a].y, acc[1]);
+        acc[2] = fmaf(cc, Q[a].x, acc[2]);
+        acc[3] = fmaf(cc, Q[a].y, acc[3]);
+    }
+    // frequency parameters: d fonfs_s = dop_s {1, xi, xi^2/2}/fstar, d phase_s =
+    // -{2 pi xi, pi xi^2, pi/3 xi^3}, d omL = {1, tm, tm^2/2}/fstar
+    {
+        const float dom0 = ifs, dom1 = tf * ifs, dom2 = 0.5f * tf * tf * ifs;
+        float2 s0 = {dom0 * W.x, dom0 * W.y}, s1 = {dom1 * W.x, dom1 * W.y},
+               s2 = {dom2 * W.x, dom2 * W.y};
+#pragma unroll
+        for (int s = 0; s < 3; s++) {
             const float x = xi[s];
-            const float hd = THIRD ? hh * dop[s] : hh;
-            const float d0 = hd * ifs, d1 = hd * x * ifs, d2 = 0.5f * hd * x * x * ifs;
+            const float c0 = dop[s] * ifs, c1 = c0 * x, c2 = 0.5f * c1 * x;
             const float p0 = -TWO_PI_F * x, p1 = -PI_F * x * x, p2 = -(PI_F / 3.0f) * x * x * x;
-            float al, be;
-            al = dl * d0; be = d0 + p0;
-            acc[4] = fmaf(al, ZG.x, fmaf(be, ZG.y, fmaf(dom0, ZdG.x, acc[4])));
-            acc[5] = fmaf(al, ZG.y, fmaf(-be, ZG.x, fmaf(dom0, ZdG.y, acc[5])));
-            al = dl * d1; be = d1 + p1;
-            acc[6] = fmaf(al, ZG.x, fmaf(be, ZG.y, fmaf(dom1, ZdG.x, acc[6])));
-            acc[7] = fmaf(al, ZG.y, fmaf(-be, ZG.x, fmaf(dom1, ZdG.y, acc[7])));
-            al = dl * d2; be = d2 + p2;
-            acc[8] = fmaf(al, ZG.x, fmaf(be, ZG.y, fmaf(dom2, ZdG.x, acc[8])));
-            acc[9] = fmaf(al, ZG.y, fmaf(-be, ZG.x, fmaf(dom2, ZdG.y, acc[9])));
+            s0 = make_float2(fmaf(c0, U[s].x, fmaf(p0, V[s].x, s0.x)), fmaf(c0, U[s].y, fmaf(p0, V[s].y, s0.y)));
+            s1 = make_float2(fmaf(c1, U[s].x, fmaf(p1, V[s].x, s1.x)), fmaf(c1, U[s].y, fmaf(p1, V[s].y, s1.y)));
+            s2 = make_float2(fmaf(c2, U[s].x, fmaf(p2, V[s].x, s2.x)), fmaf(c2, U[s].y, fmaf(p2, V[s].y, s2.y)));
         }
-        // sky angles: d/dlam (du = -ct v, dv = ct u - st k, dk = st v),
-        //             d/dbeta (du = -k, dv = 0, dk = u)
-        {
-            const float2 ZgDP = cmul(ZgE, B.DPf), ZgDC = cmul(ZgE, B.DCf);
+        acc[4] += s0.x; acc[5] += s0.y;
+        acc[6] += s1.x; acc[7] += s1.y;
+        acc[8] += s2.x; acc[9] += s2.y;
+    }
+    // sky angles: d/dlam (du = -ct v, dv = ct u - st k, dk = st v),
+    //             d/dbeta (du = -k, dv = 0, dk = u);
+    // per spacecraft d kP = (st v.P, u.P)/c moves phase_s by 2 pi f(xi) d kP
+    // and fonfs_s by -(fdot + fddot xi)/fstar dop_s d kP
+    {
+        float2 sl = {0.f, 0.f}, sb = {0.f, 0.f};
+#pragma unroll
+        for (int s = 0; s < 3; s++) {
+            const float P0 = __ldg(tabf + (size_t)(9 + 3 * s) * N + n);
+            const float P1 = __ldg(tabf + (size_t)(9 + 3 * s + 1) * N + n);
+            const float P2 = __ldg(tabf + (size_t)(9 + 3 * s + 2) * N + n);
+            const float Pv = fmaf(Gx.v[0], P0, Gx.v[1] * P1);
+            const float Pu = fmaf(Gx.u[0], P0, fmaf(Gx.u[1], P1, Gx.u[2] * P2));
+            const float dkP_l = Gx.st * Pv, dkP_b = Pu;
+            const float f_ = B.w0h + fmaf(fmaf(B.w2, xi[s], B.w1), xi[s], B.w0l);
+            const float tpf = TWO_PI_F * f_ * fstarf;
+            const float gfk = fmaf(Gx.gf1, xi[s], Gx.gf0) * dop[s];
+            const float ul = gfk * dkP_l, ub = gfk * dkP_b;     // d fonfs_s
+            const float vl_ = tpf * dkP_l, vb = tpf * dkP_b;    // d phase_s
+            sl = make_float2(fmaf(ul, U[s].x, fmaf(vl_, V[s].x, sl.x)), fmaf(ul, U[s].y, fmaf(vl_, V[s].y, sl.y)));
+            sb = make_float2(fmaf(ub, U[s].x, fmaf(vb, V[s].x, sb.x)), fmaf(ub, U[s].y, fmaf(vb, V[s].y, sb.y)));
+        }
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            // d k.r_a, d pp_a, d cc_a per angle
+            const float dkd_l = Gx.st * rv[a], dkd_b = ru[a];
             const float dru_l = -Gx.ct * rv[a], drv_l = fmaf(Gx.ct, ru[a], -Gx.st * kd[a]);
             const float dpp_l = 2.0f * fmaf(rv[a], drv_l, -ru[a] * dru_l);
             const float dcc_l = 2.0f * fmaf(dru_l, rv[a], ru[a] * drv_l);
             const float dpp_b = 2.0f * ru[a] * kd[a];
             const float dcc_b = -2.0f * kd[a] * rv[a];
-            const float dd_l = fmaf(hh, dfo_l[s], 0.5f * fo[s] * sg[q] * Gx.st * rv[a]);
-            const float dd_b = fmaf(hh, dfo_b[s], 0.5f * fo[s] * sg[q] * ru[a]);
-            float al = dl * dd_l, be = dd_l + dph_l[s];
-            acc[10] = fmaf(al, ZG.x, fmaf(be, ZG.y, fmaf(dpp_l, ZgDP.x, fmaf(dcc_l, ZgDC.x, acc[10]))));
-            acc[11] = fmaf(al, ZG.y, fmaf(-be, ZG.x, fmaf(dpp_l, ZgDP.y, fmaf(dcc_l, ZgDC.y, acc[11]))));
-            al = dl * dd_b; be = dd_b + dph_b[s];
-            acc[12] = fmaf(al, ZG.x, fmaf(be, ZG.y, fmaf(dpp_b, ZgDP.x, fmaf(dcc_b, ZgDC.x, acc[12]))));
-            acc[13] = fmaf(al, ZG.y, fmaf(-be, ZG.x, fmaf(dpp_b, ZgDP.y, fmaf(dcc_b, ZgDC.y, acc[13]))));
+            const float2 QP = cmul(Q[a], B.DPf), QC = cmul(Q[a], B.DCf);
+            sl = make_float2(fmaf(dkd_l, R[a].x, fmaf(dpp_l, QP.x, fmaf(dcc_l, QC.x, sl.x))),
+                             fmaf(dkd_l, R[a].y, fmaf(dpp_l, QP.y, fmaf(dcc_l, QC.y, sl.y))));
+            sb = make_float2(fmaf(dkd_b, R[a].x, fmaf(dpp_b, QP.x, fmaf(dcc_b, QC.x, sb.x))),
+                             fmaf(dkd_b, R[a].y, fmaf(dpp_b, QP.y, fmaf(dcc_b, QC.y, sb.y))));
         }
+        acc[10] += sl.x; acc[11] += sl.y;
+        acc[12] += sb.x; acc[13] += sb.y;
     }
     if (THIRD) {
 #pragma unroll
         for (int s = 0; s < 3; s++) {
-            cph[s] = make_float2(zg[s].y, -zg[s].x);
-            cfo[s] = zgd[s];
+            cph[s] = V[s];
+            cfo[s] = U[s];
         }
     }
 }
