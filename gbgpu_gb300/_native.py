@@ -91,7 +91,7 @@ def lib():
     L.gbx_grad_workspace_bytes.restype = ctypes.c_size_t
     L.gbx_swap_ll.argtypes = [ctypes.POINTER(WaveArgs), ctypes.POINTER(LLArgs), _vp, _vp]
     L.gbx_waveform_fill.argtypes = [ctypes.POINTER(WaveArgs), _vp, _vp, _vp, _i, _i, _ll, _vp]
-    L.gbx_math_selftest.argtypes = [_vp, _vp, _i, _i, _vp]
+    L.gbx_math_selftest.argtypes = [_vp, _vp, _i, _i, _i, _vp]
     for name in EXPORTS:
         if name not in ("gbx_last_error", "gbx_orbit_table_bytes", "gbx_wave_workspace_bytes",
                         "gbx_grad_workspace_bytes"):

@@ -209,18 +209,17 @@ __device__ __forceinline__ double exp2_int(int e)
 
 // FP64 -> FP32 with an exact power-of-two scaling, done on the integer pipe.
 // Rounds to nearest (ties away), flushes results below FP32's normal range to
-// signed zero and saturates to infinity above it.
+// signed zero and saturates to infinity above it.  (hi:lo) << 3 holds the 23
+// leading mantissa bits at [22:0] and the exponent's low 9 bits at [31:23];
+// subtracting (896 - e) << 23 modulo 2^32 leaves the FP32 biased exponent
+// ne = ex - 896 + e there whenever 0 < ne < 255.
 __device__ __forceinline__ float d2f_scaled(double x, int e)
 {
-    unsigned long long bits = (unsigned long long)__double_as_longlong(x);
-    unsigned hi = (unsigned)(bits >> 32), lo = (unsigned)bits;
-    unsigned sign = hi & 0x80000000u;
-    int ex = (int)((hi >> 20) & 0x7ffu);
-    int ne = ex - 1023 + 127 + e;
-    unsigned mag = ((unsigned)ne << 23) + (((hi & 0xfffffu) << 3) | (lo >> 29)) + ((lo >> 28) & 1u);
-    mag = (ne >= 255) ? 0x7f800000u : mag;
-    mag = (ne <= 0 || ex == 0) ? 0u : mag;
-    return __uint_as_float(sign | mag);
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const int ne = (int)((hi >> 20) & 0x7ffu) - 896 + e;
+    unsigned mag = __funnelshift_l(lo, hi, 3) - ((unsigned)(896 - e) << 23) + ((lo >> 28) & 1u);
+    mag = ((unsigned)(ne - 1) < 254u) ? mag : (ne >= 255 ? 0x7f800000u : 0u);
+    return __uint_as_float((hi & 0x80000000u) | (mag & 0x7fffffffu));
 }
 
 // ----------------------------------------------------------------------------
@@ -1712,26 +1711,31 @@ extern "C" int gbx_waveform_ll_grad(const gbx_wave_args *a, const gbx_ll_args *l
 // Diagnostic entry point for the FP32 math helpers
 // ----------------------------------------------------------------------------
 namespace gbx {
-__global__ void math_selftest_kernel(const float *x, float *out, int n, int which)
+__global__ void math_selftest_kernel(const void *x, float *out, int n, int which, int e)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (which == 2) {
+        out[i] = d2f_scaled(static_cast<const double *>(x)[i], e);
+        return;
+    }
+    const float xi = static_cast<const float *>(x)[i];
     float a, b;
-    if (which == 0) sincos_mod(x[i], a, b);
-    else sinc_cos_f(x[i], a, b);
+    if (which == 0) sincos_mod(xi, a, b);
+    else sinc_cos_f(xi, a, b);
     out[2 * i] = a;
     out[2 * i + 1] = b;
 }
 }  // namespace gbx
 
-extern "C" int gbx_math_selftest(const float *x, float *out, int n, int which, void *stream)
+extern "C" int gbx_math_selftest(const void *x, float *out, int n, int which, int e, void *stream)
 {
-    if (n < 0 || (n > 0 && (!x || !out)) || (which != 0 && which != 1))
+    if (n < 0 || (n > 0 && (!x || !out)) || which < 0 || which > 2)
         return set_error(GBX_ERR_ARG, "math selftest: bad arguments");
     if (n == 0) return GBX_OK;
-    gbx::math_selftest_kernel<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(x, out, n, which);
-    cudaError_t e = cudaGetLastError();
-    return e == cudaSuccess ? GBX_OK : cuda_error(e, "math_selftest_kernel launch");
+    gbx::math_selftest_kernel<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(x, out, n, which, e);
+    const cudaError_t err = cudaGetLastError();
+    return err == cudaSuccess ? GBX_OK : cuda_error(err, "math_selftest_kernel launch");
 }
 
 // ----------------------------------------------------------------------------

@@ -279,13 +279,15 @@ int gbx_waveform_ll_noalloc(const gbx_wave_args *a, const gbx_ll_args *l, void *
                             void *h_h, void *stream);
 
 /*
- * Diagnostic: evaluates one of the kernels' own FP32 math helpers on n device
- * inputs x (no counterpart in the reference).  which = 0: out[2i], out[2i+1]
- * = sin(x[i]), cos(x[i]) by the helper the mixed kernels use for reduced
- * phases and omega L; which = 1: sin(a)/a and cos(a) of the link transfer
- * functions.  For tests of those helpers against FP64.
+ * Diagnostic: evaluates one of the kernels' own math helpers on n device
+ * inputs x (no counterpart in the reference), for tests against FP64 or a
+ * host restatement.  which = 0: x is float, out[2i], out[2i+1] = sin(x[i]),
+ * cos(x[i]) by the helper the mixed kernels use for reduced phases and
+ * omega L; which = 1: x is float, sin(a)/a and cos(a) of the link transfer
+ * functions; which = 2: x is double, out[i] = x[i] * 2^e rounded to FP32 by
+ * the integer-pipe conversion of the mixed likelihood.
  */
-int gbx_math_selftest(const float *x, float *out, int n, int which, void *stream);
+int gbx_math_selftest(const void *x, float *out, int n, int which, int e, void *stream);
 
 #ifdef __cplusplus
 }
