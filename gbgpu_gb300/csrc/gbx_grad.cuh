@@ -440,12 +440,19 @@ template <typename R>
 __device__ __forceinline__ void fft_dit(typename C2<R>::T *buf, int nsub, int lg)
 {
     using V = typename C2<R>::T;
+    // the first five stages inside a warp: (a, b) -> (a + W b, a - W b) with a
+    // on the lower lane; the upper lane multiplies its own element by W
+    // before the exchange (w' = 1 on lower lanes and in the first stage), so
+    // both lanes finish with sg x' + y' (sg = +-1): branch-free
     const int lane = threadIdx.x & 31;
     V w[5];
+    R sg[5];
 #pragma unroll
     for (int k = 0; k < 5; k++) {
+        const bool up = (lane & (1 << k)) != 0;
         const int rp = lane & ((1 << k) - 1);
-        w[k] = tw<R>(rp * (kTwN >> (k + 1)));
+        sg[k] = up ? (R)-1 : (R)1;
+        w[k] = up ? tw<R>(rp * (kTwN >> (k + 1))) : V{(R)1, (R)0};
     }
     const int chunks = (nsub << lg) >> 5;
     for (int c = threadIdx.x >> 5; c < chunks; c += kBlock >> 5) {
@@ -454,11 +461,9 @@ __device__ __forceinline__ void fft_dit(typename C2<R>::T *buf, int nsub, int lg
         V x = buf[idx];
 #pragma unroll
         for (int k = 0; k < 5; k++) {
-            const int o = 1 << k;
-            V y = shfl_c<R>(x, o);
-            const bool up = (lane & o) != 0;
-            V t = cmul(w[k], up ? x : y);          // W times the upper element
-            x = up ? csub(y, t) : cadd(x, t);
+            const V xw = (k > 0) ? cmul(w[k], x) : x;
+            const V y = shfl_c<R>(xw, 1 << k);
+            x = V{fma(sg[k], xw.x, y.x), fma(sg[k], xw.y, y.y)};
         }
         buf[idx] = x;
     }

@@ -793,14 +793,22 @@ __device__ __forceinline__ void fft_dif(typename C2<R>::T *buf, int nsub, int lg
         hl -= rb;
         __syncthreads();
     }
-    // the last five stages inside a warp: lane l holds element 32c + l
+    // the last five stages inside a warp: lane l holds element 32c + l.  The
+    // lower lane of a pair keeps x + y, the upper one (y - x) W: both are
+    // (sg x + y) w' with sg = +-1 and w' = 1 on lower lanes (and in the last
+    // stage, whose twiddles are all 1), so the stage is branch-free.
     const int lane = threadIdx.x & 31;
-    V w[5];
+    V w[4];
+    R sg[5];
 #pragma unroll
     for (int k = 0; k < 5; k++) {
         const int hh = 4 - k;                       // half-span 2^hh = 16 >> k
-        const int rp = lane & ((1 << hh) - 1);
-        w[k] = tw<R>(rp * (kTwN >> (hh + 1)));
+        const bool up = (lane & (16 >> k)) != 0;
+        sg[k] = up ? (R)-1 : (R)1;
+        if (k < 4) {
+            const int rp = lane & ((1 << hh) - 1);
+            w[k] = up ? tw<R>(rp * (kTwN >> (hh + 1))) : V{(R)1, (R)0};
+        }
     }
     const int chunks = (nsub << lg) >> 5;
     for (int c = threadIdx.x >> 5; c < chunks; c += kBlock >> 5) {
@@ -809,10 +817,9 @@ __device__ __forceinline__ void fft_dif(typename C2<R>::T *buf, int nsub, int lg
         V x = buf[idx];
 #pragma unroll
         for (int k = 0; k < 5; k++) {
-            const int o = 16 >> k;
-            V y = shfl_c<R>(x, o);
-            // lower lane keeps x + y; upper lane gets (y - x) W, y being the lower element
-            x = (lane & o) ? cmul(csub(y, x), w[k]) : cadd(x, y);
+            const V y = shfl_c<R>(x, 16 >> k);
+            const V d = {fma(sg[k], x.x, y.x), fma(sg[k], x.y, y.y)};
+            x = (k < 4) ? cmul(d, w[k < 4 ? k : 0]) : d;
         }
         buf[idx] = x;
     }
