@@ -150,13 +150,19 @@ __device__ __forceinline__ void sincos_mod(float x, float &s, float &c)
     c = ((q + 1) & 2) ? -b : b;
 }
 
-// sin(a)/a and cos(a) from their Taylor series in x = a^2: 4 and 5 terms for
-// |a| < 0.5 (truncation below 3e-8 and 3e-10, relative), 8 terms up to
-// |a| = 1.6 (below 2e-10); sincos_mod beyond that.
+// sin(a)/a and cos(a) from their Taylor series in x = a^2: 3 and 4 terms for
+// |a| < 0.16 (truncation below 4e-9 and 1e-11), 4 and 5 terms for |a| < 0.5
+// (below 3e-8 and 3e-10), 8 terms up to |a| = 1.6 (below 2e-10); sincos_mod
+// beyond that.
 __device__ __forceinline__ void sinc_cos_f(float a, float &S, float &C)
 {
     const float x = a * a;
-    if (x < 0.25f) {
+    if (x < 0.0256f) {
+        S = fmaf(fmaf(x, 1.0f / 120.0f, -1.0f / 6.0f), x, 1.0f);
+        float c = fmaf(x, -1.0f / 720.0f, 1.0f / 24.0f);
+        c = fmaf(c, x, -0.5f);
+        C = fmaf(c, x, 1.0f);
+    } else if (x < 0.25f) {
         float s = fmaf(x, -1.0f / 5040.0f, 1.0f / 120.0f);
         s = fmaf(s, x, -1.0f / 6.0f);
         S = fmaf(s, x, 1.0f);
@@ -220,6 +226,23 @@ __device__ __forceinline__ float d2f_scaled(double x, int e)
     unsigned mag = __funnelshift_l(lo, hi, 3) - ((unsigned)(896 - e) << 23) + ((lo >> 28) & 1u);
     mag = ((unsigned)(ne - 1) < 254u) ? mag : (ne >= 255 ? 0x7f800000u : 0u);
     return __uint_as_float((hi & 0x80000000u) | (mag & 0x7fffffffu));
+}
+
+// FP32 -> FP64 (exact) on the integer pipe: exponent rebias, mantissa shift;
+// FP32 zeros and subnormals give signed zero, infinities stay infinite.
+__device__ __forceinline__ double f2d_bits(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned ex = (u >> 23) & 0xffu;
+    unsigned hi = (u & 0x80000000u) | ((ex + 896u) << 20) | ((u & 0x7fffffu) >> 3);
+    hi = ex == 0 ? (u & 0x80000000u) : (ex == 0xffu ? (u & 0x80000000u) | 0x7ff00000u : hi);
+    const unsigned lo = ex == 0 || ex == 0xffu ? 0u : (u << 29);
+    return __hiloint2double((int)hi, (int)lo);
+}
+
+__device__ __forceinline__ double2 f2d(float2 v)
+{
+    return make_double2(f2d_bits(v.x), f2d_bits(v.y));
 }
 
 // ----------------------------------------------------------------------------
@@ -1065,24 +1088,41 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                 const int pos = bitrev((i + (N >> 1)) & (N - 1), lg);   // fftshift
                 V X = buf[(p * 3 + 0) * N + swz(pos, lg)], Y = buf[(p * 3 + 1) * N + swz(pos, lg)],
                   Z = buf[(p * 3 + 2) * N + swz(pos, lg)];
-                double2 Xd = cmul(make_double2((double)X.x, (double)X.y), B.scale);
-                double2 Yd = cmul(make_double2((double)Y.x, (double)Y.y), B.scale);
-                double2 Zd = cmul(make_double2((double)Z.x, (double)Z.y), B.scale);
                 const size_t o = (size_t)B.b * 3 * N + i;
-                if (K.XYZ) {
-                    K.XYZ[o] = Xd;
-                    K.XYZ[o + N] = Yd;
-                    K.XYZ[o + 2 * N] = Zd;
-                }
-                if (K.AET) {
-                    // utility.py:24-38
-                    const double r2 = 1.4142135623730951, r6 = 2.449489742783178,
-                                 r3 = 1.7320508075688772;
-                    K.AET[o] = make_double2((Zd.x - Xd.x) / r2, (Zd.y - Xd.y) / r2);
-                    K.AET[o + N] = make_double2((Xd.x - 2.0 * Yd.x + Zd.x) / r6,
-                                                (Xd.y - 2.0 * Yd.y + Zd.y) / r6);
-                    K.AET[o + 2 * N] = make_double2((Xd.x + Yd.x + Zd.x) / r3,
-                                                    (Xd.y + Yd.y + Zd.y) / r3);
+                if constexpr (sizeof(R) == 8) {
+                    double2 Xd = cmul(X, B.scale), Yd = cmul(Y, B.scale), Zd = cmul(Z, B.scale);
+                    if (K.XYZ) {
+                        K.XYZ[o] = Xd;
+                        K.XYZ[o + N] = Yd;
+                        K.XYZ[o + 2 * N] = Zd;
+                    }
+                    if (K.AET) {
+                        // utility.py:24-38, with the divisions by sqrt 2, 6, 3 as
+                        // products with their reciprocals (<= 1 ulp apart)
+                        const double i3 = 0.57735026918962576451;
+                        K.AET[o] = make_double2((Zd.x - Xd.x) * is2, (Zd.y - Xd.y) * is2);
+                        K.AET[o + N] = make_double2((Xd.x - 2.0 * Yd.x + Zd.x) * is6,
+                                                    (Xd.y - 2.0 * Yd.y + Zd.y) * is6);
+                        K.AET[o + 2 * N] = make_double2((Xd.x + Yd.x + Zd.x) * i3,
+                                                        (Xd.y + Yd.y + Zd.y) * i3);
+                    }
+                } else {
+                    // mixed form: the channels and the scale in FP32 (the values
+                    // carry FP32 accuracy), widened to FP64 on the integer pipe
+                    const float2 sc = make_float2(d2f_scaled(B.scale.x, 0), d2f_scaled(B.scale.y, 0));
+                    if (K.XYZ) {
+                        K.XYZ[o] = f2d(cmul(X, sc));
+                        K.XYZ[o + N] = f2d(cmul(Y, sc));
+                        K.XYZ[o + 2 * N] = f2d(cmul(Z, sc));
+                    }
+                    if (K.AET) {
+                        const float i3 = 0.57735026918962576451f;
+                        K.AET[o] = f2d(cmul(make_float2((Z.x - X.x) * is2, (Z.y - X.y) * is2), sc));
+                        K.AET[o + N] = f2d(cmul(make_float2((X.x - 2.f * Y.x + Z.x) * is6,
+                                                            (X.y - 2.f * Y.y + Z.y) * is6), sc));
+                        K.AET[o + 2 * N] = f2d(cmul(make_float2((X.x + Y.x + Z.x) * i3,
+                                                                (X.y + Y.y + Z.y) * i3), sc));
+                    }
                 }
                 if (i == 0 && K.start_out) K.start_out[B.b] = B.start;
             }
