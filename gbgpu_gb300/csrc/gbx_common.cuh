@@ -10,7 +10,7 @@ namespace gbx {
 
 constexpr int kBlock = 256;        // threads per CTA for the waveform family
 constexpr int kTileMin = 512;      // default samples per tile (P = kTileMin / N binaries)
-constexpr int kMaxPack = 16;       // most binaries in one tile
+constexpr int kMaxPack = 16;       // most binaries in one tile (also the most lane groups)
 
 // binaries of N = 2^lg packed in one tile of `tile` samples (tile 0 = kTileMin)
 __host__ __device__ __forceinline__ int tile_pack(int tile, int lg, int minp)

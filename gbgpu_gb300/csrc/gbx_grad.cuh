@@ -491,9 +491,9 @@ template <bool THIRD> __host__ __device__ constexpr int grad_acc() { return THIR
 // shared memory of a grad_kernel tile of maxS samples
 // (buf: A and E per sample, 2 float2; es: 3 float2; third body: psi 3
 // doubles, v_LOS and g 3 floats each)
-__host__ __device__ constexpr size_t grad_smem_bytes(bool third, int maxS)
+__host__ __device__ constexpr size_t grad_smem_bytes(bool third, int maxS, int maxP)
 {
-    return (sizeof(Bin) + sizeof(GradExtra)) * kMaxPack + sizeof(double) * (third ? 29 : 19) * 32 +
+    return (sizeof(Bin) + sizeof(GradExtra)) * (size_t)maxP + sizeof(double) * (third ? 29 : 19) * 2 * kMaxPack +
            (size_t)maxS * (5 * sizeof(float2) + (third ? 3 * (sizeof(double) + 2 * sizeof(float)) : 0));
 }
 
@@ -506,11 +506,12 @@ __global__ void __launch_bounds__(kBlock, THIRD ? 1 : 2) grad_kernel(const GradP
     const KParams &K = GP.K;
     extern __shared__ __align__(16) unsigned char smem[];
     Bin *bins = reinterpret_cast<Bin *>(smem);
-    GradExtra *gxs = reinterpret_cast<GradExtra *>(smem + sizeof(Bin) * kMaxPack);
-    double *red = reinterpret_cast<double *>(smem + (sizeof(Bin) + sizeof(GradExtra)) * kMaxPack);
-    // red: group partial sums (float pairs) and per-binary FP64 sums, 16 x kGradAcc each
-    V *buf = reinterpret_cast<V *>(smem + (sizeof(Bin) + sizeof(GradExtra)) * kMaxPack +
-                                   sizeof(double) * kGradAcc * 32);
+    GradExtra *gxs = reinterpret_cast<GradExtra *>(smem + sizeof(Bin) * K.maxP);
+    double *red = reinterpret_cast<double *>(smem + (sizeof(Bin) + sizeof(GradExtra)) * K.maxP);
+    // red: group partial sums (float pairs, up to kMaxPack groups) and
+    // per-binary FP64 sums (up to kMaxPack binaries), kMaxPack x kGradAcc each
+    V *buf = reinterpret_cast<V *>(smem + (sizeof(Bin) + sizeof(GradExtra)) * K.maxP +
+                                   sizeof(double) * kGradAcc * 2 * kMaxPack);
     // buf: the A and E channels (forward transform, then the adjoint's);
     // es: exp(-i phase_s) per sample from the forward pass, directly after buf
     // (the third-body pre-passes use buf and es together as FP64 scratch)
@@ -720,7 +721,7 @@ __global__ void __launch_bounds__(kBlock, THIRD ? 1 : 2) grad_kernel(const GradP
         // lanes keeps it off the critical path (the FP64 pipe issues a warp
         // instruction per 64 cycles per SM sub-partition, whatever the mask).
         float2 *red2 = reinterpret_cast<float2 *>(red);
-        double *tsum = red + kGradAcc * 16;
+        double *tsum = red + kGradAcc * kMaxPack;
         {
             const bool leader = (tid & (width - 1)) == 0;
             const int g = tid / width;

@@ -88,15 +88,19 @@ struct KParams {
     double fstar;                  // c / (2 pi L)
     dfl stepd[GBX_MAX_LOG2N + 1];  // T / 2^k as float pairs (exact: division by a power of two)
     int maxS;                      // largest tile (samples) the shared memory is sized for
+    int maxP;                      // most binaries in a tile of this launch (<= kMaxPack)
 };
 
 enum { MODE_WAVE = 0, MODE_LL = 1, MODE_FILL = 2, MODE_SWAP = 4 };
 
 // doubles of the per-tile reduction scratch: 3 per 32-sample chunk, and at
 // least 8 per lane group (16 groups) for the swap epilogue
+// group partials of the likelihood (up to kMaxPack groups x 3 float pairs) and
+// the per-binary FP64 sums (up to kMaxPack x 3) after them, or the swap
+// epilogue's group x 8 FP64 partials
 __host__ __device__ __forceinline__ int red_doubles(int maxS)
 {
-    return 3 * (maxS >> 5) > 128 ? 3 * (maxS >> 5) : 128;
+    return 3 * (maxS >> 5) > 8 * kMaxPack ? 3 * (maxS >> 5) : 8 * kMaxPack;
 }
 
 __device__ __forceinline__ double quad_form(const double *e, double x, double y, double z)
@@ -965,8 +969,8 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
     const R is2 = (R)0.70710678118654752440, is6 = (R)0.40824829046386301637;
     extern __shared__ __align__(16) unsigned char smem[];
     Bin *bins = reinterpret_cast<Bin *>(smem);
-    double *red = reinterpret_cast<double *>(smem + sizeof(Bin) * kMaxPack);
-    V *buf = reinterpret_cast<V *>(smem + sizeof(Bin) * kMaxPack + sizeof(double) * red_doubles(K.maxS));
+    double *red = reinterpret_cast<double *>(smem + sizeof(Bin) * K.maxP);
+    V *buf = reinterpret_cast<V *>(smem + sizeof(Bin) * K.maxP + sizeof(double) * red_doubles(K.maxS));
     __shared__ int s_tile;
 
     const gbx_wave_args &a = K.a;
@@ -1255,10 +1259,10 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
             // Threads [p*Tpb, (p+1)*Tpb) own binary p of the tile and walk its
             // window with stride Tpb, so each warp reads a contiguous run of the
             // data/PSD window.  Per-thread sums are FP64 (plain form) or FP32
-            // (mixed form; at most N/Tpb <= 8 terms), lanes are combined with an
-            // FP64 or float-pair shuffle tree, and the <= 16 group partials of a
-            // binary are added in FP64 by one thread.
-            const int Tpb = kBlock / maxcnt;               // N/2 for N <= 512, else 256
+            // (mixed form; N/Tpb <= 16 terms), lanes are combined with an FP64 or
+            // float-pair shuffle tree, and a binary's <= 16 group partials are
+            // added by one thread per (binary, term).
+            const int Tpb = kBlock / maxcnt;               // 256 / binaries per tile
             const int width = Tpb < 32 ? Tpb : 32;
             const int p = tid / Tpb;
             const int i0 = tid - p * Tpb;
@@ -1338,7 +1342,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
             }
             __syncthreads();
             // per (binary, term) sums over the binary's groups -> tsum (FP64)
-            double *tsum = red + 64;
+            double *tsum = red + 3 * kMaxPack;
             {
                 const int per = Tpb / width;
                 for (int t = tid; t < 3 * cnt; t += kBlock) {
@@ -1441,9 +1445,9 @@ __global__ void __launch_bounds__(kPrepBlock) prep_kernel(const KParams K)
 // nch transformed channels per binary (3 for the waveform outputs, 2 = A, E
 // otherwise); the third-body pre-passes use three slots per sample of buf as
 // FP64 scratch and keep psi and v_LOS after them
-static size_t smem_bytes(int prec, bool third, int maxS, int nch)
+static size_t smem_bytes(int prec, bool third, int maxS, int nch, int maxP)
 {
-    size_t head = sizeof(Bin) * kMaxPack + sizeof(double) * (size_t)red_doubles(maxS);
+    size_t head = sizeof(Bin) * (size_t)maxP + sizeof(double) * (size_t)red_doubles(maxS);
     size_t rc = prec == GBX_FP64 ? sizeof(double2) : sizeof(float2);
     size_t r = prec == GBX_FP64 ? sizeof(double) : sizeof(float);
     size_t s = head + (third ? 3 : nch) * (size_t)maxS * rc;
@@ -1455,7 +1459,8 @@ template <typename R, int MODE, bool THIRD>
 static int launch_one(const KParams &K, int maxS, cudaStream_t st)
 {
     auto kern = wave_kernel<R, MODE, THIRD>;
-    size_t sm = smem_bytes(sizeof(R) == 8 ? GBX_FP64 : GBX_MIXED, THIRD, maxS, MODE == MODE_WAVE ? 3 : 2);
+    size_t sm = smem_bytes(sizeof(R) == 8 ? GBX_FP64 : GBX_MIXED, THIRD, maxS, MODE == MODE_WAVE ? 3 : 2,
+                           K.maxP);
     if (sm > 227 * 1024) return set_error(GBX_ERR_UNSUPPORTED, "tile needs %zu B of shared memory", sm);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute");
@@ -1491,10 +1496,21 @@ static int launch_one(const KParams &K, int maxS, cudaStream_t st)
     return GBX_OK;
 }
 
+// most binaries in one tile of this launch (the shared memory holds their constants)
+static int max_pack(const gbx_wave_args *a, int minp)
+{
+    if (a->tiles == nullptr) return tile_pack(a->tile, 31 - __builtin_clz((unsigned)a->N), minp);
+    int mp = 1;
+    for (int k = 5; k <= GBX_MAX_LOG2N; k++)
+        if (a->orbit[k]) mp = max(mp, tile_pack(a->tile, k, minp));
+    return mp;
+}
+
 template <int MODE>
 static int dispatch(KParams &K, int maxS, cudaStream_t st)
 {
     K.maxS = maxS;
+    K.maxP = max_pack(&K.a, MODE == MODE_SWAP ? 2 : 1);
     const bool third = K.a.nparams >= 14;
     if (K.a.precision == GBX_FP64) {
         return third ? launch_one<double, MODE, true>(K, maxS, st)
@@ -1719,10 +1735,11 @@ extern "C" int gbx_waveform_ll_grad(const gbx_wave_args *a, const gbx_ll_args *l
     K.d_h = (double2 *)d_h;
     K.h_h = (double2 *)h_h;
     K.maxS = maxS;
+    K.maxP = max_pack(&K.a, 1);
     G.grad = grad;
     const bool third = b.nparams == 14;
     auto kern = third ? grad_kernel<true> : grad_kernel<false>;
-    const size_t sm = grad_smem_bytes(third, maxS);
+    const size_t sm = grad_smem_bytes(third, maxS, K.maxP);
     if (sm > 227 * 1024) return set_error(GBX_ERR_UNSUPPORTED, "tile needs %zu B of shared memory", sm);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(grad)");

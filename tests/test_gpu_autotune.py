@@ -133,3 +133,29 @@ def test_args_outlive_plan_cache_eviction():
     like = (-0.5 * (h_h.real - 2 * d_h.real)).cpu().numpy()
     np.testing.assert_allclose(like, ref, rtol=1e-6, atol=1e-6)
     del junk
+
+
+def test_invalid_launch_shapes_are_rejected():
+    """Bad tile values and shapes the shared memory cannot hold return errors
+    (the autotuner skips such candidates)."""
+    from gbgpu_gb300 import GBGPU, GBGPUThirdBody
+    p, extra, data, S, s0 = _ll_setup(8, 256, 61, third=True)
+    d = [dev(x) for x in data]
+    for tile in (100, 32, 8192):
+        gb = GBGPU()
+        gb.d_d = 0.0
+        gb._launch_shape = lambda *a, _t=tile, **k: (_t, 0)
+        with pytest.raises(RuntimeError, match="tile"):
+            gb.get_ll(p, d, [dev(S), dev(S)], N=256, T=T_OBS, dt=10.0, start_freq_ind=s0)
+    # third-body gradient with N = 2048 and 4096-sample tiles: too much shared memory
+    gb3 = GBGPUThirdBody()
+    gb3.d_d = 0.0
+    gb3._launch_shape = lambda *a, **k: (4096, 0)
+    full = np.concatenate([p, np.array(extra)])
+    with pytest.raises(RuntimeError, match="shared memory"):
+        gb3.get_ll_grad(full, d, [dev(S), dev(S)], N=2048, T=T_OBS, dt=10.0, start_freq_ind=s0)
+    # the default shape works for the same call
+    gb3._launch_shape = lambda *a, **k: (0, 0)
+    like, grad = gb3.get_ll_grad(full, d, [dev(S), dev(S)], N=2048, T=T_OBS, dt=10.0,
+                                 start_freq_ind=s0)
+    assert grad.shape == (14, 8) and np.all(np.isfinite(grad))

@@ -43,8 +43,8 @@ def test_sincos_mod_against_fp64():
 
 
 def test_link_sinc_cos_against_fp64():
-    a = np.concatenate([np.linspace(-6.0, 6.0, 200001), [1e-6, -1e-6, 0.4999, 0.5001, 1.5999,
-                                                         1.6001]])
+    a = np.concatenate([np.linspace(-6.0, 6.0, 200001), [1e-6, -1e-6, 0.1599, 0.1601, 0.4999,
+                                                         0.5001, 1.5999, 1.6001]])
     a = a[a != 0]
     xs, S, C = _run(a, 1)
     ref = np.sin(xs) / xs
