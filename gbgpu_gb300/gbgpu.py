@@ -268,7 +268,7 @@ class GBGPUBase(abc.ABC):
                 f"Observation time ({T}) is larger than length of time in orbital information "
                 f"({np.max(self.orbits.t_base)})")
 
-    def _plan(self, N, T, precision, tdi2, nparams, tile=0, blocks_per_sm=0):
+    def _plan(self, N, T, precision, tdi2, nparams, tile=0, blocks_per_sm=0, nkey=None):
         """WavePlan cache: tile schedules and orbit tables are built once per
         distinct (N or N-array contents, T, precision, tdi2, nparams, launch
         shape)."""
@@ -276,7 +276,8 @@ class GBGPUBase(abc.ABC):
             key = (int(N), float(T), precision, bool(tdi2), nparams, tile, blocks_per_sm)
         else:
             arr = np.ascontiguousarray(N, dtype=np.int64)
-            key = (_array_key(arr), arr.shape[0], float(T), precision, bool(tdi2), nparams, tile,
+            key = (_array_key(arr) if nkey is None else nkey, arr.shape[0], float(T), precision,
+                   bool(tdi2), nparams, tile,
                    blocks_per_sm)
         plan = self._plans.pop(key, None)
         if plan is None:
@@ -462,12 +463,13 @@ class GBGPUBase(abc.ABC):
         noise_index = _to_device(noise_index, torch.int32, self.device).contiguous()
         return dd, pp, data_length, data_index, noise_index
 
-    def _launch_shape(self, kind, N, B, precision, tdi2, nparams, run):
+    def _launch_shape(self, kind, N, B, precision, tdi2, nparams, run, nkey=None):
         """(tile, blocks_per_sm) for this workload: the autotuner's choice when
         autotuning is on (timing ``run`` on the first call), else defaults."""
         if not self.autotune:
             return 0, 0
-        nkey = int(N) if np.ndim(N) == 0 else _array_key(np.ascontiguousarray(N, dtype=np.int64))
+        if nkey is None:
+            nkey = int(N) if np.ndim(N) == 0 else _array_key(np.ascontiguousarray(N, dtype=np.int64))
         ck = (kind, nkey, int(B), precision, bool(tdi2), int(nparams))
         shape = self._shapes.get(ck)
         if shape is None:
@@ -499,15 +501,17 @@ class GBGPUBase(abc.ABC):
             return d_h, h_h
         la = self._ll_args(dd, pp, data_length, data_index, noise_index, T)
         nparams = params.shape[0]
+        # one content key of a per-binary N array per call (plan cache, launch shape)
+        nkey = None if np.ndim(N) == 0 else _array_key(np.ascontiguousarray(N, dtype=np.int64))
 
         def run(tile, bps):
-            plan = self._plan(N, T, precision, tdi2, nparams, tile, bps)
+            plan = self._plan(N, T, precision, tdi2, nparams, tile, bps, nkey=nkey)
             a = plan.args(params, start_freq_ind, self._status)
             rc = nat.lib().gbx_waveform_ll(ctypes.byref(a), ctypes.byref(la), nat.ptr(d_h),
                                            nat.ptr(h_h), nat.stream_handle())
             nat.check(rc, "gbx_waveform_ll")
 
-        shape = self._launch_shape("ll", N, B, precision, tdi2, nparams, run)
+        shape = self._launch_shape("ll", N, B, precision, tdi2, nparams, run, nkey=nkey)
         self._status.zero_()
         run(*shape)
         return d_h, h_h
@@ -579,7 +583,10 @@ class GBGPUBase(abc.ABC):
             d_h = torch.abs(d_h).to(torch.complex128)
         self.h_h = h_h
         self.d_h = d_h
-        d_d = torch.as_tensor(self.d_d, device=self.device)
+        # the reference's order, -1/2 (d_d + h_h - 2 d_h) (gbgpu.py:728); a
+        # scalar d_d enters as a kernel argument, not a device copy
+        d_d = float(self.d_d) if np.ndim(_to_host(self.d_d)) == 0 else \
+            torch.as_tensor(self.d_d, device=self.device)
         like = -1.0 / 2.0 * (d_d + h_h - 2 * d_h).real
         out = like.cpu().numpy()
         self._check_status()
