@@ -257,9 +257,9 @@ def sparse_accuracy(gb, p, Ns, Sd, seed, count=2000):
     return (d / torch.clamp(out["fp64"][1], min=1.0)).max().item()
 
 
-def config3(gb, data, Sd, seed, steps):
-    """BASELINE config 3 shape: 50,000 binaries, N = 256, TDI-2, config-0
-    parameter distributions, on the same 4-yr data grid.  Times the FP64 and
+def n256_tdi2_bench(gb, data, Sd, seed, steps):
+    """50,000 binaries, N = 256, TDI-2, f0 uniform on [1e-3, 5e-3] Hz and the
+    other parameters as the main batch, on the same 4-yr data grid.  Times the FP64 and
     mixed fused likelihood and the likelihood + gradient kernel."""
     import ctypes
     import torch
@@ -322,7 +322,7 @@ def config3(gb, data, Sd, seed, steps):
             run()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.nvtx.range_push(f"config3_{name}")
+        torch.cuda.nvtx.range_push(f"n256_{name}")
         e0.record()
         for _ in range(steps):
             run()
@@ -335,8 +335,8 @@ def config3(gb, data, Sd, seed, steps):
     out["grad_over_forward"] = out["grad_binaries_per_s"] / out["mixed_binaries_per_s"]
     out["mixed_over_fp64"] = out["mixed_binaries_per_s"] / out["fp64_binaries_per_s"]
     out["dropin"] = dropin_kernels(gb, p, data, Sd, steps)
-    out["fisher"] = config3_fisher(gb, p, Tu)
-    out["hmc"] = config3_hmc(gb, p, data, Sd, seed)
+    out["fisher"] = fisher_bench(gb, p, Tu)
+    out["hmc"] = hmc_bench(gb, p, data, Sd, seed)
     return out
 
 
@@ -345,7 +345,7 @@ FREE8 = (0, 1, 2, 4, 5, 6, 7, 8)      # amp, f0, fdot, phi0, iota, psi, lam, bet
 
 def dropin_kernels(gb, p, data, Sd, steps):
     """The reference's two native entry points as replaced here (gbx_get_ll,
-    gbx_fill_global through the backend method table) on the config-3 batch:
+    gbx_fill_global through the backend method table) on the 50k N = 256 batch:
     point-major FP64 templates from run_wave, then the unfused likelihood and
     the scatter-add into 256 template groups.  Algorithmic bytes per binary:
     get_ll 80 N + 44 (template, data, PSD windows, indices, outputs),
@@ -388,7 +388,7 @@ def dropin_kernels(gb, p, data, Sd, steps):
     peak, src = hbm_peak()
     ll_bytes = B * (80.0 * N + 44)
     fill_bytes = B * 96.0 * N
-    return {"workload": f"config-3 batch: {B} binaries, N={N}, point-major FP64 templates",
+    return {"workload": f"{B} binaries, N={N}, point-major FP64 templates",
             "get_ll_ms": ms_ll, "get_ll_GBps": ll_bytes / (ms_ll / 1e3) / 1e9,
             "get_ll_frac": ll_bytes / (ms_ll / 1e3) / 1e9 / peak,
             "fill_global_ms": ms_fill, "fill_global_GBps": fill_bytes / (ms_fill / 1e3) / 1e9,
@@ -397,14 +397,14 @@ def dropin_kernels(gb, p, data, Sd, steps):
                                        "binary) over CUDA-event time"}
 
 
-def config3_fisher(gb, p, Tu):
-    """Per-binary 8x8 Fisher matrices of the 50k config-3 binaries (FP64
+def fisher_bench(gb, p, Tu):
+    """Per-binary 8x8 Fisher matrices of the 50k N = 256 binaries (FP64
     five-point differences of the batched waveform, TDI-2)."""
     import torch
     B = p.shape[1]
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    torch.cuda.nvtx.range_push("config3_fisher")
+    torch.cuda.nvtx.range_push("n256_fisher")
     F = gb.fisher_matrices(p, N=256, T=T_OBS, dt=DT, tdi2=True, inds=FREE8, return_gpu=True)
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
@@ -415,9 +415,9 @@ def config3_fisher(gb, p, Tu):
                                   "+ one inner-product einsum"}
 
 
-def config3_hmc(gb, p, data, Sd, seed, B=4096, transitions=100, n_leapfrog=10, step=0.2):
+def hmc_bench(gb, p, data, Sd, seed, B=4096, transitions=100, n_leapfrog=10, step=0.2):
     """1,000-step HMC leapfrog chains for 4,096 binaries in one CUDA graph: the
-    4,096 loudest config-3 binaries, injected into a copy of the data; mass
+    4,096 loudest of the 50k N = 256 binaries, injected into a copy of the data; mass
     metric from their Fisher diagonals; every leapfrog step is one fused
     likelihood + gradient launch."""
     import torch
@@ -446,7 +446,7 @@ def config3_hmc(gb, p, data, Sd, seed, B=4096, transitions=100, n_leapfrog=10, s
     smp.accepted.zero_()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.nvtx.range_push("config3_hmc")
+    torch.cuda.nvtx.range_push("n256_hmc")
     e0.record()
     smp.replay()
     e1.record()
@@ -463,8 +463,8 @@ def config3_hmc(gb, p, data, Sd, seed, B=4096, transitions=100, n_leapfrog=10, s
     return out
 
 
-def config2(gb, seed, B=1_000_000, G=256, N=256, steps=3):
-    """BASELINE config 2: 1e6 binaries, f0 density f^(-11/3) on [1e-4, 1e-2] Hz,
+def fill_bench(gb, seed, B=1_000_000, G=256, N=256, steps=3):
+    """Global templates of 1e6 binaries: f0 density f^(-11/3) on [1e-4, 1e-2] Hz,
     amp ~ f0^(2/3) with log-normal scatter (sigma 0.3), N = 256, group index
     uniform over 256 walkers, templates (256, 2, 12,623,041) complex128
     (103.4 GB).  Times the fused FP64 atomic fill and the deterministic fill
@@ -505,12 +505,12 @@ def config2(gb, seed, B=1_000_000, G=256, N=256, steps=3):
         torch.cuda.synchronize()
         return ev[0].elapsed_time(ev[1]) / steps
 
-    ms_zero = timeit(lambda: tmpl.zero_(), "config2_zero")
+    ms_zero = timeit(lambda: tmpl.zero_(), "fill_zero")
     for prec in ("fp64", "mixed"):
         for mode in ("atomic", "deterministic"):
             ms = timeit(lambda: gb.generate_global_template(pT, gi, tmpl, N=N, T=T_OBS, dt=DT,
                                                             precision=prec, fill_mode=mode),
-                        f"config2_{prec}_{mode}")
+                        f"fill_{prec}_{mode}")
             out[f"{prec}_{mode}_ms"] = ms
             out[f"{prec}_{mode}_binaries_per_s"] = B / (ms / 1e3)
     out["zeroing_ms"] = ms_zero
@@ -522,8 +522,8 @@ def config2(gb, seed, B=1_000_000, G=256, N=256, steps=3):
     return out
 
 
-def config4(seed, W=4096, K=500, N=512, steps=100, replays=3):
-    """BASELINE config 4: GBGPUThirdBody, 4,096 walkers x 500 sources, N = 512,
+def swap_bench(seed, W=4096, K=500, N=512, steps=100, replays=3):
+    """GBGPUThirdBody swap sampler: 4,096 walkers x 500 sources, N = 512,
     T = 4 yr, dt = 5 s; every walker proposes a swap of one source per step
     (swap likelihood in the mixed form, Metropolis accept, residual update);
     100 steps are captured as one CUDA graph and replayed.  Sources sit in a
@@ -565,7 +565,7 @@ def config4(seed, W=4096, K=500, N=512, steps=100, replays=3):
     smp.replay()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.nvtx.range_push("config4_graph")
+    torch.cuda.nvtx.range_push("swap_graph")
     e0.record()
     for _ in range(replays):
         smp.replay()
@@ -639,7 +639,7 @@ def run_gpu(args, rank, world):
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
               for _ in range(K)]
         t_wall = time.perf_counter()
-        torch.cuda.nvtx.range_push(f"config1_{prec}")   # ncu --nvtx-include config1_<prec>/
+        torch.cuda.nvtx.range_push(f"ll_{prec}")   # ncu --nvtx-include ll_<prec>/
         for a, b in ev:
             flush.zero_()                     # evict L2 between timed steps
             a.record(stream)
@@ -694,12 +694,12 @@ def run_gpu(args, rank, world):
         ms_mixed, wall_mixed = timed("mixed", args.steps, args.warmup)
     ms_fp64, _ = timed("fp64", max(1, min(args.steps, 3)), 1)
     ms_grad, _ = timed("grad", max(1, min(args.steps, 10)), 1)
-    cfg3 = config3(gb, data, Sd, args.seed + rank, max(1, min(args.steps, 10)))
+    cfg3 = n256_tdi2_bench(gb, data, Sd, args.seed + rank, max(1, min(args.steps, 10)))
     cfg2 = cfg4 = None
     if not args.no_fill_bench:
-        cfg2 = config2(gb, args.seed + rank)
+        cfg2 = fill_bench(gb, args.seed + rank)
     if not args.no_mcmc_bench:
-        cfg4 = config4(args.seed + rank)
+        cfg4 = swap_bench(args.seed + rank)
 
     # e2e through the public API: host params -> device, like -> host
     p_pin = torch.from_numpy(np.ascontiguousarray(p)).pin_memory()
@@ -732,7 +732,7 @@ def run_gpu(args, rank, world):
         "vs_baseline": None,
         "dtype": "f32+f64 (FP64 phase/delay/accumulation, FP32 slow part and FFT)",
         "data": "synthetic (seeded binaries; injected sum + Gaussian noise from the analytic A/E PSD)",
-        "config": {"workload": "config1: 200k binaries, uneven N in {64..2048} by f0 band, "
+        "config": {"workload": "200k binaries, uneven N in {64..2048} by f0 band, "
                                "T=4x31557600 s, dt=5 s, L=12,623,041 bins x A,E complex128",
                    "binaries_per_gpu": B, "N_mix": {str(n): int(np.count_nonzero(Ns == n))
                                                     for n in np.unique(Ns)},
@@ -754,9 +754,9 @@ def run_gpu(args, rank, world):
                       "(mixed form) on the same 200k-binary batch",
         "launch_shapes": {k: {"tile": int(v[0]), "blocks_per_sm": int(v[1])}
                           for k, v in shapes.items()} or "defaults (tile 512, full occupancy)",
-        "config3": cfg3,
-        "config2": cfg2,
-        "config4": cfg4,
+        "n256_tdi2": cfg3,
+        "fill_templates": cfg2,
+        "thirdbody_swaps": cfg4,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "issue_active_frac": profiled("issue_active_frac"),
@@ -789,7 +789,7 @@ def profiled(key):
     """A figure of the committed ncu summary of the fused kernel (a line
     ``key: value``): ``dram_bytes_per_launch`` (dram__bytes_read.sum +
     dram__bytes_write.sum of one full-size launch) or ``issue_active_frac``."""
-    path = os.path.join(ROOT, "profiles", "wave_ll_mixed_config1.txt")
+    path = os.path.join(ROOT, "profiles", "wave_ll_mixed_200k.txt")
     try:
         for line in open(path):
             if line.startswith(key + ":"):
@@ -840,7 +840,7 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded; noise-only data for the CPU timing)",
-            "config": {"workload": "config1: 200k binaries, uneven N in {64..2048} by f0 band, "
+            "config": {"workload": "200k binaries, uneven N in {64..2048} by f0 band, "
                                    "T=4x31557600 s, dt=5 s, L=12,623,041 bins x A,E complex128"},
             "impl": "reference", "cpu_baseline": base,
             "e2e": {"value": v, "unit": "binaries/s", "h2d_bytes_per_step": 0,
