@@ -60,10 +60,10 @@ _BACKEND = None
 
 
 def get_backend(name=None):
-    """The single backend of this build (CUDA on sm_103a); no CPU fallback."""
+    """The single backend of this package (CUDA on sm_103a); no CPU fallback."""
     global _BACKEND
     if name not in (None, "gpu", "cuda", "gb300", "cuda13x"):
-        raise ValueError(f"backend {name!r} is not available: this build only runs on the GPU")
+        raise ValueError(f"backend {name!r} is not available: this package only runs on the GPU")
     if _BACKEND is None:
         if not torch.cuda.is_available():
             raise RuntimeError("gbgpu_gb300 needs a CUDA GPU; no CPU fallback exists")

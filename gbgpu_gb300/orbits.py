@@ -4,7 +4,7 @@ The reference takes any ``lisatools.detector.Orbits`` object and uses only
 ``get_pos(t, sc)``, ``armlength``, ``t_base`` and ``configure`` (gbgpu/gbgpu.py:
 87-101, 181, 243, 390-397).  The same duck-typed interface is accepted here;
 ``EqualArmlengthOrbits`` is the analytic default (``lisatools``' file-based
-orbits are not available in this build).  Positions are evaluated on the host
+orbits are not available here).  Positions are evaluated on the host
 once per (N, T) and turned into a device table by ``gbx_orbit_table``.
 """
 

@@ -231,7 +231,7 @@ int gbx_waveform_fill(const gbx_wave_args *a, void *A_glob, void *E_glob,
 
 /*
  * Swap log-likelihood (no counterpart in this version of the reference; the
- * build's own definition): for each pair j, binaries 2j (the current source)
+ * library's own definition): for each pair j, binaries 2j (the current source)
  * and 2j+1 (the proposal) of the batch, with r the residual row chosen by
  * data_index[2j+1] (d minus the walker's current sum of sources) and
  * Dh = h_new - h_old,

@@ -3,7 +3,7 @@
 A CPU restatement of the reference's waveform, likelihood, global-template
 fill, third-body hooks and the swap-likelihood composition.  It is imported
 only by ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py``, as the checker; the product never calls it.  Each function
+``bench.py``, to compare against; the product never calls it.  Each function
 cites the reference lines it restates (paths relative to the reference's
 project root).  The native inner loops (get_ll / fill_global) are restated in
 C in ``oracle/gbgpu_oracle.c`` and bound here through ctypes.

@@ -3,7 +3,7 @@
 The fixtures in tests/golden were produced by tests/golden/make_golden.py,
 which runs the reference's gbgpu.py / thirdbody.py / utility.py and its
 gbgpu_utils.cu (compiled as C++).  These tests pin the oracle before it is
-used as the checker for the CUDA path.
+compared against the CUDA path.
 """
 
 import numpy as np
