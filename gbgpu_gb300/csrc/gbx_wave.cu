@@ -343,20 +343,9 @@ __device__ __forceinline__ float kepler_u_mixed(double t, const Bin &B)
     return u;
 }
 
-__device__ float vlos_mixed(double t, const Bin &B)
-{
-    float u = kepler_u_mixed(t, B);
-    const float e = B.e2f;
-    if (e > 1e-6f) {
-        float bt = (1.0f - sqrtf(1.0f - e * e)) / e;
-        float su, cu;
-        sincosf(u, &su, &cu);
-        u += 2.0f * atan2f(bt * su, 1.0f - bt * cu);
-    }
-    return B.A2f * (sinf(u + B.varpif) + e * B.sinvarpif);
-}
-
-// v_LOS (as vlos_mixed) and its time derivative dv/dt = A2 cos(phi + varpi)
+// v_LOS of the FP32 Kepler solve, A2 (sin(phi + varpi) + e sin varpi) with
+// the true anomaly phi from u, and its time derivative
+// dv/dt = A2 cos(phi + varpi)
 // dphi/dM n2, with dphi/dM = sqrt(1 - e^2) / (1 - e cos u)^2 (1 / (1 - e cos u)
 // below e = 1e-6, where the model takes phi = u).
 __device__ float vlos_dt_mixed(double t, const Bin &B, float &dvdt)
@@ -379,7 +368,7 @@ __device__ float vlos_dt_mixed(double t, const Bin &B, float &dvdt)
     return B.A2f * (sp + e * B.sinvarpif);
 }
 
-// v_LOS (as vlos_mixed) and its derivatives dv[0..4] = d/d(A2, varpi, e2,
+// v_LOS (as vlos_dt_mixed) and its derivatives dv[0..4] = d/d(A2, varpi, e2,
 // P2 [yr], T2 [yr]), dv[5] = d/dt.  With c = 1 - e cos u and M = n2 (t - T2):
 // du/dM = 1/c, du/de = sin u / c (Kepler), and for the true anomaly
 // dphi/du = sqrt(1-e^2)/c, dphi/de|u = sin u / (sqrt(1-e^2) c); below
@@ -622,7 +611,7 @@ __device__ __forceinline__ void slow_fp64(const Bin &B, int n, int N, double tm,
 template <bool THIRD, bool STORE_E = false>
 __device__ __forceinline__ void slow_mixed(const Bin &B, int n, int N, dfl step, float Loc,
                                            const double *__restrict__ tab,
-                                           const double *psi, const float *vl, float2 out[3],
+                                           const dfl *psi, const float *vl, float2 out[3],
                                            float2 *Eout = nullptr)
 {
     const float *tabf = reinterpret_cast<const float *>(tab + (size_t)18 * N);
@@ -688,7 +677,7 @@ __device__ __forceinline__ void slow_mixed(const Bin &B, int n, int N, dfl step,
         }
         ph.l += small;
         if (THIRD) {
-            ph = df_add(ph, df_neg(df_from(psi[s])));
+            ph = df_add(ph, df_neg(psi[s]));
             const float q = rintf(ph.h * inv2pi);
             ph = df_add(ph, df_neg(df_mul_f(twopi, q)));
         }
@@ -868,12 +857,11 @@ __device__ __forceinline__ double warp_sum(double v)
 //   A) v_LOS at every (sample, spacecraft) -> vl, and g = v_LOS f_GW;
 //   B) trapezoid increments (xi_n - xi_{n-1}) (g_{n-1} + g_n) pi / c -> inc;
 //   C) their inclusive prefix sum along n -> psi (the phase added to argS).
-// inc is scratch of 3 cnt N doubles; gout, when given, receives g in FP32.
+// FP64 throughout; inc is scratch of 3 cnt N doubles.
 // Called by every thread of the block (contains barriers).
-template <typename R>
 __device__ __forceinline__ void third_prepass(const Bin *bins, const double *__restrict__ tab,
-                                              int cnt, int lg, double step, double *psi, R *vl,
-                                              double *inc, float *gout)
+                                              int cnt, int lg, double step, double *psi, double *vl,
+                                              double *inc)
 {
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int N = 1 << lg, S = cnt << lg;
@@ -885,36 +873,20 @@ __device__ __forceinline__ void third_prepass(const Bin *bins, const double *__r
 #pragma unroll
             for (int s = 0; s < 3; s++) {
                 psi[(p * 3 + s) * N + n] = 0.0;
-                vl[(p * 3 + s) * N + n] = (R)0;
-                if (gout) gout[(p * 3 + s) * N + n] = 0.0f;
+                vl[(p * 3 + s) * N + n] = 0.0;
             }
             continue;
         }
-        // mixed form: one Kepler solve per sample (spacecraft 1), the other two
-        // spacecraft's delayed times are within L/c = 8.3 s of it, so v_LOS
-        // there is v + (dv/dt) dxi (second-order error < 3e-9 v for P2 >= 1 yr)
-        double xi0 = 0.0;
-        float v0 = 0.0f, dv0 = 0.0f;
 #pragma unroll
         for (int s = 0; s < 3; s++) {
             double kP = B.k[0] * __ldg(tab + (size_t)(3 * s) * N + n) +
                         B.k[1] * __ldg(tab + (size_t)(3 * s + 1) * N + n) +
                         B.k[2] * __ldg(tab + (size_t)(3 * s + 2) * N + n);
             double xi = tm - kP;
-            double v;
-            if constexpr (sizeof(R) == 8) {
-                v = vlos_fp64(xi, B);
-            } else {
-                if (s == 0) {
-                    xi0 = xi;
-                    v0 = vlos_dt_mixed(xi, B, dv0);
-                }
-                v = (double)fmaf(dv0, (float)(xi - xi0), v0);
-            }
+            double v = vlos_fp64(xi, B);
             double fgw = B.f0 + B.fdot * xi + 0.5 * B.fddot * xi * xi;
             psi[(p * 3 + s) * N + n] = v * fgw;
-            vl[(p * 3 + s) * N + n] = (R)v;
-            if (gout) gout[(p * 3 + s) * N + n] = (float)(v * fgw);
+            vl[(p * 3 + s) * N + n] = v;
         }
     }
     __syncthreads();
@@ -955,6 +927,91 @@ __device__ __forceinline__ void third_prepass(const Bin *bins, const double *__r
         for (int c = 0; c < chunk; c++) {
             run += src[c];
             dst[c] = run;
+        }
+    }
+    __syncthreads();
+}
+
+// Third-body pre-passes of the mixed form for a tile of cnt binaries with
+// N = 2^lg samples (the same model as third_prepass above, without FP64 work
+// per spacecraft):
+//   A) spacecraft 1: delayed time in FP64, one Kepler solve for v_LOS and
+//      dv/dt (vlos_dt_mixed); spacecraft 2, 3: v_LOS linearised in their
+//      k.P/c offsets (FP32, <= L/c = 8.3 s; the second-order error is below
+//      3e-9 v for P2 >= 1 yr); g = v_LOS f_GW in FP32 -> gout;
+//      k.P/c of every spacecraft in FP32 -> kps (scratch);
+//   B) increments (xi_n - xi_{n-1}) (g_{n-1} + g_n) pi / c with
+//      xi_n - xi_{n-1} = T/N - (kP_n - kP_{n-1}) (T/N as a float pair), and
+//      their inclusive prefix sum along n as float pairs -> psi.
+// Called by every thread of the block (contains barriers).
+__device__ __forceinline__ void third_prepass_mixed(const Bin *bins, const double *__restrict__ tab,
+                                                    int cnt, int lg, double step, dfl *psi,
+                                                    float *vl, float *kps, float *gout)
+{
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int N = 1 << lg, S = cnt << lg;
+    const float *tabf = reinterpret_cast<const float *>(tab + (size_t)18 * N);
+    for (int m = tid; m < S; m += kBlock) {
+        const int p = m >> lg, n = m & (N - 1);
+        const Bin &B = bins[p];
+        if (!B.valid) {                       // outputs unused: no Kepler solve
+#pragma unroll
+            for (int s = 0; s < 3; s++) {
+                vl[(p * 3 + s) * N + n] = 0.0f;
+                kps[(p * 3 + s) * N + n] = 0.0f;
+                gout[(p * 3 + s) * N + n] = 0.0f;
+            }
+            continue;
+        }
+        const double kP0 = B.k[0] * __ldg(tab + n) + B.k[1] * __ldg(tab + (size_t)N + n) +
+                           B.k[2] * __ldg(tab + (size_t)2 * N + n);
+        const double xi0 = (double)n * step - kP0;
+        float dv0;
+        const float v0 = vlos_dt_mixed(xi0, B, dv0);
+        float kPf[3];
+#pragma unroll
+        for (int s = 0; s < 3; s++)
+            kPf[s] = fmaf(B.kf[0], __ldg(tabf + (size_t)(9 + 3 * s) * N + n),
+                          fmaf(B.kf[1], __ldg(tabf + (size_t)(9 + 3 * s + 1) * N + n),
+                               B.kf[2] * __ldg(tabf + (size_t)(9 + 3 * s + 2) * N + n)));
+        const float x0 = (float)xi0;
+#pragma unroll
+        for (int s = 0; s < 3; s++) {
+            const float dk = s ? kPf[s] - kPf[0] : 0.0f;   // xi_s = xi_1 - dk
+            const float v = fmaf(-dv0, dk, v0);
+            const float xf = x0 - dk;
+            const float fgw = fmaf(fmaf(0.5f * B.fddotf, xf, B.fdotf), xf, B.f0f);
+            vl[(p * 3 + s) * N + n] = v;
+            kps[(p * 3 + s) * N + n] = kPf[s];
+            gout[(p * 3 + s) * N + n] = v * fgw;
+        }
+    }
+    __syncthreads();
+    // warp per (binary, spacecraft) row; lane owns a chunk of N/32 samples
+    const dfl stp = df_from(step);
+    const float k = (float)(kPi / kCSI);
+    const int chunk = N >> 5;
+    for (int row = warp; row < 3 * cnt; row += kBlock / 32) {
+        const float *kr = kps + (size_t)row * N, *gr = gout + (size_t)row * N;
+        dfl *dst = psi + (size_t)row * N;
+        const int c0 = lane * chunk;
+        auto inc = [&](int n) -> float {
+            if (n == 0) return 0.0f;
+            const float d = (stp.h - (kr[n] - kr[n - 1])) + stp.l;
+            return d * (gr[n - 1] + gr[n]) * k;
+        };
+        dfl t = {0.0f, 0.0f};
+        for (int c = 0; c < chunk; c++) t = df_add(t, dfl{inc(c0 + c), 0.0f});
+        dfl incl = t;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const dfl y = {__shfl_up_sync(0xffffffffu, incl.h, o), __shfl_up_sync(0xffffffffu, incl.l, o)};
+            if (lane >= o) incl = df_add(incl, y);
+        }
+        dfl run = df_add(incl, df_neg(t));
+        for (int c = 0; c < chunk; c++) {
+            run = df_add(run, dfl{inc(c0 + c), 0.0f});
+            dst[c0 + c] = run;
         }
     }
     __syncthreads();
@@ -1033,13 +1090,23 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
         const double step = a.T * exp2_int(-lg);  // tm = n T/N (gbgpu.py:269), exact
         const dfl stepd = K.stepd[lg];
 
-        double *psi = nullptr;
+        double *psi = nullptr;          // FP64 form: cumulative Doppler phase
+        dfl *psif = nullptr;            // mixed form: the same as float pairs
         R *vl = nullptr;
         if (THIRD) {
-            psi = reinterpret_cast<double *>(buf + 3 * (size_t)maxcnt * N);
-            vl = reinterpret_cast<R *>(psi + 3 * (size_t)maxcnt * N);
-            third_prepass<R>(bins, tab, cnt, lg, step, psi, vl, reinterpret_cast<double *>(buf),
-                             nullptr);
+            if constexpr (sizeof(R) == 8) {
+                psi = reinterpret_cast<double *>(buf + 3 * (size_t)maxcnt * N);
+                vl = reinterpret_cast<R *>(psi + 3 * (size_t)maxcnt * N);
+                third_prepass(bins, tab, cnt, lg, step, psi, reinterpret_cast<double *>(vl),
+                              reinterpret_cast<double *>(buf));
+            } else {
+                // scratch: k.P/c and g in buf (6 floats per sample there)
+                psif = reinterpret_cast<dfl *>(buf + 3 * (size_t)maxcnt * N);
+                vl = reinterpret_cast<R *>(psif + 3 * (size_t)maxcnt * N);
+                float *scr = reinterpret_cast<float *>(buf);
+                third_prepass_mixed(bins, tab, cnt, lg, step, psif, reinterpret_cast<float *>(vl), scr,
+                                    scr + 3 * (size_t)maxcnt * N);
+            }
         }
 
         // slow part -> buf[(p*3 + channel)*N + n]
@@ -1048,11 +1115,13 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
             const Bin &B = bins[p];
             const double tm = (double)n * step;
             double ps[3] = {0.0, 0.0, 0.0};
+            dfl psf[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
             R vv[3] = {0, 0, 0};
             if (THIRD) {
 #pragma unroll
                 for (int s = 0; s < 3; s++) {
-                    ps[s] = psi[(p * 3 + s) * N + n];
+                    if constexpr (sizeof(R) == 8) ps[s] = psi[(p * 3 + s) * N + n];
+                    else psf[s] = psif[(p * 3 + s) * N + n];
                     vv[s] = vl[(p * 3 + s) * N + n];
                 }
             }
@@ -1066,7 +1135,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                 slow_fp64<THIRD>(B, n, N, tm, 0.0, tab, fstar, ps, vd, reinterpret_cast<double2 *>(o));
             } else {
                 float vf[3] = {(float)vv[0], (float)vv[1], (float)vv[2]};
-                slow_mixed<THIRD>(B, n, N, stepd, Loc, tab, ps, vf, reinterpret_cast<float2 *>(o));
+                slow_mixed<THIRD>(B, n, N, stepd, Loc, tab, psf, vf, reinterpret_cast<float2 *>(o));
             }
             if constexpr (NCH == 3) {
 #pragma unroll
