@@ -516,9 +516,10 @@ __global__ void __launch_bounds__(kBlock, THIRD ? 1 : 2) grad_kernel(const GradP
     // es: exp(-i phase_s) per sample from the forward pass, directly after buf
     // (the third-body pre-passes use buf and es together as FP64 scratch)
     V *es = buf + 2 * (size_t)K.maxS;
-    // third body: cumulative phase (forward; reused for the phase adjoints cph
-    // in the backward pass), v_LOS and g = v_LOS f_GW per (sample, spacecraft)
-    double *psi = reinterpret_cast<double *>(es + 3 * (size_t)K.maxS);
+    // third body: cumulative phase as float pairs (forward; reused for the
+    // phase adjoints cph in the backward pass), v_LOS and g = v_LOS f_GW per
+    // (sample, spacecraft)
+    dfl *psi = reinterpret_cast<dfl *>(es + 3 * (size_t)K.maxS);
     float2 *cphs = reinterpret_cast<float2 *>(psi);
     float *vl = reinterpret_cast<float *>(psi + 3 * (size_t)K.maxS);
     float *gq = vl + 3 * (size_t)K.maxS;
@@ -571,13 +572,14 @@ __global__ void __launch_bounds__(kBlock, THIRD ? 1 : 2) grad_kernel(const GradP
         const int S = cnt << lg;
         const dfl stepd = K.stepd[lg];
         const double step = a.T * exp2_int(-lg);
-        if (THIRD) third_prepass<float>(bins, tab, cnt, lg, step, psi, vl, reinterpret_cast<double *>(buf), gq);
+        // (scratch for the pre-pass: k.P/c of every sample in buf)
+        if (THIRD) third_prepass_mixed(bins, tab, cnt, lg, step, psi, vl, reinterpret_cast<float *>(buf), gq);
 
         // forward slow part and FFT
         for (int m = tid; m < S; m += kBlock) {
             const int p = m >> lg, n = m & (N - 1);
             float2 o[3];
-            double ps[3] = {0.0, 0.0, 0.0};
+            dfl ps[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
             float vv[3] = {0.f, 0.f, 0.f};
             if (THIRD) {
 #pragma unroll
