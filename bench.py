@@ -257,23 +257,16 @@ def sparse_accuracy(gb, p, Ns, Sd, seed, count=2000):
     return (d / torch.clamp(out["fp64"][1], min=1.0)).max().item()
 
 
-def n256_tdi2_bench(gb, data, Sd, seed, steps):
-    """50,000 binaries, N = 256, TDI-2, f0 uniform on [1e-3, 5e-3] Hz and the
-    other parameters as the main batch, on the same 4-yr data grid.  Times the FP64 and
-    mixed fused likelihood and the likelihood + gradient kernel."""
+def time_ll_variants(gb, prm, data, Sd, N, tdi2, steps, tag):
+    """Binaries/s of the FP64 and mixed fused likelihood and of the likelihood
+    + gradient kernel for the batch ``prm`` (nparams, B) at one N, each at its
+    autotuned launch shape (kernel launches through the C ABI, inputs on the
+    device).  Returns (rates, launch shapes)."""
     import ctypes
     import torch
     from gbgpu_gb300 import _native as nat
-    rng = np.random.default_rng(seed + 3)
-    B = 50_000
-    f0 = rng.uniform(1e-3, 5e-3, B)
-    fdot = 10 ** rng.uniform(-18, -15, B)
-    p = np.array([10 ** rng.uniform(-23, -21, B), f0, fdot, 11.0 / 3.0 * fdot ** 2 / f0,
-                  rng.uniform(0, 2 * np.pi, B), np.arccos(rng.uniform(-1, 1, B)),
-                  rng.uniform(0, np.pi, B), rng.uniform(0, 2 * np.pi, B),
-                  np.arcsin(rng.uniform(-1, 1, B))])
-    prm = torch.as_tensor(p, device="cuda").contiguous()
     Tu = int(T_OBS / DT) * DT
+    NP, B = prm.shape
     L = data[0].shape[0]
     zeros = torch.zeros(B, dtype=torch.int32, device="cuda")
     la = nat.LLArgs()
@@ -284,17 +277,15 @@ def n256_tdi2_bench(gb, data, Sd, seed, steps):
     la.df = 1.0 / Tu
     d_h = torch.empty(B, dtype=torch.complex128, device="cuda")
     h_h = torch.empty(B, dtype=torch.complex128, device="cuda")
-    g = torch.empty((9, B), dtype=torch.float64, device="cuda")
+    g = torch.empty((NP, B), dtype=torch.float64, device="cuda")
     lib = nat.lib()
     sh = nat.stream_handle()
-    out = {"workload": "50,000 binaries, N=256, tdi2=True, T=4x31557600 s",
-           "steps": steps}
-    shapes = {}
+    out, shapes = {}, {}
     for name, prec in (("fp64", "fp64"), ("mixed", "mixed"), ("grad", "mixed")):
         box = {}
 
         def set_shape(tile, bps):
-            plan = gb._plan(256, Tu, prec, True, 9, tile, bps)
+            plan = gb._plan(N, Tu, prec, tdi2, NP, tile, bps)
             box["a"] = plan.args(prm, grad=(name == "grad"))
 
         def run():
@@ -315,14 +306,14 @@ def n256_tdi2_bench(gb, data, Sd, seed, steps):
                 set_shape(tile, bps)
                 run()
             shape = default_tuner().tune(
-                workload_key("grad" if name == "grad" else "ll", 256, B, prec, True, 9), trial)
+                workload_key("grad" if name == "grad" else "ll", N, B, prec, tdi2, NP), trial)
         shapes[name] = {"tile": int(shape[0]), "blocks_per_sm": int(shape[1])}
         set_shape(*shape)
         for _ in range(2):
             run()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.nvtx.range_push(f"n256_{name}")
+        torch.cuda.nvtx.range_push(f"{tag}_{name}")
         e0.record()
         for _ in range(steps):
             run()
@@ -331,12 +322,65 @@ def n256_tdi2_bench(gb, data, Sd, seed, steps):
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / steps
         out[f"{name}_binaries_per_s"] = B / (ms / 1e3)
+    return out, shapes
+
+
+def n256_tdi2_bench(gb, data, Sd, seed, steps):
+    """50,000 binaries, N = 256, TDI-2, f0 uniform on [1e-3, 5e-3] Hz and the
+    other parameters as the main batch, on the same 4-yr data grid.  Times the FP64 and
+    mixed fused likelihood and the likelihood + gradient kernel."""
+    import torch
+    rng = np.random.default_rng(seed + 3)
+    B = 50_000
+    f0 = rng.uniform(1e-3, 5e-3, B)
+    fdot = 10 ** rng.uniform(-18, -15, B)
+    p = np.array([10 ** rng.uniform(-23, -21, B), f0, fdot, 11.0 / 3.0 * fdot ** 2 / f0,
+                  rng.uniform(0, 2 * np.pi, B), np.arccos(rng.uniform(-1, 1, B)),
+                  rng.uniform(0, np.pi, B), rng.uniform(0, 2 * np.pi, B),
+                  np.arcsin(rng.uniform(-1, 1, B))])
+    prm = torch.as_tensor(p, device="cuda").contiguous()
+    Tu = int(T_OBS / DT) * DT
+    out = {"workload": "50,000 binaries, N=256, tdi2=True, T=4x31557600 s",
+           "steps": steps}
+    rates, shapes = time_ll_variants(gb, prm, data, Sd, 256, True, steps, "n256")
+    out.update(rates)
     out["launch_shapes"] = shapes
     out["grad_over_forward"] = out["grad_binaries_per_s"] / out["mixed_binaries_per_s"]
     out["mixed_over_fp64"] = out["mixed_binaries_per_s"] / out["fp64_binaries_per_s"]
     out["dropin"] = dropin_kernels(gb, p, data, Sd, steps)
     out["fisher"] = fisher_bench(gb, p, Tu)
     out["hmc"] = hmc_bench(gb, p, data, Sd, seed)
+    return out
+
+
+def thirdbody_n256_bench(data, Sd, seed, steps):
+    """GBGPUThirdBody: 50,000 binaries with a third body, N = 256, TDI-2, the
+    binary parameters as the N = 256 batch, A2 log-uniform on [1, 1e4] m/s,
+    varpi uniform, e2 uniform on [0, 0.9], P2 log-uniform on [1, 40] yr, T2
+    uniform on [0, P2], on the same 4-yr data grid.  Times the FP64 and mixed fused likelihood and the
+    likelihood + gradient kernel (14 parameters)."""
+    import torch
+    from gbgpu_gb300 import GBGPUThirdBody
+    rng = np.random.default_rng(seed + 5)
+    B = 50_000
+    f0 = rng.uniform(1e-3, 5e-3, B)
+    fdot = 10 ** rng.uniform(-18, -15, B)
+    P2 = 10 ** rng.uniform(0, np.log10(40), B)
+    p = np.array([10 ** rng.uniform(-23, -21, B), f0, fdot, 11.0 / 3.0 * fdot ** 2 / f0,
+                  rng.uniform(0, 2 * np.pi, B), np.arccos(rng.uniform(-1, 1, B)),
+                  rng.uniform(0, np.pi, B), rng.uniform(0, 2 * np.pi, B),
+                  np.arcsin(rng.uniform(-1, 1, B)), 10 ** rng.uniform(0, 4, B),
+                  rng.uniform(0, 2 * np.pi, B), rng.uniform(0, 0.9, B), P2,
+                  rng.uniform(0, 1, B) * P2])
+    gb = GBGPUThirdBody(precision="mixed", autotune=True)
+    prm = torch.as_tensor(p, device="cuda").contiguous()
+    out = {"workload": "GBGPUThirdBody, 50,000 binaries, N=256, tdi2=True, T=4x31557600 s",
+           "steps": steps}
+    rates, shapes = time_ll_variants(gb, prm, data, Sd, 256, True, steps, "thirdbody_n256")
+    out.update(rates)
+    out["launch_shapes"] = shapes
+    out["grad_over_forward"] = out["grad_binaries_per_s"] / out["mixed_binaries_per_s"]
+    out["mixed_over_fp64"] = out["mixed_binaries_per_s"] / out["fp64_binaries_per_s"]
     return out
 
 
@@ -695,6 +739,7 @@ def run_gpu(args, rank, world):
     ms_fp64, _ = timed("fp64", max(1, min(args.steps, 3)), 1)
     ms_grad, _ = timed("grad", max(1, min(args.steps, 10)), 1)
     cfg3 = n256_tdi2_bench(gb, data, Sd, args.seed + rank, max(1, min(args.steps, 10)))
+    cfg3tb = thirdbody_n256_bench(data, Sd, args.seed + rank, max(1, min(args.steps, 10)))
     cfg2 = cfg4 = None
     if not args.no_fill_bench:
         cfg2 = fill_bench(gb, args.seed + rank)
@@ -757,6 +802,7 @@ def run_gpu(args, rank, world):
         "n256_tdi2": cfg3,
         "fill_templates": cfg2,
         "thirdbody_swaps": cfg4,
+        "thirdbody_n256": cfg3tb,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic,
                      "issue_active_frac": profiled("issue_active_frac"),

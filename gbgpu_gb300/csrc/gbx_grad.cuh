@@ -325,37 +325,44 @@ __device__ __forceinline__ void third_grad_sample(const Bin &B, const GradExtra 
                                                   const float2 cfo[3], float acc[14], float t5[10])
 {
     const float *tabf = reinterpret_cast<const float *>(tab + (size_t)18 * N);
-    const double tmk = (double)k * step;
     const float cpsi = -(float)(kPi / kCSI);
     const float ic = (float)(1.0 / kCSI);
+    // as the forward pre-pass: one Kepler solve at spacecraft 1's delayed
+    // time (FP64 time, FP32 solve), the other spacecraft linearised in their
+    // FP32 k.P/c offsets (<= 8.3 s: relative change of dv[0..4] <= n2 8.3 s)
+    const double kP0 = B.k[0] * __ldg(tab + k) + B.k[1] * __ldg(tab + (size_t)N + k) +
+                       B.k[2] * __ldg(tab + (size_t)2 * N + k);
+    const double xi0 = (double)k * step - kP0;
+    float dv[6];
+    const float v0 = vlos_grad_mixed(xi0, B, Gx.cosvarpi, Gx.P2yr, dv);
+    const float x0 = (float)xi0;
+    const float sth = (float)step, stl = (float)(step - (double)sth);
+    auto kpf = [&](int s, int n) {
+        const float *r = tabf + (size_t)(9 + 3 * s) * N + n;
+        return fmaf(B.kf[0], __ldg(r), fmaf(B.kf[1], __ldg(r + N), B.kf[2] * __ldg(r + 2 * N)));
+    };
+    const float kPf0 = kpf(0, k);
 #pragma unroll
     for (int s = 0; s < 3; s++) {
         const float2 *Rrow = Rrow0 + (size_t)s * N;
         const float *grow = grow0 + (size_t)s * N;
-        const double *t0 = tab + (size_t)(3 * s) * N;
-        const double kPk = B.k[0] * __ldg(t0 + k) + B.k[1] * __ldg(t0 + N + k) +
-                           B.k[2] * __ldg(t0 + 2 * N + k);
-        const double xi = tmk - kPk;
-        float dv[6];
-        const float v = vlos_grad_mixed(xi, B, Gx.cosvarpi, Gx.P2yr, dv);
-        const float xf = (float)xi;
+        const float kPk = s ? kpf(s, k) : kPf0;
+        const float dk = kPk - kPf0;
+        const float v = fmaf(-dv[5], dk, v0);
+        const float xf = x0 - dk;
         const float fgw = fmaf(fmaf(0.5f * B.fddotf, xf, B.fdotf), xf, B.f0f);
         const float fgwd = fmaf(B.fddotf, xf, B.fdotf);
         const float gk = grow[k];
         float2 W = {0.f, 0.f}, H = {0.f, 0.f};
         if (k >= 1) {
-            const double kPm = B.k[0] * __ldg(t0 + k - 1) + B.k[1] * __ldg(t0 + N + k - 1) +
-                               B.k[2] * __ldg(t0 + 2 * N + k - 1);
-            const float dxi = (float)(step - (kPk - kPm));
+            const float dxi = (sth - (kPk - kpf(s, k - 1))) + stl;     // xi_k - xi_{k-1}
             const float2 R = Rrow[swz(k, lg)];
             const float gs = grow[k - 1] + gk;
             W = make_float2(R.x * dxi, R.y * dxi);
             H = make_float2(R.x * gs, R.y * gs);
         }
         if (k <= N - 2) {
-            const double kPp = B.k[0] * __ldg(t0 + k + 1) + B.k[1] * __ldg(t0 + N + k + 1) +
-                               B.k[2] * __ldg(t0 + 2 * N + k + 1);
-            const float dxi = (float)(step - (kPp - kPk));
+            const float dxi = (sth - (kpf(s, k + 1) - kPk)) + stl;     // xi_{k+1} - xi_k
             const float2 R = Rrow[swz(k + 1, lg)];
             const float gs = gk + grow[k + 1];
             W = make_float2(fmaf(R.x, dxi, W.x), fmaf(R.y, dxi, W.y));
