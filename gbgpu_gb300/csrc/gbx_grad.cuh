@@ -505,7 +505,7 @@ __host__ __device__ constexpr size_t grad_smem_bytes(bool third, int maxS, int m
 }
 
 template <bool THIRD>
-__global__ void __launch_bounds__(kBlock, THIRD ? 1 : 2) grad_kernel(const GradParams GP)
+__global__ void __launch_bounds__(kBlock, 2) grad_kernel(const GradParams GP)
 {
     using V = float2;
     constexpr int kGradAcc = grad_acc<THIRD>();
