@@ -8,6 +8,86 @@
 
 namespace gbx {
 
+// FP64 x * 2^e as an unevaluated float pair hi + lo, built on the integer
+// pipe: hi carries the 24 leading significant bits, lo the next 23 (both
+// truncated), so |x 2^e - (hi + lo)| < 2^-46 |x 2^e|.  Scaled values below
+// FP32's normal range become (signed) zero, values above it infinity; NaN
+// and infinity stay non-finite; lo is dropped below 2^-80.
+__device__ __forceinline__ dfl d2ff_scaled(double x, int e)
+{
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const unsigned sign = hi & 0x80000000u;
+    const int ne = (int)((hi >> 20) & 0x7ffu) - 896 + e;          // FP32 biased exponent
+    const int nc = min(max(ne, 0), 255);
+    const unsigned m23 = __funnelshift_l(lo, hi, 3) & 0x7fffffu;
+    const bool keep = (nc > 0 && nc < 255) || (hi & 0x7ff00000u) == 0x7ff00000u;
+    const float h = __uint_as_float(sign | ((unsigned)nc << 23) | (keep ? m23 : 0u));
+    // the next 23 mantissa bits as an exact FP32 integer, times 2^(ne - 127 - 46)
+    const float r = __uint_as_float(0x4b000000u | ((lo >> 6) & 0x7fffffu)) - 8388608.0f;
+    const float l = r * __uint_as_float((unsigned)min(max(ne - 46, 0), 254) << 23);
+    return {h, __uint_as_float(__float_as_uint(l) | sign)};
+}
+
+// a.h * b.h exactly plus the first-order cross terms: p + e ~ a * b (2^-46)
+__device__ __forceinline__ dfl df_prod(dfl a, dfl b)
+{
+    const float p = a.h * b.h;
+    float e = fmaf(a.h, b.h, -p);
+    e = fmaf(a.h, b.l, e);
+    e = fmaf(a.l, b.h, e);
+    return {p, e};
+}
+
+// a + b for unnormalised pairs (TwoSum of the high parts)
+__device__ __forceinline__ dfl df_sum(dfl a, dfl b)
+{
+    const dfl s = df_two_sum(a.h, b.h);
+    return {s.h, s.l + (a.l + b.l)};
+}
+
+// 1 / s as a float pair: rcp.approx seed, one Newton step on the pair's
+// residual (relative error ~2^-46); 1/inf = 0
+__device__ __forceinline__ dfl df_recip(dfl s)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(s.h));
+    float e = fmaf(-s.h, r, 1.0f);
+    e = fmaf(-s.l, r, e);
+    return {r, r == 0.0f ? 0.0f : r * e};
+}
+
+// conj(d) h w and |h|^2 w of one bin of one channel, accumulated into the
+// float pairs dr, di, hh
+__device__ __forceinline__ void ll_bin(double2 d, double2 hv, double S, int eD, int eS, dfl &dr,
+                                       dfl &di, dfl &hh)
+{
+    const dfl dR = d2ff_scaled(d.x, eD), dI = d2ff_scaled(d.y, eD);
+    const dfl hR = d2ff_scaled(hv.x, eD), hI = d2ff_scaled(hv.y, eD);
+    const dfl w = df_recip(d2ff_scaled(S, eS));
+    const dfl re = df_sum(df_prod(dR, hR), df_prod(dI, hI));
+    const dfl im = df_sum(df_prod(dR, hI), df_neg(df_prod(dI, hR)));
+    const dfl sq = df_sum(df_prod(hR, hR), df_prod(hI, hI));
+    dr = df_add(dr, df_prod(re, w));         // accumulators stay normalised
+    di = df_add(di, df_prod(im, w));
+    hh = df_add(hh, df_prod(sq, w));
+}
+
+__device__ __forceinline__ dfl warp_sum_df(dfl v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const dfl y = {__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o)};
+        v = df_add(v, y);
+    }
+    return v;
+}
+
+// <d|h>, <h|h> per binary (gbgpu_utils.cu:124-210).  The FP64 inputs are
+// split into float pairs with per-binary power-of-two scalings (S 2^eS and
+// d 2^eD of order one, from the PSD at the window centre) and multiplied and
+// summed as float pairs on the FP32 pipe (about 46 significant bits, so each
+// sum is within ~1e-13 of sum |terms| of the FP64 result); one FP64
+// conversion per output.
 __global__ void __launch_bounds__(256) get_ll_kernel(
     double2 *__restrict__ d_h, double2 *__restrict__ h_h, const double2 *__restrict__ A_t,
     const double2 *__restrict__ E_t, const double2 *__restrict__ A_d,
@@ -22,8 +102,14 @@ __global__ void __launch_bounds__(256) get_ll_kernel(
         const int s = start_ind[b];
         const size_t doff = (size_t)(data_index ? data_index[b] : 0) * L;
         const size_t noff = (size_t)(noise_index ? noise_index[b] : 0) * L;
-        double dr = 0.0, di = 0.0, hh = 0.0;
+        int jm = s + M / 2;
+        jm = jm < 0 ? 0 : (jm >= L ? L - 1 : jm);
+        const double Sm = __ldg(A_p + noff + jm);
+        const int lgS = (Sm > 0.0 && isfinite(Sm)) ? ilogb(Sm) : 0;
+        const int eS = -lgS, eD = -(lgS >> 1) - 14;
+        dfl dr = {0.f, 0.f}, di = {0.f, 0.f}, hh = {0.f, 0.f};
         bool out = false;
+#pragma unroll 2
         for (int i = lane; i < M; i += 32) {
             const int j = s + i;
             if (j < 0 || j >= L) {
@@ -33,23 +119,20 @@ __global__ void __launch_bounds__(256) get_ll_kernel(
             const double2 hA = __ldg(A_t + i * tsi + b * tsb);
             const double2 hE = __ldg(E_t + i * tsi + b * tsb);
             const double2 dA = __ldg(A_d + doff + j), dE = __ldg(E_d + doff + j);
-            const double wA = 1.0 / __ldg(A_p + noff + j), wE = 1.0 / __ldg(E_p + noff + j);
-            // conj(d) h / S and conj(h) h / S  (gbgpu_utils.cu:172-178)
-            dr += (dA.x * hA.x + dA.y * hA.y) * wA + (dE.x * hE.x + dE.y * hE.y) * wE;
-            di += (dA.x * hA.y - dA.y * hA.x) * wA + (dE.x * hE.y - dE.y * hE.x) * wE;
-            hh += (hA.x * hA.x + hA.y * hA.y) * wA + (hE.x * hE.x + hE.y * hE.y) * wE;
+            const double SA = __ldg(A_p + noff + j), SE = __ldg(E_p + noff + j);
+            ll_bin(dA, hA, SA, eD, eS, dr, di, hh);
+            ll_bin(dE, hE, SE, eD, eS, dr, di, hh);
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            dr += __shfl_xor_sync(0xffffffffu, dr, o);
-            di += __shfl_xor_sync(0xffffffffu, di, o);
-            hh += __shfl_xor_sync(0xffffffffu, hh, o);
-        }
+        dr = warp_sum_df(dr);
+        di = warp_sum_df(di);
+        hh = warp_sum_df(hh);
         if (__any_sync(0xffffffffu, out) && lane == 0) flag(status, GBX_FLAG_WINDOW);
         if (lane == 0) {
-            const double s4 = 4. * df;
-            d_h[b] = make_double2(s4 * dr, s4 * di);
-            h_h[b] = make_double2(s4 * hh, 0.0);
+            // undo the scalings: terms carry 2^(2 eD - eS)
+            const double s4 = 4. * df * ldexp(1.0, eS - 2 * eD);
+            d_h[b] = make_double2(s4 * ((double)dr.h + (double)dr.l),
+                                  s4 * ((double)di.h + (double)di.l));
+            h_h[b] = make_double2(s4 * ((double)hh.h + (double)hh.l), 0.0);
         }
     }
 }
