@@ -1,8 +1,8 @@
 // Drop-in replacements for the reference's two native kernels
 // (gbgpu/cutils/gbgpu_utils.cu): batched <d|h>, <h|h> over point-major
 // templates, and the scatter-add of templates into global buffers.
-// One warp per binary: lanes walk the N-point window, so the data and PSD
-// windows (contiguous in memory) are read with coalesced 16-/8-byte loads.
+// get_ll: one warp per two binaries (lanes interleaved by binary); fill: one
+// warp per binary, lanes along the window.
 #include "gbx_common.cuh"
 #include "gbx_internal.h"
 
@@ -72,22 +72,26 @@ __device__ __forceinline__ void ll_bin(double2 d, double2 hv, double S, int eD, 
     hh = df_add(hh, df_prod(sq, w));
 }
 
-__device__ __forceinline__ dfl warp_sum_df(dfl v)
+// sum over the 16 lanes of the same parity (the lanes of one binary)
+__device__ __forceinline__ dfl pair_sum_df(dfl v)
 {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
+    for (int o = 16; o > 1; o >>= 1) {
         const dfl y = {__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o)};
         v = df_add(v, y);
     }
     return v;
 }
 
-// <d|h>, <h|h> per binary (gbgpu_utils.cu:124-210).  The FP64 inputs are
-// split into float pairs with per-binary power-of-two scalings (S 2^eS and
-// d 2^eD of order one, from the PSD at the window centre) and multiplied and
-// summed as float pairs on the FP32 pipe (about 46 significant bits, so each
-// sum is within ~1e-13 of sum |terms| of the FP64 result); one FP64
-// conversion per output.
+// <d|h>, <h|h> per binary (gbgpu_utils.cu:124-210).  A warp takes two
+// binaries: lane 2q + t walks points q, q + 16, ... of binary b + t, so a
+// warp's template loads cover whole 32-byte sectors in the point-major layout
+// (the two binaries' elements are adjacent) and its data and PSD loads are
+// two contiguous runs.  The FP64 inputs are split into float pairs with
+// per-binary power-of-two scalings (S 2^eS and d 2^eD of order one, from the
+// PSD at the window centre) and multiplied and summed as float pairs on the
+// FP32 pipe (about 46 significant bits: each sum is within ~1e-13 of
+// sum |terms| of the FP64 result); one FP64 conversion per output.
 __global__ void __launch_bounds__(256) get_ll_kernel(
     double2 *__restrict__ d_h, double2 *__restrict__ h_h, const double2 *__restrict__ A_t,
     const double2 *__restrict__ E_t, const double2 *__restrict__ A_d,
@@ -96,21 +100,24 @@ __global__ void __launch_bounds__(256) get_ll_kernel(
     int num_bin, const int *__restrict__ data_index, const int *__restrict__ noise_index,
     int L, long long tsi, long long tsb, int *status)
 {
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, t = lane & 1, q = lane >> 1;
     const int warps = (gridDim.x * blockDim.x) >> 5;
-    for (int b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < num_bin; b += warps) {
-        const int s = start_ind[b];
-        const size_t doff = (size_t)(data_index ? data_index[b] : 0) * L;
-        const size_t noff = (size_t)(noise_index ? noise_index[b] : 0) * L;
+    for (int b0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 2; b0 < num_bin; b0 += 2 * warps) {
+        const int b = b0 + t;
+        const bool has = b < num_bin;                 // odd num_bin: the last warp's lane t = 1 idles
+        const int s = has ? start_ind[b] : 0;
+        const size_t doff = (size_t)(has && data_index ? data_index[b] : 0) * L;
+        const size_t noff = (size_t)(has && noise_index ? noise_index[b] : 0) * L;
         int jm = s + M / 2;
         jm = jm < 0 ? 0 : (jm >= L ? L - 1 : jm);
-        const double Sm = __ldg(A_p + noff + jm);
+        const double Sm = L > 0 ? __ldg(A_p + noff + jm) : 0.0;
         const int lgS = (Sm > 0.0 && isfinite(Sm)) ? ilogb(Sm) : 0;
         const int eS = -lgS, eD = -(lgS >> 1) - 14;
         dfl dr = {0.f, 0.f}, di = {0.f, 0.f}, hh = {0.f, 0.f};
         bool out = false;
-#pragma unroll 2
-        for (int i = lane; i < M; i += 32) {
+        const int Mh = has ? M : 0;
+#pragma unroll 4
+        for (int i = q; i < Mh; i += 16) {
             const int j = s + i;
             if (j < 0 || j >= L) {
                 out = true;
@@ -123,11 +130,11 @@ __global__ void __launch_bounds__(256) get_ll_kernel(
             ll_bin(dA, hA, SA, eD, eS, dr, di, hh);
             ll_bin(dE, hE, SE, eD, eS, dr, di, hh);
         }
-        dr = warp_sum_df(dr);
-        di = warp_sum_df(di);
-        hh = warp_sum_df(hh);
+        dr = pair_sum_df(dr);
+        di = pair_sum_df(di);
+        hh = pair_sum_df(hh);
         if (__any_sync(0xffffffffu, out) && lane == 0) flag(status, GBX_FLAG_WINDOW);
-        if (lane == 0) {
+        if (q == 0 && has) {
             // undo the scalings: terms carry 2^(2 eD - eS)
             const double s4 = 4. * df * ldexp(1.0, eS - 2 * eD);
             d_h[b] = make_double2(s4 * ((double)dr.h + (double)dr.l),
@@ -259,7 +266,7 @@ extern "C" int gbx_get_ll_ex(void *d_h, void *h_h, const void *A_template,
         return set_error(GBX_ERR_ARG, "NULL pointer");
     int rc = ensure_init((cudaStream_t)stream);
     if (rc) return rc;
-    get_ll_kernel<<<grid_for(num_bin), 256, 0, (cudaStream_t)stream>>>(
+    get_ll_kernel<<<grid_for((num_bin + 1) / 2), 256, 0, (cudaStream_t)stream>>>(
         (double2 *)d_h, (double2 *)h_h, (const double2 *)A_template, (const double2 *)E_template,
         (const double2 *)A_data, (const double2 *)E_data, A_psd, E_psd, df, start_ind, M, num_bin,
         data_index, noise_index, data_length, t_stride_i, t_stride_b, status);

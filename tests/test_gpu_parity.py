@@ -103,6 +103,69 @@ def test_backend_get_ll_dropin_matches_oracle(gbgpu):
     np.testing.assert_allclose(h_h.cpu().numpy().real, ref_hh.real, rtol=1e-12)
 
 
+def test_backend_get_ll_edges_odd_batch(gbgpu):
+    """Drop-in get_ll on windows that cross both ends of the data (those bins
+    count as zero and raise GBX_FLAG_WINDOW), an odd batch, two data and noise
+    rows, a PSD bin at infinity (contributes zero, as 1/inf in FP64) and an
+    all-zero template; then data_length = 0.  Reference sums in NumPy FP64;
+    bound 1e-12 of sum |terms| per output."""
+    from gbgpu_gb300 import _native as nat
+    rng = np.random.default_rng(7)
+    L, M, B = 600, 128, 5
+    s = np.array([-40, 10, 300, 520, 472], dtype=np.int32)
+    di = np.array([0, 1, 1, 0, 1], dtype=np.int32)
+    ni = np.array([1, 0, 1, 1, 0], dtype=np.int32)
+    cplx = lambda *shape: rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    A_d, E_d = 1e-20 * cplx(2, L), 1e-20 * cplx(2, L)
+    A_p = 1e-40 * (1 + rng.random((2, L)))
+    E_p = 2e-40 * (1 + rng.random((2, L)))
+    A_p[1, 350] = np.inf
+    A_t, E_t = 1e-21 * cplx(B, M), 1e-21 * cplx(B, M)
+    A_t[2] = E_t[2] = 0.0
+    df = 1.0 / 3.15e7
+    ref_dh = np.zeros(B, complex)
+    ref_hh = np.zeros(B)
+    bound_dh = np.zeros(B)
+    bound_hh = np.zeros(B)
+    for b in range(B):
+        j = s[b] + np.arange(M)
+        ok = (j >= 0) & (j < L)
+        jj = j[ok]
+        for d, p, t in ((A_d, A_p, A_t), (E_d, E_p, E_t)):
+            dh = np.conj(d[di[b], jj]) * t[b, ok] / p[ni[b], jj]
+            hh = np.abs(t[b, ok]) ** 2 / p[ni[b], jj]
+            ref_dh[b] += 4 * df * dh.sum()
+            ref_hh[b] += 4 * df * hh.sum()
+            bound_dh[b] += 4 * df * np.abs(dh).sum()
+            bound_hh[b] += 4 * df * hh.sum()
+    gb = gbgpu()
+    d_h = torch.zeros(B, dtype=torch.complex128, device="cuda")
+    h_h = torch.zeros(B, dtype=torch.complex128, device="cuda")
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    gb.backend.get_ll(d_h, h_h, dev(O.point_major(A_t)), dev(O.point_major(E_t)),
+                      dev(A_d.ravel()), dev(E_d.ravel()), dev(A_p.ravel()), dev(E_p.ravel()),
+                      df, dev(s), M, B, dev(di), dev(ni), L, status=st)
+    got_dh, got_hh = d_h.cpu().numpy(), h_h.cpu().numpy()
+    assert np.all(np.abs(got_dh - ref_dh) <= 1e-12 * bound_dh + 1e-300)
+    assert np.all(np.abs(got_hh.real - ref_hh) <= 1e-12 * bound_hh + 1e-300)
+    assert got_dh[2] == 0 and got_hh[2] == 0
+    assert int(st.item()) & nat.GBX_FLAG_WINDOW
+    # windows inside the data raise no flag
+    st.zero_()
+    sel = [1, 2, 4]
+    gb.backend.get_ll(d_h[:3], h_h[:3], dev(O.point_major(A_t[sel])), dev(O.point_major(E_t[sel])),
+                      dev(A_d.ravel()), dev(E_d.ravel()), dev(A_p.ravel()), dev(E_p.ravel()),
+                      df, dev(s[sel]), M, 3, dev(di[sel]), dev(ni[sel]), L, status=st)
+    assert int(st.item()) == 0
+    np.testing.assert_allclose(d_h[:3].cpu().numpy(), got_dh[sel], rtol=0, atol=0)
+    # no data at all: every bin is outside, sums are zero
+    gb.backend.get_ll(d_h, h_h, dev(O.point_major(A_t)), dev(O.point_major(E_t)),
+                      dev(A_d.ravel()), dev(E_d.ravel()), dev(A_p.ravel()), dev(E_p.ravel()),
+                      df, dev(s), M, B, dev(di), dev(ni), 0, status=st)
+    assert not torch.any(d_h != 0) and not torch.any(h_h != 0)
+    assert int(st.item()) & nat.GBX_FLAG_WINDOW
+
+
 def test_fill_global_template_matches_reference(gbgpu):
     g = load_golden("fill_basic")
     gb = gbgpu()
