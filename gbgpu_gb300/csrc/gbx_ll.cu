@@ -8,24 +8,25 @@
 
 namespace gbx {
 
-// FP64 x * 2^e as an unevaluated float pair hi + lo, built on the integer
-// pipe: hi carries the 24 leading significant bits, lo the next 23 (both
-// truncated), so |x 2^e - (hi + lo)| < 2^-46 |x 2^e|.  Scaled values below
-// FP32's normal range become (signed) zero, values above it infinity; NaN
-// and infinity stay non-finite; lo is dropped below 2^-80.
+// FP64 x * 2^e as an unevaluated float pair hi + lo, built mostly on the
+// integer pipe: hi carries the 24 leading significant bits, lo the next 23
+// (both truncated), so |x 2^e - (hi + lo)| < 2^-46 |x 2^e|.  (hi:lo) << 3
+// holds the 23 leading mantissa bits at [22:0] and the exponent's low 9 bits
+// at [31:23]; subtracting (896 - e) << 23 leaves the FP32 biased exponent
+// there when it is in range.  Scaled values below FP32's normal range become
+// signed zero, values above it (and infinities, NaN) infinity; lo is the
+// next 23 bits as an exact FP32 integer times hi's power of two times 2^-46
+// (so it underflows to zero for |hi| < 2^-80).
 __device__ __forceinline__ dfl d2ff_scaled(double x, int e)
 {
     const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
-    const unsigned sign = hi & 0x80000000u;
     const int ne = (int)((hi >> 20) & 0x7ffu) - 896 + e;          // FP32 biased exponent
-    const int nc = min(max(ne, 0), 255);
-    const unsigned m23 = __funnelshift_l(lo, hi, 3) & 0x7fffffu;
-    const bool keep = (nc > 0 && nc < 255) || (hi & 0x7ff00000u) == 0x7ff00000u;
-    const float h = __uint_as_float(sign | ((unsigned)nc << 23) | (keep ? m23 : 0u));
-    // the next 23 mantissa bits as an exact FP32 integer, times 2^(ne - 127 - 46)
+    unsigned mag = __funnelshift_l(lo, hi, 3) - ((unsigned)(896 - e) << 23);
+    mag = ((unsigned)(ne - 1) < 254u) ? mag : (ne >= 255 ? 0x7f800000u : 0u);
+    const unsigned hb = (hi & 0x80000000u) | (mag & 0x7fffffffu);
     const float r = __uint_as_float(0x4b000000u | ((lo >> 6) & 0x7fffffu)) - 8388608.0f;
-    const float l = r * __uint_as_float((unsigned)min(max(ne - 46, 0), 254) << 23);
-    return {h, __uint_as_float(__float_as_uint(l) | sign)};
+    const float l = r * (__uint_as_float(hb & 0xff800000u) * 0x1p-46f);
+    return {__uint_as_float(hb), l};
 }
 
 // a.h * b.h exactly plus the first-order cross terms: p + e ~ a * b (2^-46)
