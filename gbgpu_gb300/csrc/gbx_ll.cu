@@ -111,13 +111,16 @@ __global__ void __launch_bounds__(256) get_ll_kernel(
         const size_t noff = (size_t)(has && noise_index ? noise_index[b] : 0) * L;
         int jm = s + M / 2;
         jm = jm < 0 ? 0 : (jm >= L ? L - 1 : jm);
-        const double Sm = L > 0 ? __ldg(A_p + noff + jm) : 0.0;
-        const int lgS = (Sm > 0.0 && isfinite(Sm)) ? ilogb(Sm) : 0;
+        // exponent of the PSD at the window centre, on the integer pipe
+        // (0 for zero, negative, subnormal or non-finite values)
+        const int hS = L > 0 ? __double2hiint(__ldg(A_p + noff + jm)) : 0;
+        const int exS = (hS >> 20) & 0x7ff;
+        const int lgS = (hS > 0 && exS > 0 && exS < 0x7ff) ? exS - 1023 : 0;
         const int eS = -lgS, eD = -(lgS >> 1) - 14;
         dfl dr = {0.f, 0.f}, di = {0.f, 0.f}, hh = {0.f, 0.f};
         bool out = false;
         const int Mh = has ? M : 0;
-#pragma unroll 4
+#pragma unroll 2
         for (int i = q; i < Mh; i += 16) {
             const int j = s + i;
             if (j < 0 || j >= L) {
@@ -137,7 +140,7 @@ __global__ void __launch_bounds__(256) get_ll_kernel(
         if (__any_sync(0xffffffffu, out) && lane == 0) flag(status, GBX_FLAG_WINDOW);
         if (q == 0 && has) {
             // undo the scalings: terms carry 2^(2 eD - eS)
-            const double s4 = 4. * df * ldexp(1.0, eS - 2 * eD);
+            const double s4 = 4. * df * __hiloint2double((eS - 2 * eD + 1023) << 20, 0);
             d_h[b] = make_double2(s4 * ((double)dr.h + (double)dr.l),
                                   s4 * ((double)di.h + (double)di.l));
             h_h[b] = make_double2(s4 * ((double)hh.h + (double)hh.l), 0.0);
