@@ -185,8 +185,9 @@ def cpu_baseline(p, Ns, dA, dE, S, workers, per_class=CPU_SAMPLE, pool=None):
 
 
 # ------------------------------------------------------------------ GPU side
-def make_data(gb, p, Ns, seed):
-    """Injected sum of all binaries + Gaussian noise from the analytic A/E PSD."""
+def make_noise(seed):
+    """Seeded Gaussian A/E noise from the analytic PSD on the 4-yr, 5-s grid
+    (rfft bins 0 ... L-1; bin 0 has infinite PSD and no noise)."""
     import torch
     from gbgpu_gb300.sensitivity import A1TDISens
     T = int(T_OBS / DT) * DT
@@ -204,6 +205,15 @@ def make_data(gb, p, Ns, seed):
         re = torch.randn(L, device="cuda", dtype=torch.float64, generator=g)
         im = torch.randn(L, device="cuda", dtype=torch.float64, generator=g)
         data.append(torch.complex(re * sig, im * sig))
+    return data, Sd, S
+
+
+def make_data(gb, p, Ns, seed):
+    """Injected sum of all binaries + Gaussian noise from the analytic A/E PSD."""
+    import torch
+    T = int(T_OBS / DT) * DT
+    L = int(int(T_OBS / DT) / 2) + 1
+    data, Sd, S = make_noise(seed)
     # the sources, one N class at a time (the FP64 fused fill kernel)
     tmpl = torch.zeros((1, 2, L), dtype=torch.complex128, device="cuda")
     acc = torch.zeros_like(tmpl)
@@ -325,19 +335,38 @@ def time_ll_variants(gb, prm, data, Sd, N, tdi2, steps, tag):
     return out, shapes
 
 
+def n256_params(seed, B=50_000):
+    """(9, B) parameters of the N = 256 batch: f0 uniform on [1e-3, 5e-3] Hz,
+    the other parameters as the main batch."""
+    rng = np.random.default_rng(seed + 3)
+    f0 = rng.uniform(1e-3, 5e-3, B)
+    fdot = 10 ** rng.uniform(-18, -15, B)
+    return np.array([10 ** rng.uniform(-23, -21, B), f0, fdot, 11.0 / 3.0 * fdot ** 2 / f0,
+                     rng.uniform(0, 2 * np.pi, B), np.arccos(rng.uniform(-1, 1, B)),
+                     rng.uniform(0, np.pi, B), rng.uniform(0, 2 * np.pi, B),
+                     np.arcsin(rng.uniform(-1, 1, B))])
+
+
+def dropin_section(args):
+    """The drop-in kernels alone (``--section dropin``): the N = 256 batch's
+    point-major templates against seeded noise on the 4-yr grid, no injected
+    sources; one JSON line.  A small, quick case for profiling the two entry
+    points (about 1 GB on the device)."""
+    import torch
+    from gbgpu_gb300 import GBGPU
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    data, Sd, _ = make_noise(args.seed)
+    out = dropin_kernels(GBGPU(), n256_params(args.seed), data, Sd, max(1, args.steps))
+    out["section"] = "dropin"
+    return out
+
+
 def n256_tdi2_bench(gb, data, Sd, seed, steps):
     """50,000 binaries, N = 256, TDI-2, f0 uniform on [1e-3, 5e-3] Hz and the
     other parameters as the main batch, on the same 4-yr data grid.  Times the FP64 and
     mixed fused likelihood and the likelihood + gradient kernel."""
     import torch
-    rng = np.random.default_rng(seed + 3)
-    B = 50_000
-    f0 = rng.uniform(1e-3, 5e-3, B)
-    fdot = 10 ** rng.uniform(-18, -15, B)
-    p = np.array([10 ** rng.uniform(-23, -21, B), f0, fdot, 11.0 / 3.0 * fdot ** 2 / f0,
-                  rng.uniform(0, 2 * np.pi, B), np.arccos(rng.uniform(-1, 1, B)),
-                  rng.uniform(0, np.pi, B), rng.uniform(0, 2 * np.pi, B),
-                  np.arcsin(rng.uniform(-1, 1, B))])
+    p = n256_params(seed)
     prm = torch.as_tensor(p, device="cuda").contiguous()
     Tu = int(T_OBS / DT) * DT
     out = {"workload": "50,000 binaries, N=256, tdi2=True, T=4x31557600 s",
@@ -911,7 +940,12 @@ def main():
     ap.add_argument("--no-mcmc-bench", action="store_true")
     ap.add_argument("--no-autotune", action="store_true",
                     help="use the kernels' default launch shape instead of the autotuner's")
+    ap.add_argument("--section", choices=["dropin"], default=None,
+                    help="run one sub-benchmark alone (not the bench line)")
     args = ap.parse_args()
+    if args.section == "dropin":
+        print(json.dumps(dropin_section(args)), flush=True)
+        return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
