@@ -379,6 +379,7 @@ def n256_tdi2_bench(gb, data, Sd, seed, steps):
     out["dropin"] = dropin_kernels(gb, p, data, Sd, steps)
     out["fisher"] = fisher_bench(gb, p, Tu)
     out["hmc"] = hmc_bench(gb, p, data, Sd, seed)
+    out["ensemble"] = ensemble_bench(gb, p, data, Sd, seed)
     return out
 
 
@@ -537,7 +538,49 @@ def hmc_bench(gb, p, data, Sd, seed, B=4096, transitions=100, n_leapfrog=10, ste
             "acceptance": float(smp.accepted.sum().item()) / (B * transitions),
             "note": "whitened coordinates (Fisher-diagonal sigmas); one fused likelihood + "
                     "gradient launch per leapfrog step, all captured in one CUDA graph"}
-    return out
+
+
+def ensemble_bench(gb, p, data, Sd, seed, B=512, W=64, steps=50):
+    """Stretch-move ensembles (affine-invariant, Goodman & Weare): the 512
+    loudest of the 50k N = 256 binaries, injected into a copy of the data, 64
+    walkers each started in a 0.1-sigma ball of their Fisher diagonals; 50
+    steps (100 fused likelihood launches of 16,384 points) in one CUDA graph."""
+    import torch
+    from gbgpu_gb300.mcmc import StretchSampler, stretch_draws
+    sel = np.argsort(-p[0])[:B]
+    q = np.ascontiguousarray(p[:, sel])
+    dA, dE = data[0].clone(), data[1].clone()
+    gb.add_to_templates(torch.as_tensor(q, device="cuda"),
+                        torch.zeros(B, dtype=torch.int32, device="cuda"),
+                        (dA[None], dE[None]), N=256, T=T_OBS, dt=DT, tdi2=True, precision="fp64")
+    F = gb.fisher_matrices(q, N=256, T=T_OBS, dt=DT, tdi2=True, inds=FREE8, return_gpu=True)
+    sig = (1.0 / torch.sqrt(torch.diagonal(F, dim1=1, dim2=2))).T
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed + 55)
+    x = torch.as_tensor(q, device="cuda")[:, :, None].repeat(1, 1, W)
+    x[list(FREE8)] += 0.1 * sig[:, :, None] * torch.randn((len(FREE8), B, W), generator=g,
+                                                          device="cuda", dtype=torch.float64)
+    d_d = gb.d_d
+    gb.d_d = 0.0
+    smp = StretchSampler(gb, x, [dA, dE], [Sd, Sd], N=256, T=T_OBS, dt=DT, tdi2=True, free=FREE8)
+    gb.d_d = d_d
+    u, j, lu = stretch_draws(steps, B, W // 2, g, "cuda")
+    smp.capture(u, j, lu)
+    smp.accepted.zero_()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("n256_ensemble")
+    e0.record()
+    smp.replay()
+    e1.record()
+    torch.cuda.nvtx.range_pop()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    return {"binaries": B, "walkers": W, "steps": steps, "graph_ms": ms,
+            "walker_steps_per_s": B * W * steps / (ms / 1e3),
+            "acceptance": float(smp.accepted.sum().item()) / (B * W * steps),
+            "note": "stretch move, two half-ensemble updates per step, each one fused "
+                    "likelihood launch over all binaries; all steps captured in one CUDA graph"}
 
 
 def fill_bench(gb, seed, B=1_000_000, G=256, N=256, steps=3):

@@ -1,4 +1,8 @@
-"""Ensemble swap sampler on the GPU: the caller of the swap likelihood.
+"""Samplers on the GPU that drive the fused kernels: an ensemble swap sampler
+(the caller of the swap likelihood), an affine-invariant stretch-move
+ensemble (the fused likelihood) and HMC (the fused likelihood + gradient).
+
+Swap sampler:
 
 Each of W walkers holds K sources and a residual r_w = d - sum_k h(theta_wk)
 restricted to a frequency band.  One proposal step replaces, in every walker,
@@ -241,6 +245,172 @@ class HMCSampler:
             for i in range(moms.shape[0]):
                 self.transition(moms[i], log_us[i])
         self._graph_keep = (self.args, self.la)
+        return self.graph
+
+    def replay(self):
+        self.graph.replay()
+
+
+# ---------------------------------------------------------------------------
+# affine-invariant ensemble (stretch move)
+# ---------------------------------------------------------------------------
+
+def stretch_z(u, a=2.0):
+    """Stretch factors z with density g(z) proportional to 1/sqrt(z) on
+    [1/a, a], from uniforms u by the inverse CDF: z = ((a - 1) u + 1)^2 / a
+    (Goodman & Weare 2010, eq. 9)."""
+    return ((a - 1.0) * u + 1.0) ** 2 / a
+
+
+def stretch_draws(steps, B, Wh, gen, device, dtype=torch.float64):
+    """Random numbers for ``steps`` stretch-move steps of B ensembles of 2 Wh
+    walkers: uniforms for z, partner indices into the other half, and log
+    uniforms for the accept test, each (steps, 2, B, Wh)."""
+    u = torch.rand((steps, 2, B, Wh), generator=gen, device=device, dtype=dtype)
+    j = torch.randint(0, Wh, (steps, 2, B, Wh), generator=gen, device=device)
+    lu = torch.rand((steps, 2, B, Wh), generator=gen, device=device, dtype=dtype)
+    return u, j, torch.log(lu.clamp_min(math.ldexp(1.0, -60)))
+
+
+def stretch_update(x, logL, accepted, h, u, j, log_u, loglike, free, a=2.0, bounds=None):
+    """Update half ``h`` (0 or 1) of every ensemble in place by one stretch
+    move (Goodman & Weare 2010; the move of emcee and Eryn).
+
+    ``x`` (npar, B, W) walkers of B independent ensembles, W even; ``logL``
+    (B, W) their log-likelihoods; ``accepted`` (B, W) counters.  Walker k of
+    the half moves to Y = C_j + z (X_k - C_j) in the ``free`` coordinates,
+    with C_j the partner ``j`` (B, W/2) of the other half and z = stretch_z(u),
+    and is accepted when log_u < (n_free - 1) log z + logL(Y) - logL(X) and Y
+    lies inside ``bounds`` ((n_free, 2) lower/upper, optional).  ``loglike``
+    maps (npar, B, W/2) points to (B, W/2) log-likelihoods.  Returns the
+    accept mask (B, W/2)."""
+    npar, B, W = x.shape
+    Wh = W // 2
+    sl = slice(h * Wh, (h + 1) * Wh)
+    X = x[:, :, sl]
+    C = x[:, :, Wh:] if h == 0 else x[:, :, :Wh]
+    z = stretch_z(u, a)
+    Cj = torch.gather(C, 2, j[None].expand(npar, B, Wh))
+    Y = X.clone()
+    Y[free] = Cj[free] + z[None] * (X[free] - Cj[free])
+    ll = loglike(Y)
+    cur = logL[:, sl]
+    lp = (len(free) - 1) * torch.log(z) + ll - cur
+    if bounds is not None:
+        yf = Y[free]
+        ok = ((yf >= bounds[:, 0, None, None]) & (yf <= bounds[:, 1, None, None])).all(0)
+        lp = torch.where(ok, lp, torch.full_like(lp, -math.inf))
+    acc = (log_u < lp) & torch.isfinite(ll)
+    X.copy_(torch.where(acc[None], Y, X))
+    cur.copy_(torch.where(acc, ll, cur))
+    accepted[:, sl] += acc
+    return acc
+
+
+class StretchSampler:
+    """Affine-invariant ensemble sampler (stretch move) over B independent
+    binaries with W walkers each, driven by the fused likelihood kernel.
+
+    A step updates the two halves of every ensemble in turn; each half-update
+    evaluates the B W/2 proposed points in one fused waveform + likelihood
+    launch (the plan is bound once to a fixed proposal buffer), so the random
+    numbers of any number of steps (``stretch_draws``) are prepared on the
+    device and the steps are captured and replayed as one CUDA graph.  The
+    target is the likelihood (flat prior inside optional ``bounds`` on the
+    free parameters); fddot is held fixed by default.  The reference's
+    sampler-facing caller is an ensemble sampler of this kind (Eryn, its
+    optional ``sampling`` dependency); the move itself follows Goodman &
+    Weare (2010).
+    """
+
+    FREE = (0, 1, 2, 4, 5, 6, 7, 8)
+
+    def __init__(self, gb, params, data, psd, N, T, dt, a=2.0, start_freq_ind=0, tdi2=False,
+                 free=FREE, bounds=None, precision="mixed"):
+        import ctypes
+        from . import _native as nat
+        self._nat, self._ctypes = nat, ctypes
+        self.gb = gb
+        dev = gb.device
+        x = params.to(device=dev, dtype=torch.float64)
+        if x.ndim != 3:
+            raise ValueError("params must be (nparams, B, W)")
+        npar, B, W = x.shape
+        if npar != gb.NPARAMS:
+            raise ValueError(f"params must be ({gb.NPARAMS}, B, W)")
+        if W < 4 or W % 2:
+            raise ValueError("the number of walkers per ensemble must be even and >= 4")
+        self.x = x.clone().contiguous()
+        self.B, self.W, self.Wh = B, W, W // 2
+        self.a = float(a)
+        self.free = torch.as_tensor(list(free), device=dev, dtype=torch.long)
+        self.bounds = None if bounds is None else \
+            torch.as_tensor(bounds, device=dev, dtype=torch.float64).reshape(len(free), 2)
+        n = B * self.Wh
+        self.prop = torch.empty((npar, n), dtype=torch.float64, device=dev)
+        Tu = int(T / dt) * dt
+        dd, pp, L, di, ni = gb._prepare_data(data, psd, None, None, n)
+        self.la = gb._ll_args(dd, pp, L, di, ni, Tu)
+        self.d_h = torch.zeros(n, dtype=torch.complex128, device=dev)
+        self.h_h = torch.zeros(n, dtype=torch.complex128, device=dev)
+        self.d_d = 0.0 if gb.d_d is None else float(gb.d_d)
+        self._lib = nat.lib()
+        self.prop.copy_(self.x[:, :, :self.Wh].reshape(npar, n))
+
+        def bind(tile, bps):
+            plan = gb._plan(N, Tu, precision, tdi2, npar, tile, bps)
+            self.args = plan.args(self.prop, start_freq_ind, gb._status)
+            self._plan_keep = plan
+
+        def run(tile, bps):
+            bind(tile, bps)
+            self._evaluate()
+        self.args = None
+        bind(*gb._launch_shape("ll", N, n, precision, tdi2, npar, run))
+        self.logL = torch.empty((B, W), dtype=torch.float64, device=dev)
+        for h in (0, 1):
+            self.logL[:, h * self.Wh:(h + 1) * self.Wh] = self._loglike(
+                self.x[:, :, h * self.Wh:(h + 1) * self.Wh])
+        self.accepted = torch.zeros((B, W), dtype=torch.int64, device=dev)
+        self.graph = None
+
+    def _evaluate(self):
+        nat, ct = self._nat, self._ctypes
+        rc = self._lib.gbx_waveform_ll(ct.byref(self.args), ct.byref(self.la), nat.ptr(self.d_h),
+                                       nat.ptr(self.h_h), nat.stream_handle())
+        nat.check(rc, "gbx_waveform_ll")
+
+    def _loglike(self, Y):
+        """log-likelihoods (B, W/2) of the points Y (npar, B, W/2)."""
+        self.prop.copy_(Y.reshape(self.prop.shape))
+        self._evaluate()
+        like = -0.5 * (self.d_d + self.h_h.real - 2.0 * self.d_h.real)
+        return like.reshape(self.B, self.Wh)
+
+    def step(self, u, j, log_u):
+        """One step: both halves of every ensemble, ``u``/``j``/``log_u`` of
+        shape (2, B, W/2) as made by ``stretch_draws``."""
+        for h in (0, 1):
+            stretch_update(self.x, self.logL, self.accepted, h, u[h], j[h], log_u[h],
+                           self._loglike, self.free, self.a, self.bounds)
+
+    def capture(self, us, js, log_us):
+        """Capture len(us) steps (arrays (S, 2, B, W/2)) as one CUDA graph."""
+        self.us, self.js, self.log_us = us, js, log_us
+        snap = (self.x.clone(), self.logL.clone(), self.accepted.clone())
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):                 # warm-up outside capture
+            self.step(us[0], js[0], log_us[0])
+        torch.cuda.current_stream().wait_stream(s)
+        torch.cuda.synchronize()
+        for dst, src in zip((self.x, self.logL, self.accepted), snap):
+            dst.copy_(src)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            for i in range(us.shape[0]):
+                self.step(us[i], js[i], log_us[i])
+        self._graph_keep = (self.args, self.la, self._plan_keep)
         return self.graph
 
     def replay(self):
