@@ -275,6 +275,7 @@ def time_ll_variants(gb, prm, data, Sd, N, tdi2, steps, tag):
     import ctypes
     import torch
     from gbgpu_gb300 import _native as nat
+    from gbgpu_gb300.utility import flops_per_binary
     Tu = int(T_OBS / DT) * DT
     NP, B = prm.shape
     L = data[0].shape[0]
@@ -332,6 +333,9 @@ def time_ll_variants(gb, prm, data, Sd, N, tdi2, steps, tag):
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / steps
         out[f"{name}_binaries_per_s"] = B / (ms / 1e3)
+        if name != "grad":
+            out[f"{name}_tflops"] = float(flops_per_binary(N, tdi2, NP == 14, True)) * B / \
+                (ms / 1e3) / 1e12
     return out, shapes
 
 
@@ -888,6 +892,7 @@ def run_gpu(args, rank, world):
                              "in L2).  The kernel is instruction-issue bound on the FP32/ALU "
                              "pipes (issue_active_frac from ncu), so the HBM fraction is low "
                              "by construction"},
+        "compute": compute_roofline(Ns, t_max, clk),
         "e2e": {"value": world * B / e2e_max, "unit": "binaries/s",
                 "h2d_bytes_per_step": int(p.nbytes), "d2h_bytes_per_step": int(B * 8)},
         "clocks": clk.summary(),
@@ -905,6 +910,24 @@ def hbm_peak():
             return float(json.load(f)["hbm_gbs"]), "of measured (MEASURED_PEAKS.json hbm_gbs)"
     except (OSError, KeyError, ValueError):
         return 6800.0, "of fallback (6.8 TB/s)"
+
+
+def compute_roofline(Ns, ms, clk):
+    """The step's algorithmic FLOPs (``flops_per_binary``: waveform + likelihood,
+    the restated formula, not the instructions the kernel issues) over its
+    time, against the nominal FP32 rate of the device (SMs x 128 lanes x 2 x
+    the maximum SM clock sampled)."""
+    import torch
+    from gbgpu_gb300.utility import flops_per_binary
+    F = float(np.sum(flops_per_binary(Ns, likelihood=True)))
+    props = torch.cuda.get_device_properties(torch.cuda.current_device())
+    mhz = (clk.summary() or {}).get("sm_max_mhz") or 2070.0
+    peak = props.multi_processor_count * 128 * 2 * mhz * 1e6 / 1e12
+    achieved = F / (ms / 1e3) / 1e12
+    return {"flops_per_step": F, "achieved": achieved, "unit": "TFLOP/s", "peak": peak,
+            "frac": achieved / peak,
+            "note": "algorithmic FLOPs (gbgpu_gb300.utility.flops_per_binary) per timed step; "
+                    "peak = nominal FP32 (SMs x 128 x 2 x max SM clock), not measured"}
 
 
 def profiled(key):

@@ -108,6 +108,33 @@ def get_N(amp, f0, Tobs, oversample=1):
     return (N * oversample).astype(int)
 
 
+def flops_per_binary(N, tdi2=False, third_body=False, likelihood=False):
+    """Algorithmic floating-point operations of one binary: the single count
+    every FLOP figure of this package is quoted with.
+
+    Per time sample of the slow part (gbgpu.py:348-540): k.P 9, delayed times
+    3, instantaneous frequencies 12, carrier phase 24, six link transfer
+    functions 6 x 20, three arm projections 3 x 30, TDI X/Y/Z 40, the
+    frequency factors f(t), omL, fctr, fctr2 and their products 32 (330 in
+    all), plus 15 transcendental evaluations counted as one each; then three
+    N-point FFTs at 5 N log2 N each.  TDI-2 adds its factor (20 per sample);
+    the third body adds v_LOS (Kepler solve), f_GW and the trapezoid
+    increment at three spacecraft (3 x 56) plus 9 transcendentals per sample
+    (thirdbody.py:155-380); the likelihood adds conj(d) h / S and |h|^2 / S on
+    A and E (24 per bin).  ``N`` may be an array (one N per binary).
+    """
+    N = np.asarray(N, dtype=np.float64)
+    per_sample = 330.0 + 15.0
+    if tdi2:
+        per_sample += 20.0
+    if third_body:
+        per_sample += 3 * 56.0 + 9.0
+    f = per_sample * N + 3 * 5.0 * N * np.log2(N)
+    if likelihood:
+        f = f + 24.0 * N
+    return f
+
+
 def cuda_set_device(dev):
     """Select the CUDA device used by subsequent calls."""
     import torch

@@ -142,3 +142,15 @@ def test_autotune_workload_keys():
     # batches of similar size and the same N mix share a key
     assert workload_key("ll", np.array([64] * 1100 + [2048] * 29), 1129, "mixed", False, 14) \
         == k2.replace("grad", "ll")
+
+
+def test_flops_per_binary_count():
+    """The frozen FLOP count: 345 per sample + 3 FFTs of 5 N log2 N; TDI-2,
+    third body and likelihood terms add per sample / per bin; arrays work."""
+    from gbgpu_gb300.utility import flops_per_binary
+    assert flops_per_binary(256) == 345 * 256 + 15 * 256 * 8          # 119,040
+    assert flops_per_binary(256, tdi2=True) - flops_per_binary(256) == 20 * 256
+    assert flops_per_binary(256, third_body=True) - flops_per_binary(256) == 177 * 256
+    assert flops_per_binary(256, likelihood=True) - flops_per_binary(256) == 24 * 256
+    Ns = np.array([64, 128, 2048])
+    np.testing.assert_array_equal(flops_per_binary(Ns), [flops_per_binary(n) for n in Ns])
