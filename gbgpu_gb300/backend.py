@@ -19,6 +19,8 @@ def _addr(x):
         return None
     if isinstance(x, int):
         return ctypes.c_void_p(x)
+    if not isinstance(x, torch.Tensor) and hasattr(x, "__cuda_array_interface__"):
+        x = torch.as_tensor(x, device="cuda")            # CuPy, Numba, ...: no copy
     if isinstance(x, torch.Tensor):
         if not x.is_cuda:
             raise TypeError("backend arrays must be CUDA tensors")

@@ -36,13 +36,38 @@ def _is_pow2(n):
     return n >= 1 and (n & (n - 1)) == 0
 
 
+def _as_tensor(x):
+    """A torch view of an array from another library without a copy: objects
+    with ``__cuda_array_interface__`` (CuPy, Numba, ...) or ``__dlpack__``;
+    None for anything else (NumPy arrays, lists, scalars)."""
+    if isinstance(x, (torch.Tensor, np.ndarray)):
+        return None
+    if hasattr(x, "__cuda_array_interface__"):
+        return torch.as_tensor(x, device="cuda")
+    if hasattr(x, "__dlpack__"):
+        return torch.from_dlpack(x)
+    return None
+
+
+def _native(x):
+    """``x`` itself, or a torch view of a foreign device array (see _as_tensor)."""
+    t = _as_tensor(x)
+    return x if t is None else t
+
+
 def _to_device(x, dtype, device, non_blocking=False):
-    """``non_blocking`` queues a copy from pinned host memory on the current
+    """``x`` as a ``dtype`` tensor on ``device``: torch tensors, NumPy arrays
+    and sequences, and device arrays of other libraries (CUDA array
+    interface or DLPack, taken without a copy when dtype and device match).
+    ``non_blocking`` queues a copy from pinned host memory on the current
     stream; only for callers that read their results back before returning."""
-    if isinstance(x, torch.Tensor):
-        nb = non_blocking and x.device.type == "cpu" and x.is_pinned() and x.dtype == dtype
-        return x.to(device=device, dtype=dtype, non_blocking=nb)
-    return torch.as_tensor(np.asarray(x), dtype=dtype, device=device)
+    if not isinstance(x, torch.Tensor):
+        t = _as_tensor(x)
+        if t is None:
+            return torch.as_tensor(np.asarray(x), dtype=dtype, device=device)
+        x = t
+    nb = non_blocking and x.device.type == "cpu" and x.is_pinned() and x.dtype == dtype
+    return x.to(device=device, dtype=dtype, non_blocking=nb)
 
 
 _KEY_MULT = np.zeros((2, 0), dtype=np.uint64)
@@ -65,9 +90,12 @@ def _array_key(arr):
 
 
 def _to_host(x):
-    if isinstance(x, torch.Tensor):
-        return x.detach().cpu().numpy()
-    return np.asarray(x)
+    if not isinstance(x, torch.Tensor):
+        t = _as_tensor(x)
+        if t is None:
+            return np.asarray(x)
+        x = t
+    return x.detach().cpu().numpy()
 
 
 def plan_tiles(N_per_bin, tile=0):
@@ -290,6 +318,8 @@ class GBGPUBase(abc.ABC):
         return plan
 
     def _params(self, base, add_args):
+        if not isinstance(base, (list, tuple)):
+            base = _native(base)
         if isinstance(base, (np.ndarray, torch.Tensor)) and base.ndim == 2 and not add_args:
             return _to_device(base, torch.float64, self.device).contiguous()
         cols = [torch.atleast_1d(_to_device(x, torch.float64, self.device)) for x in base]
@@ -435,6 +465,10 @@ class GBGPUBase(abc.ABC):
 
     # ------------------------------------------------------------ likelihood
     def _prepare_data(self, data, psd, data_index, noise_index, num_bin):
+        data = [_native(x) for x in data]
+        psd = [_native(x) for x in psd]
+        data_index = None if data_index is None else _native(data_index)
+        noise_index = None if noise_index is None else _native(noise_index)
         if not isinstance(data[0], (torch.Tensor, np.ndarray)):
             raise TypeError("Make sure the data arrays are torch tensors (or NumPy arrays).")
         d0 = data[0]
@@ -551,6 +585,7 @@ class GBGPUBase(abc.ABC):
             raise TypeError(f"unexpected keyword arguments {list(kwargs)}")
         T = int(T / dt) * dt
         self._check_T(T)
+        params = params if isinstance(params, (list, tuple)) else _native(params)
         if isinstance(params, (np.ndarray, torch.Tensor)) and params.ndim == 2 and \
                 params.shape[0] == self.NPARAMS:
             # get_ll reads the likelihood back before returning
@@ -738,6 +773,7 @@ class GBGPUBase(abc.ABC):
         by (group, start) and gathers every output bin in that order, giving
         identical bits on every run.
         """
+        templates = _native(templates)
         if mode not in ("atomic", "deterministic"):
             raise ValueError("mode must be 'atomic' or 'deterministic'")
         total_groups, nchannels, data_length = templates.shape
@@ -821,6 +857,7 @@ class GBGPUBase(abc.ABC):
 
         ``params`` is (B, nparams), transposed relative to ``get_ll``.
         """
+        templates = _native(templates)
         precision = kwargs.pop("precision", self.precision)
         fill_mode = kwargs.pop("fill_mode", "atomic")
         if fill_mode not in ("atomic", "deterministic"):

@@ -403,3 +403,61 @@ def test_workspace_and_in_tile_setup_agree(gbgpu, precision):
         outs.append((d_h.cpu().numpy(), h_h.cpu().numpy()))
     np.testing.assert_array_equal(outs[0][0], outs[1][0])
     np.testing.assert_array_equal(outs[0][1], outs[1][1])
+
+
+class _CudaArrayOnly:
+    """A device array of another library (CuPy, Numba, ...): only the CUDA array
+    interface, no torch type."""
+
+    def __init__(self, t):
+        self._t = t
+
+    @property
+    def __cuda_array_interface__(self):
+        return self._t.__cuda_array_interface__
+
+    @property
+    def shape(self):
+        return tuple(self._t.shape)
+
+
+def test_cuda_array_interface_inputs(gbgpu):
+    """get_ll, fill_global_template (in place) and backend.get_ll take device
+    arrays of other libraries without copies, with results identical to torch
+    inputs."""
+    g = load_golden("ll_multi")
+    gb = gbgpu()
+    gb.d_d = float(g["d_d"])
+    kw = dict(N=int(g["N"]), T=float(g["T"]), dt=float(g["dt"]), tdi2=bool(g["tdi2"]),
+              start_freq_ind=int(g["start_freq_ind"]),
+              data_index=dev(g["data_index"], torch.int32),
+              noise_index=dev(g["noise_index"], torch.int32))
+    prm, dA, dE = dev(g["params"]), dev(g["A_data"]), dev(g["E_data"])
+    pA, pE = dev(g["A_psd"]), dev(g["E_psd"])
+    ref = gb.get_ll(prm, [dA, dE], [pA, pE], **kw)
+    kw["data_index"] = _CudaArrayOnly(kw["data_index"])
+    got = gb.get_ll(_CudaArrayOnly(prm), [_CudaArrayOnly(dA), _CudaArrayOnly(dE)],
+                    [_CudaArrayOnly(pA), _CudaArrayOnly(pE)], **kw)
+    np.testing.assert_array_equal(got, ref)
+    # templates of another library are filled in place
+    f = load_golden("fill_basic")
+    t = dev(f["templates_before"]).clone()
+    gb.fill_global_template(dev(f["group_index"]), _CudaArrayOnly(t), dev(f["A"]), dev(f["E"]),
+                            dev(f["start_inds"]), start_freq_ind=int(f["start_freq_ind"]),
+                            mode="deterministic")
+    assert rel_err(t.cpu().numpy()[:, :2], f["templates_after"][:, :2]) < 1e-13
+    # the backend method table takes them as well
+    d_h = torch.zeros(3, dtype=torch.complex128, device="cuda")
+    h_h = torch.zeros(3, dtype=torch.complex128, device="cuda")
+    W = O.waveform(g["params"][:, :3], int(g["N"]), T=float(g["T"]), dt=float(g["dt"]), tdi2=True)
+    si = (W["start_inds"] - int(g["start_freq_ind"])).astype(np.int32)
+    A_pm, E_pm = O.point_major(W["AETf"][:, 0]), O.point_major(W["AETf"][:, 1])
+    L = g["A_data"].shape[-1]
+    z = torch.zeros(3, dtype=torch.int32, device="cuda")
+    args = (dev(A_pm), dev(E_pm), dev(g["A_data"][0]), dev(g["E_data"][0]), dev(g["A_psd"][0]),
+            dev(g["E_psd"][0]))
+    gb.backend.get_ll(d_h, h_h, *args, W["df"], dev(si), int(g["N"]), 3, z, z, L)
+    ref_dh = d_h.clone()
+    gb.backend.get_ll(_CudaArrayOnly(d_h), h_h, *[_CudaArrayOnly(a) for a in args], W["df"],
+                      _CudaArrayOnly(dev(si)), int(g["N"]), 3, z, z, L)
+    assert torch.equal(d_h, ref_dh)

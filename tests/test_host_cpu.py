@@ -154,3 +154,32 @@ def test_flops_per_binary_count():
     assert flops_per_binary(256, likelihood=True) - flops_per_binary(256) == 24 * 256
     Ns = np.array([64, 128, 2048])
     np.testing.assert_array_equal(flops_per_binary(Ns), [flops_per_binary(n) for n in Ns])
+
+
+class _DLPackOnly:
+    """An array of another library that only speaks DLPack."""
+
+    def __init__(self, t):
+        self._t = t
+
+    def __dlpack__(self, *args, **kwargs):
+        return self._t.__dlpack__(*args, **kwargs)
+
+    def __dlpack_device__(self):
+        return self._t.__dlpack_device__()
+
+
+def test_foreign_arrays_enter_without_copy():
+    """Arrays of other libraries (DLPack here; the CUDA array interface on the
+    GPU) become torch views: same memory when dtype and device match."""
+    torch = pytest.importorskip("torch")
+    from gbgpu_gb300.gbgpu import _native, _to_device, _to_host
+    t = torch.arange(6, dtype=torch.float64)
+    x = _to_device(_DLPackOnly(t), torch.float64, "cpu")
+    assert torch.equal(x, t) and x.data_ptr() == t.data_ptr()
+    np.testing.assert_array_equal(_to_host(_DLPackOnly(t)), t.numpy())
+    assert _to_device(_DLPackOnly(t), torch.float32, "cpu").dtype == torch.float32
+    # NumPy arrays and plain sequences keep their own path
+    a = np.arange(3.0)
+    assert _native(a) is a and _native([1, 2]) == [1, 2]
+    np.testing.assert_array_equal(_to_device([1, 2], torch.int32, "cpu").numpy(), [1, 2])
