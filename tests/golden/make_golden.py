@@ -146,7 +146,43 @@ def case_fill(name, seed):
          A=gb.A, E=gb.E)
 
 
-def case_third(name, seed, B, N, T, dt):
+def case_ll_third(name, seed, B, N, T, dt, tdi2):
+    """GBGPUThirdBody.get_ll with (14, B) parameters against injected data."""
+    rng = np.random.default_rng(seed)
+    p = draw_params(rng, B, f_lo=2.0e-3, f_hi=2.006e-3)
+    A2 = 10 ** rng.uniform(-2, 2, B)
+    P2 = 10 ** rng.uniform(0, np.log10(40), B)
+    e2 = rng.uniform(0, 0.9, B)
+    varpi = rng.uniform(0, 2 * np.pi, B)
+    T2 = rng.uniform(0, 1, B) * P2
+    third = np.array([A2, varpi, e2, P2, T2])
+    gb = ref_third.GBGPUThirdBody()
+    gb.run_wave(*p, *third.copy(), N=N, T=T, dt=dt, tdi2=tdi2)
+    si = np.asarray(gb.start_inds)
+    start_freq_ind = int(si.min()) - 29
+    L = int(si.max()) + N + 33 - start_freq_ind
+    f = (np.arange(L) + start_freq_ind) / (int(T / dt) * dt)
+    S = lisatools.sensitivity.A1TDISens.get_Sn(f)
+    data = []
+    for ch in range(2):
+        d = np.zeros(L, np.complex128)
+        for b in range(B):
+            o = si[b] - start_freq_ind
+            d[o:o + N] += gb.AETf[b, ch]
+        sig = np.sqrt(S * (int(T / dt) * dt) / 4.0)
+        d += sig * (rng.standard_normal(L) + 1j * rng.standard_normal(L)) / np.sqrt(2.0)
+        data.append(d)
+    gb.d_d = 77.0
+    params = np.concatenate([p, third])
+    like = gb.get_ll(params.copy(), data, [S, S], N=N, T=T, dt=dt, tdi2=tdi2,
+                     start_freq_ind=start_freq_ind)
+    save(name, params=params, N=N, T=T, dt=dt, tdi2=tdi2, like=like,
+         d_h=np.asarray(gb.d_h), h_h=np.asarray(gb.h_h), d_d=77.0,
+         start_freq_ind=start_freq_ind, A_data=data[0], E_data=data[1], A_psd=S, E_psd=S,
+         start_inds=si)
+
+
+def case_third(name, seed, B, N, T, dt, tdi2=False):
     rng = np.random.default_rng(seed)
     p = draw_params(rng, B)
     A2 = 10 ** rng.uniform(-2, 2, B)
@@ -158,9 +194,9 @@ def case_third(name, seed, B, N, T, dt):
     T2 = rng.uniform(0, 1, B) * P2
     T2[2] = 3.5 * P2[2]  # pericentre after the window: negative mean anomaly
     gb = ref_third.GBGPUThirdBody()
-    gb.run_wave(*p, A2, varpi, e2, P2, T2.copy(), N=N, T=T, dt=dt)
+    gb.run_wave(*p, A2, varpi, e2, P2, T2.copy(), N=N, T=T, dt=dt, tdi2=tdi2)
     save(name, params=p, A2=A2, varpi=varpi, e2=e2, P2=P2, T2=T2, N=N, T=T,
-         dt=dt, XYZf=gb.XYZf, AETf=gb.AETf, start_inds=np.asarray(gb.start_inds))
+         dt=dt, tdi2=tdi2, XYZf=gb.XYZf, AETf=gb.AETf, start_inds=np.asarray(gb.start_inds))
 
 
 def case_kepler(name, seed):
@@ -250,6 +286,10 @@ if __name__ == "__main__":
     case_fill("fill_basic", 9)
     case_third("third_n256", 10, B=6, N=256, T=TJ4, dt=5.0)
     case_third("third_n512_1yr", 16, B=4, N=512, T=YRSID_SI, dt=15.0)
+    case_third("third_n128_tdi2", 17, B=4, N=128, T=TJ4, dt=10.0, tdi2=True)
+    case_ll_third("ll_third", 18, B=6, N=256, T=TJ4, dt=5.0, tdi2=True)
+    case_wave("wave_n4096", 19, B=1, N=4096, T=TJ4, dt=5.0, tdi2=False,
+              f_lo=2.0e-2, f_hi=2.5e-2)
     case_kepler("kepler", 12)
     case_get_n("get_n", 13)
     case_misc("misc")

@@ -16,7 +16,7 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 WAVE_CASES = ["wave_n128", "wave_n256_tdi2", "wave_n64_1yr", "wave_n512_hf",
-              "wave_n2048_hf", "wave_b1"]
+              "wave_n2048_hf", "wave_b1", "wave_n4096"]
 FP64_TOL = 1e-10
 MIXED_LL_TOL = 1e-6
 
@@ -215,16 +215,37 @@ def test_generate_global_template_matches_reference(gbgpu, precision):
     assert err < (FP64_TOL if precision == "fp64" else 2e-6), err
 
 
-@pytest.mark.parametrize("case", ["third_n256", "third_n512_1yr"])
+@pytest.mark.parametrize("case", ["third_n256", "third_n512_1yr", "third_n128_tdi2"])
 def test_third_body_matches_reference(case):
     from gbgpu_gb300 import GBGPUThirdBody
     g = load_golden(case)
     gb = GBGPUThirdBody()
     gb.run_wave(*g["params"], g["A2"], g["varpi"], g["e2"], g["P2"], g["T2"], N=int(g["N"]),
-                T=float(g["T"]), dt=float(g["dt"]))
+                T=float(g["T"]), dt=float(g["dt"]), tdi2=bool(g["tdi2"]))
     np.testing.assert_array_equal(gb.start_inds.cpu().numpy(), g["start_inds"])
     assert np.max(rel_err(gb.XYZf.cpu().numpy(), g["XYZf"], axis=(1, 2))) < FP64_TOL
     assert np.max(rel_err(gb.AETf.cpu().numpy(), g["AETf"], axis=(1, 2))) < FP64_TOL
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_third_body_get_ll_matches_reference(precision):
+    """GBGPUThirdBody.get_ll, (14, B) parameters, TDI-2, against the reference's."""
+    from gbgpu_gb300 import GBGPUThirdBody
+    g = load_golden("ll_third")
+    gb = GBGPUThirdBody()
+    gb.d_d = float(g["d_d"])
+    like = gb.get_ll(g["params"], [dev(g["A_data"]), dev(g["E_data"])],
+                     [dev(g["A_psd"]), dev(g["E_psd"])], N=int(g["N"]), T=float(g["T"]),
+                     dt=float(g["dt"]), tdi2=bool(g["tdi2"]),
+                     start_freq_ind=int(g["start_freq_ind"]), precision=precision)
+    snr2 = np.abs(g["h_h"].real)
+    if precision == "fp64":
+        np.testing.assert_allclose(gb.d_h.cpu().numpy(), g["d_h"], rtol=FP64_TOL, atol=0)
+        np.testing.assert_allclose(gb.h_h.cpu().numpy().real, g["h_h"].real, rtol=FP64_TOL)
+        np.testing.assert_allclose(like, g["like"], rtol=FP64_TOL)
+    else:
+        assert np.max(np.abs(like - g["like"]) / np.maximum(1.0, snr2)) < MIXED_LL_TOL
+    np.testing.assert_array_equal(gb.start_inds.cpu().numpy(), g["start_inds"])
 
 
 def _ll_setup(B, N, seed, f_lo=2e-3, f_hi=2.02e-3, T=4 * 31557600.0, dt=10.0, third=False):

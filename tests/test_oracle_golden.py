@@ -13,7 +13,7 @@ import fastgb_oracle as O
 from conftest import load_golden, rel_err
 
 WAVE_CASES = ["wave_n128", "wave_n256_tdi2", "wave_n64_1yr", "wave_n512_hf",
-              "wave_n2048_hf", "wave_b1"]
+              "wave_n2048_hf", "wave_b1", "wave_n4096"]
 
 
 @pytest.mark.parametrize("case", WAVE_CASES)
@@ -76,14 +76,29 @@ def test_fill_global_matches_reference():
     assert rel_err(gen, g["generated"]) < 1e-12
 
 
-@pytest.mark.parametrize("case", ["third_n256", "third_n512_1yr"])
+@pytest.mark.parametrize("case", ["third_n256", "third_n512_1yr", "third_n128_tdi2"])
 def test_third_body_matches_reference(case):
     g = load_golden(case)
     w = O.waveform(g["params"], int(g["N"]), T=float(g["T"]), dt=float(g["dt"]),
+                   tdi2=bool(g["tdi2"]),
                    third=(g["A2"], g["varpi"], g["e2"], g["P2"], g["T2"]))
     np.testing.assert_array_equal(w["start_inds"], g["start_inds"])
     assert np.max(rel_err(w["XYZf"], g["XYZf"], axis=(1, 2))) < 1e-11
     assert np.max(rel_err(w["AETf"], g["AETf"], axis=(1, 2))) < 1e-11
+
+
+def test_third_body_get_ll_matches_reference():
+    """GBGPUThirdBody.get_ll with (14, B) parameters, TDI-2, injected data."""
+    g = load_golden("ll_third")
+    p = g["params"]
+    like, d_h, h_h, w = O.get_ll(
+        p[:9], [g["A_data"], g["E_data"]], [g["A_psd"], g["E_psd"]], int(g["N"]),
+        T=float(g["T"]), dt=float(g["dt"]), tdi2=bool(g["tdi2"]), d_d=float(g["d_d"]),
+        start_freq_ind=int(g["start_freq_ind"]), third=tuple(p[9:14]), return_terms=True)
+    np.testing.assert_array_equal(w["start_inds"], g["start_inds"])
+    assert rel_err(d_h, g["d_h"]) < 1e-11
+    assert rel_err(h_h, g["h_h"]) < 1e-11
+    np.testing.assert_allclose(like, g["like"], rtol=1e-10)
 
 
 def test_kepler_matches_reference():
