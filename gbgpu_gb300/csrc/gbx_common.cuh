@@ -42,10 +42,6 @@ template <typename V> __device__ __forceinline__ V cmul(V a, V b)
     r.y = a.x * b.y + a.y * b.x;
     return r;
 }
-template <typename V, typename S> __device__ __forceinline__ V cscale(V a, S s)
-{
-    V r; r.x = a.x * s; r.y = a.y * s; return r;
-}
 
 // bit reversal of the low `bits` bits
 __device__ __forceinline__ int bitrev(int k, int bits) { return (int)(__brev((unsigned)k) >> (32 - bits)); }

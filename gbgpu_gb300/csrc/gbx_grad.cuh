@@ -94,21 +94,6 @@ __device__ __forceinline__ void sinc_cos_d_f(float a, float &S, float &C, float 
     }
 }
 
-// X = G21 - G31 + (G12 - G13) fc and cyclic (gbgpu.py:370-372); links in the
-// order 12, 23, 31, 21, 32, 13
-__device__ __forceinline__ void tdi_xyz(const float2 G[6], float2 fc, float2 out[3])
-{
-    out[0] = cadd(csub(G[3], G[2]), cmul(csub(G[0], G[5]), fc));
-    out[1] = cadd(csub(G[4], G[0]), cmul(csub(G[1], G[3]), fc));
-    out[2] = cadd(csub(G[5], G[1]), cmul(csub(G[2], G[4]), fc));
-}
-
-__device__ __forceinline__ void cmac(float &re, float &im, float2 y, float2 x)
-{
-    re = fmaf(y.x, x.x, fmaf(-y.y, x.y, re));
-    im = fmaf(y.x, x.y, fmaf(y.y, x.x, im));
-}
-
 // Backward pass at one sample: recomputes the slow part with its derivatives
 // and accumulates sum_c Y_c x'_c for x' in {x_P, x_C, dx/df0, dx/dfdot,
 // dx/dfddot, dx/dlam, dx/dbeta} (7 complex accumulators in acc[14]).

@@ -108,23 +108,6 @@ __device__ __forceinline__ double quad_form(const double *e, double x, double y,
     return e[0] * x * x + e[1] * y * y + e[2] * z * z +
            2.0 * (e[3] * x * y + e[4] * x * z + e[5] * y * z);
 }
-// sin(a)/a from its Taylor series (error < 1e-11 for |a| <= 1.6), falls back
-// to sinf(a)/a for larger arguments.
-__device__ __forceinline__ float sinc_f(float a)
-{
-    float x = a * a;
-    if (x < 2.56f) {
-        float p = -1.0f / 1307674368000.0f;
-        p = fmaf(p, x, 1.0f / 6227020800.0f);
-        p = fmaf(p, x, -1.0f / 39916800.0f);
-        p = fmaf(p, x, 1.0f / 362880.0f);
-        p = fmaf(p, x, -1.0f / 5040.0f);
-        p = fmaf(p, x, 1.0f / 120.0f);
-        p = fmaf(p, x, -1.0f / 6.0f);
-        return fmaf(p, x, 1.0f);
-    }
-    return sinf(a) / a;
-}
 
 // sin(x) and cos(x) for moderate |x| (the carrier phase reduced to [-pi, pi],
 // omega L, link arguments: |x| < 8).  Cody-Waite reduction r = x - k pi/2
@@ -840,13 +823,6 @@ __device__ __forceinline__ void fft_dif(typename C2<R>::T *buf, int nsub, int lg
         buf[idx] = x;
     }
     __syncthreads();
-}
-
-__device__ __forceinline__ double warp_sum(double v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
 }
 
 // ----------------------------------------------------------------------------
