@@ -61,7 +61,10 @@ int gbx_init(void);
  * with templates in the reference's point-major layout (element i*num_bin+b).
  * Differences: bins outside [0, data_length) contribute zero and set
  * GBX_FLAG_WINDOW in *status (the reference reads out of bounds); the call is
- * asynchronous on `stream` (the reference synchronises the device).
+ * asynchronous on `stream` (the reference synchronises the device); the
+ * products and sums run in float-pair arithmetic (46 significant bits per
+ * input), so each output is within 1e-12 of sum |terms| of the FP64 sums
+ * (the reference sums in FP64); a PSD bin at infinity contributes zero.
  * `status` may be NULL.
  */
 int gbx_get_ll(void *d_h, void *h_h, const void *A_template, const void *E_template,
