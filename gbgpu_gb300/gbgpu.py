@@ -226,6 +226,7 @@ class GBGPUBase(abc.ABC):
         self._tables = {}
         self._plans = {}
         self._shapes = {}
+        self._n_last = None
         self._status = torch.zeros(1, dtype=torch.int32, device=self.device)
         self._lazy = None
         self._XYZf = self._AETf = self._start_inds = None
@@ -535,8 +536,11 @@ class GBGPUBase(abc.ABC):
             return d_h, h_h
         la = self._ll_args(dd, pp, data_length, data_index, noise_index, T)
         nparams = params.shape[0]
-        # one content key of a per-binary N array per call (plan cache, launch shape)
-        nkey = None if np.ndim(N) == 0 else _array_key(np.ascontiguousarray(N, dtype=np.int64))
+        # content key of a per-binary N array (plan cache, launch shape); see _n_key
+        arr, nkey, verify = None, None, False
+        if np.ndim(N) != 0:
+            arr = np.ascontiguousarray(N, dtype=np.int64)
+            nkey, verify = self._n_key(arr)
 
         def run(tile, bps):
             plan = self._plan(N, T, precision, tdi2, nparams, tile, bps, nkey=nkey)
@@ -548,7 +552,34 @@ class GBGPUBase(abc.ABC):
         shape = self._launch_shape("ll", N, B, precision, tdi2, nparams, run, nkey=nkey)
         self._status.zero_()
         run(*shape)
+        if verify:
+            # the full key, computed while the kernel runs; if the array changed
+            # in place, the launch is repeated with the right plan (same stream:
+            # its outputs replace the first launch's before anyone reads them)
+            full = _array_key(arr)
+            self._n_last = self._n_last[:3] + (full,)
+            if full != nkey:
+                nkey = full
+                shape = self._launch_shape("ll", N, B, precision, tdi2, nparams, run, nkey=nkey)
+                self._status.zero_()
+                run(*shape)
         return d_h, h_h
+
+    def _n_key(self, arr):
+        """(content key, needs verification) of an int64 N array.  A buffer
+        that comes back at the same address with the same length and the same
+        64 sampled entries reuses the previous call's key, to be verified
+        against the full key after the launch (the full key costs a pass over
+        the array on the host, which then overlaps the kernel); any other
+        array gets its full key now."""
+        n = arr.shape[0]
+        sample = arr[::max(1, n // 64)].tobytes()
+        last = self._n_last
+        if last is not None and last[0] == arr.ctypes.data and last[1] == n and last[2] == sample:
+            return last[3], True
+        key = _array_key(arr)
+        self._n_last = (arr.ctypes.data, n, sample, key)
+        return key, False
 
     def _check_status(self):
         st = int(self._status.item())

@@ -159,3 +159,29 @@ def test_invalid_launch_shapes_are_rejected():
     like, grad = gb3.get_ll_grad(full, d, [dev(S), dev(S)], N=2048, T=T_OBS, dt=10.0,
                                  start_freq_ind=s0)
     assert grad.shape == (14, 8) and np.all(np.isfinite(grad))
+
+
+def test_n_array_changed_in_place_is_detected():
+    """get_ll reuses the previous call's N-array key when the same buffer comes
+    back with the same sampled entries, and verifies it after the launch: a
+    buffer changed in place at an entry the quick check does not sample must
+    still give the new assignment's likelihoods (those of a fresh object)."""
+    from gbgpu_gb300 import GBGPU
+    B = 200
+    rng = np.random.default_rng(51)
+    Ns = (2 ** rng.integers(7, 10, B)).astype(np.int64)
+    p, _, data, S, s0 = _ll_setup(B, Ns, 52)
+    kw = dict(T=T_OBS, dt=10.0, start_freq_ind=s0, precision="mixed")
+    dd, SS = [dev(x) for x in data], [dev(S), dev(S)]
+    gb = GBGPU()
+    gb.d_d = 0.0
+    first = gb.get_ll(p, dd, SS, N=Ns, **kw)
+    again = gb.get_ll(p, dd, SS, N=Ns, **kw)                 # unchanged: same key, same bits
+    np.testing.assert_array_equal(again, first)
+    k = 1                                                    # the quick check samples 0, 3, 6, ...
+    Ns[k] = 64
+    second = gb.get_ll(p, dd, SS, N=Ns, **kw)
+    fresh = GBGPU()
+    fresh.d_d = 0.0
+    np.testing.assert_array_equal(second, fresh.get_ll(p, dd, SS, N=Ns.copy(), **kw))
+    assert second[k] != first[k]
