@@ -305,7 +305,7 @@ __device__ __forceinline__ void slow_grad_mixed(const Bin &B, const GradExtra &G
 // fddot, lam, beta slots (acc[4..13] of the 7-accumulator block) and the
 // five third-body slots t5[10] (A2, varpi, e2, P2, T2).
 __device__ __forceinline__ void third_grad_sample(const Bin &B, const GradExtra &Gx, int k, int N,
-                                                  int lg, double step, const double *__restrict__ tab,
+                                                  int lg, dfl stepd, const double *__restrict__ tab,
                                                   float ifs, const float2 *Rrow0, const float *grow0,
                                                   const float2 cfo[3], float acc[14], float t5[10])
 {
@@ -313,15 +313,14 @@ __device__ __forceinline__ void third_grad_sample(const Bin &B, const GradExtra 
     const float cpsi = -(float)(kPi / kCSI);
     const float ic = (float)(1.0 / kCSI);
     // as the forward pre-pass: one Kepler solve at spacecraft 1's delayed
-    // time (FP64 time, FP32 solve), the other spacecraft linearised in their
-    // FP32 k.P/c offsets (<= 8.3 s: relative change of dv[0..4] <= n2 8.3 s)
-    const double kP0 = B.k[0] * __ldg(tab + k) + B.k[1] * __ldg(tab + (size_t)N + k) +
-                       B.k[2] * __ldg(tab + (size_t)2 * N + k);
-    const double xi0 = (double)k * step - kP0;
+    // time (float-pair time and mean anomaly, FP32 solve), the other
+    // spacecraft linearised in their FP32 k.P/c offsets (<= 8.3 s: relative
+    // change of dv[0..4] <= n2 8.3 s)
+    const dfl xi0 = df_add(df_mul_f(stepd, (float)k), df_neg(kP1_pair(B, tabf, N, k)));
     float dv[6];
     const float v0 = vlos_grad_mixed(xi0, B, Gx.cosvarpi, Gx.P2yr, dv);
-    const float x0 = (float)xi0;
-    const float sth = (float)step, stl = (float)(step - (double)sth);
+    const float x0 = xi0.h + xi0.l;
+    const float sth = stepd.h, stl = stepd.l;
     auto kpf = [&](int s, int n) {
         const float *r = tabf + (size_t)(9 + 3 * s) * N + n;
         return fmaf(B.kf[0], __ldg(r), fmaf(B.kf[1], __ldg(r + N), B.kf[2] * __ldg(r + 2 * N)));
@@ -563,9 +562,8 @@ __global__ void __launch_bounds__(kBlock, 2) grad_kernel(const GradParams GP)
         __syncthreads();
         const int S = cnt << lg;
         const dfl stepd = K.stepd[lg];
-        const double step = a.T * exp2_int(-lg);
         // (scratch for the pre-pass: k.P/c of every sample in buf)
-        if (THIRD) third_prepass_mixed(bins, tab, cnt, lg, step, psi, vl, reinterpret_cast<float *>(buf), gq);
+        if (THIRD) third_prepass_mixed(bins, tab, cnt, lg, stepd, psi, vl, reinterpret_cast<float *>(buf), gq);
 
         // forward slow part and FFT
         for (int m = tid; m < S; m += kBlock) {
@@ -703,7 +701,7 @@ __global__ void __launch_bounds__(kBlock, 2) grad_kernel(const GradParams GP)
                 for (int k = i0; k < N; k += Tpb) {
                     const float2 *cf = es + 3 * ((size_t)(p << lg) + k);
                     const float2 cfo[3] = {cf[0], cf[1], cf[2]};
-                    third_grad_sample(B, Gx, k, N, lg, step, tab, ifs, cphs + (size_t)(p * 3) * N,
+                    third_grad_sample(B, Gx, k, N, lg, stepd, tab, ifs, cphs + (size_t)(p * 3) * N,
                                       gq + (size_t)(p * 3) * N, cfo, acc + 5, acc + 19);
                 }
             }

@@ -48,7 +48,9 @@ struct __align__(16) Bin {
     double ep[6], ec[6];           // e+ and ex, order xx yy zz xy xz yz
     double2 DP, DC;                // polarisation factors divided by amp
     double2 scale;                 // amp * 0.5 T / N [* tdi2 factor]
-    double A2, varpi, e2, n2, T2;  // third body (n2, T2 in SI)
+    double A2, varpi, e2;          // third body (FP64 form)
+    union { double n2; dfl n2d; }; // n2 [rad/s]: FP64 form / float pair (mixed form)
+    union { double T2; dfl T2d; }; // T2 [s], likewise
     float kf[3], uf[3], vf[3];      // k, u, v in FP32 (mixed form; r.e+.r = (r.v)^2 - (r.u)^2)
     float2 DPf, DCf;
     float f0f, fdotf, fddotf;
@@ -286,25 +288,15 @@ __device__ double vlos_fp64(double t, const Bin &B)
     return B.A2 * (sin(u + B.varpi) + e * sin(B.varpi));
 }
 
-// Same model with the Kepler solve in FP32.  The mean anomaly and its 2 pi
-// reductions stay in FP64; since only sin/cos of the anomaly are used, the
-// un-reduction is applied modulo 2 pi, which keeps |u| <= pi in FP32.
-// Returns the eccentric anomaly u (mod 2 pi) at mean anomaly n2 (t - T2).
-__device__ __forceinline__ float kepler_u_mixed(double t, const Bin &B)
+// Same model with the Kepler solve in FP32: eccentric anomaly u for a mean
+// anomaly l in [0, pi] (Mikkola's starter and a fourth-order Newton step, as
+// the FP64 form).
+__device__ __forceinline__ float kepler_solve_f(float l, float e)
 {
-    double ld = B.n2 * (t - B.T2);
-    bool neg = ld < 0.0;
-    ld = fabs(ld);
-    if (ld > 2.0 * kPi) ld -= floor(ld * kInvTwoPi) * 2.0 * kPi;
-    bool overpi = ld > kPi;
-    if (overpi) ld = 2.0 * kPi - ld;
-    float l = (float)ld;
-    float e = B.e2f;
     float alpha = (1.0f - e) / (4.0f * e + 0.5f);
     float beta = 0.5f * l / (4.0f * e + 0.5f);
     float z = sqrtf(beta * beta + alpha * alpha * alpha);
-    z = neg ? beta - z : beta + z;
-    z = cbrtf(z);
+    z = cbrtf(beta + z);
     float s = z - alpha / z;
     float s2 = s * s;
     float w = s - 0.078f * s2 * s2 * s / (1.0f + e);
@@ -320,10 +312,23 @@ __device__ __forceinline__ float kepler_u_mixed(double t, const Bin &B)
     float u2 = -f / (f1 + f2 * u1);
     float u3 = -f / (f1 + f2 * u2 + f3 * u2 * u2);
     float u4 = -f / (f1 + f2 * u3 + f3 * u3 * u3 + f4 * u3 * u3 * u3);
-    float u = u0 + u4;
-    if (overpi) u = -u;
-    if (neg) u = -u;
-    return u;
+    return u0 + u4;
+}
+
+// Eccentric anomaly (mod 2 pi) at the delayed time xi (a float pair): the
+// mean anomaly M = n2 (xi - T2) and its reduction to [-pi, pi] in float-pair
+// arithmetic (~1e-13 rad), then the FP32 solve on |M| with the sign put back
+// (only sin/cos of the anomaly are used, so the reduction changes nothing).
+// Also returns M itself (unreduced, FP32).
+__device__ __forceinline__ float kepler_u_df(dfl xi, const Bin &B, float &Mout)
+{
+    const dfl M = df_mul(B.n2d, df_add(xi, df_neg(B.T2d)));
+    Mout = M.h + M.l;
+    const float q = rintf(M.h * (float)kInvTwoPi);
+    const dfl r = df_add(M, df_neg(df_mul_f(df_from(kTwoPi), q)));
+    const float l = r.h + r.l;
+    const float u = kepler_solve_f(fminf(fabsf(l), (float)kPi), B.e2f);
+    return l < 0.0f ? -u : u;
 }
 
 // v_LOS of the FP32 Kepler solve, A2 (sin(phi + varpi) + e sin varpi) with
@@ -331,9 +336,10 @@ __device__ __forceinline__ float kepler_u_mixed(double t, const Bin &B)
 // dv/dt = A2 cos(phi + varpi)
 // dphi/dM n2, with dphi/dM = sqrt(1 - e^2) / (1 - e cos u)^2 (1 / (1 - e cos u)
 // below e = 1e-6, where the model takes phi = u).
-__device__ float vlos_dt_mixed(double t, const Bin &B, float &dvdt)
+__device__ float vlos_dt_mixed(dfl t, const Bin &B, float &dvdt)
 {
-    const float u = kepler_u_mixed(t, B);
+    float M;
+    const float u = kepler_u_df(t, B, M);
     const float e = B.e2f;
     float su, cu;
     sincosf(u, &su, &cu);
@@ -347,7 +353,7 @@ __device__ float vlos_dt_mixed(double t, const Bin &B, float &dvdt)
     }
     float sp, cp;
     sincosf(phi + B.varpif, &sp, &cp);
-    dvdt = B.A2f * cp * dphi_dM * (float)B.n2;
+    dvdt = B.A2f * cp * dphi_dM * B.n2d.h;
     return B.A2f * (sp + e * B.sinvarpif);
 }
 
@@ -358,9 +364,10 @@ __device__ float vlos_dt_mixed(double t, const Bin &B, float &dvdt)
 // e = 1e-6 the model takes phi = u (gbgpu/thirdbody.py:339-350).
 // n2 = 2 pi / (P2 yr) and T2 [s] = T2 yr give dM/dP2 = -M/P2 and
 // dM/dT2 = -n2 yr = -2 pi / P2.
-__device__ float vlos_grad_mixed(double t, const Bin &B, float cosvarpi, float P2yr, float dv[6])
+__device__ float vlos_grad_mixed(dfl t, const Bin &B, float cosvarpi, float P2yr, float dv[6])
 {
-    const float u = kepler_u_mixed(t, B);
+    float M;
+    const float u = kepler_u_df(t, B, M);
     const float e = B.e2f;
     float su, cu;
     sincosf(u, &su, &cu);
@@ -385,9 +392,9 @@ __device__ float vlos_grad_mixed(double t, const Bin &B, float cosvarpi, float P
     dv[2] = A * fmaf(cp, dphi_de, B.sinvarpif);
     const float dvdM = A * cp * dphi_dM;
     const float iP2 = 1.0f / P2yr;
-    dv[3] = dvdM * (float)(B.n2 * (t - B.T2)) * -iP2;
+    dv[3] = dvdM * M * -iP2;
     dv[4] = dvdM * (float)(-kTwoPi) * iP2;
-    dv[5] = dvdM * (float)B.n2;
+    dv[5] = dvdM * B.n2d.h;
     return A * dv[0];
 }
 
@@ -479,8 +486,14 @@ __device__ void setup_bin(Bin &B, const KParams &K, int b, int N, int mode)
         B.varpi = p[10 * nb + b];
         B.e2 = p[11 * nb + b];
         double P2 = p[12 * nb + b];
-        B.n2 = 2.0 * kPi / (P2 * a.year);
-        B.T2 = p[13 * nb + b] * a.year;
+        const double n2 = 2.0 * kPi / (P2 * a.year), T2 = p[13 * nb + b] * a.year;
+        if (a.precision == GBX_FP64) {
+            B.n2 = n2;
+            B.T2 = T2;
+        } else {
+            B.n2d = df_from(n2);
+            B.T2d = df_from(T2);
+        }
         B.A2f = (float)B.A2;
         B.e2f = (float)B.e2;
         double vr = B.varpi - 2.0 * kPi * floor(B.varpi * kInvTwoPi);
@@ -587,6 +600,25 @@ __device__ __forceinline__ void slow_fp64(const Bin &B, int n, int N, double tm,
     out[2] = cmul(fc2, Z);
 }
 
+// Spacecraft 1's delay k . P_1 / c at sample n as a float pair, from the
+// orbit table's hi/lo rows: exact products (FMA), TwoSum accumulation.
+__device__ __forceinline__ dfl kP1_pair(const Bin &B, const float *tabf, int N, int n)
+{
+    dfl P[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+        P[c] = {__ldg(tabf + (size_t)(9 + c) * N + n), __ldg(tabf + (size_t)(18 + c) * N + n)};
+    float p0 = B.kd[0].h * P[0].h, p1 = B.kd[1].h * P[1].h, p2 = B.kd[2].h * P[2].h;
+    float e = fmaf(B.kd[0].h, P[0].h, -p0);
+    e += fmaf(B.kd[1].h, P[1].h, -p1);
+    e += fmaf(B.kd[2].h, P[2].h, -p2);
+#pragma unroll
+    for (int c = 0; c < 3; c++) e = fmaf(B.kd[c].h, P[c].l, fmaf(B.kd[c].l, P[c].h, e));
+    const dfl s01 = df_two_sum(p0, p1);
+    const dfl s012 = df_two_sum(s01.h, p2);
+    return df_fast(s012.h, (s01.l + s012.l) + e);
+}
+
 // Mixed form: the carrier phase om k.P - argS (gbgpu.py:495-505), the delays
 // k.P/c and the delayed times are evaluated in float-pair arithmetic (about
 // 48 bits, so ~1e-12 rad at 100 rad) and reduced modulo 2 pi; everything else
@@ -625,20 +657,7 @@ __device__ __forceinline__ void slow_mixed(const Bin &B, int n, int N, dfl step,
     Phi0 = df_neg(Phi0);
     const dfl wt = df_add(B.omd, df_add(df_mul(B.tpfd, tm), dfl{B.pfddf * tf * tf, 0.0f}));
     const float fdt = fmaf(B.fddotf, tf, B.fdotf);
-    // spacecraft 1: k . P_1 / c as a float pair (exact products, TwoSum accumulation)
-    dfl P[3];
-#pragma unroll
-    for (int c = 0; c < 3; c++)
-        P[c] = {__ldg(tabf + (size_t)(9 + c) * N + n), __ldg(tabf + (size_t)(18 + c) * N + n)};
-    float p0 = B.kd[0].h * P[0].h, p1 = B.kd[1].h * P[1].h, p2 = B.kd[2].h * P[2].h;
-    float e = fmaf(B.kd[0].h, P[0].h, -p0);
-    e += fmaf(B.kd[1].h, P[1].h, -p1);
-    e += fmaf(B.kd[2].h, P[2].h, -p2);
-#pragma unroll
-    for (int c = 0; c < 3; c++) e = fmaf(B.kd[c].h, P[c].l, fmaf(B.kd[c].l, P[c].h, e));
-    const dfl s01 = df_two_sum(p0, p1);
-    const dfl s012 = df_two_sum(s01.h, p2);
-    const dfl kP0 = df_fast(s012.h, (s01.l + s012.l) + e);
+    const dfl kP0 = kP1_pair(B, tabf, N, n);
     // its phase, reduced mod 2 pi
     dfl ph0 = df_add(Phi0, df_mul(kP0, wt));
     if (!THIRD) {
@@ -921,7 +940,7 @@ __device__ __forceinline__ void third_prepass(const Bin *bins, const double *__r
 //      their inclusive prefix sum along n as float pairs -> psi.
 // Called by every thread of the block (contains barriers).
 __device__ __forceinline__ void third_prepass_mixed(const Bin *bins, const double *__restrict__ tab,
-                                                    int cnt, int lg, double step, dfl *psi,
+                                                    int cnt, int lg, dfl stp, dfl *psi,
                                                     float *vl, float *kps, float *gout)
 {
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -939,9 +958,8 @@ __device__ __forceinline__ void third_prepass_mixed(const Bin *bins, const doubl
             }
             continue;
         }
-        const double kP0 = B.k[0] * __ldg(tab + n) + B.k[1] * __ldg(tab + (size_t)N + n) +
-                           B.k[2] * __ldg(tab + (size_t)2 * N + n);
-        const double xi0 = (double)n * step - kP0;
+        // spacecraft 1's delayed time n T/N - k.P_1/c as a float pair
+        const dfl xi0 = df_add(df_mul_f(stp, (float)n), df_neg(kP1_pair(B, tabf, N, n)));
         float dv0;
         const float v0 = vlos_dt_mixed(xi0, B, dv0);
         float kPf[3];
@@ -950,7 +968,7 @@ __device__ __forceinline__ void third_prepass_mixed(const Bin *bins, const doubl
             kPf[s] = fmaf(B.kf[0], __ldg(tabf + (size_t)(9 + 3 * s) * N + n),
                           fmaf(B.kf[1], __ldg(tabf + (size_t)(9 + 3 * s + 1) * N + n),
                                B.kf[2] * __ldg(tabf + (size_t)(9 + 3 * s + 2) * N + n)));
-        const float x0 = (float)xi0;
+        const float x0 = xi0.h + xi0.l;
 #pragma unroll
         for (int s = 0; s < 3; s++) {
             const float dk = s ? kPf[s] - kPf[0] : 0.0f;   // xi_s = xi_1 - dk
@@ -964,7 +982,6 @@ __device__ __forceinline__ void third_prepass_mixed(const Bin *bins, const doubl
     }
     __syncthreads();
     // warp per (binary, spacecraft) row; lane owns a chunk of N/32 samples
-    const dfl stp = df_from(step);
     const float k = (float)(kPi / kCSI);
     const int chunk = N >> 5;
     for (int row = warp; row < 3 * cnt; row += kBlock / 32) {
@@ -1080,7 +1097,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                 psif = reinterpret_cast<dfl *>(buf + 3 * (size_t)maxcnt * N);
                 vl = reinterpret_cast<R *>(psif + 3 * (size_t)maxcnt * N);
                 float *scr = reinterpret_cast<float *>(buf);
-                third_prepass_mixed(bins, tab, cnt, lg, step, psif, reinterpret_cast<float *>(vl), scr,
+                third_prepass_mixed(bins, tab, cnt, lg, stepd, psif, reinterpret_cast<float *>(vl), scr,
                                     scr + 3 * (size_t)maxcnt * N);
             }
         }
