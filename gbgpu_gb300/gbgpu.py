@@ -22,7 +22,7 @@ import torch
 
 from . import _native as nat
 from .backend import get_backend
-from .constants import C_SI, YRSID_SI
+from .constants import YRSID_SI
 from .orbits import EqualArmlengthOrbits, Orbits
 from .utility import get_N
 
