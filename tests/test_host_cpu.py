@@ -183,3 +183,78 @@ def test_foreign_arrays_enter_without_copy():
     a = np.arange(3.0)
     assert _native(a) is a and _native([1, 2]) == [1, 2]
     np.testing.assert_array_equal(_to_device([1, 2], torch.int32, "cpu").numpy(), [1, 2])
+
+
+def test_c_abi_rejects_bad_arguments_before_touching_a_device():
+    """Argument checks of the C ABI return their status codes (and a message
+    in gbx_last_error) before any CUDA call, so they run here without a GPU."""
+    from gbgpu_gb300 import build, _native as nat
+    build.build()
+    lib = ctypes.CDLL(build.LIB)
+    vp, i, d, ll = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_longlong
+    lib.gbx_last_error.restype = ctypes.c_char_p
+    lib.gbx_get_ll_ex.argtypes = [vp] * 8 + [d, vp, i, i, vp, vp, i, ll, ll, vp, vp]
+    lib.gbx_fill_global_ex.argtypes = [vp] * 5 + [i, i, vp, i, i, ll, ll, ll, vp, vp]
+    lib.gbx_waveform_ll.argtypes = [vp, vp, vp, vp, vp]
+    lib.gbx_waveform_ll_grad.argtypes = [vp, vp, vp, vp, vp, vp]
+    lib.gbx_wave_workspace_bytes.restype = ctypes.c_size_t
+    lib.gbx_wave_workspace_bytes.argtypes = [i]
+    ERR_ARG, ERR_UNSUPPORTED = 1, 2
+    fake = ctypes.c_void_p(0x1000)               # never dereferenced: the checks fail first
+    ptrs = [fake] * 8
+
+    def msg():
+        return lib.gbx_last_error().decode()
+
+    # drop-in get_ll: negative sizes, NULL pointers; an empty batch is a no-op
+    assert lib.gbx_get_ll_ex(*ptrs, 1.0, fake, 16, -1, None, None, 100, 1, 1, None, None) == ERR_ARG
+    assert "negative" in msg()
+    assert lib.gbx_get_ll_ex(None, *ptrs[1:], 1.0, fake, 16, 4, None, None, 100, 4, 1,
+                             None, None) == ERR_ARG
+    assert "NULL" in msg()
+    assert lib.gbx_get_ll_ex(*ptrs, 1.0, fake, 16, 0, None, None, 100, 0, 1, None, None) == 0
+    # fill: group stride shorter than the data
+    assert lib.gbx_fill_global_ex(*ptrs[:4], fake, 16, 4, fake, 100, 2, 50, 4, 1,
+                                  None, None) == ERR_ARG
+    assert "group_stride" in msg()
+
+    # waveform family: the struct checks
+    def args(**kw):
+        a = nat.WaveArgs()
+        a.params, a.num_bin, a.nparams, a.N = fake, 4, 9, 256
+        a.precision, a.T, a.armlength, a.year = nat.GBX_MIXED, 1e7, 2.5e9, 3.15e7
+        a.orbit[8] = fake
+        for k, v in kw.items():
+            setattr(a, k, v)
+        return a
+    la = nat.LLArgs()
+    la.A_data = la.E_data = la.A_psd = la.E_psd = fake
+    la.data_length, la.num_data, la.num_psd, la.df = 100, 1, 1, 1e-7
+    cases = [
+        (args(nparams=10), ERR_ARG, "nparams"),
+        (args(precision=7), ERR_ARG, "precision"),
+        (args(T=0.0), ERR_ARG, "T and armlength"),
+        (args(N=100), ERR_UNSUPPORTED, "power of two"),
+        (args(N=16384), ERR_UNSUPPORTED, "limit"),
+        (args(N=512), ERR_ARG, "orbit table"),
+        (args(tile=100), ERR_ARG, "tile"),
+        (args(tile=8192), ERR_ARG, "tile"),
+        (args(blocks_per_sm=-1), ERR_ARG, "blocks_per_sm"),
+        (args(workspace=ctypes.c_void_p(0x1008).value, workspace_bytes=1 << 20), ERR_ARG,
+         "aligned"),
+        (args(workspace=fake.value, workspace_bytes=16), ERR_ARG, "workspace smaller"),
+    ]
+    for a, code, text in cases:
+        assert lib.gbx_waveform_ll(ctypes.byref(a), ctypes.byref(la), fake, fake, None) == code, text
+        assert text in msg(), (text, msg())
+    bad = nat.LLArgs()
+    assert lib.gbx_waveform_ll(ctypes.byref(args()), ctypes.byref(bad), fake, fake, None) == ERR_ARG
+    # gradients: the mixed form only, 9 or 14 parameters, an aligned workspace of the right size
+    g = ctypes.c_void_p(0x1000)
+    assert lib.gbx_waveform_ll_grad(ctypes.byref(args(precision=nat.GBX_FP64)), ctypes.byref(la),
+                                    fake, fake, g, None) == ERR_UNSUPPORTED
+    assert "mixed" in msg()
+    assert lib.gbx_waveform_ll_grad(ctypes.byref(args()), ctypes.byref(la), fake, fake, g,
+                                    None) == ERR_ARG
+    assert "workspace" in msg()
+    assert lib.gbx_wave_workspace_bytes(0) == 0 and lib.gbx_wave_workspace_bytes(3) % 256 == 0
