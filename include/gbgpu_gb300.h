@@ -65,6 +65,10 @@ int gbx_init(void);
  * products and sums run in float-pair arithmetic (46 significant bits per
  * input), so each output is within 1e-12 of sum |terms| of the FP64 sums
  * (the reference sums in FP64); a PSD bin at infinity contributes zero.
+ * data_index / noise_index may be NULL (row 0 for every binary); their rows
+ * are trusted as in the reference, whose argument list carries no row
+ * counts: the caller keeps di*L and ni*L inside its data and PSD arrays
+ * (gbx_waveform_ll, which takes num_data / num_psd, checks them).
  * `status` may be NULL.
  */
 int gbx_get_ll(void *d_h, void *h_h, const void *A_template, const void *E_template,
