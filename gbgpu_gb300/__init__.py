@@ -8,7 +8,7 @@ include/gbgpu_gb300.h.
 
 from . import constants, utility
 from .constants import *  # noqa: F401,F403
-from .orbits import EqualArmlengthOrbits, Orbits
+from .orbits import EqualArmlengthOrbits, Orbits, TabulatedOrbits
 from .utility import (AET, get_N, get_fGW, get_amplitude, get_fdot, get_chirp_mass,
                       get_eta, get_chirp_mass_from_f_fdot, cuda_set_device)
 

@@ -3,9 +3,11 @@
 The reference takes any ``lisatools.detector.Orbits`` object and uses only
 ``get_pos(t, sc)``, ``armlength``, ``t_base`` and ``configure`` (gbgpu/gbgpu.py:
 87-101, 181, 243, 390-397).  The same duck-typed interface is accepted here;
-``EqualArmlengthOrbits`` is the analytic default (``lisatools``' file-based
-orbits are not available here).  Positions are evaluated on the host
-once per (N, T) and turned into a device table by ``gbx_orbit_table``.
+``EqualArmlengthOrbits`` is the analytic default and ``TabulatedOrbits``
+takes numerically integrated positions on a time grid (arrays or an ``.npz``
+file), as the file-based orbits of ``lisatools`` do.  Positions are
+evaluated on the host once per (N, T) and turned into a device table by
+``gbx_orbit_table``.
 """
 
 import numpy as np
@@ -54,3 +56,47 @@ class EqualArmlengthOrbits(Orbits):
         y = R * np.sin(alpha) + 0.5 * eR * (np.sin(2.0 * alpha - beta) - 3.0 * np.sin(beta))
         z = -np.sqrt(3.0) * eR * np.cos(alpha - beta)
         return np.stack([x, y, z], axis=-1)
+
+
+class TabulatedOrbits(Orbits):
+    """Spacecraft positions tabulated on a time grid, interpolated per
+    coordinate by a not-a-knot cubic spline (scipy.interpolate.CubicSpline).
+
+    ``t``: (T,) increasing times [s]; ``pos``: (3, T, 3) positions [m] of
+    spacecraft 1, 2, 3; ``armlength`` [m] (the nominal arm length the
+    transfer frequency uses).  Times outside the grid raise ValueError (the
+    waveform also checks T against ``t_base``).  The spline's error on a
+    heliocentric orbit sampled every h seconds is about (5/384) (2 pi h / yr)^4
+    R: ~400 m (1.3e-6 s of light travel time) for daily samples, ~2 m for
+    6-hourly ones.
+    """
+
+    def __init__(self, t, pos, armlength=2.5e9):
+        from scipy.interpolate import CubicSpline
+        t = np.asarray(t, dtype=np.float64)
+        pos = np.asarray(pos, dtype=np.float64)
+        if t.ndim != 1 or t.size < 4 or np.any(np.diff(t) <= 0):
+            raise ValueError("t must be increasing with at least 4 samples")
+        if pos.shape != (3, t.size, 3):
+            raise ValueError(f"pos must have shape (3, {t.size}, 3), got {pos.shape}")
+        self.armlength = float(armlength)
+        self.t_base = t
+        self._splines = [CubicSpline(t, pos[s], axis=0) for s in range(3)]
+
+    @classmethod
+    def from_file(cls, path):
+        """Load ``t``, ``pos`` and ``armlength`` from an ``.npz`` file."""
+        with np.load(path) as f:
+            return cls(f["t"], f["pos"], float(f["armlength"]) if "armlength" in f else 2.5e9)
+
+    def get_pos(self, t, sc):
+        t = np.asarray(t, dtype=np.float64)
+        if t.size and (t.min() < self.t_base[0] or t.max() > self.t_base[-1]):
+            raise ValueError("time outside the tabulated orbit")
+        sc = np.broadcast_to(np.asarray(sc), t.shape)
+        out = np.empty(t.shape + (3,))
+        for s in (1, 2, 3):
+            m = sc == s
+            if np.any(m):
+                out[m] = self._splines[s - 1](t[m])
+        return out

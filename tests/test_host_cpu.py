@@ -258,3 +258,28 @@ def test_c_abi_rejects_bad_arguments_before_touching_a_device():
                                     None) == ERR_ARG
     assert "workspace" in msg()
     assert lib.gbx_wave_workspace_bytes(0) == 0 and lib.gbx_wave_workspace_bytes(3) % 256 == 0
+
+
+def test_tabulated_orbits_interpolate_the_analytic_orbit(tmp_path):
+    """TabulatedOrbits (positions on a grid, cubic spline) reproduces the
+    analytic orbit it was sampled from to a few metres at 6-hour sampling,
+    loads from an .npz file, and refuses times outside its grid."""
+    from gbgpu_gb300.orbits import EqualArmlengthOrbits, TabulatedOrbits
+    ana = EqualArmlengthOrbits()
+    t = np.arange(0.0, 5 * 31557600.0, 21600.0)
+    pos = np.stack([ana.get_pos(t, np.full(t.size, s)) for s in (1, 2, 3)])
+    tab = TabulatedOrbits(t, pos, ana.armlength)
+    rng = np.random.default_rng(3)
+    tt = np.sort(rng.uniform(0, t[-1], 2000))
+    for s in (1, 2, 3):
+        err = np.abs(tab.get_pos(tt, np.full(tt.size, s)) - ana.get_pos(tt, np.full(tt.size, s)))
+        assert err.max() < 5.0, err.max()                        # metres (2e-8 s of light time)
+    mixed = tab.get_pos(tt[:6], np.array([1, 2, 3, 3, 2, 1]))
+    np.testing.assert_array_equal(mixed[2], tab.get_pos(tt[2:3], np.array([3]))[0])
+    np.savez(tmp_path / "orb.npz", t=t, pos=pos, armlength=ana.armlength)
+    f = TabulatedOrbits.from_file(tmp_path / "orb.npz")
+    np.testing.assert_array_equal(f.get_pos(tt[:5], np.ones(5, int)), tab.get_pos(tt[:5], np.ones(5, int)))
+    with pytest.raises(ValueError):
+        tab.get_pos(np.array([t[-1] + 1.0]), np.array([1]))
+    with pytest.raises(ValueError):
+        TabulatedOrbits(t, pos[:, :10])
