@@ -9,7 +9,7 @@ the same names and semantics.
 
 import numpy as np
 
-from .constants import C_SI, PI, YRSID_SI
+from .constants import C_SI, G, MSUN_SI, Mjup, PI, YRSID_SI
 from .gbgpu import GBGPUBase
 from .utility import get_fGW, get_N
 
@@ -110,8 +110,103 @@ class GBGPUThirdBody(GBGPUBase):
         return A2[:, None, None] * (np.sin(phi2 + varpi[:, None, None])
                                     + e2[:, None, None] * np.sin(varpi[:, None, None]))
 
+    def get_aLOS(self, A2, varpi, e2, P2, T2, t, eps=1e-9):
+        """Line-of-sight acceleration by a central difference of v_LOS with
+        step ``eps`` [s] at times ``t`` (B, ..., ...) [s]; P2 in years, T2 in
+        seconds (thirdbody.py:430-461).  The reference passes v_LOS's
+        arguments in another order than its signature; here they are passed
+        as that signature defines them."""
+        A2, varpi, e2, T2 = (np.atleast_1d(np.asarray(x, dtype=np.float64))
+                             for x in (A2, varpi, e2, T2))
+        n2 = 2 * np.pi / (np.atleast_1d(np.asarray(P2, dtype=np.float64)) * YRSID_SI)
+        t = np.asarray(t, dtype=np.float64)
+        up = self.get_vLOS(t + eps, A2, varpi, e2, n2, T2)
+        down = self.get_vLOS(t - eps, A2, varpi, e2, n2, T2)
+        return (up - down) / (2 * eps)
+
+    def get_f_derivatives(self, f0, fdot, fddot, A2, varpi, e2, P2, T2, t=None, eps=5e4):
+        """Instantaneous frequency f (1 + v_LOS/c) and its first and second
+        time derivatives by central differences (thirdbody.py:463-535).
+
+        ``t`` is (B, n, 3): per binary and evaluation point the times
+        ``[t_d - eps, t_d, t_d + eps]``; by default one point per binary at
+        t_d = 0.  P2 in years, T2 in seconds.  Returns (f, fdot, fddot), each
+        (B, n).  The reference differences along the binary axis and passes
+        v_LOS's arguments out of order; the differences here run along the
+        last (time) axis, as its docstring describes."""
+        A2, varpi, e2, T2, f0, fdot, fddot = (np.atleast_1d(np.asarray(x, dtype=np.float64))
+                                              for x in (A2, varpi, e2, T2, f0, fdot, fddot))
+        n2 = 2 * np.pi / (np.atleast_1d(np.asarray(P2, dtype=np.float64)) * YRSID_SI)
+        if t is None:
+            t = np.tile(np.array([-eps, 0.0, eps]), (len(A2), 1, 1))
+        elif not isinstance(t, (list, np.ndarray)):
+            raise ValueError("t must be a list or an np.ndarray")
+        t = np.asarray(t, dtype=np.float64)
+        assert t.ndim == 3 and t.shape[-1] == 3 and t.shape[0] == len(A2)
+        h = (t[..., 2] - t[..., 0]) / 2.0
+        ft = f0[:, None, None] + fdot[:, None, None] * t + 0.5 * fddot[:, None, None] * t * t
+        ft = ft * (1.0 + self.get_vLOS(t, A2, varpi, e2, n2, T2) / C_SI)
+        return (ft[..., 1], (ft[..., 2] - ft[..., 0]) / (2 * h),
+                (ft[..., 2] - 2 * ft[..., 1] + ft[..., 0]) / (h * h))
+
     def parab_step_ET(self, f0, fdot, fddot, A2, varpi, e2, n2, T2, t0, t0_old):
         dtt = t0 - t0_old
         g1 = self.get_vLOS(t0_old, A2, varpi, e2, n2, T2) * get_fGW(f0, fdot, fddot, t0_old)
         g3 = self.get_vLOS(t0, A2, varpi, e2, n2, T2) * get_fGW(f0, fdot, fddot, t0)
         return dtt * (g1 + g3) / 2.0 * PI * 2 / C_SI
+
+
+def get_T2(P2, e2, phi2, third_period_unit="yrs"):
+    """Time of pericentre T2 [yr] from the orbital phase phi2 (thirdbody.py:
+    648-684): u2 = 2 atan(sqrt((1-e2)/(1+e2)) tan(phi2/2)), T2 = (u2 - e2 sin u2)
+    / n2, moved into [0, P2) when negative.  ``P2`` in years ("yrs") or
+    seconds ("sec"); the caller's arrays are not modified."""
+    P2 = np.array(P2, dtype=np.float64, copy=True)
+    if third_period_unit == "yrs":
+        P2 *= YRSID_SI
+    elif third_period_unit != "sec":
+        raise NotImplementedError
+    u2 = 2.0 * np.arctan(np.sqrt((1 - e2) / (1 + e2)) * np.tan(phi2 / 2.0))
+    n2 = 2 * np.pi / P2
+    temp_T2 = (u2 - e2 * np.sin(u2)) / n2
+    return (temp_T2 / YRSID_SI) * (temp_T2 >= 0.0) + \
+        ((P2 - np.abs(temp_T2)) / YRSID_SI) * (temp_T2 < 0.0)
+
+
+def third_body_factors(M, mc, P2, e2, iota, Omega2, omega2, phi2, lam, beta,
+                       third_mass_unit="Mjup", third_period_unit="yrs"):
+    """(A2, varpi, T2) from the physical parameters of the third body
+    (thirdbody.py:538-645; Robson et al. 2018, arXiv:1806.00500): inner-binary
+    mass M [Msun], third-body mass mc ("Mjup" or "MSUN"), period P2 ("yrs" or
+    "sec"), eccentricity e2, orbital Euler angles iota, Omega2, omega2,
+    orbital phase phi2, sky position lam, beta.  Same formulas as the
+    reference (semi-major axis from the inner mass M, as there); the caller's
+    arrays are not modified (the reference scales M, mc and P2 in place)."""
+    M = np.array(M, dtype=np.float64, copy=True) * MSUN_SI
+    if third_mass_unit == "Mjup":
+        factor = Mjup
+    elif third_mass_unit == "MSUN":
+        factor = MSUN_SI
+    else:
+        raise NotImplementedError
+    mc = np.array(mc, dtype=np.float64, copy=True) * factor
+    P2 = np.array(P2, dtype=np.float64, copy=True)
+    if third_period_unit == "yrs":
+        P2 *= YRSID_SI
+    elif third_period_unit != "sec":
+        raise NotImplementedError
+    m2 = M + mc
+    theta = np.pi / 2 - beta
+    phi = lam
+    for x in (M, m2, iota, Omega2, omega2, phi2, theta, phi):
+        assert np.shape(x) == P2.shape
+    a2 = (G * M * P2 ** 2 / (4 * np.pi ** 2)) ** (1 / 3)
+    p2 = a2 * (1 - e2 ** 2)
+    C = np.cos(theta) * np.sin(iota) + np.sin(theta) * np.cos(iota) * np.sin(phi - Omega2)
+    S = np.sin(theta) * np.cos(phi - Omega2)
+    A_bar = np.sqrt(C ** 2 + S ** 2)
+    phi_bar = np.arctan(C / (-S))
+    omega_bar = (omega2 + phi_bar) % (2 * np.pi)
+    amp2 = (mc / m2) * np.sqrt(G * m2 / p2) * A_bar
+    T2 = get_T2(P2, e2, phi2, third_period_unit="sec")
+    return amp2, omega_bar, T2

@@ -199,6 +199,33 @@ def case_third(name, seed, B, N, T, dt, tdi2=False):
          dt=dt, tdi2=tdi2, XYZf=gb.XYZf, AETf=gb.AETf, start_inds=np.asarray(gb.start_inds))
 
 
+def case_third_converters(name, seed):
+    """The reference's third_body_factors and get_T2 on seeded inputs (copies:
+    the reference scales its M, mc and P2 arguments in place)."""
+    rng = np.random.default_rng(seed)
+    n = 16
+    M = rng.uniform(0.3, 1.5, n)
+    mc = 10 ** rng.uniform(0, 3, n)
+    P2 = 10 ** rng.uniform(-0.5, 1.5, n)
+    e2 = rng.uniform(0, 0.9, n)
+    iota = np.arccos(rng.uniform(-1, 1, n))
+    Omega2 = rng.uniform(0, 2 * np.pi, n)
+    omega2 = rng.uniform(0, 2 * np.pi, n)
+    phi2 = rng.uniform(-np.pi, np.pi, n)
+    lam = rng.uniform(0, 2 * np.pi, n)
+    beta = np.arcsin(rng.uniform(-1, 1, n))
+    A2, varpi, T2 = ref_third.third_body_factors(M.copy(), mc.copy(), P2.copy(), e2, iota,
+                                                 Omega2, omega2, phi2, lam, beta)
+    A2s, varpis, T2s = ref_third.third_body_factors(M.copy(), mc.copy() * 1e-3, P2.copy() * YRSID_SI,
+                                                    e2, iota, Omega2, omega2, phi2, lam, beta,
+                                                    third_mass_unit="MSUN",
+                                                    third_period_unit="sec")
+    T2_yrs = ref_third.get_T2(P2.copy(), e2, phi2)
+    save(name, M=M, mc=mc, P2=P2, e2=e2, iota=iota, Omega2=Omega2, omega2=omega2, phi2=phi2,
+         lam=lam, beta=beta, A2=A2, varpi=varpi, T2=T2, A2_msun=A2s, varpi_msun=varpis,
+         T2_msun=T2s, T2_yrs=T2_yrs)
+
+
 def case_kepler(name, seed):
     rng = np.random.default_rng(seed)
     gb = ref_third.GBGPUThirdBody()
@@ -290,6 +317,7 @@ if __name__ == "__main__":
     case_ll_third("ll_third", 18, B=6, N=256, T=TJ4, dt=5.0, tdi2=True)
     case_wave("wave_n4096", 19, B=1, N=4096, T=TJ4, dt=5.0, tdi2=False,
               f_lo=2.0e-2, f_hi=2.5e-2)
+    case_third_converters("third_converters", 20)
     case_kepler("kepler", 12)
     case_get_n("get_n", 13)
     case_misc("misc")
