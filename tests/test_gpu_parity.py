@@ -499,3 +499,35 @@ def test_tabulated_orbits_match_the_analytic_orbit(gbgpu):
     b.run_wave(*g["params"], **kw)
     np.testing.assert_array_equal(b.start_inds.cpu().numpy(), a.start_inds.cpu().numpy())
     assert np.max(rel_err(b.AETf.cpu().numpy(), a.AETf.cpu().numpy(), axis=(1, 2))) < 1e-6
+
+
+def test_out_of_range_rows_raise_and_leave_other_binaries_intact(gbgpu):
+    """A data_index / noise_index row outside the data or PSD arrays, or a
+    group_index outside the templates, is caught in the kernel (that binary is
+    skipped, GBX_FLAG_INDEX is set) and raised on the host as ValueError; the
+    other binaries' results are those of a call without the bad row."""
+    g = load_golden("ll_multi")                      # 3 data rows, 2 PSD rows, 10 binaries
+    gb = gbgpu()
+    gb.d_d = float(g["d_d"])
+    data = [dev(g["A_data"]), dev(g["E_data"])]
+    psd = [dev(g["A_psd"]), dev(g["E_psd"])]
+    kw = dict(N=int(g["N"]), T=float(g["T"]), dt=float(g["dt"]), tdi2=bool(g["tdi2"]),
+              start_freq_ind=int(g["start_freq_ind"]))
+    di, ni = g["data_index"].astype(np.int32), g["noise_index"].astype(np.int32)
+    gb.get_ll(g["params"], data, psd, data_index=dev(di), noise_index=dev(ni), **kw)
+    good = gb.d_h.cpu().numpy()
+    bad_di, bad_ni = di.copy(), ni.copy()
+    bad_di[3] = 7
+    bad_ni[3] = 7
+    for d_rows, n_rows in ((bad_di, ni), (di, bad_ni)):
+        with pytest.raises(ValueError, match="out of range"):
+            gb.get_ll(g["params"], data, psd, data_index=dev(d_rows), noise_index=dev(n_rows),
+                      **kw)
+        np.testing.assert_array_equal(np.delete(gb.d_h.cpu().numpy(), 3), np.delete(good, 3))
+    f = load_golden("fill_basic")
+    gi = f["group_index"].astype(np.int32).copy()
+    gi[0] = 99
+    t = dev(f["templates_before"]).clone()
+    with pytest.raises(ValueError, match="out of range"):
+        gb.fill_global_template(dev(gi), t, dev(f["A"]), dev(f["E"]), dev(f["start_inds"]),
+                                start_freq_ind=int(f["start_freq_ind"]))
