@@ -16,7 +16,8 @@ tdi_available = True
 
 
 def AET(X, Y, Z):
-    """(A, E, T) = ((Z - X)/sqrt2, (X - 2Y + Z)/sqrt6, (X + Y + Z)/sqrt3)."""
+    """(A, E, T) = ((Z - X)/sqrt2, (X - 2Y + Z)/sqrt6, (X + Y + Z)/sqrt3)
+    (gbgpu/utils/utility.py:24-38)."""
     return (
         (Z - X) / np.sqrt(2.0),
         (X - 2.0 * Y + Z) / np.sqrt(6.0),
@@ -25,7 +26,8 @@ def AET(X, Y, Z):
 
 
 def get_fGW(f0, fdot, fddot, t, xp=None):
-    """f(t) = f0 + fdot t + fddot t^2 / 2, broadcasting binaries along axis 0."""
+    """f(t) = f0 + fdot t + fddot t^2 / 2, broadcasting binaries along axis 0
+    (gbgpu/utils/utility.py:41-81)."""
     if xp is None:
         xp = np
     tdim = t.ndim
@@ -40,21 +42,26 @@ def get_fGW(f0, fdot, fddot, t, xp=None):
 
 
 def get_chirp_mass(m1, m2):
+    """(m1 m2)^(3/5) / (m1 + m2)^(1/5) (gbgpu/utils/utility.py:84-96)."""
     return (m1 * m2) ** (3 / 5) / (m1 + m2) ** (1 / 5)
 
 
 def get_eta(m1, m2):
+    """Symmetric mass ratio m1 m2 / (m1 + m2)^2 (gbgpu/utils/utility.py:99-111)."""
     return (m1 * m2) / (m1 + m2) ** 2
 
 
 def get_amplitude(m1, m2, f, d):
-    """Strain amplitude; masses in solar masses, f in Hz, d in kpc."""
+    """Strain amplitude; masses in solar masses, f in Hz, d in kpc
+    (gbgpu/utils/utility.py:114-130)."""
     Mc = get_chirp_mass(m1, m2) * MSUN_SI
     d = d * 1e3 * PC_SI
     return 2 * (G_SI * Mc) ** (5.0 / 3.0) / (C_SI ** 4 * d) * (np.pi * f) ** (2.0 / 3.0)
 
 
 def get_fdot(f, m1=None, m2=None, Mc=None):
+    """Quadrupole frequency derivative from component masses or the chirp
+    mass (solar masses) (gbgpu/utils/utility.py:133-169)."""
     if m1 is None and m2 is None and Mc is None:
         raise ValueError("Must provide either m1 & m2 or Mc.")
     elif m1 is not None or m2 is not None:
@@ -66,6 +73,8 @@ def get_fdot(f, m1=None, m2=None, Mc=None):
 
 
 def get_chirp_mass_from_f_fdot(f, fdot):
+    """Chirp mass (solar masses) from f and fdot, the inverse of get_fdot
+    (gbgpu/utils/utility.py:172-194)."""
     Mc_SI = (5.0 / 96.0 * np.pi ** (-8 / 3) * (G_SI / C_SI ** 3) ** (-5 / 3)
              * f ** (-11 / 3) * fdot) ** (3 / 5)
     return Mc_SI / MSUN_SI
@@ -136,6 +145,6 @@ def flops_per_binary(N, tdi2=False, third_body=False, likelihood=False):
 
 
 def cuda_set_device(dev):
-    """Select the CUDA device used by subsequent calls."""
+    """Select the CUDA device used by subsequent calls (gbgpu/utils/utility.py:276)."""
     import torch
     torch.cuda.set_device(dev)
