@@ -413,54 +413,67 @@ class GBGPUBase(abc.ABC):
 
     @property
     def X_out(self):
+        """X window, point-major flat (index i*B + b) (gbgpu.py:318-322)."""
         return self.XYZf[:, 0].T.flatten()
 
     @property
     def Y_out(self):
+        """Y window, point-major flat (gbgpu.py:323-327)."""
         return self.XYZf[:, 1].T.flatten()
 
     @property
     def Z_out(self):
+        """Z window, point-major flat (gbgpu.py:328-332)."""
         return self.XYZf[:, 2].T.flatten()
 
     @property
     def A_out(self):
+        """A window, point-major flat (gbgpu.py:333-337)."""
         return self.AETf[:, 0].T.flatten()
 
     @property
     def E_out(self):
+        """E window, point-major flat (gbgpu.py:338-342)."""
         return self.AETf[:, 1].T.flatten()
 
     @property
     def T_out(self):
+        """T window, point-major flat (gbgpu.py:343-346)."""
         return self.AETf[:, 2].T.flatten()
 
     @property
     def A(self):
+        """A windows (B, N) (gbgpu.py:542-546)."""
         return self.AETf[:, 0]
 
     @property
     def E(self):
+        """E windows (B, N) (gbgpu.py:547-551)."""
         return self.AETf[:, 1]
 
     @property
     def T(self):
+        """T windows (B, N) (gbgpu.py:552-556)."""
         return self.AETf[:, 2]
 
     @property
     def X(self):
+        """X windows (B, N) (gbgpu.py:557-561)."""
         return self.XYZf[:, 0]
 
     @property
     def Y(self):
+        """Y windows (B, N) (gbgpu.py:562-566)."""
         return self.XYZf[:, 1]
 
     @property
     def Z(self):
+        """Z windows (B, N) (gbgpu.py:567-571)."""
         return self.XYZf[:, 2]
 
     @property
     def freqs(self):
+        """Frequencies of the window bins, (start_inds + arange(N)) df, (B, N) (gbgpu.py:572-578)."""
         k = torch.arange(self.N, device=self.device)[None, :] + self.start_inds[:, None]
         return k.to(torch.float64) * self.df
 
@@ -1157,18 +1170,22 @@ class GBGPUBase(abc.ABC):
     # ----------------------------------------------------------------- hooks
     @abc.abstractmethod
     def add_to_argS(self, argS, f0, fdot, fddot, xi, *args):
+        """Abstract hook: add a model's phase term to argS (gbgpu.py:1141-1168)."""
         raise NotImplementedError
 
     @abc.abstractmethod
     def prepare_additional_args(self, *args):
+        """Abstract hook: convert a model's extra parameters (gbgpu.py:1170-1186)."""
         raise NotImplementedError
 
     @abc.abstractmethod
     def special_get_N(self, amp, f0, T, *args, oversample=1):
+        """Abstract hook: N for a model's extra parameters (gbgpu.py:1188-1212)."""
         raise NotImplementedError
 
     @abc.abstractmethod
     def shift_frequency(self, fi, xi, *args):
+        """Abstract hook: a model's shift of the instantaneous frequency (gbgpu.py:1214-1238)."""
         raise NotImplementedError
 
 
@@ -1176,15 +1193,19 @@ class GBGPU(GBGPUBase):
     """Circular Galactic binaries (reference gbgpu/gbgpu.py:1233-1327)."""
 
     def prepare_additional_args(self, *args):
+        """No extra parameters: extra arguments are an error (gbgpu.py:1240-1257)."""
         raise ValueError(
             "If providing more args than the base args, must be a class derived from GBGPUBase "
             "with an adjusted 'prepare_additional_args' method.")
 
     def special_get_N(self, amp, f0, T, *args, oversample=1):
+        """get_N's band table and SNR bump (gbgpu.py:1259-1282)."""
         return get_N(amp, f0, T, oversample=oversample)
 
     def shift_frequency(self, fi, xi, *args):
+        """No shift of the instantaneous frequency (gbgpu.py:1284-1299)."""
         return fi
 
     def add_to_argS(self, argS, f0, fdot, fddot, xi, *args):
+        """No extra phase term (gbgpu.py:1301-1327)."""
         return argS
