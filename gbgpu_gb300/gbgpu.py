@@ -235,30 +235,37 @@ class GBGPUBase(abc.ABC):
     # ------------------------------------------------------------- plumbing
     @property
     def backend(self):
+        """The backend method table (get_ll, fill_global, xp)."""
         return self._backend
 
     @property
     def xp(self):
+        """The array module of the backend (torch here; CuPy/NumPy in the reference)."""
         return torch
 
     @classmethod
     def supported_backends(cls):
+        """Backends this class runs on (gbgpu.py:72-74): the GB300 CUDA build only."""
         return ["gpu"]
 
     @property
     def get_ll_func(self):
+        """The backend's native get_ll (gbgpu.py:76-79)."""
         return self.backend.get_ll
 
     @property
     def fill_global_func(self):
+        """The backend's native fill_global (gbgpu.py:81-84)."""
         return self.backend.fill_global
 
     @property
     def orbits(self):
+        """The spacecraft orbits (gbgpu.py:86-90)."""
         return self._orbits
 
     @orbits.setter
     def orbits(self, orbits):
+        """Set the orbits; None selects the analytic EqualArmlengthOrbits (gbgpu.py:91-101)."""
         if orbits is None:
             self._orbits = EqualArmlengthOrbits()
         elif not (hasattr(orbits, "get_pos") and hasattr(orbits, "armlength")):
@@ -271,6 +278,7 @@ class GBGPUBase(abc.ABC):
 
     @property
     def citation(self):
+        """References to cite (gbgpu.py:103-106)."""
         return ("Katz et al. arXiv:2205.03461; Cornish & Littenberg arXiv:0704.1808; "
                 "Robson et al. arXiv:1806.00500")
 
@@ -382,6 +390,7 @@ class GBGPUBase(abc.ABC):
 
     @property
     def XYZf(self):
+        """X, Y, Z windows (B, 3, N), computed on first access after a fused call."""
         self._materialize()
         return self._XYZf
 
@@ -391,6 +400,7 @@ class GBGPUBase(abc.ABC):
 
     @property
     def AETf(self):
+        """A, E, T windows (B, 3, N), computed on first access after a fused call."""
         self._materialize()
         return self._AETf
 
@@ -400,6 +410,7 @@ class GBGPUBase(abc.ABC):
 
     @property
     def start_inds(self):
+        """First frequency bin of each window (B,), bit-exact with the reference (gbgpu.py:296-307)."""
         self._materialize()
         return self._start_inds
 
@@ -409,6 +420,7 @@ class GBGPUBase(abc.ABC):
 
     @property
     def kmin(self):
+        """Alias of start_inds."""
         return self.start_inds
 
     @property
