@@ -13,12 +13,14 @@ import torch
 class _LogLikelihood(torch.autograd.Function):
     @staticmethod
     def forward(ctx, params, gb, data, psd, kwargs):
+        """Likelihood and its gradient in one fused launch; the gradient is kept for backward."""
         like, grad = gb._ll_grad_tensors(params.detach(), data, psd, **kwargs)
         ctx.save_for_backward(grad)
         return like
 
     @staticmethod
     def backward(ctx, g):
+        """Chain rule: d like / d params scaled by the incoming gradient per binary."""
         (grad,) = ctx.saved_tensors
         return grad * g.to(grad.dtype)[None, :], None, None, None, None
 

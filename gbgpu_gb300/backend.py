@@ -42,6 +42,7 @@ class GB300Backend:
 
     def get_ll(self, d_h, h_h, A_template, E_template, A_data, E_data, A_psd, E_psd, df,
                start_ind, M, num_bin, data_index, noise_index, data_length, status=None):
+        """gbx_get_ll with the reference's method-table arguments (gbgpu_utils_wrap.pyx:20-48)."""
         rc = self._lib.gbx_get_ll(
             _addr(d_h), _addr(h_h), _addr(A_template), _addr(E_template), _addr(A_data),
             _addr(E_data), _addr(A_psd), _addr(E_psd), float(df), _addr(start_ind), int(M),
@@ -51,6 +52,7 @@ class GB300Backend:
 
     def fill_global(self, A_glob, E_glob, A_template, E_template, start_ind, M, num_bin,
                     group_index, data_length, status=None):
+        """gbx_fill_global with the reference's method-table arguments (gbgpu_utils_wrap.pyx:51-69)."""
         rc = self._lib.gbx_fill_global(
             _addr(A_glob), _addr(E_glob), _addr(A_template), _addr(E_template),
             _addr(start_ind), int(M), int(num_bin), _addr(group_index), int(data_length),
@@ -74,6 +76,7 @@ def get_backend(name=None):
 
 
 def has_backend(name):
+    """True when get_backend(name) succeeds (a CUDA device and the library)."""
     try:
         get_backend(name)
         return True

@@ -29,15 +29,21 @@ def _budget(f):
 
 
 class X1TDISens:
+    """TDI 1.5 X-channel PSD (the S_X formula above)."""
+
     @staticmethod
     def get_Sn(f, **kwargs):
+        """S_X(f) in fractional-frequency units; extra keywords are ignored."""
         s_op, s_pm, x = _budget(f)
         return 16.0 * np.sin(x) ** 2 * (s_op + 2.0 * (1.0 + np.cos(x) ** 2) * s_pm)
 
 
 class A1TDISens:
+    """TDI 1.5 A/E-channel PSD (the S_A formula above)."""
+
     @staticmethod
     def get_Sn(f, **kwargs):
+        """S_A(f) = S_E(f) in fractional-frequency units; extra keywords are ignored."""
         s_op, s_pm, x = _budget(f)
         return 8.0 * np.sin(x) ** 2 * (
             (2.0 + np.cos(x)) * s_op

@@ -15,10 +15,15 @@ from .utility import get_fGW, get_N
 
 
 class GBGPUThirdBody(GBGPUBase):
+    """GBGPU with a third body on an eccentric orbit around the binary
+    (thirdbody.py:22-428): five more parameters, A2, varpi, e2, P2 [yr] and
+    T2 [yr]."""
+
     NPARAMS = 14
 
     @property
     def citation(self):
+        """References to cite (thirdbody.py:34-37)."""
         return super().citation
 
     def prepare_additional_args(self, A2, varpi, e2, P2, T2):
@@ -51,10 +56,12 @@ class GBGPUThirdBody(GBGPUBase):
 
     # ---- host-side hooks (the CUDA kernel has its own fused versions) ----
     def shift_frequency(self, fi, xi, A2, varpi, e2, n2, T2):
+        """fi (1 + v_LOS(xi)/c) (thirdbody.py:155-180)."""
         fi *= 1 + self.get_vLOS(xi, A2, varpi, e2, n2, T2) / C_SI
         return fi
 
     def add_to_argS(self, argS, f0, fdot, fddot, xi, A2, varpi, e2, n2, T2):
+        """argS plus the trapezoid-integrated Doppler phase along the samples (thirdbody.py:182-226)."""
         term = np.zeros_like(xi)
         term[:, :, 1:] = np.cumsum(
             self.parab_step_ET(f0, fdot, fddot, A2, varpi, e2, n2, T2, xi[:, :, 1:], xi[:, :, :-1]),
@@ -97,6 +104,7 @@ class GBGPUThirdBody(GBGPUBase):
         return np.where(neg, -u, u)
 
     def get_phi(self, t, T, e, n):
+        """True anomaly at times t from the Kepler solution (thirdbody.py:322-350)."""
         u = self.get_u(n[:, None, None] * (t - T[:, None, None]),
                        np.broadcast_to(e[:, None, None], t.shape))
         ee = np.broadcast_to(e[:, None, None], t.shape)
@@ -106,6 +114,7 @@ class GBGPUThirdBody(GBGPUBase):
         return np.where(adjust, u + 2.0 * np.arctan2(beta * np.sin(u), 1.0 - beta * np.cos(u)), u)
 
     def get_vLOS(self, t, A2, varpi, e2, n2, T2):
+        """Line-of-sight velocity A2 (sin(phi + varpi) + e2 sin varpi) (thirdbody.py:352-380)."""
         phi2 = self.get_phi(t, T2, e2, n2)
         return A2[:, None, None] * (np.sin(phi2 + varpi[:, None, None])
                                     + e2[:, None, None] * np.sin(varpi[:, None, None]))
@@ -150,6 +159,7 @@ class GBGPUThirdBody(GBGPUBase):
                 (ft[..., 2] - 2 * ft[..., 1] + ft[..., 0]) / (h * h))
 
     def parab_step_ET(self, f0, fdot, fddot, A2, varpi, e2, n2, T2, t0, t0_old):
+        """One trapezoid step of the Doppler phase between t0_old and t0 (thirdbody.py:382-428)."""
         dtt = t0 - t0_old
         g1 = self.get_vLOS(t0_old, A2, varpi, e2, n2, T2) * get_fGW(f0, fdot, fddot, t0_old)
         g3 = self.get_vLOS(t0, A2, varpi, e2, n2, T2) * get_fGW(f0, fdot, fddot, t0)
