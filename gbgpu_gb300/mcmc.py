@@ -21,6 +21,10 @@ import torch
 
 
 class SwapSampler:
+    """Ensemble swap sampler over W walkers of K sources each (see the module
+    docstring): one swap-likelihood launch and one residual update per step,
+    any number of steps captured as one CUDA graph."""
+
     def __init__(self, gb, params, data, psd, N, T, dt, start_freq_ind, tdi2=False,
                  precision="mixed"):
         """``params``: (nparams, W, K) FP64 CUDA tensor of the current sources;
@@ -97,6 +101,7 @@ class SwapSampler:
         return self.graph
 
     def replay(self):
+        """Replay the captured graph (all its steps)."""
         self.graph.replay()
 
     def log_likelihood(self):
@@ -120,6 +125,7 @@ def random_proposals(params_k, scale, gen):
 
 
 def log_uniforms(W, steps, gen, device):
+    """(steps, W) logs of uniforms in (0, 1], clamped away from log 0."""
     u = torch.rand((steps, W), generator=gen, device=device, dtype=torch.float64)
     return torch.log(u.clamp_min(math.ldexp(1.0, -60)))
 
@@ -248,6 +254,7 @@ class HMCSampler:
         return self.graph
 
     def replay(self):
+        """Replay the captured graph (all its steps)."""
         self.graph.replay()
 
 
@@ -414,4 +421,5 @@ class StretchSampler:
         return self.graph
 
     def replay(self):
+        """Replay the captured graph (all its steps)."""
         self.graph.replay()
