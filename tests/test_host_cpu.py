@@ -283,3 +283,30 @@ def test_tabulated_orbits_interpolate_the_analytic_orbit(tmp_path):
         tab.get_pos(np.array([t[-1] + 1.0]), np.array([1]))
     with pytest.raises(ValueError):
         TabulatedOrbits(t, pos[:, :10])
+
+
+def test_n_array_key_reuse_and_verification_flags():
+    """GBGPUBase._n_key: a new buffer gets its full content key at once; the
+    same buffer with the same 64 sampled entries reuses the key and asks for
+    verification after the launch; a change at a sampled entry, another
+    length or another buffer computes the key at once again."""
+    from gbgpu_gb300.gbgpu import GBGPU, _array_key
+    gb = object.__new__(GBGPU)                 # host logic only: no device state
+    gb._n_last = None
+    Ns = (2 ** np.random.default_rng(2).integers(5, 12, 1000)).astype(np.int64)
+    key, verify = gb._n_key(Ns)
+    assert key == _array_key(Ns) and not verify
+    key2, verify = gb._n_key(Ns)
+    assert key2 == key and verify                  # same buffer, same samples
+    Ns[1] = 64 if Ns[1] != 64 else 128             # not a sampled entry (step 15)
+    key3, verify = gb._n_key(Ns)
+    assert verify and key3 == key                  # stale until verified after the launch
+    assert _array_key(Ns) != key                   # ... which is why the call verifies it
+    Ns[15] = 64 if Ns[15] != 64 else 128           # a sampled entry
+    key4, verify = gb._n_key(Ns)
+    assert not verify and key4 == _array_key(Ns)
+    other = Ns.copy()                              # same content, another buffer
+    key5, verify = gb._n_key(other)
+    assert not verify and key5 == key4
+    key6, verify = gb._n_key(Ns[:500].copy())      # another length
+    assert not verify
