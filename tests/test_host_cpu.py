@@ -4,6 +4,7 @@ import ctypes
 import os
 import re
 import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -310,3 +311,24 @@ def test_n_array_key_reuse_and_verification_flags():
     assert not verify and key5 == key4
     key6, verify = gb._n_key(Ns[:500].copy())      # another length
     assert not verify
+
+
+def test_reference_arm_json_line_on_cpu():
+    """`bench.py --impl reference` (the oracle port timed on the host cores)
+    needs no GPU and prints one JSON line with the contract's keys."""
+    import json
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
+                        "--steps", "1", "--warmup", "1"], capture_output=True, text=True,
+                       timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [x for x in r.stdout.splitlines() if x.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+              "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config", "e2e",
+              "cpu_baseline"):
+        assert k in d, k
+    assert d["impl"] == "reference" and d["unit"] == "binaries/s" and d["value"] > 0
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
+    assert "workload" in d["config"]
