@@ -332,3 +332,23 @@ def test_reference_arm_json_line_on_cpu():
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
     assert "workload" in d["config"]
+
+
+def test_N_none_resolves_to_the_batch_maximum_as_the_reference():
+    """run_wave / get_ll with N=None take special_get_N's largest N over the
+    batch (gbgpu.py:204-206), with oversample applied; for the third body the
+    five extra parameters go to its special_get_N."""
+    from gbgpu_gb300 import GBGPU, GBGPUThirdBody
+    from gbgpu_gb300.constants import YRSID_SI
+    g = load_golden("get_n")
+    gb = object.__new__(GBGPU)                     # host logic only
+    for os_ in (1, 2, 4):
+        N = gb._resolve_N(None, g["amp"], g["f0"], 4.0 * YRSID_SI, (), os_)
+        assert N == int(np.max(g[f"N_{4.0 * YRSID_SI:.1f}_{os_}"]))
+    tb = object.__new__(GBGPUThirdBody)
+    extra = (np.ones(64), np.zeros(64), np.zeros(64), g["P2"], np.zeros(64))
+    assert tb._resolve_N(None, g["amp"], g["f0"], 4 * YRSID_SI, extra, 2) == int(np.max(g["third_N"]))
+    # an explicit N passes through; an array stays per binary
+    assert gb._resolve_N(256, g["amp"], g["f0"], YRSID_SI, (), 1) == 256
+    Ns = gb._resolve_N(np.full(64, 128), g["amp"], g["f0"], YRSID_SI, (), 1)
+    assert Ns.dtype == np.int64 and Ns.shape == (64,)
