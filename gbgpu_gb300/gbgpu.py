@@ -305,17 +305,23 @@ class GBGPUBase(abc.ABC):
                 f"Observation time ({T}) is larger than length of time in orbital information "
                 f"({np.max(self.orbits.t_base)})")
 
-    def _plan(self, N, T, precision, tdi2, nparams, tile=0, blocks_per_sm=0, nkey=None):
+    def _plan(self, N, T, precision, tdi2, nparams, tile=0, blocks_per_sm=0, nkey=None,
+              trusted=True):
         """WavePlan cache: tile schedules and orbit tables are built once per
         distinct (N or N-array contents, T, precision, tdi2, nparams, launch
-        shape)."""
+        shape).  ``nkey`` is the N array's content key when the caller has it;
+        with ``trusted=False`` it is the previous call's key for the same
+        buffer, not yet verified against the contents, and serves only to find
+        an existing plan: a new plan is always filed under the key of the
+        contents it was built from."""
         if np.ndim(N) == 0:
             key = (int(N), float(T), precision, bool(tdi2), nparams, tile, blocks_per_sm)
         else:
             arr = np.ascontiguousarray(N, dtype=np.int64)
-            key = (_array_key(arr) if nkey is None else nkey, arr.shape[0], float(T), precision,
-                   bool(tdi2), nparams, tile,
-                   blocks_per_sm)
+            rest = (arr.shape[0], float(T), precision, bool(tdi2), nparams, tile, blocks_per_sm)
+            if nkey is None or (not trusted and (nkey,) + rest not in self._plans):
+                nkey = _array_key(arr)
+            key = (nkey,) + rest
         plan = self._plans.pop(key, None)
         if plan is None:
             # least recently used plans go first; a plan stays alive while any
@@ -523,15 +529,21 @@ class GBGPUBase(abc.ABC):
         noise_index = _to_device(noise_index, torch.int32, self.device).contiguous()
         return dd, pp, data_length, data_index, noise_index
 
-    def _launch_shape(self, kind, N, B, precision, tdi2, nparams, run, nkey=None):
+    def _launch_shape(self, kind, N, B, precision, tdi2, nparams, run, nkey=None, trusted=True):
         """(tile, blocks_per_sm) for this workload: the autotuner's choice when
-        autotuning is on (timing ``run`` on the first call), else defaults."""
+        autotuning is on (timing ``run`` on the first call), else defaults.
+        An unverified ``nkey`` (``trusted=False``) only looks up a cached
+        shape; a shape tuned now is filed under the contents' own key."""
         if not self.autotune:
             return 0, 0
         if nkey is None:
             nkey = int(N) if np.ndim(N) == 0 else _array_key(np.ascontiguousarray(N, dtype=np.int64))
         ck = (kind, nkey, int(B), precision, bool(tdi2), int(nparams))
         shape = self._shapes.get(ck)
+        if shape is None and not trusted and np.ndim(N) != 0:
+            nkey = _array_key(np.ascontiguousarray(N, dtype=np.int64))
+            ck = (kind, nkey, int(B), precision, bool(tdi2), int(nparams))
+            shape = self._shapes.get(ck)
         if shape is None:
             from .autotune import default_tuner, workload_key
             shape = default_tuner().tune(workload_key(kind, N, B, precision, tdi2, nparams), run)
@@ -568,13 +580,15 @@ class GBGPUBase(abc.ABC):
             nkey, verify = self._n_key(arr)
 
         def run(tile, bps):
-            plan = self._plan(N, T, precision, tdi2, nparams, tile, bps, nkey=nkey)
+            plan = self._plan(N, T, precision, tdi2, nparams, tile, bps, nkey=nkey,
+                              trusted=not verify)
             a = plan.args(params, start_freq_ind, self._status)
             rc = nat.lib().gbx_waveform_ll(ctypes.byref(a), ctypes.byref(la), nat.ptr(d_h),
                                            nat.ptr(h_h), nat.stream_handle())
             nat.check(rc, "gbx_waveform_ll")
 
-        shape = self._launch_shape("ll", N, B, precision, tdi2, nparams, run, nkey=nkey)
+        shape = self._launch_shape("ll", N, B, precision, tdi2, nparams, run, nkey=nkey,
+                                   trusted=not verify)
         self._status.zero_()
         run(*shape)
         if verify:
@@ -583,6 +597,7 @@ class GBGPUBase(abc.ABC):
             # its outputs replace the first launch's before anyone reads them)
             full = _array_key(arr)
             self._n_last = self._n_last[:3] + (full,)
+            verify = False
             if full != nkey:
                 nkey = full
                 shape = self._launch_shape("ll", N, B, precision, tdi2, nparams, run, nkey=nkey)

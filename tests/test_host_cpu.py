@@ -313,6 +313,57 @@ def test_n_array_key_reuse_and_verification_flags():
     assert not verify
 
 
+def test_unverified_n_key_never_files_a_new_plan(monkeypatch):
+    """An N array changed in place at an unsampled entry comes back with the
+    previous call's (stale) key.  When that key misses the plan cache (here:
+    another precision), the plan built from the new contents must be filed
+    under the new contents' key; otherwise a later call whose array holds the
+    old contents would get a tile schedule for other N values."""
+    import gbgpu_gb300.gbgpu as G
+    from gbgpu_gb300 import autotune
+
+    class FakePlan:
+        def __init__(self, owner, N, T, precision, tdi2=False, nparams=9, tile=0,
+                     blocks_per_sm=0):
+            self.N = np.array(N, copy=True)
+            self.precision = precision
+
+    class FakeTuner:
+        def tune(self, key, run):
+            return (128, 0)
+
+    monkeypatch.setattr(G, "WavePlan", FakePlan)
+    monkeypatch.setattr(autotune, "default_tuner", lambda: FakeTuner())
+    gb = object.__new__(G.GBGPU)
+    gb._plans, gb._shapes, gb._n_last, gb.autotune = {}, {}, None, True
+    T = 1e8
+    Ns = (2 ** np.random.default_rng(3).integers(5, 12, 1000)).astype(np.int64)
+    original = Ns.copy()
+    key, verify = gb._n_key(Ns)
+    assert not verify
+    p1 = gb._plan(Ns, T, "mixed", False, 9, nkey=key, trusted=True)
+    np.testing.assert_array_equal(p1.N, original)
+    Ns[1] = 64 if Ns[1] != 64 else 128               # unsampled entry, same buffer
+    stale, verify = gb._n_key(Ns)
+    assert verify and stale == key
+    p2 = gb._plan(Ns, T, "fp64", False, 9, nkey=stale, trusted=False)   # cache miss
+    np.testing.assert_array_equal(p2.N, Ns)
+    assert (G._array_key(Ns), len(Ns), T, "fp64", False, 9, 0, 0) in gb._plans
+    assert (stale, len(Ns), T, "fp64", False, 9, 0, 0) not in gb._plans
+    # a hit under the stale key is still allowed (the launch is verified afterwards)
+    assert gb._plan(Ns, T, "mixed", False, 9, nkey=stale, trusted=False) is p1
+    # the old contents at a new address get a plan built from the old contents
+    again = original.copy()
+    k_old, _ = gb._n_key(again)
+    p3 = gb._plan(again, T, "fp64", False, 9, nkey=k_old, trusted=True)
+    np.testing.assert_array_equal(p3.N, original)
+    # launch shapes: a shape tuned under an unverified key is filed under the contents' key
+    gb._n_key(Ns)
+    gb._launch_shape("ll", Ns, len(Ns), "mixed", False, 9, None, nkey=stale, trusted=False)
+    assert ("ll", G._array_key(Ns), len(Ns), "mixed", False, 9) in gb._shapes
+    assert ("ll", stale, len(Ns), "mixed", False, 9) not in gb._shapes
+
+
 def test_reference_arm_json_line_on_cpu():
     """`bench.py --impl reference` (the oracle port timed on the host cores)
     needs no GPU and prints one JSON line with the contract's keys."""
