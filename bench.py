@@ -8,16 +8,20 @@ fdot log-U(1e-18, 1e-15), fddot = 11/3 fdot^2/f0, angles isotropic; T = 4 x
 Gaussian noise drawn from the analytic A/E PSD on the full 0-0.1 Hz grid
 (L = 12,623,041 bins, A and E, complex128).  Synthetic, seeded.
 
-``value``: binaries/s of the mixed-precision fused kernel (one persistent
-work-queue launch per step; parameters, data and PSD resident in HBM).
+``value``: binaries/s of the pair-form fused kernel (slow part, FFT and
+<d|h> in float-pair arithmetic on the FP32 pipe; one persistent work-queue
+launch per step; parameters, data and PSD resident in HBM), the form whose
+log-likelihood stays within 1e-6 max(1, <h|h>) of FP64 on this crowded data.
 ``e2e``: the same metric through ``GBGPU.get_ll`` with the parameters copied
-from pinned host memory every step and the log-likelihoods read back.
-The plain-FP64 form of the same kernel is timed on the same batch
-(``fp64_binaries_per_s``).  ``--impl reference`` times the reference's CPU
-path (its algorithm restated in the oracle) on the host cores instead.
+from pinned host memory every step and the log-likelihoods read back.  The
+plain-FP64 and the FP32 mixed forms of the same kernel are timed on the same
+batch (``fp64_binaries_per_s``, ``mixed_fp32_binaries_per_s``).
+``--impl reference`` times the reference's CPU path (its algorithm restated
+in the oracle) on the host cores instead, over the whole batch per step.
 """
 
 import argparse
+import contextlib
 import json
 import os
 import subprocess
@@ -61,7 +65,9 @@ def alg_bytes(Ns):
 
 
 class ClockSampler:
-    """nvidia-smi SM clock / throttle sampling while the timed region runs."""
+    """nvidia-smi SM clock / throttle sampling while the timed region runs
+    (every 20 ms; entering waits for the first sample, and only samples taken
+    after that count)."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -80,10 +86,14 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "100"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            t0 = time.perf_counter()
+            while not self.rows and time.perf_counter() - t0 < 5.0 and self.proc.poll() is None:
+                time.sleep(0.005)
+            self.rows = []
         except OSError:
             self.proc = None
         return self
@@ -114,81 +124,145 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ CPU side
-def _cpu_warm(_):
+_SHARED = {}
+
+
+def _cpu_init(spec):
+    """Pool initializer: attach the A/E data and PSD (shared memory written by
+    the parent) and load the oracle's C loops, once per worker."""
+    from multiprocessing import shared_memory
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import fastgb_oracle as O
     O._lib()
+    for key, (name, dtype, n) in spec.items():
+        # the parent created the segment and unlinks it (the workers share its
+        # resource tracker)
+        shm = shared_memory.SharedMemory(name=name)
+        _SHARED[key] = (shm, np.ndarray((n,), dtype=np.dtype(dtype), buffer=shm.buf))
+
+
+def _cpu_noop(_):
     return 0
 
 
 def _cpu_task(args):
-    """One oracle chunk: waveform (NumPy) + native get_ll (C) for binaries of
-    one N whose windows lie in the given data slice."""
-    import time as _t
+    """One chunk of binaries of one N (sorted by f0): the oracle's NumPy
+    waveform and its C likelihood loop against the resident data window
+    [a, b).  Returns the number of binaries."""
+    import fastgb_oracle as O
+    p, N, a, b = args
+    dA, dE, S = (_SHARED[k][1] for k in ("dA", "dE", "S"))
+    O.get_ll(p, [dA[a:b], dE[a:b]], [S[a:b], S[a:b]], N, T=T_OBS, dt=DT, start_freq_ind=a)
+    return p.shape[1]
+
+
+def _cpu_inject_task(args):
+    """The A/E windows of one chunk summed into one slice [a, b) of the grid
+    (the oracle's waveform and its scatter-add loop)."""
+    import fastgb_oracle as O
+    p, N = args
+    w = O.waveform(p, N, T=T_OBS, dt=DT)
+    si = w["start_inds"]
+    a, b = int(si.min()), int(si.max()) + N
+    tA = np.zeros(b - a, np.complex128)
+    tE = np.zeros(b - a, np.complex128)
+    B = p.shape[1]
+    O.fill_global_native(tA, tE, O.point_major(w["AETf"][:, 0]), O.point_major(w["AETf"][:, 1]),
+                         (si - a).astype(np.int32), N, B, np.zeros(B, np.int32), b - a)
+    return a, tA, tE
+
+
+def cpu_tasks(p, Ns, idx, with_window=True):
+    """Tasks over the binaries ``idx``: per N (largest first), sorted by f0,
+    about 32k samples each (NumPy's (B, 3, N) temporaries stay cache-sized)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import fastgb_oracle as O
-    p, N, dA, dE, S, s0 = args
-    t0 = _t.perf_counter()
-    O.get_ll(p, [dA, dE], [S, S], N, T=T_OBS, dt=DT, start_freq_ind=s0)
-    return _t.perf_counter() - t0, p.shape[1]
-
-
-CPU_SAMPLE = (25600, 25600, 12800, 6400, 3200, 2400)   # ~10 s of CPU work in total
-
-
-def cpu_baseline(p, Ns, dA, dE, S, workers, per_class=CPU_SAMPLE, pool=None):
-    """Times the oracle port on a bounded sample of every N class with a spawn
-    pool of ``workers`` processes and extrapolates to the workload's N mix."""
-    import multiprocessing as mp
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import fastgb_oracle as O
-    O._lib()                                  # build/load before the pool starts
+    L = int(int(T_OBS / DT) / 2) + 1
     tasks = []
-    sample = {}
-    for (lo, hi, n), m in zip(BANDS, per_class):
-        idx = np.nonzero(Ns == n)[0][:m]
-        idx = idx[np.argsort(p[1, idx])]
-        sample[n] = len(idx)
-        # ~32k samples of work per task: NumPy's (B, 3, N) temporaries stay
-        # cache-sized, the fastest way to run the oracle on these cores
+    for n in sorted(np.unique(Ns[idx]).tolist(), reverse=True):
+        sel = idx[Ns[idx] == n]
+        sel = sel[np.argsort(p[1, sel], kind="stable")]
         chunk = max(8, 32768 // n)
-        for c in range(0, len(idx), chunk):
-            sel = idx[c:c + chunk]
-            si = O.start_indices(p[1, sel], n, T_OBS, DT)
-            a, b = int(si.min()) - 1, int(si.max()) + n + 1
-            tasks.append((p[:, sel].copy(), n, dA[a:b].copy(), dE[a:b].copy(), S[a:b].copy(), a))
-    own = pool is None
-    if own:
-        pool = mp.get_context("spawn").Pool(workers)
-        pool.map(_cpu_warm, range(workers), chunksize=1)     # imports done before timing
-    try:
+        for c in range(0, len(sel), chunk):
+            s = sel[c:c + chunk]
+            if not with_window:
+                tasks.append((p[:, s].copy(), int(n)))
+                continue
+            si = O.start_indices(p[1, s], n, T_OBS, DT)
+            tasks.append((p[:, s].copy(), int(n), max(0, int(si.min()) - 1),
+                          min(L, int(si.max()) + n + 1)))
+    return tasks
+
+
+class CpuPool:
+    """Spawn pool over the host cores with the A/E data and PSD resident in
+    shared memory: each timed pass sends only parameters."""
+
+    def __init__(self, dA, dE, S, workers):
+        import multiprocessing as mp
+        from multiprocessing import shared_memory
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import fastgb_oracle as O
+        O._lib()                              # build the C loops before the workers start
+        self.shm, spec = [], {}
+        self.arrays = {}
+        for key, arr in (("dA", dA), ("dE", dE), ("S", S)):
+            shm = shared_memory.SharedMemory(create=True, size=max(1, arr.nbytes))
+            view = np.ndarray(arr.shape, arr.dtype, buffer=shm.buf)
+            view[:] = arr
+            self.shm.append(shm)
+            self.arrays[key] = view
+            spec[key] = (shm.name, arr.dtype.str, arr.shape[0])
+        self.workers = workers
+        self.pool = mp.get_context("spawn").Pool(workers, initializer=_cpu_init, initargs=(spec,))
+        self.pool.map(_cpu_noop, range(4 * workers), chunksize=1)
+
+    def inject(self, p, Ns):
+        """Add the sum of all binaries' A/E windows to the resident data."""
+        for a, tA, tE in self.pool.imap_unordered(
+                _cpu_inject_task, cpu_tasks(p, Ns, np.arange(p.shape[1]), False)):
+            self.arrays["dA"][a:a + len(tA)] += tA
+            self.arrays["dE"][a:a + len(tE)] += tE
+
+    def run(self, tasks):
+        """One pass over ``tasks``: (wall seconds, binaries)."""
         t0 = time.perf_counter()
-        res = pool.map(_cpu_task, tasks, chunksize=1)
-        wall = time.perf_counter() - t0
+        n = sum(self.pool.map(_cpu_task, tasks, chunksize=1))
+        return time.perf_counter() - t0, n
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
+        self.arrays = {}
+        for shm in self.shm:
+            shm.close()
+            shm.unlink()
+
+
+def cpu_baseline(p, Ns, dA, dE, S, workers, stride=2):
+    """The oracle port (the reference's algorithm: NumPy waveform + the C
+    likelihood loop) on every ``stride``-th binary of the batch (the same N
+    mix) with the data resident in the workers; one warm-up pass, one timed."""
+    pool = CpuPool(dA, dE, S, workers)
+    try:
+        idx = np.arange(0, p.shape[1], stride)
+        tasks = cpu_tasks(p, Ns, idx)
+        pool.run(tasks[:: max(1, len(tasks) // (4 * workers))])
+        wall, n = pool.run(tasks)
     finally:
-        if own:
-            pool.close()
-            pool.join()
-    busy = {}
-    for (task, (dt_, nb)) in zip(tasks, res):
-        busy[task[1]] = busy.get(task[1], 0.0) + dt_
-    per_bin = {n: busy[n] / sample[n] for n in busy}
-    total_cpu = sum(per_bin[n] * np.count_nonzero(Ns == n) for n in per_bin)
-    eff = sum(busy.values()) / wall                    # effective parallel workers
-    value = len(Ns) / (total_cpu / max(eff, 1e-9))
-    return {"value": value, "unit": "binaries/s", "cores": int(workers), "kind": "port",
-            "sample": (f"oracle (NumPy waveform + C get_ll) on {sum(sample.values())} binaries "
-                       f"({', '.join(f'{sample[n]}xN={n}' for n in sorted(sample))}), "
-                       f"{workers} spawn workers, wall {wall:.1f} s, extrapolated by "
-                       f"per-N cost to the {len(Ns)}-binary mix"),
-            "seconds_per_binary": {str(n): per_bin[n] for n in sorted(per_bin)}}
+        pool.close()
+    return {"value": n / wall, "unit": "binaries/s", "cores": int(workers), "kind": "port",
+            "sample": (f"oracle (NumPy waveform + C get_ll) on every {stride}nd binary of the "
+                       f"batch ({n} binaries, the same N mix), {workers} spawn workers with the "
+                       f"data in shared memory, wall {wall:.1f} s")}
 
 
 # ------------------------------------------------------------------ GPU side
-def make_noise(seed):
-    """Seeded Gaussian A/E noise from the analytic PSD on the 4-yr, 5-s grid
-    (rfft bins 0 ... L-1; bin 0 has infinite PSD and no noise)."""
-    import torch
+def host_noise(seed):
+    """Seeded Gaussian A/E noise from the analytic A/E PSD on the 4-yr, 5-s
+    grid (rfft bins 0 ... L-1; bin 0 has infinite PSD and no noise), drawn on
+    the host so that the GPU arm and the CPU reference arm hold the same
+    data.  Returns (A, E, S) NumPy arrays."""
     from gbgpu_gb300.sensitivity import A1TDISens
     T = int(T_OBS / DT) * DT
     L = int(int(T_OBS / DT) / 2) + 1
@@ -196,16 +270,20 @@ def make_noise(seed):
     S = np.empty(L)
     S[1:] = A1TDISens.get_Sn(f[1:])
     S[0] = np.inf
-    Sd = torch.as_tensor(S, device="cuda")
-    g = torch.Generator(device="cuda").manual_seed(seed)
-    sig = torch.sqrt(Sd * (T / 4.0))
+    sig = np.sqrt(S * (T / 4.0))
     sig[0] = 0.0
-    data = []
-    for _ in range(2):
-        re = torch.randn(L, device="cuda", dtype=torch.float64, generator=g)
-        im = torch.randn(L, device="cuda", dtype=torch.float64, generator=g)
-        data.append(torch.complex(re * sig, im * sig))
-    return data, Sd, S
+    rng = np.random.default_rng(seed)
+    dA = (rng.standard_normal(L) + 1j * rng.standard_normal(L)) * sig
+    dE = (rng.standard_normal(L) + 1j * rng.standard_normal(L)) * sig
+    return dA, dE, S
+
+
+def make_noise(seed):
+    """host_noise on the device: ([A, E] complex128 tensors, PSD tensor, PSD array)."""
+    import torch
+    dA, dE, S = host_noise(seed)
+    data = [torch.as_tensor(dA, device="cuda"), torch.as_tensor(dE, device="cuda")]
+    return data, torch.as_tensor(S, device="cuda"), S
 
 
 def make_data(gb, p, Ns, seed):
@@ -231,8 +309,8 @@ def make_data(gb, p, Ns, seed):
 
 
 def sparse_accuracy(gb, p, Ns, Sd, seed, count=2000):
-    """max |dlogL| / max(1, <h|h>) of the mixed form vs FP64 on data holding
-    only well-separated sources plus noise."""
+    """max |dlogL| / max(1, <h|h>) of the pair and mixed forms vs FP64 on data
+    holding only well-separated sources plus noise: {"pair": x, "mixed": y}."""
     import torch
     Tu = int(T_OBS / DT) * DT
     order = np.argsort(p[1])
@@ -245,13 +323,8 @@ def sparse_accuracy(gb, p, Ns, Sd, seed, count=2000):
         if len(keep) >= count:
             break
     keep = np.array(keep)
+    dat, _, _ = make_noise(seed + 7)
     L = Sd.shape[0]
-    g = torch.Generator(device="cuda").manual_seed(seed + 7)
-    sig = torch.sqrt(Sd * (Tu / 4.0))
-    sig[0] = 0.0
-    dat = [torch.complex(torch.randn(L, device="cuda", dtype=torch.float64, generator=g) * sig,
-                         torch.randn(L, device="cuda", dtype=torch.float64, generator=g) * sig)
-           for _ in range(2)]
     tmpl = torch.zeros((1, 2, L), dtype=torch.complex128, device="cuda")
     for n in np.unique(Ns[keep]):
         sel = keep[Ns[keep] == n]
@@ -260,18 +333,21 @@ def sparse_accuracy(gb, p, Ns, Sd, seed, count=2000):
         dat[0] += tmpl[0, 0]
         dat[1] += tmpl[0, 1]
     out = {}
-    for prec in ("fp64", "mixed"):
+    for prec in ("fp64", "pair", "mixed"):
         gb.get_ll(p[:, keep], dat, [Sd, Sd], N=Ns[keep], T=T_OBS, dt=DT, precision=prec)
         out[prec] = (gb.d_h.real.clone(), gb.h_h.real.clone())
-    d = (-0.5 * ((out["mixed"][1] - out["fp64"][1]) - 2 * (out["mixed"][0] - out["fp64"][0]))).abs()
-    return (d / torch.clamp(out["fp64"][1], min=1.0)).max().item()
+    res = {}
+    for prec in ("pair", "mixed"):
+        d = (-0.5 * ((out[prec][1] - out["fp64"][1]) - 2 * (out[prec][0] - out["fp64"][0]))).abs()
+        res[prec] = (d / torch.clamp(out["fp64"][1], min=1.0)).max().item()
+    return res
 
 
 def time_ll_variants(gb, prm, data, Sd, N, tdi2, steps, tag):
-    """Binaries/s of the FP64 and mixed fused likelihood and of the likelihood
-    + gradient kernel for the batch ``prm`` (nparams, B) at one N, each at its
-    autotuned launch shape (kernel launches through the C ABI, inputs on the
-    device).  Returns (rates, launch shapes)."""
+    """Binaries/s of the FP64, pair (9 parameters) and mixed fused likelihood
+    and of the likelihood + gradient kernel for the batch ``prm`` (nparams, B)
+    at one N, each at its autotuned launch shape (kernel launches through the
+    C ABI, inputs on the device).  Returns (rates, launch shapes)."""
     import ctypes
     import torch
     from gbgpu_gb300 import _native as nat
@@ -292,7 +368,10 @@ def time_ll_variants(gb, prm, data, Sd, N, tdi2, steps, tag):
     lib = nat.lib()
     sh = nat.stream_handle()
     out, shapes = {}, {}
-    for name, prec in (("fp64", "fp64"), ("mixed", "mixed"), ("grad", "mixed")):
+    variants = (("fp64", "fp64"), ("pair", "pair"), ("mixed", "mixed"), ("grad", "mixed"))
+    for name, prec in variants:
+        if prec == "pair" and NP != 9:
+            continue                          # the pair form covers the 9-parameter model
         box = {}
 
         def set_shape(tile, bps):
@@ -380,6 +459,7 @@ def n256_tdi2_bench(gb, data, Sd, seed, steps):
     out["launch_shapes"] = shapes
     out["grad_over_forward"] = out["grad_binaries_per_s"] / out["mixed_binaries_per_s"]
     out["mixed_over_fp64"] = out["mixed_binaries_per_s"] / out["fp64_binaries_per_s"]
+    out["pair_over_fp64"] = out["pair_binaries_per_s"] / out["fp64_binaries_per_s"]
     out["dropin"] = dropin_kernels(gb, p, data, Sd, steps)
     out["fisher"] = fisher_bench(gb, p, Tu)
     out["hmc"] = hmc_bench(gb, p, data, Sd, seed)
@@ -703,6 +783,22 @@ def swap_bench(seed, W=4096, K=500, N=512, steps=100, replays=3):
             "acceptance": float(smp.accepted.sum().item()) / (W * steps * (replays + 1))}
 
 
+HEADLINE = "pair"      # the precision whose logL meets <= 1e-6 max(1, <h|h>) on this data
+
+
+def accuracy(dh, hh, dh64, hh64, ddw=None):
+    """max |dlogL| / max(1, <h|h>) against the FP64 form (and / max(1, <h|h>,
+    <d|d>_window) when ddw is given)."""
+    import torch
+    dl = (-0.5 * (hh.real - hh64.real) + (dh.real - dh64.real)).abs()
+    out = {"max_dlogL_over_max1_hh": (dl / torch.clamp(hh64.real, min=1.0)).max().item(),
+           "count_over_1e-6": int((dl / torch.clamp(hh64.real, min=1.0) > 1e-6).sum().item())}
+    if ddw is not None:
+        out["max_dlogL_over_max1_hh_ddwindow"] = \
+            (dl / torch.clamp(torch.maximum(hh64.real, ddw), min=1.0)).max().item()
+    return out
+
+
 def run_gpu(args, rank, world):
     import torch
     from gbgpu_gb300 import GBGPU, sharding
@@ -712,7 +808,7 @@ def run_gpu(args, rank, world):
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
     B = args.binaries
     p, Ns = draw_workload(B, args.seed + rank)
-    gb = GBGPU(precision="mixed", autotune=not args.no_autotune)
+    gb = GBGPU(precision=HEADLINE, autotune=not args.no_autotune)
     data, Sd, d_d, S_host = make_data(gb, p, Ns, args.seed + rank)
     gb.d_d = d_d
     L = data[0].shape[0]
@@ -732,13 +828,14 @@ def run_gpu(args, rank, world):
     stream = torch.cuda.current_stream()
     sh = nat.stream_handle(stream)
     grad_out = torch.empty((9, B), dtype=torch.float64, device="cuda")
+    variants = ("pair", "mixed", "fp64", "grad")
 
     def set_shape(prec, tile, bps):
         plan = gb._plan(Ns, Tu_, "mixed" if prec == "grad" else prec, False, 9, tile, bps)
         wargs[prec] = plan.args(params_d, grad=(prec == "grad"))
 
     wargs = {}
-    for prec in ("mixed", "fp64", "grad"):
+    for prec in variants:
         set_shape(prec, 0, 0)
 
     def step(prec):
@@ -755,23 +852,24 @@ def run_gpu(args, rank, world):
 
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
-    def timed(prec, K, W):
+    def timed(prec, K, W, clk=None):
         for _ in range(W):
             step(prec)
         torch.cuda.synchronize()
         sharding.barrier()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
               for _ in range(K)]
-        t_wall = time.perf_counter()
-        torch.cuda.nvtx.range_push(f"ll_{prec}")   # ncu --nvtx-include ll_<prec>/
-        for a, b in ev:
-            flush.zero_()                     # evict L2 between timed steps
-            a.record(stream)
-            step(prec)
-            b.record(stream)
-        torch.cuda.nvtx.range_pop()
-        torch.cuda.synchronize()
-        t_wall = time.perf_counter() - t_wall
+        with (clk if clk is not None else contextlib.nullcontext()):
+            t_wall = time.perf_counter()
+            torch.cuda.nvtx.range_push(f"ll_{prec}")   # ncu --nvtx-include ll_<prec>/
+            for a, b in ev:
+                flush.zero_()                     # evict L2 between timed steps
+                a.record(stream)
+                step(prec)
+                b.record(stream)
+            torch.cuda.nvtx.range_pop()
+            torch.cuda.synchronize()
+            t_wall = time.perf_counter() - t_wall
         ms = [a.elapsed_time(b) for a, b in ev]
         return float(np.mean(ms)), t_wall
 
@@ -781,7 +879,7 @@ def run_gpu(args, rank, world):
     if not args.no_autotune:
         from gbgpu_gb300.autotune import default_tuner, workload_key
 
-        for prec in ("mixed", "fp64", "grad"):
+        for prec in variants:
             kind = "grad" if prec == "grad" else "ll"
             pr = "mixed" if prec == "grad" else prec
 
@@ -792,30 +890,30 @@ def run_gpu(args, rank, world):
             set_shape(prec, *shapes[prec])
     torch.cuda.synchronize()
 
-    # accuracy of the mixed form on the full batch against the FP64 form
-    step("fp64")
-    hh64 = h_h.clone()
-    dh64 = d_h.clone()
-    step("mixed")
-    torch.cuda.synchronize()
-    dlogl = (-0.5 * ((h_h.real - hh64.real) - 2 * (d_h.real - dh64.real))).abs()
-    scaled = (dlogl / torch.clamp(hh64.real, min=1.0)).max().item()
+    # accuracy of the pair and mixed forms on the full batch against the FP64 form
+    res = {}
+    for prec in ("fp64", "pair", "mixed"):
+        step(prec)
+        torch.cuda.synchronize()
+        res[prec] = (d_h.clone(), h_h.clone())
     # <d|d> restricted to each template window (the data's own SNR^2 there)
     Tu = int(T_OBS / DT) * DT
     w = 4.0 / Tu / Sd
     w[0] = 0.0
     cs = torch.cumsum(w * (data[0].abs() ** 2 + data[1].abs() ** 2), 0)
     cs = torch.cat([torch.zeros(1, device="cuda", dtype=cs.dtype), cs])
-    from gbgpu_gb300.gbgpu import GBGPU as _G  # noqa: F401
-    si = torch.as_tensor(np.rint((np.rint(p[1] * Tu) - Ns / 2) / Tu * Tu).astype(np.int64),
-                         device="cuda")
+    si = torch.as_tensor(np.rint(np.rint(p[1] * Tu) - Ns / 2).astype(np.int64), device="cuda")
     nn = torch.as_tensor(Ns, device="cuda")
     ddw = cs[torch.clamp(si + nn, 0, L)] - cs[torch.clamp(si, 0, L)]
-    scaled_w = (dlogl / torch.clamp(torch.maximum(hh64.real, ddw), min=1.0)).max().item()
+    acc = {prec: accuracy(*res[prec], *res["fp64"], ddw) for prec in ("pair", "mixed")}
     sparse = sparse_accuracy(gb, p, Ns, Sd, args.seed + rank)
+    for prec in ("pair", "mixed"):
+        acc[prec]["sparse_max_dlogL_over_max1_hh"] = sparse[prec]
+    del res
 
-    with ClockSampler(torch.cuda.current_device()) as clk:
-        ms_mixed, wall_mixed = timed("mixed", args.steps, args.warmup)
+    clk = ClockSampler(torch.cuda.current_device())
+    ms_head, wall_head = timed(HEADLINE, args.steps, args.warmup, clk)
+    ms_mixed, _ = timed("mixed", max(1, min(args.steps, 20)), 1)
     ms_fp64, _ = timed("fp64", max(1, min(args.steps, 3)), 1)
     ms_grad, _ = timed("grad", max(1, min(args.steps, 10)), 1)
     cfg3 = n256_tdi2_bench(gb, data, Sd, args.seed + rank, max(1, min(args.steps, 10)))
@@ -829,19 +927,19 @@ def run_gpu(args, rank, world):
     # e2e through the public API: host params -> device, like -> host
     p_pin = torch.from_numpy(np.ascontiguousarray(p)).pin_memory()
     for _ in range(max(1, args.warmup)):
-        gb.get_ll(p_pin, data, [Sd, Sd], N=Ns, T=T_OBS, dt=DT, precision="mixed")
+        gb.get_ll(p_pin, data, [Sd, Sd], N=Ns, T=T_OBS, dt=DT, precision=HEADLINE)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        gb.get_ll(p_pin, data, [Sd, Sd], N=Ns, T=T_OBS, dt=DT, precision="mixed")
+        gb.get_ll(p_pin, data, [Sd, Sd], N=Ns, T=T_OBS, dt=DT, precision=HEADLINE)
     e2e_s = (time.perf_counter() - t0) / args.steps
 
     # weak scaling: every rank times its own batch; the job's step time is the
     # slowest rank's
-    t_max, e2e_max = sharding.max_over_ranks([ms_mixed, e2e_s], device="cuda")
+    t_max, e2e_max = sharding.max_over_ranks([ms_head, e2e_s], device="cuda")
     value = world * B / (t_max / 1e3)
     ab = alg_bytes(Ns)
-    achieved = ab / (ms_mixed / 1e3) / 1e9
+    achieved = ab / (ms_head / 1e3) / 1e9
     peak, peak_src = hbm_peak()
     traffic = profiled("dram_bytes_per_launch")
     out = {
@@ -855,28 +953,27 @@ def run_gpu(args, rank, world):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32+f64 (FP64 phase/delay/accumulation, FP32 slow part and FFT)",
+        "dtype": "f32 pairs (slow part, FFT and <d|h> in float-pair arithmetic on the FP32 "
+                 "pipe, ~44 bits); FP64 start indices, scalings and outputs",
         "data": "synthetic (seeded binaries; injected sum + Gaussian noise from the analytic A/E PSD)",
-        "config": {"workload": "200k binaries, uneven N in {64..2048} by f0 band, "
-                               "T=4x31557600 s, dt=5 s, L=12,623,041 bins x A,E complex128",
-                   "binaries_per_gpu": B, "N_mix": {str(n): int(np.count_nonzero(Ns == n))
-                                                    for n in np.unique(Ns)},
-                   "precision": "mixed", "l2": "flushed (256 MB write) before every timed step; "
-                   "data+PSD (606 MB) also exceed L2",
-                   "parallelism": f"replicas x{world} (binaries sharded, no collective)"},
-        "gpu_launches": args.steps,
+        "config": workload_config(B, Ns),
+        "precision": HEADLINE,
+        "parallelism": f"replicas x{world} (binaries sharded, no collective)",
+        "gpu_launches": 2 * args.steps,
+        "gpu_launches_note": "per step: prep_kernel (per-binary constants) + pair_kernel<LL>",
         "fp64_binaries_per_s": B / (ms_fp64 / 1e3),
-        "mixed_over_fp64": ms_fp64 / ms_mixed,
-        "mixed_accuracy": {
-            "max_dlogL_over_max1_hh_crowded": scaled,
-            "max_dlogL_over_max1_hh_ddwindow_crowded": scaled_w,
-            "max_dlogL_over_max1_hh_sparse": sparse,
-            "note": "vs the FP64 form of the same kernel (itself within 1e-10 of the "
-                    "reference); crowded = the 200k-source data, sparse = 2000 "
-                    "non-overlapping sources + noise"},
+        "pair_over_fp64": ms_fp64 / ms_head,
+        "mixed_fp32_binaries_per_s": B / (ms_mixed / 1e3),
+        "accuracy": {
+            "pair": acc["pair"], "mixed_fp32": acc["mixed"],
+            "note": "vs the FP64 form of the same kernels (itself within 1e-10 of the "
+                    "reference) on this step's data (the injected sum of all binaries + "
+                    "noise); sparse = 2000 non-overlapping sources + noise.  The pair form "
+                    "meets |dlogL| <= 1e-6 max(1, <h|h>); the FP32 mixed form's stated bound "
+                    "is |dlogL| <= 1e-6 max(1, <h|h>, <d|d>_window)"},
         "grads_per_s": B / (ms_grad / 1e3),
         "grads_note": "binaries/s of the fused likelihood + 9-parameter gradient kernel "
-                      "(mixed form) on the same 200k-binary batch",
+                      "(FP32 mixed form) on the same batch",
         "launch_shapes": {k: {"tile": int(v[0]), "blocks_per_sm": int(v[1])}
                           for k, v in shapes.items()} or "defaults (tile 512, full occupancy)",
         "n256_tdi2": cfg3,
@@ -887,11 +984,11 @@ def run_gpu(args, rank, world):
                      "frac": achieved / peak, "traffic": traffic,
                      "issue_active_frac": profiled("issue_active_frac"),
                      "note": f"peak {peak_src}; achieved = algorithmic bytes (48 N + 104 per "
-                             "binary) / the timed step (prep_kernel + wave_kernel); traffic = "
-                             "ncu DRAM bytes of one full-size wave_kernel launch (windows overlap "
-                             "in L2).  The kernel is instruction-issue bound on the FP32/ALU "
-                             "pipes (issue_active_frac from ncu), so the HBM fraction is low "
-                             "by construction"},
+                             "binary) / the timed step (prep_kernel + pair_kernel); traffic = "
+                             "ncu DRAM bytes per launch (profiles/pair_ll_200k.txt).  The kernel "
+                             "is instruction-issue bound on the FP32/ALU pipes (float-pair "
+                             "arithmetic; issue_active_frac from ncu), so the HBM fraction is "
+                             "low by construction"},
         "compute": compute_roofline(Ns, t_max, clk),
         "e2e": {"value": world * B / e2e_max, "unit": "binaries/s",
                 "h2d_bytes_per_step": int(p.nbytes), "d2h_bytes_per_step": int(B * 8)},
@@ -930,11 +1027,11 @@ def compute_roofline(Ns, ms, clk):
                     "peak = nominal FP32 (SMs x 128 x 2 x max SM clock), not measured"}
 
 
-def profiled(key):
-    """A figure of the committed ncu summary of the fused kernel (a line
+def profiled(key, name="pair_ll_200k.txt"):
+    """A figure of the committed ncu summary of the headline kernel (a line
     ``key: value``): ``dram_bytes_per_launch`` (dram__bytes_read.sum +
-    dram__bytes_write.sum of one full-size launch) or ``issue_active_frac``."""
-    path = os.path.join(ROOT, "profiles", "wave_ll_mixed_200k.txt")
+    dram__bytes_write.sum per full-size launch) or ``issue_active_frac``."""
+    path = os.path.join(ROOT, "profiles", name)
     try:
         for line in open(path):
             if line.startswith(key + ":"):
@@ -944,51 +1041,49 @@ def profiled(key):
     return None
 
 
+def workload_config(B, Ns):
+    """The ``config`` of both arms' JSON lines (the workload, not the arm)."""
+    return {"workload": f"{B} binaries, uneven N in {{64..2048}} by f0 band, T=4x31557600 s, "
+                        "dt=5 s, L=12,623,041 bins x A,E complex128; data = injected sum of all "
+                        "binaries + Gaussian noise from the analytic A/E PSD",
+            "binaries_per_gpu": int(B),
+            "N_mix": {str(n): int(np.count_nonzero(Ns == n)) for n in np.unique(Ns)},
+            "l2": "inputs larger than L2 (data + PSD: 606 MB); the GPU arm also writes 256 MB "
+                  "before every timed step"}
+
+
 def run_reference(args):
-    """CPU reference arm: the reference's algorithm (oracle port) on all host cores."""
+    """CPU reference arm: the reference's algorithm (the oracle port: NumPy
+    waveform + the C likelihood loop, FP64) over the whole batch in every step
+    on all host cores, on the same data as the GPU arm (host noise plus the
+    injected sum of all binaries, built here by the oracle)."""
     p, Ns = draw_workload(args.binaries, args.seed)
-    from gbgpu_gb300.sensitivity import A1TDISens
-    T = int(T_OBS / DT) * DT
-    L = int(int(T_OBS / DT) / 2) + 1
-    rng = np.random.default_rng(args.seed)
-    f = np.arange(L) / T
-    S = np.empty(L)
-    S[1:] = A1TDISens.get_Sn(f[1:])
-    S[0] = np.inf
-    sig = np.sqrt(S * T / 4.0)
-    sig[0] = 0.0
-    dA = (rng.standard_normal(L) + 1j * rng.standard_normal(L)) * sig
-    dE = (rng.standard_normal(L) + 1j * rng.standard_normal(L)) * sig
-    import multiprocessing as mp
+    dA, dE, S = host_noise(args.seed)
     workers = os.cpu_count() or 1
-    vals = []
-    base = None
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import fastgb_oracle as O
-    O._lib()
-    pool = mp.get_context("spawn").Pool(workers)
+    pool = CpuPool(dA, dE, S, workers)
+    walls = []
     try:
-        pool.map(_cpu_warm, range(workers), chunksize=1)
-        for _ in range(max(1, args.warmup)):
-            cpu_baseline(p, Ns, dA, dE, S, workers=workers, per_class=(256, 256, 128, 64, 32, 24),
-                         pool=pool)
+        pool.inject(p, Ns)
+        tasks = cpu_tasks(p, Ns, np.arange(p.shape[1]))
+        for _ in range(max(0, args.warmup)):
+            pool.run(tasks)
         for _ in range(max(1, args.steps)):
-            base = cpu_baseline(p, Ns, dA, dE, S, workers=workers,
-                                per_class=(2560, 2560, 1280, 640, 320, 240), pool=pool)
-            vals.append(base["value"])
+            walls.append(pool.run(tasks)[0])
     finally:
         pool.close()
-        pool.join()
-    v = float(np.median(vals))
-    base["value"] = v
+    ms = float(np.mean(walls)) * 1e3
+    v = args.binaries / (ms / 1e3)
     return {"metric": METRIC, "value": v, "unit": "binaries/s", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": args.binaries / v * 1e3,      # one full batch at the sampled rate
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic (seeded; noise-only data for the CPU timing)",
-            "config": {"workload": "200k binaries, uneven N in {64..2048} by f0 band, "
-                                   "T=4x31557600 s, dt=5 s, L=12,623,041 bins x A,E complex128"},
-            "impl": "reference", "cpu_baseline": base,
+            "dtype": "f64", "data": "synthetic (seeded binaries; injected sum + Gaussian noise "
+                                    "from the analytic A/E PSD; the GPU arm's data)",
+            "config": workload_config(args.binaries, Ns),
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": "binaries/s", "cores": int(workers), "kind": "port",
+                             "sample": f"the whole {args.binaries}-binary batch in every step "
+                                       f"(oracle: NumPy waveform + C get_ll), {workers} spawn "
+                                       "workers, data resident in shared memory"},
             "e2e": {"value": v, "unit": "binaries/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
 

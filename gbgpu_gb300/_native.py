@@ -14,6 +14,7 @@ from .build import LIB
 GBX_OK = 0
 GBX_FP64 = 0
 GBX_MIXED = 1
+GBX_PAIR = 2
 GBX_MAX_LOG2N = 13
 GBX_FLAG_WINDOW = 1
 GBX_FLAG_INDEX = 2

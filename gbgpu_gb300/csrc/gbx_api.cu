@@ -89,6 +89,7 @@ extern "C" int gbx_device_info(int *num_sms_out, int *arch)
 // double rows (3s+c)*N + n : P_s[c]/c ;  rows (9 + 3a + c)*N + n : r_a[c]
 // float  rows (3a+c)*N + n : r_a[c]    (a = 12, 23, 31)
 //        rows (9 + 3s + c)*N + n, (18 + 3s + c)*N + n : P_s[c]/c as a float pair hi, lo
+//        rows (27 + 3a + c)*N + n : r_a[c] - (float)r_a[c] (the pair form's tails)
 __global__ void orbit_table_kernel(double *tab, const double *pos, int N, double L)
 {
     int n = blockIdx.x * blockDim.x + threadIdx.x;
@@ -113,16 +114,19 @@ __global__ void orbit_table_kernel(double *tab, const double *pos, int N, double
         tab[(size_t)(9 + c) * N + n] = r12;
         tab[(size_t)(12 + c) * N + n] = r23;
         tab[(size_t)(15 + c) * N + n] = r31;
-        tf[(size_t)c * N + n] = (float)r12;
-        tf[(size_t)(3 + c) * N + n] = (float)r23;
-        tf[(size_t)(6 + c) * N + n] = (float)r31;
+        const double rr[3] = {r12, r23, r31};
+        for (int a = 0; a < 3; a++) {
+            const float hi = (float)rr[a];
+            tf[(size_t)(3 * a + c) * N + n] = hi;
+            tf[(size_t)(27 + 3 * a + c) * N + n] = (float)(rr[a] - (double)hi);
+        }
     }
 }
 
 extern "C" size_t gbx_orbit_table_bytes(int N)
 {
     if (N <= 0) return 0;
-    return (size_t)N * (18 * sizeof(double) + 27 * sizeof(float));
+    return (size_t)N * (18 * sizeof(double) + 36 * sizeof(float));
 }
 
 extern "C" int gbx_orbit_table(void *table, const double *sc_pos, int N, double armlength,

@@ -91,6 +91,65 @@ __host__ __device__ __forceinline__ dfl df_from(double x)
     float h = (float)x;
     return {h, (float)(x - (double)h)};
 }
+// the pair of a double known at compile time (folded by the compiler)
+__host__ __device__ constexpr dfl dconst(double x)
+{
+    return dfl{(float)x, (float)(x - (double)(float)x)};
+}
+
+// complex number with float-pair parts (16 bytes, one vector access)
+struct __align__(16) cpx {
+    dfl x, y;
+};
+
+// FP64 x * 2^e as an unevaluated float pair hi + lo, built mostly on the
+// integer pipe: hi carries the 24 leading significant bits, lo the next 23
+// (both truncated), so |x 2^e - (hi + lo)| < 2^-46 |x 2^e|.  (hi:lo) << 3
+// holds the 23 leading mantissa bits at [22:0] and the exponent's low 9 bits
+// at [31:23]; subtracting (896 - e) << 23 leaves the FP32 biased exponent
+// there when it is in range.  Scaled values below FP32's normal range become
+// signed zero, values above it (and infinities, NaN) infinity; lo is the
+// next 23 bits as an exact FP32 integer times hi's power of two times 2^-46
+// (so it underflows to zero for |hi| < 2^-80).
+__device__ __forceinline__ dfl d2ff_scaled(double x, int e)
+{
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const int ne = (int)((hi >> 20) & 0x7ffu) - 896 + e;          // FP32 biased exponent
+    unsigned mag = __funnelshift_l(lo, hi, 3) - ((unsigned)(896 - e) << 23);
+    mag = ((unsigned)(ne - 1) < 254u) ? mag : (ne >= 255 ? 0x7f800000u : 0u);
+    const unsigned hb = (hi & 0x80000000u) | (mag & 0x7fffffffu);
+    const float r = __uint_as_float(0x4b000000u | ((lo >> 6) & 0x7fffffu)) - 8388608.0f;
+    const float l = r * (__uint_as_float(hb & 0xff800000u) * 0x1p-46f);
+    return {__uint_as_float(hb), l};
+}
+
+// a.h * b.h exactly plus the first-order cross terms: p + e ~ a * b (2^-46)
+__device__ __forceinline__ dfl df_prod(dfl a, dfl b)
+{
+    const float p = a.h * b.h;
+    float e = fmaf(a.h, b.h, -p);
+    e = fmaf(a.h, b.l, e);
+    e = fmaf(a.l, b.h, e);
+    return {p, e};
+}
+
+// a + b for unnormalised pairs (TwoSum of the high parts)
+__device__ __forceinline__ dfl df_sum(dfl a, dfl b)
+{
+    const dfl s = df_two_sum(a.h, b.h);
+    return {s.h, s.l + (a.l + b.l)};
+}
+
+// 1 / s as a float pair: rcp.approx seed, one Newton step on the pair's
+// residual (relative error ~2^-46); 1/inf = 0
+__device__ __forceinline__ dfl df_recip(dfl s)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(s.h));
+    float e = fmaf(-s.h, r, 1.0f);
+    e = fmaf(-s.l, r, e);
+    return {r, r == 0.0f ? 0.0f : r * e};
+}
 
 // ---------------------------------------------------------------- status
 __device__ __forceinline__ void flag(int *status, int bit)

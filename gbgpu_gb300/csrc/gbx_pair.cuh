@@ -1,0 +1,550 @@
+// Pair form of the waveform family: the slow part, the N-point FFTs and the
+// inner product <d|h> in float-pair arithmetic on the FP32 pipe.
+//
+// A value is the unevaluated sum h + l of two FP32 numbers (Dekker 1971;
+// error-free TwoSum, Knuth TAOCP vol. 2, 4.2.2, and TwoProd through FMA), so
+// sums and products keep about 44 significant bits while every instruction
+// runs on the FP32 pipe (on GB300 one FP64 instruction takes the issue time
+// of 64 FP32 ones).  An FP32 template carries ~1e-7 relative error, and in
+// crowded data (a window 10-100x louder than the template) that error meets
+// the loud bins: an FP32-valued template misses |dlogL| <= 1e-6 max(1, <h|h>)
+// there even when rounded once from exact values.  The pair template carries
+// ~1e-11 and the likelihood's <d|h> and <h|h> are summed in pairs, so every
+// output stays within ~1e-9 of the FP64 form.
+//
+// This file is included inside namespace gbx by gbx_wave.cu.
+
+// ---------------------------------------------------------------- arithmetic
+__device__ __forceinline__ dfl p_sub(dfl a, dfl b) { return df_add(a, dfl{-b.h, -b.l}); }
+
+// a + b when |a| >= |b| (or a = 0): Fast2Sum of the heads, renormalised
+__device__ __forceinline__ dfl p_addf(dfl a, dfl b)
+{
+    const float s = a.h + b.h;
+    const float e = b.h - (s - a.h);
+    return df_fast(s, e + (a.l + b.l));
+}
+
+__device__ __forceinline__ dfl p_scale(dfl a, float pow2) { return dfl{a.h * pow2, a.l * pow2}; }
+
+__device__ __forceinline__ dfl p_sqr(dfl a)
+{
+    const float p = a.h * a.h;
+    float e = fmaf(a.h, a.h, -p);
+    e = fmaf(a.h + a.h, a.l, e);
+    return df_fast(p, e);
+}
+
+// a b + c d
+__device__ __forceinline__ dfl p_dot2(dfl a, dfl b, dfl c, dfl d)
+{
+    const float p = a.h * b.h, q = c.h * d.h;
+    float e = fmaf(a.h, b.h, -p);
+    float f = fmaf(c.h, d.h, -q);
+    e = fmaf(a.h, b.l, fmaf(a.l, b.h, e));
+    f = fmaf(c.h, d.l, fmaf(c.l, d.h, f));
+    const dfl s = df_two_sum(p, q);
+    return df_fast(s.h, s.l + (e + f));
+}
+
+// a b + c d + e f
+__device__ __forceinline__ dfl p_dot3(dfl a, dfl b, dfl c, dfl d, dfl e, dfl f)
+{
+    const float p = a.h * b.h, q = c.h * d.h, r = e.h * f.h;
+    float ep = fmaf(a.h, b.h, -p), eq = fmaf(c.h, d.h, -q), er = fmaf(e.h, f.h, -r);
+    ep = fmaf(a.h, b.l, fmaf(a.l, b.h, ep));
+    eq = fmaf(c.h, d.l, fmaf(c.l, d.h, eq));
+    er = fmaf(e.h, f.l, fmaf(e.l, f.h, er));
+    const dfl s1 = df_two_sum(p, q);
+    const dfl s2 = df_two_sum(s1.h, r);
+    return df_fast(s2.h, (s1.l + s2.l) + (ep + (eq + er)));
+}
+
+// n / d (FP32 quotient of the heads, one correction from the pair residual)
+__device__ __forceinline__ dfl p_div(dfl n, dfl d)
+{
+    const float q1 = n.h / d.h;
+    const dfl r = df_add(n, df_neg(df_mul_f(d, q1)));
+    return df_fast(q1, r.h / d.h);
+}
+
+__device__ __forceinline__ cpx cp_add(cpx a, cpx b) { return {df_add(a.x, b.x), df_add(a.y, b.y)}; }
+__device__ __forceinline__ cpx cp_sub(cpx a, cpx b) { return {p_sub(a.x, b.x), p_sub(a.y, b.y)}; }
+__device__ __forceinline__ cpx cp_neg(cpx a) { return {df_neg(a.x), df_neg(a.y)}; }
+__device__ __forceinline__ cpx cp_pow2(cpx a, float s) { return {p_scale(a.x, s), p_scale(a.y, s)}; }
+__device__ __forceinline__ cpx cp_mul(cpx a, cpx b)
+{
+    return {p_dot2(a.x, b.x, df_neg(a.y), b.y), p_dot2(a.x, b.y, a.y, b.x)};
+}
+__device__ __forceinline__ cpx cp_scale(cpx a, dfl r) { return {df_mul(a.x, r), df_mul(a.y, r)}; }
+__device__ __forceinline__ cpx cp_zero() { return {{0.f, 0.f}, {0.f, 0.f}}; }
+__device__ __forceinline__ double pd(dfl a) { return (double)a.h + (double)a.l; }
+
+// ---------------------------------------------------------------- functions
+// cos x and sin x for a pair |x| < 100 from a table of the pairs cos, sin at
+// j pi/128 (tab[j & 255]) and the Taylor series on the remainder |d| <= pi/256:
+// sin d = d - d^3/6 (next term below 3e-12), cos d = 1 - d^2/2 + d^4/24
+// (below 5e-15), combined by the angle-addition formulas.  pi/128 = C1 + C2
+// + C3 with C1 of 12 significant bits, so j C1 is exact for |j| < 4096 and
+// x.h - j C1 is formed exactly by TwoSum.
+constexpr int kScN = 256;
+
+__device__ __forceinline__ void sincos_pair(dfl x, const float4 *__restrict__ tab, dfl &c, dfl &s)
+{
+    constexpr float kInv = 40.743663787841797f;     // 128/pi (picks j only)
+    constexpr float C1 = 0.02454376220703125f;     // 3217 * 2^-17
+    constexpr float C2 = -6.960085841001273e-08f;
+    constexpr float C3 = -2.581268532253489e-15f;
+    const float jf = rintf(x.h * kInv);
+    const dfl h = df_two_sum(x.h, -jf * C1);
+    const dfl d = df_fast(h.h, h.l + fmaf(-jf, C3, fmaf(-jf, C2, x.l)));
+    const float4 t = tab[(int)jf & (kScN - 1)];
+    const float d2 = d.h * d.h;
+    const dfl sd = {d.h, fmaf(d.h * d2, -1.0f / 6.0f, d.l)};
+    const float eps = d2 * fmaf(d2, 1.0f / 24.0f, -0.5f);   // cos d - 1
+    const dfl Tc = {t.x, t.y}, Ts = {t.z, t.w};
+    const dfl cc = df_add(Tc, df_neg(df_mul(Ts, sd)));
+    const dfl ss = df_add(Ts, df_mul(Tc, sd));
+    c = df_fast(cc.h, fmaf(Tc.h, eps, cc.l));
+    s = df_fast(ss.h, fmaf(Ts.h, eps, ss.l));
+}
+
+// sin(a)/a and cos(a) for a pair a >= 0: Taylor series in x = a^2 for
+// x < 2.56 (terms to x^7; truncation below 5e-12 and 9e-11), the leading three
+// coefficients as pairs and the rest as an FP32 tail (at most 4e-10 of the
+// result); beyond that cos and sin from sincos_pair and one pair division.
+__device__ __forceinline__ void sinc_cos_pair(dfl a, const float4 *__restrict__ tab, dfl &S, dfl &C)
+{
+    const dfl x = p_sqr(a);
+    const float xf = x.h;
+    if (xf < 2.56f) {
+        constexpr dfl s2 = dconst(1.0 / 120.0), s1 = dconst(-1.0 / 6.0);
+        float q = fmaf(xf, -1.0f / 1307674368000.0f, 1.0f / 6227020800.0f);
+        q = fmaf(q, xf, -1.0f / 39916800.0f);
+        q = fmaf(q, xf, 1.0f / 362880.0f);
+        q = fmaf(q, xf, -1.0f / 5040.0f);
+        dfl r = p_addf(s2, dfl{xf * q, 0.f});
+        r = p_addf(s1, df_mul(x, r));
+        S = p_addf(dfl{1.f, 0.f}, df_mul(x, r));
+        constexpr dfl c2 = dconst(1.0 / 24.0);
+        float u = fmaf(xf, -1.0f / 87178291200.0f, 1.0f / 479001600.0f);
+        u = fmaf(u, xf, -1.0f / 3628800.0f);
+        u = fmaf(u, xf, 1.0f / 40320.0f);
+        u = fmaf(u, xf, -1.0f / 720.0f);
+        dfl v = p_addf(c2, dfl{xf * u, 0.f});
+        v = p_addf(dfl{-0.5f, 0.f}, df_mul(x, v));
+        C = df_add(dfl{1.f, 0.f}, df_mul(x, v));
+    } else {
+        dfl sn;
+        sincos_pair(a, tab, C, sn);
+        S = p_div(sn, a);
+    }
+}
+
+// ---------------------------------------------------------------- slow part
+// The slow part at one sample (gbgpu.py:399-540 and 348-375), as slow_mixed
+// but every quantity a pair.  AE: out[0], out[1] = A, E (formed before the
+// transform); otherwise out[0..2] = X, Y, Z.  Amplitude divided out.
+//
+// The six links are grouped by the spacecraft whose carrier exp(-i phi_s)
+// they carry: with P_q = T_q A_arm(q) (T = sinc(a) e^{-ia} / 4) and
+// F_s = fc (P_q - P_q') for the two links of spacecraft s,
+//   X = fc2 (F_1 E_1 + P_21 E_2 - P_31 E_3), Y and Z cyclic.
+template <bool AE>
+__device__ __forceinline__ void slow_pair(const Bin &B, int n, int N, dfl step, dfl Loc,
+                                          const double *__restrict__ tab,
+                                          const float4 *__restrict__ sct, cpx out[3])
+{
+    const float *tabf = reinterpret_cast<const float *>(tab + (size_t)18 * N);
+    dfl r[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+            r[a][c] = {__ldg(tabf + (size_t)(3 * a + c) * N + n),
+                       __ldg(tabf + (size_t)(27 + 3 * a + c) * N + n)};
+    dfl kr[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+        kr[a] = p_dot3(B.kd[0], r[a][0], B.kd[1], r[a][1], B.kd[2], r[a][2]);
+    const dfl tm = df_mul_f(step, (float)n);                 // n T/N
+    const float tf = tm.h;
+    const dfl tm2 = p_sqr(tm);
+    // carrier phase of spacecraft 1 (the expansion in slow_mixed):
+    //   Phi0(tm) + kP w(tm) - pi kP^2 fd(tm) + pi/3 fddot kP^3
+    dfl Phi0 = df_add(df_mul(B.omdfad, tm), B.phi0d);
+    Phi0 = df_neg(df_add(Phi0, df_mul(tm2, df_add(B.pfd, df_mul(B.p3d, tm)))));
+    const dfl wt = df_add(B.omd, df_add(df_mul(B.tpfd, tm), df_mul(B.pfddd, tm2)));
+    const float fdt = fmaf(B.fddotf, tf, B.fdotf);
+    const dfl kP0 = kP1_pair(B, tabf, N, n);
+    dfl ph0 = df_add(Phi0, df_mul(kP0, wt));
+    {
+        const float q = rintf(ph0.h * (float)kInvTwoPi);
+        ph0 = df_add(ph0, df_neg(df_mul_f(dconst(kTwoPi), q)));
+    }
+    // spacecraft 2 and 3: k.P_s/c = k.P_1/c + (L/c) k.r_12 and - (L/c) k.r_31
+    const dfl dk[3] = {dfl{0.f, 0.f}, df_mul(Loc, kr[0]), df_neg(df_mul(Loc, kr[2]))};
+    // f(t)/fstar = w0 + w1 t + w2 t^2 with w1 t a pair: at f0 = 1e-4 Hz and
+    // fdot = 1e-15 that term is 1e-3 of w0, and omL enters fc2 squared
+    const dfl base = p_addf(dfl{B.w0h, B.w0l}, df_mul(dfl{B.w1, B.w1l}, tm));
+    cpx E[3];
+    dfl fo[3];
+#pragma unroll
+    for (int s = 0; s < 3; s++) {
+        dfl ph = s == 0 ? ph0 : df_add(ph0, df_mul(dk[s], wt));
+        const float kPf = kP0.h + dk[s].h;
+        ph.l += kPf * kPf * fmaf(kPf, B.p3d.h, -(float)kPi * fdt);   // below 1e-8 rad
+        dfl cs, sn;
+        sincos_pair(ph, sct, cs, sn);
+        E[s] = {cs, df_neg(sn)};
+        // f(xi)/fstar at xi = t - kP: - w1 kP + w2 xi^2 are below 3e-6 of w0
+        const float xf = tf - kPf;
+        fo[s] = p_addf(base, dfl{fmaf(B.w2 * xf, xf, -B.w1 * kPf), 0.f});
+    }
+    // antenna patterns per arm, with the 1/4 of the transfer functions:
+    // r.e+.r = (r.v)^2 - (r.u)^2, r.ex.r = 2 (r.u)(r.v)
+    cpx A[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const dfl ru = p_dot3(B.pr.ud[0], r[a][0], B.pr.ud[1], r[a][1], B.pr.ud[2], r[a][2]);
+        const dfl rv = p_dot2(B.pr.vd[0], r[a][0], B.pr.vd[1], r[a][1]);
+        const dfl pp = p_scale(p_dot2(rv, rv, df_neg(ru), ru), 0.25f);
+        const dfl cc = p_scale(df_mul(ru, rv), 0.5f);
+        A[a] = {p_dot2(pp, B.pr.DP.x, cc, B.pr.DC.x), p_dot2(pp, B.pr.DP.y, cc, B.pr.DC.y)};
+    }
+    // links (ij, arm, spacecraft): 12,23,31 (+k.r), 21,32,13 (-k.r)
+    cpx P[6];
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+        const int arm = q < 3 ? q : q - 3;
+        const int s = q < 3 ? q : (q - 2) % 3;
+        const dfl k = q < 3 ? kr[arm] : df_neg(kr[arm]);
+        const dfl a = p_scale(df_mul(fo[s], p_addf(dfl{1.f, 0.f}, k)), 0.5f);
+        dfl S, C;
+        sinc_cos_pair(a, sct, S, C);
+        const cpx T = {df_mul(S, C), df_neg(df_mul(df_mul(a, S), S))};   // sinc(a) e^{-ia}
+        P[q] = cp_mul(T, A[arm]);
+    }
+    // omega L, fc = e^{-i omL}, fc2 = 4 omL sin(omL) fc (gbgpu.py:362-368)
+    const dfl omL = p_addf(base, dfl{B.w2 * tf * tf, 0.f});
+    dfl co, so;
+    sincos_pair(omL, sct, co, so);
+    const cpx fc = {co, df_neg(so)};
+    const dfl g4 = p_scale(df_mul(omL, so), 4.f);
+    const cpx fc2 = {df_mul(g4, co), df_neg(df_mul(g4, so))};
+    // F_s = fc (P12 - P13), fc (P23 - P21), fc (P31 - P32)
+    const cpx F0 = cp_mul(fc, cp_sub(P[0], P[5]));
+    const cpx F1 = cp_mul(fc, cp_sub(P[1], P[3]));
+    const cpx F2 = cp_mul(fc, cp_sub(P[2], P[4]));
+    if constexpr (AE) {
+        // A = (Z - X)/sqrt2, E = (X - 2Y + Z)/sqrt6 (utility.py:24-38)
+        const cpx a0 = cp_sub(P[5], F0), a1 = cp_neg(cp_add(P[1], P[3])), a2 = cp_add(F2, P[2]);
+        const cpx b0 = cp_add(cp_add(F0, P[5]), cp_pow2(P[0], 2.f));
+        const cpx b1 = cp_sub(cp_sub(P[3], P[1]), cp_pow2(F1, 2.f));
+        const cpx b2 = cp_sub(F2, cp_add(P[2], cp_pow2(P[4], 2.f)));
+        const cpx sA = cp_add(cp_add(cp_mul(a0, E[0]), cp_mul(a1, E[1])), cp_mul(a2, E[2]));
+        const cpx sE = cp_add(cp_add(cp_mul(b0, E[0]), cp_mul(b1, E[1])), cp_mul(b2, E[2]));
+        out[0] = cp_mul(cp_scale(fc2, dconst(0.70710678118654752440)), sA);
+        out[1] = cp_mul(cp_scale(fc2, dconst(0.40824829046386301637)), sE);
+    } else {
+        const cpx X = cp_add(cp_mul(F0, E[0]), cp_sub(cp_mul(P[3], E[1]), cp_mul(P[2], E[2])));
+        const cpx Y = cp_add(cp_mul(F1, E[1]), cp_sub(cp_mul(P[4], E[2]), cp_mul(P[0], E[0])));
+        const cpx Z = cp_add(cp_mul(F2, E[2]), cp_sub(cp_mul(P[5], E[0]), cp_mul(P[1], E[1])));
+        out[0] = cp_mul(fc2, X);
+        out[1] = cp_mul(fc2, Y);
+        out[2] = cp_mul(fc2, Z);
+    }
+}
+
+// ---------------------------------------------------------------- FFT
+// fft_dif in pair arithmetic: same passes, swizzle and output order; the
+// twiddles are pairs of the FP64 table.
+__device__ __forceinline__ cpx tw_pair(int m)
+{
+    const float4 t = g_tw_p[m];
+    return {{t.x, t.y}, {t.z, t.w}};
+}
+
+template <int RB>
+__device__ __forceinline__ void fft_reg_pass_pair(cpx *buf, int nsub, int lg, int hl)
+{
+    constexpr int M = 1 << RB;
+    const int q = hl - RB + 1;
+    const int groups = nsub << (lg - RB);
+    for (int g = threadIdx.x; g < groups; g += kBlock) {
+        const int a = g >> (lg - RB);
+        const int rem = g & ((1 << (lg - RB)) - 1);
+        const int blk = rem >> q;
+        const int r = rem & ((1 << q) - 1);
+        cpx *sub = buf + ((size_t)a << lg);
+        const int p0 = (blk << (hl + 1)) + r;
+        cpx x[M];
+#pragma unroll
+        for (int m = 0; m < M; m++) x[m] = sub[swz(p0 + (m << q), lg)];
+#pragma unroll
+        for (int j = 0; j < RB; j++) {
+            const int dm = M >> (j + 1);
+            const int hh = hl - j;
+            const int ts = kTwN >> (hh + 1);
+#pragma unroll
+            for (int m = 0; m < M; m++) {
+                if (m & dm) continue;
+                const int rp = r + ((m & (dm - 1)) << q);
+                const cpx u = x[m], v = x[m + dm];
+                x[m] = cp_add(u, v);
+                x[m + dm] = cp_mul(cp_sub(u, v), tw_pair(rp * ts));
+            }
+        }
+#pragma unroll
+        for (int m = 0; m < M; m++) sub[swz(p0 + (m << q), lg)] = x[m];
+    }
+}
+
+__device__ __forceinline__ float shfl4(float v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+
+__device__ __forceinline__ void fft_dif_pair(cpx *buf, int nsub, int lg)
+{
+    int hl = lg - 1;
+    while (hl >= 5) {
+        const int rb = (hl - 4) >= 3 ? 3 : (hl - 4);
+        if (rb == 3) fft_reg_pass_pair<3>(buf, nsub, lg, hl);
+        else if (rb == 2) fft_reg_pass_pair<2>(buf, nsub, lg, hl);
+        else fft_reg_pass_pair<1>(buf, nsub, lg, hl);
+        hl -= rb;
+        __syncthreads();
+    }
+    // last five stages inside a warp (lane l holds element 32c + l): the
+    // lower lane of a pair keeps x + y, the upper one (y - x) W
+    const int lane = threadIdx.x & 31;
+    cpx w[4];
+    float sg[5];
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        const int hh = 4 - k;
+        const bool up = (lane & (16 >> k)) != 0;
+        sg[k] = up ? -1.f : 1.f;
+        if (k < 4) {
+            const int rp = lane & ((1 << hh) - 1);
+            w[k] = up ? tw_pair(rp * (kTwN >> (hh + 1))) : cpx{{1.f, 0.f}, {0.f, 0.f}};
+        }
+    }
+    const int chunks = (nsub << lg) >> 5;
+    for (int c = threadIdx.x >> 5; c < chunks; c += kBlock >> 5) {
+        const int e = (c << 5) + lane;
+        const int idx = ((e >> lg) << lg) + swz(e & ((1 << lg) - 1), lg);
+        cpx x = buf[idx];
+#pragma unroll
+        for (int k = 0; k < 5; k++) {
+            const int o = 16 >> k;
+            const cpx y = {{shfl4(x.x.h, o), shfl4(x.x.l, o)}, {shfl4(x.y.h, o), shfl4(x.y.l, o)}};
+            const cpx sx = {{sg[k] * x.x.h, sg[k] * x.x.l}, {sg[k] * x.y.h, sg[k] * x.y.l}};
+            const cpx d = cp_add(sx, y);
+            x = (k < 4) ? cp_mul(d, w[k < 4 ? k : 0]) : d;
+        }
+        buf[idx] = x;
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------- kernel
+// One CTA per tile as wave_kernel; MODE_WAVE writes the reference's output
+// arrays (the transformed pairs rounded once to FP64, then the FP64 scale
+// and AET), MODE_LL folds the window into <d|h> and <h|h> (pairs).  Shared memory: the binaries' constants, the reduction
+// scratch, the sin/cos table and the transform buffers.
+template <int MODE>
+__global__ void __launch_bounds__(kBlock, 2) pair_kernel(const KParams K)
+{
+    constexpr int NCH = MODE == MODE_WAVE ? 3 : 2;
+    extern __shared__ __align__(16) unsigned char smem[];
+    Bin *bins = reinterpret_cast<Bin *>(smem);
+    double *red = reinterpret_cast<double *>(smem + sizeof(Bin) * K.maxP);
+    float4 *sct = reinterpret_cast<float4 *>(smem + sizeof(Bin) * K.maxP +
+                                             sizeof(double) * red_doubles(K.maxS));
+    cpx *buf = reinterpret_cast<cpx *>(sct + kScN);
+    __shared__ int s_tile;
+
+    const gbx_wave_args &a = K.a;
+    const int tid = threadIdx.x;
+    for (int k = tid; k < kScN; k += kBlock) sct[k] = g_sc_p[k];
+    const int ntiles = a.tiles ? a.ntiles : (a.num_bin + K.P - 1) / K.P;
+    int iter = 0;
+
+    for (;;) {
+        if (tid == 0) {
+            if (a.queue) s_tile = atomicAdd(a.queue, 1);
+            else s_tile = blockIdx.x + iter * gridDim.x;
+        }
+        __syncthreads();
+        const int tile = s_tile;
+        iter++;
+        if (tile >= ntiles) break;
+        int lg, first, cnt;
+        if (a.tiles) {
+            lg = a.tiles[4 * tile];
+            first = a.tiles[4 * tile + 1];
+            cnt = a.tiles[4 * tile + 2];
+        } else {
+            lg = 31 - __clz(a.N);
+            first = tile * K.P;
+            cnt = min(K.P, a.num_bin - first);
+        }
+        const int N = 1 << lg;
+        const double *tab = (lg >= 5 && lg <= kPairMaxLog2N)
+                                ? reinterpret_cast<const double *>(a.orbit[lg]) : nullptr;
+        const int maxcnt = tile_pack(a.tile, lg, 1);
+        if (tab == nullptr || cnt < 1 || cnt > maxcnt || first < 0 || first + cnt > a.num_bin ||
+            (cnt << lg) > K.maxS) {
+            flag(a.status, GBX_FLAG_TILE);
+            __syncthreads();
+            continue;
+        }
+        if (a.workspace) {
+            const int4 *src = reinterpret_cast<const int4 *>(static_cast<const Bin *>(a.workspace) + first);
+            int4 *dst = reinterpret_cast<int4 *>(bins);
+            const int n16 = cnt * (int)(sizeof(Bin) / 16);
+            for (int k = tid; k < n16; k += kBlock) dst[k] = src[k];
+        } else if (tid < cnt) {
+            const int slot = first + tid;
+            const int b = a.order ? a.order[slot] : slot;
+            if (b < 0 || b >= a.num_bin) {
+                flag(a.status, GBX_FLAG_TILE);
+                memset(&bins[tid], 0, sizeof(Bin));
+                bins[tid].b = -1;
+            } else {
+                setup_bin(bins[tid], K, b, N, MODE);
+            }
+        }
+        __syncthreads();
+
+        const int S = cnt << lg;
+        const dfl stepd = K.stepd[lg];
+        for (int m = tid; m < S; m += kBlock) {
+            const int p = m >> lg, n = m & (N - 1);
+            const Bin &B = bins[p];
+            cpx o[3];
+            if (!B.valid) {
+                o[0] = o[1] = o[2] = cp_zero();
+            } else {
+                slow_pair<NCH == 2>(B, n, N, stepd, K.Locd, tab, sct, o);
+            }
+#pragma unroll
+            for (int c = 0; c < NCH; c++) buf[(p * NCH + c) * N + swz(n, lg)] = o[c];
+        }
+        __syncthreads();
+
+        fft_dif_pair(buf, NCH * cnt, lg);
+
+        if constexpr (MODE == MODE_WAVE) {
+            for (int m = tid; m < S; m += kBlock) {
+                const int p = m >> lg, i = m & (N - 1);
+                const Bin &B = bins[p];
+                if (B.b < 0) continue;
+                const int pos = swz(bitrev((i + (N >> 1)) & (N - 1), lg), lg);   // fftshift
+                const cpx X = buf[(p * 3 + 0) * N + pos], Y = buf[(p * 3 + 1) * N + pos],
+                          Z = buf[(p * 3 + 2) * N + pos];
+                const double2 Xd = cmul(make_double2(pd(X.x), pd(X.y)), B.scale);
+                const double2 Yd = cmul(make_double2(pd(Y.x), pd(Y.y)), B.scale);
+                const double2 Zd = cmul(make_double2(pd(Z.x), pd(Z.y)), B.scale);
+                const size_t o = (size_t)B.b * 3 * N + i;
+                if (K.XYZ) {
+                    K.XYZ[o] = Xd;
+                    K.XYZ[o + N] = Yd;
+                    K.XYZ[o + 2 * N] = Zd;
+                }
+                if (K.AET) {
+                    const double is2 = 0.70710678118654752440, is6 = 0.40824829046386301637;
+                    const double i3 = 0.57735026918962576451;
+                    K.AET[o] = make_double2((Zd.x - Xd.x) * is2, (Zd.y - Xd.y) * is2);
+                    K.AET[o + N] = make_double2((Xd.x - 2.0 * Yd.x + Zd.x) * is6,
+                                                (Xd.y - 2.0 * Yd.y + Zd.y) * is6);
+                    K.AET[o + 2 * N] = make_double2((Xd.x + Yd.x + Zd.x) * i3, (Xd.y + Yd.y + Zd.y) * i3);
+                }
+                if (i == 0 && K.start_out) K.start_out[B.b] = B.start;
+            }
+        } else {
+            // Threads [p Tpb, (p+1) Tpb) own binary p and stride its window (a
+            // warp reads contiguous runs of data and PSD).  <d|h> and <h|h> per
+            // thread and over lanes in pairs.
+            const int Tpb = kBlock / maxcnt;
+            const int width = Tpb < 32 ? Tpb : 32;
+            const int p = tid / Tpb;
+            const int i0 = tid - p * Tpb;
+            dfl sr = {0.f, 0.f}, si = {0.f, 0.f}, xh = {0.f, 0.f};
+            if (p < cnt) {
+                const Bin &B = bins[p];
+                bool out = false;
+                if (B.valid) {
+                    for (int i = i0; i < N; i += Tpb) {
+                        const int j = B.start + i;
+                        if (j < 0 || j >= K.L) {
+                            out = true;
+                            continue;
+                        }
+                        const int pos = swz(bitrev((i + (N >> 1)) & (N - 1), lg), lg);
+                        const cpx tA = buf[(p * 2 + 0) * N + pos], tE = buf[(p * 2 + 1) * N + pos];
+                        const size_t jd = (size_t)B.di * K.L + j, jn = (size_t)B.ni * K.L + j;
+                        const double2 dA = __ldg(K.A_data + jd), dE = __ldg(K.E_data + jd);
+                        const dfl wA = df_recip(d2ff_scaled(__ldg(K.A_psd + jn), B.eS));
+                        const dfl wE = df_recip(d2ff_scaled(__ldg(K.E_psd + jn), B.eS));
+                        // conj(d) h / S  (gbgpu_utils.cu:172-178), d / S first
+                        const dfl ar = df_mul(d2ff_scaled(dA.x, B.eD), wA);
+                        const dfl ai = df_mul(d2ff_scaled(dA.y, B.eD), wA);
+                        const dfl er = df_mul(d2ff_scaled(dE.x, B.eD), wE);
+                        const dfl ei = df_mul(d2ff_scaled(dE.y, B.eD), wE);
+                        sr = df_add(sr, df_add(p_dot2(ar, tA.x, ai, tA.y), p_dot2(er, tE.x, ei, tE.y)));
+                        si = df_add(si, df_add(p_dot2(ar, tA.y, df_neg(ai), tA.x),
+                                               p_dot2(er, tE.y, df_neg(ei), tE.x)));
+                        xh = df_add(xh, p_dot2(p_dot2(tA.x, tA.x, tA.y, tA.y), wA,
+                                               p_dot2(tE.x, tE.x, tE.y, tE.y), wE));
+                    }
+                }
+                if (out) flag(a.status, GBX_FLAG_WINDOW);
+            }
+            for (int o = width >> 1; o > 0; o >>= 1) {
+                sr = df_add(sr, dfl{shfl4(sr.h, o), shfl4(sr.l, o)});
+                si = df_add(si, dfl{shfl4(si.h, o), shfl4(si.l, o)});
+                xh = df_add(xh, dfl{shfl4(xh.h, o), shfl4(xh.l, o)});
+            }
+            if ((tid & (width - 1)) == 0) {
+                float2 *red2 = reinterpret_cast<float2 *>(red);
+                const int g = tid / width;
+                red2[3 * g] = make_float2(sr.h, sr.l);
+                red2[3 * g + 1] = make_float2(si.h, si.l);
+                red2[3 * g + 2] = make_float2(xh.h, xh.l);
+            }
+            __syncthreads();
+            double *tsum = red + 3 * kMaxPack;
+            {
+                const int per = Tpb / width;
+                const float2 *red2 = reinterpret_cast<const float2 *>(red);
+                for (int t = tid; t < 3 * cnt; t += kBlock) {
+                    const int q = t / 3, c = t - 3 * q;
+                    dfl x = {0.f, 0.f};
+                    for (int g = q * per; g < (q + 1) * per; g++) {
+                        const float2 y = red2[3 * g + c];
+                        x = df_add(x, dfl{y.x, y.y});
+                    }
+                    tsum[t] = pd(x);
+                }
+            }
+            __syncthreads();
+            if (tid < cnt) {
+                const Bin &B = bins[tid];
+                const double s4 = 4.0 * K.df;
+                const double cd = s4 * exp2_int(B.eS - B.eD);
+                const double ch = s4 * exp2_int(B.eS) * (B.scale.x * B.scale.x + B.scale.y * B.scale.y);
+                double2 dh = cmul(make_double2(cd * tsum[3 * tid], cd * tsum[3 * tid + 1]), B.scale);
+                double2 hv = make_double2(ch * tsum[3 * tid + 2], 0.0);
+                if (!B.valid) {
+                    dh = make_double2(0.0, 0.0);
+                    hv = make_double2(0.0, 0.0);
+                }
+                if (B.b >= 0) {
+                    K.d_h[B.b] = dh;
+                    K.h_h[B.b] = hv;
+                }
+            }
+        }
+        __syncthreads();
+    }
+}

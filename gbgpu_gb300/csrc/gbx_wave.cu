@@ -21,6 +21,8 @@ namespace gbx {
 
 __device__ double2 g_tw_d[kTwN / 2];
 __device__ float2 g_tw_f[kTwN / 2];
+__device__ float4 g_tw_p[kTwN / 2];   // the same twiddles as float pairs (c.h, c.l, s.h, s.l)
+__device__ float4 g_sc_p[256];        // cos, sin of j pi/128 as float pairs (pair form)
 
 __global__ void tw_init_kernel()
 {
@@ -30,6 +32,14 @@ __global__ void tw_init_kernel()
         sincospi(-2.0 * (double)m / (double)kTwN, &s, &c);
         g_tw_d[m] = make_double2(c, s);
         g_tw_f[m] = make_float2((float)c, (float)s);
+        const dfl cp = df_from(c), sp = df_from(s);
+        g_tw_p[m] = make_float4(cp.h, cp.l, sp.h, sp.l);
+    }
+    if (m < 256) {
+        double s, c;
+        sincospi((double)m / 128.0, &s, &c);
+        const dfl cp = df_from(c), sp = df_from(s);
+        g_sc_p[m] = make_float4(cp.h, cp.l, sp.h, sp.l);
     }
 }
 
@@ -45,7 +55,15 @@ struct __align__(16) Bin {
     double om, om_m_dfa;           // 2 pi f0, 2 pi f0 - 2 pi q/T   (gbgpu.py:462-464)
     double pifdot, pi3fddot;       // pi fdot, pi/3 fddot           (gbgpu.py:495-500)
     double k[3];
-    double ep[6], ec[6];           // e+ and ex, order xx yy zz xy xz yz
+    union {
+        struct {
+            double ep[6], ec[6];   // e+ and ex, order xx yy zz xy xz yz (FP64 form)
+        } q;
+        struct {
+            dfl ud[3], vd[2];      // u and v (v has no z component) as pairs (pair form)
+            cpx DP, DC;            // polarisation factors divided by amp, as pairs
+        } pr;
+    };
     double2 DP, DC;                // polarisation factors divided by amp
     double2 scale;                 // amp * 0.5 T / N [* tdi2 factor]
     double A2, varpi, e2;          // third body (FP64 form)
@@ -55,9 +73,10 @@ struct __align__(16) Bin {
     float2 DPf, DCf;
     float f0f, fdotf, fddotf;
     float w0h, w0l, w1, w2;        // f(t)/fstar = (w0h + w0l) + w1 t + w2 t^2 (w0 split hi/lo)
+    float w1l;                     // w1 - (float)w1 (the pair form's w1 t term)
     dfl kd[3], omd, omdfad, phi0d, pfd;   // float-pair copies for the mixed carrier phase
     dfl tpfd;                      // 2 pi fdot as a float pair
-    float p3f, pfddf;              // pi/3 fddot, pi fddot
+    dfl p3d, pfddd;                // pi/3 fddot, pi fddot (the mixed form uses the heads)
     float A2f, e2f, varpif, sinvarpif;
     int start;                     // start index - start_freq_ind
     int b;                         // binary index
@@ -89,6 +108,7 @@ struct KParams {
     int P;                         // binaries per tile in uniform mode
     double fstar;                  // c / (2 pi L)
     dfl stepd[GBX_MAX_LOG2N + 1];  // T / 2^k as float pairs (exact: division by a power of two)
+    dfl Locd;                      // L / c as a float pair (pair form)
     int maxS;                      // largest tile (samples) the shared memory is sized for
     int maxP;                      // most binaries in a tile of this launch (<= kMaxPack)
 };
@@ -435,9 +455,16 @@ __device__ void setup_bin(Bin &B, const KParams &K, int b, int N, int mode)
     double v[3] = {sp, -cp, 0.0};
     B.k[0] = -st * cp; B.k[1] = -st * sp; B.k[2] = -ct;
     const int ia[6] = {0, 1, 2, 0, 0, 1}, ib[6] = {0, 1, 2, 1, 2, 2};
-    for (int c = 0; c < 6; c++) {
-        B.ep[c] = v[ia[c]] * v[ib[c]] - u[ia[c]] * u[ib[c]];
-        B.ec[c] = u[ia[c]] * v[ib[c]] + v[ia[c]] * u[ib[c]];
+    if (a.precision == GBX_PAIR) {
+        for (int c = 0; c < 3; c++) B.pr.ud[c] = df_from(u[c]);
+        for (int c = 0; c < 2; c++) B.pr.vd[c] = df_from(v[c]);
+        B.pr.DP = {df_from(B.DP.x), df_from(B.DP.y)};
+        B.pr.DC = {df_from(B.DC.x), df_from(B.DC.y)};
+    } else {
+        for (int c = 0; c < 6; c++) {
+            B.q.ep[c] = v[ia[c]] * v[ib[c]] - u[ia[c]] * u[ib[c]];
+            B.q.ec[c] = u[ia[c]] * v[ib[c]] + v[ia[c]] * u[ib[c]];
+        }
     }
     for (int c = 0; c < 3; c++) {
         B.kf[c] = (float)B.k[c];
@@ -450,8 +477,8 @@ __device__ void setup_bin(Bin &B, const KParams &K, int b, int N, int mode)
     B.phi0d = df_from(phi0);
     B.pfd = df_from(B.pifdot);
     B.tpfd = df_from(2.0 * B.pifdot);
-    B.p3f = (float)B.pi3fddot;
-    B.pfddf = (float)(kPi * fddot);
+    B.p3d = df_from(B.pi3fddot);
+    B.pfddd = df_from(kPi * fddot);
     B.DPf = make_float2((float)B.DP.x, (float)B.DP.y);
     B.DCf = make_float2((float)B.DC.x, (float)B.DC.y);
     B.f0f = (float)f0; B.fdotf = (float)fdot; B.fddotf = (float)fddot;
@@ -462,7 +489,9 @@ __device__ void setup_bin(Bin &B, const KParams &K, int b, int N, int mode)
         double w0 = f0 / fstar;
         B.w0h = (float)w0;
         B.w0l = (float)(w0 - (double)B.w0h);
-        B.w1 = (float)(fdot / fstar);
+        const double w1 = fdot / fstar;
+        B.w1 = (float)w1;
+        B.w1l = (float)(w1 - (double)B.w1);
         B.w2 = (float)(0.5 * fddot / fstar);
     }
     // start index, bit-exact with round(((q - N/2)/T)/(1/T))  (gbgpu.py:296, 387)
@@ -567,8 +596,8 @@ __device__ __forceinline__ void slow_fp64(const Bin &B, int n, int N, double tm,
     double2 A[3];
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        double pp = quad_form(B.ep, r[a][0], r[a][1], r[a][2]);
-        double cc = quad_form(B.ec, r[a][0], r[a][1], r[a][2]);
+        double pp = quad_form(B.q.ep, r[a][0], r[a][1], r[a][2]);
+        double cc = quad_form(B.q.ec, r[a][0], r[a][1], r[a][2]);
         A[a] = make_double2(pp * B.DP.x + cc * B.DC.x, pp * B.DP.y + cc * B.DC.y);
     }
     // links (ij, sym arm, spacecraft, sign of kdotr): 12,23,31,21,32,13
@@ -653,9 +682,9 @@ __device__ __forceinline__ void slow_mixed(const Bin &B, int n, int N, dfl step,
     const float tf = tm.h;
     dfl Phi0 = df_add(df_mul(B.omdfad, tm), B.phi0d);
     const dfl tm2 = df_mul(tm, tm);
-    Phi0 = df_add(Phi0, df_mul(tm2, df_fast(B.pfd.h, fmaf(B.p3f, tf, B.pfd.l))));
+    Phi0 = df_add(Phi0, df_mul(tm2, df_fast(B.pfd.h, fmaf(B.p3d.h, tf, B.pfd.l))));
     Phi0 = df_neg(Phi0);
-    const dfl wt = df_add(B.omd, df_add(df_mul(B.tpfd, tm), dfl{B.pfddf * tf * tf, 0.0f}));
+    const dfl wt = df_add(B.omd, df_add(df_mul(B.tpfd, tm), dfl{B.pfddd.h * tf * tf, 0.0f}));
     const float fdt = fmaf(B.fddotf, tf, B.fdotf);
     const dfl kP0 = kP1_pair(B, tabf, N, n);
     // its phase, reduced mod 2 pi
@@ -671,7 +700,7 @@ __device__ __forceinline__ void slow_mixed(const Bin &B, int n, int N, dfl step,
 #pragma unroll
     for (int s = 0; s < 3; s++) {
         const float kPf = kP0.h + dk[s];
-        const float small = kPf * kPf * fmaf(kPf, (1.0f / 3.0f) * B.pfddf, -(float)kPi * fdt);
+        const float small = kPf * kPf * fmaf(kPf, (1.0f / 3.0f) * B.pfddd.h, -(float)kPi * fdt);
         dfl ph = ph0;
         if (s > 0) {
             const dfl d = df_two_sum(ph0.h, dk[s] * wt.h);
@@ -1499,6 +1528,8 @@ __global__ void __launch_bounds__(kPrepBlock) prep_kernel(const KParams K)
     for (int k = threadIdx.x; k < n16; k += kPrepBlock) dst[k] = src[k];
 }
 
+constexpr int kPairMaxLog2N = 12;  // pair form: N <= 4096 (two 16-byte channels of 4096 fit)
+#include "gbx_pair.cuh"
 #include "gbx_grad.cuh"
 
 // ----------------------------------------------------------------------------
@@ -1517,12 +1548,18 @@ static size_t smem_bytes(int prec, bool third, int maxS, int nch, int maxP)
     return s;
 }
 
-template <typename R, int MODE, bool THIRD>
-static int launch_one(const KParams &K, int maxS, cudaStream_t st)
+// the pair form's layout: constants, reduction scratch, sin/cos table, buffers
+static size_t pair_smem_bytes(int maxS, int nch, int maxP)
 {
-    auto kern = wave_kernel<R, MODE, THIRD>;
-    size_t sm = smem_bytes(sizeof(R) == 8 ? GBX_FP64 : GBX_MIXED, THIRD, maxS, MODE == MODE_WAVE ? 3 : 2,
-                           K.maxP);
+    return sizeof(Bin) * (size_t)maxP + sizeof(double) * (size_t)red_doubles(maxS) +
+           sizeof(float4) * (size_t)kScN + (size_t)nch * maxS * sizeof(cpx);
+}
+
+// persistent launch of one tile kernel (after the per-binary prep_kernel when
+// the caller gave a workspace)
+template <int MODE>
+static int launch_tiles(void (*kern)(const KParams), size_t sm, const KParams &K, cudaStream_t st)
+{
     if (sm > 227 * 1024) return set_error(GBX_ERR_UNSUPPORTED, "tile needs %zu B of shared memory", sm);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute");
@@ -1558,6 +1595,14 @@ static int launch_one(const KParams &K, int maxS, cudaStream_t st)
     return GBX_OK;
 }
 
+template <typename R, int MODE, bool THIRD>
+static int launch_one(const KParams &K, int maxS, cudaStream_t st)
+{
+    const size_t sm = smem_bytes(sizeof(R) == 8 ? GBX_FP64 : GBX_MIXED, THIRD, maxS,
+                                 MODE == MODE_WAVE ? 3 : 2, K.maxP);
+    return launch_tiles<MODE>(wave_kernel<R, MODE, THIRD>, sm, K, st);
+}
+
 // most binaries in one tile of this launch (the shared memory holds their constants)
 static int max_pack(const gbx_wave_args *a, int minp)
 {
@@ -1574,6 +1619,15 @@ static int dispatch(KParams &K, int maxS, cudaStream_t st)
     K.maxS = maxS;
     K.maxP = max_pack(&K.a, MODE == MODE_SWAP ? 2 : 1);
     const bool third = K.a.nparams >= 14;
+    if (K.a.precision == GBX_PAIR) {
+        if constexpr (MODE == MODE_WAVE || MODE == MODE_LL) {
+            if (third) return set_error(GBX_ERR_UNSUPPORTED, "the pair form covers the 9-parameter model");
+            return launch_tiles<MODE>(pair_kernel<MODE>,
+                                      pair_smem_bytes(maxS, MODE == MODE_WAVE ? 3 : 2, K.maxP), K, st);
+        } else {
+            return set_error(GBX_ERR_UNSUPPORTED, "the pair form covers gbx_waveform and gbx_waveform_ll");
+        }
+    }
     if (K.a.precision == GBX_FP64) {
         return third ? launch_one<double, MODE, true>(K, maxS, st)
                      : launch_one<double, MODE, false>(K, maxS, st);
@@ -1588,7 +1642,7 @@ static int check_wave(const gbx_wave_args *a, int *maxS)
     if (!a || !a->params) return set_error(GBX_ERR_ARG, "NULL wave args / params");
     if (a->num_bin < 0) return set_error(GBX_ERR_ARG, "num_bin < 0");
     if (a->nparams != 9 && a->nparams != 14) return set_error(GBX_ERR_ARG, "nparams must be 9 or 14");
-    if (a->precision != GBX_FP64 && a->precision != GBX_MIXED)
+    if (a->precision != GBX_FP64 && a->precision != GBX_MIXED && a->precision != GBX_PAIR)
         return set_error(GBX_ERR_ARG, "unknown precision %d", a->precision);
     if (!(a->T > 0.0) || !(a->armlength > 0.0)) return set_error(GBX_ERR_ARG, "T and armlength must be > 0");
     if (a->nparams == 14 && !(a->year > 0.0)) return set_error(GBX_ERR_ARG, "year must be > 0");
@@ -1600,7 +1654,7 @@ static int check_wave(const gbx_wave_args *a, int *maxS)
     if (a->tile != 0 && (a->tile < 64 || a->tile > 4096 || (a->tile & (a->tile - 1)) != 0))
         return set_error(GBX_ERR_ARG, "tile=%d: need 0 or a power of two in [64, 4096]", a->tile);
     if (a->blocks_per_sm < 0) return set_error(GBX_ERR_ARG, "blocks_per_sm < 0");
-    const int maxlg = a->precision == GBX_FP64 ? 12 : GBX_MAX_LOG2N;
+    const int maxlg = a->precision == GBX_MIXED ? GBX_MAX_LOG2N : 12;
     if (a->tiles == nullptr) {
         int N = a->N;
         if (N < 32 || (N & (N - 1)) != 0) return set_error(GBX_ERR_UNSUPPORTED, "N=%d: need a power of two >= 32", N);
@@ -1627,6 +1681,7 @@ static KParams base_params(const gbx_wave_args *a)
     K.a = *a;
     K.fstar = kCSI / (a->armlength * 2.0 * kPi);
     for (int k = 0; k <= GBX_MAX_LOG2N; k++) K.stepd[k] = df_from(ldexp(a->T, -k));
+    K.Locd = df_from(a->armlength / kCSI);
     K.P = a->tiles == nullptr ? tile_pack(a->tile, 31 - __builtin_clz((unsigned)a->N), 1) : 1;
     return K;
 }

@@ -26,7 +26,7 @@ from .constants import YRSID_SI
 from .orbits import EqualArmlengthOrbits, Orbits
 from .utility import get_N
 
-_PRECISIONS = {"fp64": nat.GBX_FP64, "mixed": nat.GBX_MIXED}
+_PRECISIONS = {"fp64": nat.GBX_FP64, "mixed": nat.GBX_MIXED, "pair": nat.GBX_PAIR}
 _TILE_MIN = 512       # default samples per tile of the fused kernels
 _MAX_PACK = 16        # most binaries in one tile
 _PLAN_CACHE = 64      # WavePlans kept per GBGPU object
@@ -356,8 +356,15 @@ class GBGPUBase(abc.ABC):
 
     # -------------------------------------------------------------- waveform
     def run_wave(self, amp, f0, fdot, fddot, phi0, iota, psi, lam, beta, *args, N=None,
-                 T=4 * YRSID_SI, dt=10.0, oversample=1, tdi2=False):
-        """Batched X/Y/Z and A/E/T windows (reference gbgpu/gbgpu.py:108-316)."""
+                 T=4 * YRSID_SI, dt=10.0, oversample=1, tdi2=False, precision="fp64"):
+        """Batched X/Y/Z and A/E/T windows (reference gbgpu/gbgpu.py:108-316).
+
+        ``precision`` (not in the reference) is ``"fp64"`` (the plain form,
+        default) or ``"pair"`` (float-pair arithmetic, within ~1e-10 of it);
+        the FP32 ``"mixed"`` form is also accepted.
+        """
+        if precision not in _PRECISIONS:
+            raise ValueError(f"precision must be one of {list(_PRECISIONS)}")
         N_obs = int(T / dt)
         T = N_obs * dt
         self._check_T(T)
@@ -366,14 +373,14 @@ class GBGPUBase(abc.ABC):
         if np.ndim(N) != 0:
             raise NotImplementedError("run_wave takes one N per call (as the reference)")
         params = self._params((amp, f0, fdot, fddot, phi0, iota, psi, lam, beta), add_args)
-        self._wave_from_params(params, N, T, tdi2)
+        self._wave_from_params(params, N, T, tdi2, precision)
 
-    def _wave_from_params(self, params, N, T, tdi2):
+    def _wave_from_params(self, params, N, T, tdi2, precision="fp64"):
         B = params.shape[1]
         self.num_bin = B
         self.N = N
         self.df = 1 / T
-        plan = self._plan(N, T, "fp64", tdi2, params.shape[0])
+        plan = self._plan(N, T, precision, tdi2, params.shape[0])
         XYZ = torch.empty((B, 3, N), dtype=torch.complex128, device=self.device)
         AET = torch.empty((B, 3, N), dtype=torch.complex128, device=self.device)
         start = torch.empty(B, dtype=torch.int32, device=self.device)

@@ -33,6 +33,8 @@ extern "C" {
 /* ---- precision of the waveform family ---- */
 #define GBX_FP64 0             /* every step in FP64 (the plain form) */
 #define GBX_MIXED 1            /* FP64 carrier phase, delays and reductions; FP32 slow part + FFT */
+#define GBX_PAIR 2             /* slow part, FFT and <d|h> in float pairs (FP32 pipe, ~44 bits);
+                                  gbx_waveform and gbx_waveform_ll only, 9 parameters, N <= 4096 */
 
 #define GBX_MAX_LOG2N 13       /* N = 2^k, 5 <= k <= 13 (FP64 form: k <= 12) */
 
@@ -138,6 +140,9 @@ int gbx_fill_global_det(void *A_glob, void *E_glob, const void *A_template,
  * holds P_s/c and the arm unit vectors r_12, r_23, r_31 = (P_j - P_i)/L
  * (gbgpu/gbgpu.py:424-427) in FP64 and FP32; it is what the waveform family
  * reads.  `table` must hold gbx_orbit_table_bytes(N) bytes, 16-byte aligned.
+ * Layout (rows of N, sample n fastest): 18 FP64 rows P_s/c, r_12, r_23,
+ * r_31; then 36 FP32 rows: r (9), P_s/c as float pairs (9 heads, 9 tails),
+ * r's tails (9).
  */
 size_t gbx_orbit_table_bytes(int N);
 int gbx_orbit_table(void *table, const double *sc_pos, int N, double armlength,

@@ -2,8 +2,11 @@
 
 Tolerances: start indices bit-exact; the FP64 form within 1e-10 relative
 (normwise per binary for waveform windows, per value for <d|h>, <h|h>,
-templates); the mixed form within |dlogL| <= 1e-6 max(1, SNR^2) with
-SNR^2 = <h|h>, plus a stated per-output bound on the raw terms.
+templates); the pair form within 1e-10 normwise on the waveform windows and
+1e-9 relative on <d|h> and <h|h>, with |dlogL| <= 1e-8 max(1, SNR^2); the
+mixed form within |dlogL| <= 1e-6
+max(1, SNR^2) with SNR^2 = <h|h>, plus a stated per-output bound on the raw
+terms.
 """
 
 import numpy as np
@@ -19,6 +22,7 @@ WAVE_CASES = ["wave_n128", "wave_n256_tdi2", "wave_n64_1yr", "wave_n512_hf",
               "wave_n2048_hf", "wave_b1", "wave_n4096"]
 FP64_TOL = 1e-10
 MIXED_LL_TOL = 1e-6
+PAIR_LL_TOL = 1e-8
 
 
 def dev(x, dtype=None):
@@ -32,12 +36,13 @@ def gbgpu():
     return GBGPU
 
 
+@pytest.mark.parametrize("precision", ["fp64", "pair"])
 @pytest.mark.parametrize("case", WAVE_CASES)
-def test_run_wave_matches_reference(gbgpu, case):
+def test_run_wave_matches_reference(gbgpu, case, precision):
     g = load_golden(case)
     gb = gbgpu()
     gb.run_wave(*g["params"], N=int(g["N"]), T=float(g["T"]), dt=float(g["dt"]),
-                tdi2=bool(g["tdi2"]))
+                tdi2=bool(g["tdi2"]), precision=precision)
     np.testing.assert_array_equal(gb.start_inds.cpu().numpy(), g["start_inds"])
     assert np.max(rel_err(gb.XYZf.cpu().numpy(), g["XYZf"], axis=(1, 2))) < FP64_TOL
     assert np.max(rel_err(gb.AETf.cpu().numpy(), g["AETf"], axis=(1, 2))) < FP64_TOL
@@ -47,7 +52,7 @@ def test_run_wave_matches_reference(gbgpu, case):
 
 
 @pytest.mark.parametrize("case", ["ll_basic", "ll_multi", "ll_phasemarg"])
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "pair", "mixed"])
 def test_get_ll_matches_reference(gbgpu, case, precision):
     g = load_golden(case)
     gb = gbgpu()
@@ -69,13 +74,17 @@ def test_get_ll_matches_reference(gbgpu, case, precision):
         np.testing.assert_allclose(d_h, g["d_h"], rtol=FP64_TOL, atol=0)
         np.testing.assert_allclose(h_h.real, g["h_h"].real, rtol=FP64_TOL, atol=0)
         np.testing.assert_allclose(like, g["like"], rtol=FP64_TOL)
+    elif precision == "pair":
+        np.testing.assert_allclose(d_h, g["d_h"], rtol=1e-9, atol=0)
+        np.testing.assert_allclose(h_h.real, g["h_h"].real, rtol=1e-9, atol=0)
+        assert np.max(np.abs(like - g["like"]) / np.maximum(1.0, snr2)) < PAIR_LL_TOL
     else:
         assert np.max(np.abs(like - g["like"]) / np.maximum(1.0, snr2)) < MIXED_LL_TOL
         # stated per-output bound of the mixed form: |d(h_h)| <= 1e-6 h_h
         assert np.max(np.abs(h_h.real - g["h_h"].real) / snr2) < 1e-6
     if bool(g["phase_marginalize"]):
         np.testing.assert_allclose(gb.non_marg_d_h, g["non_marg_d_h"],
-                                   rtol=FP64_TOL if precision == "fp64" else 1e-5)
+                                   rtol={"fp64": FP64_TOL, "pair": 1e-9}.get(precision, 1e-5))
     # the waveform attributes are produced on demand after the fused call
     np.testing.assert_array_equal(gb.start_inds.cpu().numpy(), g["start_inds"])
 
@@ -225,6 +234,19 @@ def test_third_body_matches_reference(case):
     np.testing.assert_array_equal(gb.start_inds.cpu().numpy(), g["start_inds"])
     assert np.max(rel_err(gb.XYZf.cpu().numpy(), g["XYZf"], axis=(1, 2))) < FP64_TOL
     assert np.max(rel_err(gb.AETf.cpu().numpy(), g["AETf"], axis=(1, 2))) < FP64_TOL
+
+
+def test_pair_form_declines_the_third_body():
+    """The pair form covers the 9-parameter model; the third body's 14 raise."""
+    from gbgpu_gb300 import GBGPUThirdBody
+    g = load_golden("ll_third")
+    gb = GBGPUThirdBody()
+    gb.d_d = float(g["d_d"])
+    with pytest.raises(RuntimeError, match="pair form"):
+        gb.get_ll(g["params"], [dev(g["A_data"]), dev(g["E_data"])],
+                  [dev(g["A_psd"]), dev(g["E_psd"])], N=int(g["N"]), T=float(g["T"]),
+                  dt=float(g["dt"]), tdi2=bool(g["tdi2"]),
+                  start_freq_ind=int(g["start_freq_ind"]), precision="pair")
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])

@@ -369,8 +369,8 @@ def test_reference_arm_json_line_on_cpu():
     needs no GPU and prints one JSON line with the contract's keys."""
     import json
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
-                        "--steps", "1", "--warmup", "1"], capture_output=True, text=True,
-                       timeout=600, cwd=ROOT)
+                        "--steps", "1", "--warmup", "1", "--binaries", "20000"],
+                       capture_output=True, text=True, timeout=600, cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [x for x in r.stdout.splitlines() if x.startswith("{")]
     assert len(lines) == 1
@@ -382,7 +382,10 @@ def test_reference_arm_json_line_on_cpu():
     assert d["impl"] == "reference" and d["unit"] == "binaries/s" and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
-    assert "workload" in d["config"]
+    assert "workload" in d["config"] and d["config"]["binaries_per_gpu"] == 20000
+    # the whole batch is timed in every step: steps x ms_per_step is the timed region
+    assert abs(d["value"] * d["ms_per_step"] / 1e3 - 20000) < 1.0
+    assert sum(d["config"]["N_mix"].values()) == 20000
 
 
 def test_N_none_resolves_to_the_batch_maximum_as_the_reference():
