@@ -15,14 +15,36 @@
 // This file is included inside namespace gbx by gbx_wave.cu.
 
 // ---------------------------------------------------------------- arithmetic
-__device__ __forceinline__ dfl p_sub(dfl a, dfl b) { return df_add(a, dfl{-b.h, -b.l}); }
+// Sums are renormalised (Fast2Sum of head and tail): after a cancellation
+// the tail of an unnormalised sum can reach the size of its head, and a later
+// product would then round its cross term on that tail to FP32 precision.
+// Products are not: their tail is the exact rounding error of the head plus
+// the operands' cross terms, within a few units in the last place of the
+// head, so the next operation keeps ~44 significant bits without the three
+// instructions of a renormalisation.
+__device__ __forceinline__ dfl p_add(dfl a, dfl b) { return df_add(a, b); }
+__device__ __forceinline__ dfl p_sub(dfl a, dfl b) { return p_add(a, dfl{-b.h, -b.l}); }
 
-// a + b when |a| >= |b| (or a = 0): Fast2Sum of the heads, renormalised
+// a + b when |a.h| >= |b.h| (or a = 0): Fast2Sum of the heads, renormalised
 __device__ __forceinline__ dfl p_addf(dfl a, dfl b)
 {
     const float s = a.h + b.h;
-    const float e = b.h - (s - a.h);
-    return df_fast(s, e + (a.l + b.l));
+    return df_fast(s, (b.h - (s - a.h)) + (a.l + b.l));
+}
+
+__device__ __forceinline__ dfl p_mul(dfl a, dfl b)
+{
+    const float p = a.h * b.h;
+    float e = fmaf(a.h, b.h, -p);
+    e = fmaf(a.h, b.l, e);
+    e = fmaf(a.l, b.h, e);
+    return {p, e};
+}
+
+__device__ __forceinline__ dfl p_mulf(dfl a, float b)
+{
+    const float p = a.h * b;
+    return {p, fmaf(a.l, b, fmaf(a.h, b, -p))};
 }
 
 __device__ __forceinline__ dfl p_scale(dfl a, float pow2) { return dfl{a.h * pow2, a.l * pow2}; }
@@ -30,9 +52,7 @@ __device__ __forceinline__ dfl p_scale(dfl a, float pow2) { return dfl{a.h * pow
 __device__ __forceinline__ dfl p_sqr(dfl a)
 {
     const float p = a.h * a.h;
-    float e = fmaf(a.h, a.h, -p);
-    e = fmaf(a.h + a.h, a.l, e);
-    return df_fast(p, e);
+    return {p, fmaf(a.h + a.h, a.l, fmaf(a.h, a.h, -p))};
 }
 
 // a b + c d
@@ -64,11 +84,11 @@ __device__ __forceinline__ dfl p_dot3(dfl a, dfl b, dfl c, dfl d, dfl e, dfl f)
 __device__ __forceinline__ dfl p_div(dfl n, dfl d)
 {
     const float q1 = n.h / d.h;
-    const dfl r = df_add(n, df_neg(df_mul_f(d, q1)));
-    return df_fast(q1, r.h / d.h);
+    const dfl r = p_sub(n, p_mulf(d, q1));
+    return df_fast(q1, (r.h + r.l) / d.h);
 }
 
-__device__ __forceinline__ cpx cp_add(cpx a, cpx b) { return {df_add(a.x, b.x), df_add(a.y, b.y)}; }
+__device__ __forceinline__ cpx cp_add(cpx a, cpx b) { return {p_add(a.x, b.x), p_add(a.y, b.y)}; }
 __device__ __forceinline__ cpx cp_sub(cpx a, cpx b) { return {p_sub(a.x, b.x), p_sub(a.y, b.y)}; }
 __device__ __forceinline__ cpx cp_neg(cpx a) { return {df_neg(a.x), df_neg(a.y)}; }
 __device__ __forceinline__ cpx cp_pow2(cpx a, float s) { return {p_scale(a.x, s), p_scale(a.y, s)}; }
@@ -76,7 +96,7 @@ __device__ __forceinline__ cpx cp_mul(cpx a, cpx b)
 {
     return {p_dot2(a.x, b.x, df_neg(a.y), b.y), p_dot2(a.x, b.y, a.y, b.x)};
 }
-__device__ __forceinline__ cpx cp_scale(cpx a, dfl r) { return {df_mul(a.x, r), df_mul(a.y, r)}; }
+__device__ __forceinline__ cpx cp_scale(cpx a, dfl r) { return {p_mul(a.x, r), p_mul(a.y, r)}; }
 __device__ __forceinline__ cpx cp_zero() { return {{0.f, 0.f}, {0.f, 0.f}}; }
 __device__ __forceinline__ double pd(dfl a) { return (double)a.h + (double)a.l; }
 
@@ -103,8 +123,8 @@ __device__ __forceinline__ void sincos_pair(dfl x, const float4 *__restrict__ ta
     const dfl sd = {d.h, fmaf(d.h * d2, -1.0f / 6.0f, d.l)};
     const float eps = d2 * fmaf(d2, 1.0f / 24.0f, -0.5f);   // cos d - 1
     const dfl Tc = {t.x, t.y}, Ts = {t.z, t.w};
-    const dfl cc = df_add(Tc, df_neg(df_mul(Ts, sd)));
-    const dfl ss = df_add(Ts, df_mul(Tc, sd));
+    const dfl cc = p_add(Tc, df_neg(p_mul(Ts, sd)));
+    const dfl ss = p_add(Ts, p_mul(Tc, sd));
     c = df_fast(cc.h, fmaf(Tc.h, eps, cc.l));
     s = df_fast(ss.h, fmaf(Ts.h, eps, ss.l));
 }
@@ -124,16 +144,16 @@ __device__ __forceinline__ void sinc_cos_pair(dfl a, const float4 *__restrict__ 
         q = fmaf(q, xf, 1.0f / 362880.0f);
         q = fmaf(q, xf, -1.0f / 5040.0f);
         dfl r = p_addf(s2, dfl{xf * q, 0.f});
-        r = p_addf(s1, df_mul(x, r));
-        S = p_addf(dfl{1.f, 0.f}, df_mul(x, r));
+        r = p_addf(s1, p_mul(x, r));
+        S = p_addf(dfl{1.f, 0.f}, p_mul(x, r));
         constexpr dfl c2 = dconst(1.0 / 24.0);
         float u = fmaf(xf, -1.0f / 87178291200.0f, 1.0f / 479001600.0f);
         u = fmaf(u, xf, -1.0f / 3628800.0f);
         u = fmaf(u, xf, 1.0f / 40320.0f);
         u = fmaf(u, xf, -1.0f / 720.0f);
         dfl v = p_addf(c2, dfl{xf * u, 0.f});
-        v = p_addf(dfl{-0.5f, 0.f}, df_mul(x, v));
-        C = df_add(dfl{1.f, 0.f}, df_mul(x, v));
+        v = p_addf(dfl{-0.5f, 0.f}, p_mul(x, v));
+        C = p_add(dfl{1.f, 0.f}, p_mul(x, v));
     } else {
         dfl sn;
         sincos_pair(a, tab, C, sn);
@@ -167,31 +187,31 @@ __device__ __forceinline__ void slow_pair(const Bin &B, int n, int N, dfl step, 
 #pragma unroll
     for (int a = 0; a < 3; a++)
         kr[a] = p_dot3(B.kd[0], r[a][0], B.kd[1], r[a][1], B.kd[2], r[a][2]);
-    const dfl tm = df_mul_f(step, (float)n);                 // n T/N
+    const dfl tm = p_mulf(step, (float)n);                 // n T/N
     const float tf = tm.h;
     const dfl tm2 = p_sqr(tm);
     // carrier phase of spacecraft 1 (the expansion in slow_mixed):
     //   Phi0(tm) + kP w(tm) - pi kP^2 fd(tm) + pi/3 fddot kP^3
-    dfl Phi0 = df_add(df_mul(B.omdfad, tm), B.phi0d);
-    Phi0 = df_neg(df_add(Phi0, df_mul(tm2, df_add(B.pfd, df_mul(B.p3d, tm)))));
-    const dfl wt = df_add(B.omd, df_add(df_mul(B.tpfd, tm), df_mul(B.pfddd, tm2)));
+    dfl Phi0 = p_add(p_mul(B.omdfad, tm), B.phi0d);
+    Phi0 = df_neg(p_add(Phi0, p_mul(tm2, p_add(B.pfd, p_mul(B.p3d, tm)))));
+    const dfl wt = p_add(B.omd, p_add(p_mul(B.tpfd, tm), p_mul(B.pfddd, tm2)));
     const float fdt = fmaf(B.fddotf, tf, B.fdotf);
     const dfl kP0 = kP1_pair(B, tabf, N, n);
-    dfl ph0 = df_add(Phi0, df_mul(kP0, wt));
+    dfl ph0 = p_add(Phi0, p_mul(kP0, wt));
     {
         const float q = rintf(ph0.h * (float)kInvTwoPi);
-        ph0 = df_add(ph0, df_neg(df_mul_f(dconst(kTwoPi), q)));
+        ph0 = p_add(ph0, df_neg(p_mulf(dconst(kTwoPi), q)));
     }
     // spacecraft 2 and 3: k.P_s/c = k.P_1/c + (L/c) k.r_12 and - (L/c) k.r_31
-    const dfl dk[3] = {dfl{0.f, 0.f}, df_mul(Loc, kr[0]), df_neg(df_mul(Loc, kr[2]))};
+    const dfl dk[3] = {dfl{0.f, 0.f}, p_mul(Loc, kr[0]), df_neg(p_mul(Loc, kr[2]))};
     // f(t)/fstar = w0 + w1 t + w2 t^2 with w1 t a pair: at f0 = 1e-4 Hz and
     // fdot = 1e-15 that term is 1e-3 of w0, and omL enters fc2 squared
-    const dfl base = p_addf(dfl{B.w0h, B.w0l}, df_mul(dfl{B.w1, B.w1l}, tm));
+    const dfl base = p_addf(dfl{B.w0h, B.w0l}, p_mul(dfl{B.w1, B.w1l}, tm));
     cpx E[3];
     dfl fo[3];
 #pragma unroll
     for (int s = 0; s < 3; s++) {
-        dfl ph = s == 0 ? ph0 : df_add(ph0, df_mul(dk[s], wt));
+        dfl ph = s == 0 ? ph0 : p_add(ph0, p_mul(dk[s], wt));
         const float kPf = kP0.h + dk[s].h;
         ph.l += kPf * kPf * fmaf(kPf, B.p3d.h, -(float)kPi * fdt);   // below 1e-8 rad
         dfl cs, sn;
@@ -209,7 +229,7 @@ __device__ __forceinline__ void slow_pair(const Bin &B, int n, int N, dfl step, 
         const dfl ru = p_dot3(B.pr.ud[0], r[a][0], B.pr.ud[1], r[a][1], B.pr.ud[2], r[a][2]);
         const dfl rv = p_dot2(B.pr.vd[0], r[a][0], B.pr.vd[1], r[a][1]);
         const dfl pp = p_scale(p_dot2(rv, rv, df_neg(ru), ru), 0.25f);
-        const dfl cc = p_scale(df_mul(ru, rv), 0.5f);
+        const dfl cc = p_scale(p_mul(ru, rv), 0.5f);
         A[a] = {p_dot2(pp, B.pr.DP.x, cc, B.pr.DC.x), p_dot2(pp, B.pr.DP.y, cc, B.pr.DC.y)};
     }
     // links (ij, arm, spacecraft): 12,23,31 (+k.r), 21,32,13 (-k.r)
@@ -219,10 +239,10 @@ __device__ __forceinline__ void slow_pair(const Bin &B, int n, int N, dfl step, 
         const int arm = q < 3 ? q : q - 3;
         const int s = q < 3 ? q : (q - 2) % 3;
         const dfl k = q < 3 ? kr[arm] : df_neg(kr[arm]);
-        const dfl a = p_scale(df_mul(fo[s], p_addf(dfl{1.f, 0.f}, k)), 0.5f);
+        const dfl a = p_scale(p_mul(fo[s], p_addf(dfl{1.f, 0.f}, k)), 0.5f);
         dfl S, C;
         sinc_cos_pair(a, sct, S, C);
-        const cpx T = {df_mul(S, C), df_neg(df_mul(df_mul(a, S), S))};   // sinc(a) e^{-ia}
+        const cpx T = {p_mul(S, C), df_neg(p_mul(p_mul(a, S), S))};   // sinc(a) e^{-ia}
         P[q] = cp_mul(T, A[arm]);
     }
     // omega L, fc = e^{-i omL}, fc2 = 4 omL sin(omL) fc (gbgpu.py:362-368)
@@ -230,8 +250,8 @@ __device__ __forceinline__ void slow_pair(const Bin &B, int n, int N, dfl step, 
     dfl co, so;
     sincos_pair(omL, sct, co, so);
     const cpx fc = {co, df_neg(so)};
-    const dfl g4 = p_scale(df_mul(omL, so), 4.f);
-    const cpx fc2 = {df_mul(g4, co), df_neg(df_mul(g4, so))};
+    const dfl g4 = p_scale(p_mul(omL, so), 4.f);
+    const cpx fc2 = {p_mul(g4, co), df_neg(p_mul(g4, so))};
     // F_s = fc (P12 - P13), fc (P23 - P21), fc (P31 - P32)
     const cpx F0 = cp_mul(fc, cp_sub(P[0], P[5]));
     const cpx F1 = cp_mul(fc, cp_sub(P[1], P[3]));
@@ -487,23 +507,23 @@ __global__ void __launch_bounds__(kBlock, 2) pair_kernel(const KParams K)
                         const dfl wA = df_recip(d2ff_scaled(__ldg(K.A_psd + jn), B.eS));
                         const dfl wE = df_recip(d2ff_scaled(__ldg(K.E_psd + jn), B.eS));
                         // conj(d) h / S  (gbgpu_utils.cu:172-178), d / S first
-                        const dfl ar = df_mul(d2ff_scaled(dA.x, B.eD), wA);
-                        const dfl ai = df_mul(d2ff_scaled(dA.y, B.eD), wA);
-                        const dfl er = df_mul(d2ff_scaled(dE.x, B.eD), wE);
-                        const dfl ei = df_mul(d2ff_scaled(dE.y, B.eD), wE);
-                        sr = df_add(sr, df_add(p_dot2(ar, tA.x, ai, tA.y), p_dot2(er, tE.x, ei, tE.y)));
-                        si = df_add(si, df_add(p_dot2(ar, tA.y, df_neg(ai), tA.x),
+                        const dfl ar = p_mul(d2ff_scaled(dA.x, B.eD), wA);
+                        const dfl ai = p_mul(d2ff_scaled(dA.y, B.eD), wA);
+                        const dfl er = p_mul(d2ff_scaled(dE.x, B.eD), wE);
+                        const dfl ei = p_mul(d2ff_scaled(dE.y, B.eD), wE);
+                        sr = p_add(sr, p_add(p_dot2(ar, tA.x, ai, tA.y), p_dot2(er, tE.x, ei, tE.y)));
+                        si = p_add(si, p_add(p_dot2(ar, tA.y, df_neg(ai), tA.x),
                                                p_dot2(er, tE.y, df_neg(ei), tE.x)));
-                        xh = df_add(xh, p_dot2(p_dot2(tA.x, tA.x, tA.y, tA.y), wA,
+                        xh = p_add(xh, p_dot2(p_dot2(tA.x, tA.x, tA.y, tA.y), wA,
                                                p_dot2(tE.x, tE.x, tE.y, tE.y), wE));
                     }
                 }
                 if (out) flag(a.status, GBX_FLAG_WINDOW);
             }
             for (int o = width >> 1; o > 0; o >>= 1) {
-                sr = df_add(sr, dfl{shfl4(sr.h, o), shfl4(sr.l, o)});
-                si = df_add(si, dfl{shfl4(si.h, o), shfl4(si.l, o)});
-                xh = df_add(xh, dfl{shfl4(xh.h, o), shfl4(xh.l, o)});
+                sr = p_add(sr, dfl{shfl4(sr.h, o), shfl4(sr.l, o)});
+                si = p_add(si, dfl{shfl4(si.h, o), shfl4(si.l, o)});
+                xh = p_add(xh, dfl{shfl4(xh.h, o), shfl4(xh.l, o)});
             }
             if ((tid & (width - 1)) == 0) {
                 float2 *red2 = reinterpret_cast<float2 *>(red);
@@ -522,7 +542,7 @@ __global__ void __launch_bounds__(kBlock, 2) pair_kernel(const KParams K)
                     dfl x = {0.f, 0.f};
                     for (int g = q * per; g < (q + 1) * per; g++) {
                         const float2 y = red2[3 * g + c];
-                        x = df_add(x, dfl{y.x, y.y});
+                        x = p_add(x, dfl{y.x, y.y});
                     }
                     tsum[t] = pd(x);
                 }
