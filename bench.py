@@ -308,6 +308,78 @@ def make_data(gb, p, Ns, seed):
     return data, Sd, d_d, S
 
 
+def draw_config0(seed, B=1000):
+    """(9, B) parameters of the plain-FP64 workload: amp log-U(1e-23, 1e-21),
+    f0 U(1e-3, 5e-3) Hz, fdot log-U(1e-18, 1e-15), fddot = 11/3 fdot^2/f0,
+    phi0, lam U[0, 2 pi), psi U[0, pi), iota = arccos U[-1, 1], beta =
+    arcsin U[-1, 1]."""
+    rng = np.random.default_rng(seed)
+    f0 = rng.uniform(1e-3, 5e-3, B)
+    fdot = 10 ** rng.uniform(-18, -15, B)
+    return np.array([10 ** rng.uniform(-23, -21, B), f0, fdot, 11.0 / 3.0 * fdot ** 2 / f0,
+                     rng.uniform(0, 2 * np.pi, B), np.arccos(rng.uniform(-1, 1, B)),
+                     rng.uniform(0, np.pi, B), rng.uniform(0, 2 * np.pi, B),
+                     np.arcsin(rng.uniform(-1, 1, B))])
+
+
+CFG0_N, CFG0_DT = 128, 10.0
+
+
+def config0_bench(gb, seed, steps):
+    """The plain-FP64 workload: 1,000 binaries, N = 128, dt = 10 s, on the
+    4-yr grid from 0 to 0.1 Hz (the same 12,623,041 bins: T is a multiple of
+    10 s too; the configuration's 0-0.1 Hz is taken literally although 10 s
+    samples put Nyquist at 0.05 Hz); data = the injected sum of the 1,000
+    binaries + noise.  A step is run_wave (A/E/T and X/Y/Z windows) and
+    get_ll through the class API, parameters on the device.  The CPU leg
+    times the oracle's FP64 run_wave + get_ll on one core."""
+    import torch
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    p = draw_config0(seed)
+    B = p.shape[1]
+    data, Sd, S = make_noise(seed + 11)
+    tmpl = torch.zeros((1, 2, Sd.shape[0]), dtype=torch.complex128, device="cuda")
+    gb.generate_global_template(p.T, np.zeros(B, np.int32), tmpl, N=CFG0_N, T=T_OBS, dt=CFG0_DT,
+                                precision="fp64")
+    data[0] += tmpl[0, 0]
+    data[1] += tmpl[0, 1]
+    del tmpl
+    gb.d_d = 0.0
+    prm = torch.as_tensor(p, device="cuda")
+    out = {"workload": "1,000 binaries, N=128, T=4x31557600 s, dt=10 s, oversample=1, tdi2=False; "
+                       "data = injected sum + noise on the 0-0.1 Hz grid (12,623,041 bins)",
+           "steps": steps}
+
+    def step(prec):
+        if prec == "fp64":
+            gb.run_wave(*prm, N=CFG0_N, T=T_OBS, dt=CFG0_DT)
+        gb.get_ll(prm, data, [Sd, Sd], N=CFG0_N, T=T_OBS, dt=CFG0_DT, precision=prec)
+
+    for prec in ("fp64", "pair", "mixed"):
+        step(prec)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            step(prec)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        key = "fp64_wave_and_ll" if prec == "fp64" else f"{prec}_ll"
+        out[f"{key}_ms"] = ms
+        out[f"{key}_binaries_per_s"] = B / (ms / 1e3)
+    import fastgb_oracle as O
+    dA, dE = data[0].cpu().numpy(), data[1].cpu().numpy()
+    O.get_ll(p[:, :50], [dA, dE], [S, S], CFG0_N, T=T_OBS, dt=CFG0_DT)      # warm
+    t0 = time.perf_counter()
+    O.get_ll(p, [dA, dE], [S, S], CFG0_N, T=T_OBS, dt=CFG0_DT)
+    wall = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": B / wall, "unit": "binaries/s", "cores": 1, "kind": "port",
+                           "sample": "the whole 1,000-binary batch once: oracle FP64 run_wave "
+                                     "(NumPy) + get_ll (C), one core"}
+    return out
+
+
 def sparse_accuracy(gb, p, Ns, Sd, seed, count=2000):
     """max |dlogL| / max(1, <h|h>) of the pair and mixed forms vs FP64 on data
     holding only well-separated sources plus noise: {"pair": x, "mixed": y}."""
@@ -916,6 +988,7 @@ def run_gpu(args, rank, world):
     ms_mixed, _ = timed("mixed", max(1, min(args.steps, 20)), 1)
     ms_fp64, _ = timed("fp64", max(1, min(args.steps, 3)), 1)
     ms_grad, _ = timed("grad", max(1, min(args.steps, 10)), 1)
+    cfg0 = config0_bench(GBGPU(), args.seed + rank, max(1, min(args.steps, 10)))
     cfg3 = n256_tdi2_bench(gb, data, Sd, args.seed + rank, max(1, min(args.steps, 10)))
     cfg3tb = thirdbody_n256_bench(data, Sd, args.seed + rank, max(1, min(args.steps, 10)))
     cfg2 = cfg4 = None
@@ -976,6 +1049,7 @@ def run_gpu(args, rank, world):
                       "(FP32 mixed form) on the same batch",
         "launch_shapes": {k: {"tile": int(v[0]), "blocks_per_sm": int(v[1])}
                           for k, v in shapes.items()} or "defaults (tile 512, full occupancy)",
+        "plain_fp64_1000": cfg0,
         "n256_tdi2": cfg3,
         "fill_templates": cfg2,
         "thirdbody_swaps": cfg4,

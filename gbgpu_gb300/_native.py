@@ -73,7 +73,8 @@ def lib():
     L.gbx_device_info.argtypes = [ctypes.POINTER(_i), ctypes.POINTER(_i)]
     L.gbx_init.restype = _i
     L.gbx_get_ll.argtypes = [_vp] * 8 + [_d, _vp, _i, _i, _vp, _vp, _i, _vp, _vp]
-    L.gbx_get_ll_ex.argtypes = [_vp] * 8 + [_d, _vp, _i, _i, _vp, _vp, _i, _ll, _ll, _vp, _vp]
+    L.gbx_get_ll_ex.argtypes = [_vp] * 8 + [_d, _vp, _i, _i, _vp, _vp, _i, _ll, _ll, _i, _i,
+                                            _vp, _vp]
     L.gbx_fill_global.argtypes = [_vp] * 5 + [_i, _i, _vp, _i, _vp, _vp]
     L.gbx_fill_global_ex.argtypes = [_vp] * 5 + [_i, _i, _vp, _i, _i, _ll, _ll, _ll, _vp, _vp]
     L.gbx_fill_global_det.argtypes = [_vp] * 5 + [_i, _i, _vp, _vp, _i, _i, _ll, _ll, _ll, _vp]

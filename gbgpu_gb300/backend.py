@@ -30,6 +30,19 @@ def _addr(x):
     raise TypeError(f"unsupported array type {type(x)!r}")
 
 
+def _numel(x):
+    """Elements of an array argument (0 for a raw address: size unknown)."""
+    if isinstance(x, int) or x is None:
+        return 0
+    if not isinstance(x, torch.Tensor) and hasattr(x, "__cuda_array_interface__"):
+        shape = x.__cuda_array_interface__["shape"]
+        n = 1
+        for d in shape:
+            n *= int(d)
+        return n
+    return int(x.numel()) if isinstance(x, torch.Tensor) else 0
+
+
 class GB300Backend:
     """``backend.get_ll`` / ``backend.fill_global`` / ``backend.xp``."""
 
@@ -42,12 +55,19 @@ class GB300Backend:
 
     def get_ll(self, d_h, h_h, A_template, E_template, A_data, E_data, A_psd, E_psd, df,
                start_ind, M, num_bin, data_index, noise_index, data_length, status=None):
-        """gbx_get_ll with the reference's method-table arguments (gbgpu_utils_wrap.pyx:20-48)."""
-        rc = self._lib.gbx_get_ll(
+        """gbx_get_ll with the reference's method-table arguments (gbgpu_utils_wrap.pyx:20-48).
+
+        When the data and PSD arrive as arrays (not raw addresses) their row
+        counts are passed on, so out-of-range data_index / noise_index rows are
+        flagged in ``status`` and skipped instead of being read."""
+        rows = lambda x: (_numel(x) // int(data_length)) if data_length else 0
+        nd = min(rows(A_data), rows(E_data))
+        npsd = min(rows(A_psd), rows(E_psd))
+        rc = self._lib.gbx_get_ll_ex(
             _addr(d_h), _addr(h_h), _addr(A_template), _addr(E_template), _addr(A_data),
             _addr(E_data), _addr(A_psd), _addr(E_psd), float(df), _addr(start_ind), int(M),
             int(num_bin), _addr(data_index), _addr(noise_index), int(data_length),
-            _addr(status), nat.stream_handle())
+            int(num_bin), 1, int(nd), int(npsd), _addr(status), nat.stream_handle())
         nat.check(rc, "gbx_get_ll")
 
     def fill_global(self, A_glob, E_glob, A_template, E_template, start_ind, M, num_bin,

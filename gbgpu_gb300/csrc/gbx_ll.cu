@@ -43,14 +43,16 @@ __device__ __forceinline__ dfl pair_sum_df(dfl v)
 // per-binary power-of-two scalings (S 2^eS and d 2^eD of order one, from the
 // PSD at the window centre) and multiplied and summed as float pairs on the
 // FP32 pipe (about 46 significant bits: each sum is within ~1e-13 of
-// sum |terms| of the FP64 result); one FP64 conversion per output.
+// sum |terms| of the FP64 result); one FP64 conversion per output.  A
+// negative row, or one at or above num_data / num_psd when those are
+// positive, is flagged (GBX_FLAG_INDEX), never read, and gives zero outputs.
 __global__ void __launch_bounds__(256) get_ll_kernel(
     double2 *__restrict__ d_h, double2 *__restrict__ h_h, const double2 *__restrict__ A_t,
     const double2 *__restrict__ E_t, const double2 *__restrict__ A_d,
     const double2 *__restrict__ E_d, const double *__restrict__ A_p,
     const double *__restrict__ E_p, double df, const int *__restrict__ start_ind, int M,
     int num_bin, const int *__restrict__ data_index, const int *__restrict__ noise_index,
-    int L, long long tsi, long long tsb, int *status)
+    int L, long long tsi, long long tsb, int num_data, int num_psd, int *status)
 {
     const int lane = threadIdx.x & 31, t = lane & 1, q = lane >> 1;
     const int warps = (gridDim.x * blockDim.x) >> 5;
@@ -58,19 +60,25 @@ __global__ void __launch_bounds__(256) get_ll_kernel(
         const int b = b0 + t;
         const bool has = b < num_bin;                 // odd num_bin: the last warp's lane t = 1 idles
         const int s = has ? start_ind[b] : 0;
-        const size_t doff = (size_t)(has && data_index ? data_index[b] : 0) * L;
-        const size_t noff = (size_t)(has && noise_index ? noise_index[b] : 0) * L;
+        const int drow = has && data_index ? data_index[b] : 0;
+        const int nrow = has && noise_index ? noise_index[b] : 0;
+        const bool bad = drow < 0 || nrow < 0 || (num_data > 0 && drow >= num_data) ||
+                         (num_psd > 0 && nrow >= num_psd);
+        if (bad && q == 0) flag(status, GBX_FLAG_INDEX);
+        const bool use = has && !bad;
+        const size_t doff = (size_t)(use ? drow : 0) * L;
+        const size_t noff = (size_t)(use ? nrow : 0) * L;
         int jm = s + M / 2;
         jm = jm < 0 ? 0 : (jm >= L ? L - 1 : jm);
         // exponent of the PSD at the window centre, on the integer pipe
         // (0 for zero, negative, subnormal or non-finite values)
-        const int hS = L > 0 ? __double2hiint(__ldg(A_p + noff + jm)) : 0;
+        const int hS = L > 0 && use ? __double2hiint(__ldg(A_p + noff + jm)) : 0;
         const int exS = (hS >> 20) & 0x7ff;
         const int lgS = (hS > 0 && exS > 0 && exS < 0x7ff) ? exS - 1023 : 0;
         const int eS = -lgS, eD = -(lgS >> 1) - 14;
         dfl dr = {0.f, 0.f}, di = {0.f, 0.f}, hh = {0.f, 0.f};
         bool out = false;
-        const int Mh = has ? M : 0;
+        const int Mh = use ? M : 0;
 #pragma unroll 2
         for (int i = q; i < Mh; i += 16) {
             const int j = s + i;
@@ -212,7 +220,8 @@ extern "C" int gbx_get_ll_ex(void *d_h, void *h_h, const void *A_template,
                              const double *A_psd, const double *E_psd, double df,
                              const int *start_ind, int M, int num_bin, const int *data_index,
                              const int *noise_index, int data_length, long long t_stride_i,
-                             long long t_stride_b, int *status, void *stream)
+                             long long t_stride_b, int num_data, int num_psd, int *status,
+                             void *stream)
 {
     if (num_bin < 0 || M < 0 || data_length < 0) return set_error(GBX_ERR_ARG, "negative size");
     if (num_bin == 0) return GBX_OK;
@@ -224,7 +233,7 @@ extern "C" int gbx_get_ll_ex(void *d_h, void *h_h, const void *A_template,
     get_ll_kernel<<<grid_for((num_bin + 1) / 2), 256, 0, (cudaStream_t)stream>>>(
         (double2 *)d_h, (double2 *)h_h, (const double2 *)A_template, (const double2 *)E_template,
         (const double2 *)A_data, (const double2 *)E_data, A_psd, E_psd, df, start_ind, M, num_bin,
-        data_index, noise_index, data_length, t_stride_i, t_stride_b, status);
+        data_index, noise_index, data_length, t_stride_i, t_stride_b, num_data, num_psd, status);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_error(e, "get_ll launch");
     return GBX_OK;
@@ -238,7 +247,7 @@ extern "C" int gbx_get_ll(void *d_h, void *h_h, const void *A_template, const vo
 {
     return gbx_get_ll_ex(d_h, h_h, A_template, E_template, A_data, E_data, A_psd, E_psd, df,
                          start_ind, M, num_bin, data_index, noise_index, data_length,
-                         (long long)num_bin, 1LL, status, stream);
+                         (long long)num_bin, 1LL, 0, 0, status, stream);
 }
 
 extern "C" int gbx_fill_global_ex(void *A_glob, void *E_glob, const void *A_template,

@@ -4,7 +4,10 @@
  * Every entry point takes caller-owned DEVICE pointers, plain sizes and a
  * CUDA stream handle (cudaStream_t passed as void*, NULL = legacy default
  * stream), launches asynchronously on that stream and returns a status code
- * (GBX_OK = 0).  Nothing is allocated per call, nothing is synchronised, and
+ * (GBX_OK = 0).  The library works in the CUDA runtime's context of the
+ * current device (its primary context): its per-device set-up (FFT tables,
+ * the allocation-free scratch address) is done once per device in that
+ * context, so making another context current is not supported.  Nothing is allocated per call, nothing is synchronised, and
  * no call ever terminates the process (the reference's gpuAssert calls
  * exit(), gbgpu/cutils/global.h:46-54).  Complex arrays are interleaved
  * double[2] (complex128), the layout of the reference's
@@ -67,11 +70,11 @@ int gbx_init(void);
  * products and sums run in float-pair arithmetic (46 significant bits per
  * input), so each output is within 1e-12 of sum |terms| of the FP64 sums
  * (the reference sums in FP64); a PSD bin at infinity contributes zero.
- * data_index / noise_index may be NULL (row 0 for every binary); their rows
- * are trusted as in the reference, whose argument list carries no row
- * counts: the caller keeps di*L and ni*L inside its data and PSD arrays
- * (gbx_waveform_ll, which takes num_data / num_psd, checks them).
- * `status` may be NULL.
+ * data_index / noise_index may be NULL (row 0 for every binary).  The
+ * reference's argument list carries no row counts, so only negative rows are
+ * rejected here (flagged GBX_FLAG_INDEX, not read, zero outputs); the caller
+ * keeps di*L and ni*L inside its data and PSD arrays, or calls gbx_get_ll_ex
+ * with the row counts.  `status` may be NULL.
  */
 int gbx_get_ll(void *d_h, void *h_h, const void *A_template, const void *E_template,
                const void *A_data, const void *E_data, const double *A_psd,
@@ -84,12 +87,17 @@ int gbx_get_ll(void *d_h, void *h_h, const void *A_template, const void *E_templ
  * read at A_template[i * t_stride_i + b * t_stride_b] (in complex elements).
  * (num_bin, 1) is the reference's point-major layout; (1, M) reads a
  * (num_bin, M) row-major array without the transpose the reference makes.
+ * num_data / num_psd > 0 are the rows of the data and PSD arrays: a binary
+ * whose data_index / noise_index lies outside them is flagged GBX_FLAG_INDEX,
+ * not read, and gets zero outputs (0 = rows not known; negative rows are
+ * always rejected).
  */
 int gbx_get_ll_ex(void *d_h, void *h_h, const void *A_template, const void *E_template,
                   const void *A_data, const void *E_data, const double *A_psd,
                   const double *E_psd, double df, const int *start_ind, int M, int num_bin,
                   const int *data_index, const int *noise_index, int data_length,
-                  long long t_stride_i, long long t_stride_b, int *status, void *stream);
+                  long long t_stride_i, long long t_stride_b, int num_data, int num_psd,
+                  int *status, void *stream);
 
 /*
  * Drop-in for fill_global_wrap (reference: gbgpu/cutils/gbgpu_utils.hh:6-7,
@@ -284,7 +292,9 @@ int gbx_waveform_ll_grad(const gbx_wave_args *a, const gbx_ll_args *l, void *d_h
  * capture.  All calls share the array: calls whose kernels overlap on the GPU
  * (different streams, or different host threads) race on it and must be
  * serialised by the caller.  The counter is cleared on the stream before
- * each launch; the workspace is fully rewritten by every call.
+ * each launch; the workspace is fully rewritten by every call.  The caller
+ * still provides its inputs, outputs, orbit tables and (uneven N) tile and
+ * order lists as device memory of its own.
  */
 #define GBX_NOALLOC_MAX_BINS 8192
 int gbx_waveform_ll_noalloc(const gbx_wave_args *a, const gbx_ll_args *l, void *d_h,

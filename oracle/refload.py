@@ -14,8 +14,11 @@ import os
 import sys
 import types
 
-REF_ROOT = os.environ.get("GBGPU_REFERENCE_ROOT", "/root/reference")
 _HERE = os.path.dirname(os.path.abspath(__file__))
+# the reference project checked out beside this repository (../reference),
+# or wherever GBGPU_REFERENCE_ROOT points
+REF_ROOT = os.environ.get("GBGPU_REFERENCE_ROOT",
+                          os.path.join(os.path.dirname(os.path.dirname(_HERE)), "reference"))
 
 
 def reference_available():

@@ -1,7 +1,7 @@
 """Generate golden vectors by running the reference's own FastGB code.
 
-Run in a container where the reference tree is mounted (default
-/root/reference, override with GBGPU_REFERENCE_ROOT) after
+Run where the reference project is checked out beside this repository
+(../reference; override with GBGPU_REFERENCE_ROOT) after
 ``make -C oracle all``:
 
     python tests/golden/make_golden.py

@@ -175,6 +175,39 @@ def test_backend_get_ll_edges_odd_batch(gbgpu):
     assert int(st.item()) & nat.GBX_FLAG_WINDOW
 
 
+def test_backend_get_ll_rows_outside_the_arrays_are_flagged(gbgpu):
+    """Drop-in get_ll with a data_index row past the data array and a
+    negative noise_index row: those binaries are flagged GBX_FLAG_INDEX, not
+    read, and get zero outputs; the other binaries match the FP64 sums."""
+    from gbgpu_gb300 import _native as nat
+    rng = np.random.default_rng(11)
+    L, M, B = 400, 64, 4
+    cplx = lambda *shape: rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    A_d, E_d = 1e-20 * cplx(2, L), 1e-20 * cplx(2, L)
+    A_p = 1e-40 * (1 + rng.random((2, L)))
+    E_p = 1e-40 * (1 + rng.random((2, L)))
+    A_t, E_t = 1e-20 * cplx(B, M), 1e-20 * cplx(B, M)
+    s = np.array([10, 100, 200, 300], dtype=np.int32)
+    di = np.array([0, 5, 1, 1], dtype=np.int32)        # row 5 is past the two data rows
+    ni = np.array([1, 0, -1, 0], dtype=np.int32)       # row -1 is before the first
+    df = 1e-8
+    gb = gbgpu()
+    d_h = torch.full((B,), 7.0, dtype=torch.complex128, device="cuda")
+    h_h = torch.full((B,), 7.0, dtype=torch.complex128, device="cuda")
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    gb.backend.get_ll(d_h, h_h, dev(O.point_major(A_t)), dev(O.point_major(E_t)),
+                      dev(A_d.ravel()), dev(E_d.ravel()), dev(A_p.ravel()), dev(E_p.ravel()),
+                      df, dev(s), M, B, dev(di), dev(ni), L, status=st)
+    assert int(st.item()) & nat.GBX_FLAG_INDEX
+    got = d_h.cpu().numpy()
+    assert got[1] == 0 and got[2] == 0 and h_h[1].item() == 0 and h_h[2].item() == 0
+    for b in (0, 3):
+        j = s[b] + np.arange(M)
+        ref = 4 * df * sum((np.conj(d[di[b], j]) * t[b] / p[ni[b], j]).sum()
+                           for d, p, t in ((A_d, A_p, A_t), (E_d, E_p, E_t)))
+        np.testing.assert_allclose(got[b], ref, rtol=1e-12)
+
+
 def test_fill_global_template_matches_reference(gbgpu):
     g = load_golden("fill_basic")
     gb = gbgpu()

@@ -194,7 +194,7 @@ def test_c_abi_rejects_bad_arguments_before_touching_a_device():
     lib = ctypes.CDLL(build.LIB)
     vp, i, d, ll = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_longlong
     lib.gbx_last_error.restype = ctypes.c_char_p
-    lib.gbx_get_ll_ex.argtypes = [vp] * 8 + [d, vp, i, i, vp, vp, i, ll, ll, vp, vp]
+    lib.gbx_get_ll_ex.argtypes = [vp] * 8 + [d, vp, i, i, vp, vp, i, ll, ll, i, i, vp, vp]
     lib.gbx_fill_global_ex.argtypes = [vp] * 5 + [i, i, vp, i, i, ll, ll, ll, vp, vp]
     lib.gbx_waveform_ll.argtypes = [vp, vp, vp, vp, vp]
     lib.gbx_waveform_ll_grad.argtypes = [vp, vp, vp, vp, vp, vp]
@@ -208,12 +208,14 @@ def test_c_abi_rejects_bad_arguments_before_touching_a_device():
         return lib.gbx_last_error().decode()
 
     # drop-in get_ll: negative sizes, NULL pointers; an empty batch is a no-op
-    assert lib.gbx_get_ll_ex(*ptrs, 1.0, fake, 16, -1, None, None, 100, 1, 1, None, None) == ERR_ARG
+    assert lib.gbx_get_ll_ex(*ptrs, 1.0, fake, 16, -1, None, None, 100, 1, 1, 0, 0,
+                             None, None) == ERR_ARG
     assert "negative" in msg()
-    assert lib.gbx_get_ll_ex(None, *ptrs[1:], 1.0, fake, 16, 4, None, None, 100, 4, 1,
+    assert lib.gbx_get_ll_ex(None, *ptrs[1:], 1.0, fake, 16, 4, None, None, 100, 4, 1, 0, 0,
                              None, None) == ERR_ARG
     assert "NULL" in msg()
-    assert lib.gbx_get_ll_ex(*ptrs, 1.0, fake, 16, 0, None, None, 100, 0, 1, None, None) == 0
+    assert lib.gbx_get_ll_ex(*ptrs, 1.0, fake, 16, 0, None, None, 100, 0, 1, 0, 0,
+                             None, None) == 0
     # fill: group stride shorter than the data
     assert lib.gbx_fill_global_ex(*ptrs[:4], fake, 16, 4, fake, 100, 2, 50, 4, 1,
                                   None, None) == ERR_ARG

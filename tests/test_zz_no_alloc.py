@@ -5,7 +5,8 @@ application owns all device allocations, an FFI binding without a CUDA
 allocator): its scratch is a static device array instead of a caller
 workspace.  Checked through the C ABI against gbx_waveform_ll with a
 workspace, twice in a row so the shared array's leftover contents and the
-work-queue counter reset are exercised; runs alone or after the other tests.
+work-queue counter reset are exercised, and against the CPU oracle (the
+reference's algorithm) per N class; runs alone or after the other tests.
 """
 
 import ctypes
@@ -59,7 +60,20 @@ def _run(fn, gb, p, Ns, data, S, s0, T, precision):
     return d_h.cpu().numpy(), h_h.cpu().numpy()
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def _oracle(p, Ns, data, S, s0, T):
+    """(d_h, h_h) of the CPU oracle, one N class at a time."""
+    B = p.shape[1]
+    d_h = np.zeros(B, np.complex128)
+    h_h = np.zeros(B, np.complex128)
+    for n in np.unique(Ns):
+        sel = Ns == n
+        _, dh, hh, _ = O.get_ll(p[:, sel], data, [S, S], int(n), T=T, dt=10.0,
+                                start_freq_ind=s0, return_terms=True)
+        d_h[sel], h_h[sel] = dh, hh
+    return d_h, h_h
+
+
+@pytest.mark.parametrize("precision", ["fp64", "pair", "mixed"])
 def test_noalloc_matches_workspace_entry_point_twice(precision):
     from gbgpu_gb300 import GBGPU
     from gbgpu_gb300 import _native as nat
@@ -74,6 +88,16 @@ def test_noalloc_matches_workspace_entry_point_twice(precision):
         np.testing.assert_allclose(got[0], ref[0], rtol=1e-12, atol=0)
         np.testing.assert_allclose(got[1], ref[1], rtol=1e-12, atol=0)
         assert np.all(np.isfinite(got[0])) and np.all(np.isfinite(got[1]))
+        # and the reference's algorithm: FP64 and pair forms to 1e-10 / 1e-9
+        # relative per term, the mixed form to |dlogL| <= 1e-6 max(1, <h|h>)
+        odh, ohh = _oracle(p, Ns, data, S, s0, T)
+        if precision == "mixed":
+            dl = np.abs((got[0].real - odh.real) - 0.5 * (got[1].real - ohh.real))
+            assert np.max(dl / np.maximum(1.0, ohh.real)) < 1e-6
+        else:
+            tol = 1e-10 if precision == "fp64" else 1e-9
+            np.testing.assert_allclose(got[0], odh, rtol=tol, atol=0)
+            np.testing.assert_allclose(got[1].real, ohh.real, rtol=tol, atol=0)
 
 
 def test_noalloc_rejects_batches_above_the_static_size():
