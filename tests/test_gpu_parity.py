@@ -175,13 +175,16 @@ def test_backend_get_ll_edges_odd_batch(gbgpu):
     assert int(st.item()) & nat.GBX_FLAG_WINDOW
 
 
-def test_backend_get_ll_rows_outside_the_arrays_are_flagged(gbgpu):
+@pytest.mark.parametrize("L", [400, 401])
+def test_backend_get_ll_rows_outside_the_arrays_are_flagged(gbgpu, L):
     """Drop-in get_ll with a data_index row past the data array and a
     negative noise_index row: those binaries are flagged GBX_FLAG_INDEX, not
-    read, and get zero outputs; the other binaries match the FP64 sums."""
+    read, and get zero outputs; the other binaries match the FP64 sums.  An
+    odd data length puts odd PSD rows at odd element offsets (the staged
+    copies start at the even element below)."""
     from gbgpu_gb300 import _native as nat
     rng = np.random.default_rng(11)
-    L, M, B = 400, 64, 4
+    M, B = 64, 4
     cplx = lambda *shape: rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
     A_d, E_d = 1e-20 * cplx(2, L), 1e-20 * cplx(2, L)
     A_p = 1e-40 * (1 + rng.random((2, L)))
