@@ -516,6 +516,45 @@ def dropin_section(args):
     return out
 
 
+def pair_section(args):
+    """The headline kernel alone (``--section pair``): the uneven-N workload's
+    first ``--binaries`` binaries (20,000 gives a small case of about 1 GB on
+    the device) against seeded noise on the 4-yr grid, through
+    gbx_waveform_ll in the pair form at the bench's launch shape (tile 2048),
+    one untimed call and ``--steps`` timed ones; one JSON line."""
+    import ctypes
+    import torch
+    from gbgpu_gb300 import GBGPU
+    from gbgpu_gb300 import _native as nat
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    p, Ns = draw_workload(args.binaries, args.seed)
+    data, Sd, _ = make_noise(args.seed)
+    Tu = int(T_OBS / DT) * DT
+    gb = GBGPU()
+    B = p.shape[1]
+    prm = torch.as_tensor(p, device="cuda").contiguous()
+    zeros = torch.zeros(B, dtype=torch.int32, device="cuda")
+    la = gb._ll_args(data, [Sd, Sd], data[0].shape[0], zeros, zeros, Tu)
+    a = gb._plan(Ns, Tu, "pair", False, 9, 2048, 0).args(prm)
+    d_h = torch.empty(B, dtype=torch.complex128, device="cuda")
+    h_h = torch.empty(B, dtype=torch.complex128, device="cuda")
+
+    def run():
+        nat.check(nat.lib().gbx_waveform_ll(ctypes.byref(a), ctypes.byref(la), nat.ptr(d_h),
+                                            nat.ptr(h_h), nat.stream_handle()), "gbx_waveform_ll")
+    run()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(max(1, args.steps)):
+        run()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / max(1, args.steps)
+    return {"section": "pair", "binaries": B, "samples": int(Ns.sum()), "ms": ms,
+            "binaries_per_s": B / (ms / 1e3), "alg_bytes": alg_bytes(Ns)}
+
+
 def n256_tdi2_bench(gb, data, Sd, seed, steps):
     """50,000 binaries, N = 256, TDI-2, f0 uniform on [1e-3, 5e-3] Hz and the
     other parameters as the main batch, on the same 4-yr data grid.  Times the FP64 and
@@ -1176,11 +1215,14 @@ def main():
     ap.add_argument("--no-mcmc-bench", action="store_true")
     ap.add_argument("--no-autotune", action="store_true",
                     help="use the kernels' default launch shape instead of the autotuner's")
-    ap.add_argument("--section", choices=["dropin"], default=None,
+    ap.add_argument("--section", choices=["dropin", "pair"], default=None,
                     help="run one sub-benchmark alone (not the bench line)")
     args = ap.parse_args()
     if args.section == "dropin":
         print(json.dumps(dropin_section(args)), flush=True)
+        return
+    if args.section == "pair":
+        print(json.dumps(pair_section(args)), flush=True)
         return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
