@@ -19,7 +19,6 @@ GBX_MAX_LOG2N = 13
 GBX_FLAG_WINDOW = 1
 GBX_FLAG_INDEX = 2
 GBX_FLAG_TILE = 4
-GBX_FLAG_TIMEOUT = 8
 
 EXPORTS = (
     "gbx_version", "gbx_last_error", "gbx_device_info", "gbx_init",

@@ -32,7 +32,6 @@ extern "C" {
 #define GBX_FLAG_WINDOW 1      /* a template window left [0, data_length): those bins count as 0 */
 #define GBX_FLAG_INDEX 2       /* a data_index / noise_index / group_index out of range: binary skipped */
 #define GBX_FLAG_TILE 4        /* malformed tile descriptor: tile skipped */
-#define GBX_FLAG_TIMEOUT 8     /* a bounded wait for an asynchronous copy gave up: outputs incomplete */
 
 /* ---- precision of the waveform family ---- */
 #define GBX_FP64 0             /* every step in FP64 (the plain form) */
