@@ -6,9 +6,12 @@ and (2) the five-point central difference (relative step 1e-7 -- for fddot a
 step moving its phase term by 1e-4 rad -- with the stencil of the
 reference's information_matrix, gbgpu.py:1108-1110) of the plain FP64 fused
 likelihood, which itself matches the reference's likelihood to 1e-10.
-Tolerance: |g - g_ref| <= 2e-3 |g_ref| + 2e-3 rms_b(g_ref) per parameter,
-covering the mixed form's ~1e-6 relative template error amplified by
-cancellation in the residual and the stencil's truncation error.  The
+Tolerances, per parameter: |g - g_ref| <= tol (|g_ref| + rms_b g_ref) with
+tol = 3e-5 against forward mode (only the mixed form's rounding: its ~1e-7
+relative template error amplified by cancellation in the residual; measured
+worst 1.1e-5, amp and iota of the third-body case) and tol = 5e-5 against
+the differences (their FP64 rounding and truncation; measured worst 1.3e-5,
+f0).  Each test prints the measured worst value per parameter.  The
 third-body model (14 parameters) is checked the same way.
 """
 
@@ -21,6 +24,8 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 T_OBS = 4 * 31557600.0
+FD_TOL = 5e-5        # five-point differences (measured worst: 1.3e-5)
+FWD_TOL = 3e-5       # forward mode: only the mixed form's rounding (measured worst: 1.1e-5)
 
 
 def _case(B, N, seed, dt=10.0, tdi2=False, third=False):
@@ -92,13 +97,7 @@ def test_gradient_matches_fp64_finite_differences(N, tdi2):
     gb.d_d = 0.0
     like, grad = gb.get_ll_grad(p, data, [Sd, Sd], N=N, T=T_OBS, dt=dt, tdi2=tdi2,
                                 start_freq_ind=s0)
-    ref = _fd(gb, p, data, Sd, s0, N, dt, tdi2)
-    names = ["amp", "f0", "fdot", "fddot", "phi0", "iota", "psi", "lam", "beta"]
-    for k in range(9):
-        rms = np.sqrt(np.mean(ref[k] ** 2))
-        err = np.abs(grad[k] - ref[k])
-        bad = err > 2e-3 * np.abs(ref[k]) + 2e-3 * rms
-        assert not np.any(bad), (names[k], np.max(err / (np.abs(ref[k]) + rms)))
+    _check(grad, _fd(gb, p, data, Sd, s0, N, dt, tdi2), FD_TOL, f"N={N} tdi2={tdi2} vs FD:")
     # the likelihood returned with the gradient is the mixed fused likelihood
     like_m = gb.get_ll(p, data, [Sd, Sd], N=N, T=T_OBS, dt=dt, tdi2=tdi2, start_freq_ind=s0,
                        precision="mixed")
@@ -131,12 +130,20 @@ NAMES14 = ["amp", "f0", "fdot", "fddot", "phi0", "iota", "psi", "lam", "beta",
            "A2", "varpi", "e2", "P2", "T2"]
 
 
-def _check(grad, ref, tol=2e-3):
+def _worst(grad, ref):
+    """Per parameter: max_b |g - g_ref| / (|g_ref| + rms_b g_ref)."""
+    out = []
     for k in range(ref.shape[0]):
         rms = np.sqrt(np.mean(ref[k] ** 2))
-        err = np.abs(grad[k] - ref[k])
-        bad = err > tol * np.abs(ref[k]) + tol * rms
-        assert not np.any(bad), (NAMES14[k], np.max(err / (np.abs(ref[k]) + rms)))
+        out.append(float(np.max(np.abs(grad[k] - ref[k]) / (np.abs(ref[k]) + rms))))
+    return np.array(out)
+
+
+def _check(grad, ref, tol=FD_TOL, what=""):
+    w = _worst(grad, ref)
+    print(f"{what} worst normalised error per parameter: " +
+          ", ".join(f"{NAMES14[k]} {w[k]:.1e}" for k in range(len(w))))
+    assert np.all(w <= tol), dict(zip(NAMES14, w))
 
 
 def _forward_mode(p, data, Sd, s0, N, dt, tdi2):
@@ -153,7 +160,8 @@ def test_gradient_matches_forward_mode(N, tdi2):
     gb, p, data, Sd, s0, dt = _case(16, N, 90 + N, tdi2=tdi2)
     gb.d_d = 0.0
     _, grad = gb.get_ll_grad(p, data, [Sd, Sd], N=N, T=T_OBS, dt=dt, tdi2=tdi2, start_freq_ind=s0)
-    _check(grad, _forward_mode(p, data, Sd, s0, N, dt, tdi2))
+    _check(grad, _forward_mode(p, data, Sd, s0, N, dt, tdi2), FWD_TOL,
+           f"N={N} tdi2={tdi2} vs forward mode:")
 
 
 @pytest.mark.parametrize("N", [256, 512])
@@ -162,7 +170,8 @@ def test_third_body_gradient(N):
     gb.d_d = 0.0
     like, grad = gb.get_ll_grad(p, data, [Sd, Sd], N=N, T=T_OBS, dt=dt, start_freq_ind=s0)
     assert grad.shape == (14, 16)
-    _check(grad, _forward_mode(p, data, Sd, s0, N, dt, False))
-    _check(grad, _fd(gb, p, data, Sd, s0, N, dt, False))
+    _check(grad, _forward_mode(p, data, Sd, s0, N, dt, False), FWD_TOL,
+           f"third body N={N} vs forward mode:")
+    _check(grad, _fd(gb, p, data, Sd, s0, N, dt, False), FD_TOL, f"third body N={N} vs FD:")
     like_m = gb.get_ll(p, data, [Sd, Sd], N=N, T=T_OBS, dt=dt, start_freq_ind=s0, precision="mixed")
     np.testing.assert_allclose(like, like_m, rtol=1e-12, atol=1e-9)
