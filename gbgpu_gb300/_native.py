@@ -16,6 +16,8 @@ GBX_FP64 = 0
 GBX_MIXED = 1
 GBX_PAIR = 2
 GBX_MAX_LOG2N = 13
+GBX_TDI2_BIT = 1
+GBX_TDI_UNEQUAL = 2
 GBX_FLAG_WINDOW = 1
 GBX_FLAG_INDEX = 2
 GBX_FLAG_TILE = 4

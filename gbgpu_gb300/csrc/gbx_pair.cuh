@@ -129,6 +129,30 @@ __device__ __forceinline__ void sincos_pair(dfl x, const float4 *__restrict__ ta
     s = df_fast(ss.h, fmaf(Ts.h, eps, ss.l));
 }
 
+// sincos_pair to ~1e-13 absolute, for angles whose sine enters a small
+// factor relative to its own size (omL ~ 1e-2 in the TDI factors): the
+// d^5 term of sin d, cos d - 1 = -d^2/2 + d^4/24 - d^6/720 as a pair with
+// the d.l cross term, and pair products of the table values with it.
+__device__ __forceinline__ void sincos_pair_acc(dfl x, const float4 *__restrict__ tab, dfl &c, dfl &s)
+{
+    constexpr float kInv = 40.743663787841797f;
+    constexpr float C1 = 0.02454376220703125f;
+    constexpr float C2 = -6.960085841001273e-08f;
+    constexpr float C3 = -2.581268532253489e-15f;
+    const float jf = rintf(x.h * kInv);
+    const dfl h = df_two_sum(x.h, -jf * C1);
+    const dfl d = df_fast(h.h, h.l + fmaf(-jf, C3, fmaf(-jf, C2, x.l)));
+    const float4 t = tab[(int)jf & (kScN - 1)];
+    const float d2 = d.h * d.h;
+    const float d2l = fmaf(d.h + d.h, d.l, fmaf(d.h, d.h, -d2));
+    const dfl sd = df_fast(d.h, fmaf(d.h * d2, fmaf(d2, 1.0f / 120.0f, -1.0f / 6.0f), d.l));
+    const dfl em = df_fast(-0.5f * d2, fmaf(d2 * d2, fmaf(d2, -1.0f / 720.0f, 1.0f / 24.0f),
+                                            -0.5f * d2l));
+    const dfl Tc = {t.x, t.y}, Ts = {t.z, t.w};
+    c = p_add(p_add(Tc, p_mul(Tc, em)), df_neg(p_mul(Ts, sd)));
+    s = p_add(p_add(Ts, p_mul(Ts, em)), p_mul(Tc, sd));
+}
+
 // sin(a)/a and cos(a) for a pair a >= 0: Taylor series in x = a^2 for
 // x < 2.56 (terms to x^7; truncation below 5e-12 and 9e-11), the leading three
 // coefficients as pairs and the rest as an FP32 tail (at most 4e-10 of the
@@ -161,6 +185,85 @@ __device__ __forceinline__ void sinc_cos_pair(dfl a, const float4 *__restrict__ 
     }
 }
 
+// ---------------------------------------------------------------- unequal arms
+// slow_unequal_fp64 (gbx_wave.cu) in pair arithmetic: arm lengths ell_a L
+// with ell_a = |r_a|, per-link transfer argument (f/f*)(ell_a +- k.r_a)/2,
+// antenna pattern over ell_a, delays D_a = exp(-i x_a), x_a = omL ell_a, and
+//   X = -2i omL [(1 - D_31^2)(G21 + D_12 G12) - (1 - D_12^2)(G31 + D_31 G13)]
+// (Y, Z cyclic; TDI-2: times 1 - D_12^2 D_31^2, cyclic).  The small factors
+// are formed without cancellation, 1 - e^{-2ix} = 2i sin(x) e^{-ix}, so
+//   X = 4 omL [s_31 D_31 (G21 + D_12 G12) - s_12 D_12 (G31 + D_31 G13)]
+// with s_a = sin x_a, and the TDI-2 factor is 2i sin(x_12 + x_31) D_12 D_31.
+// A[] holds the arm patterns r.e.r / 4, E[] the spacecraft carriers, fo[]
+// f/f* per spacecraft.
+__device__ __forceinline__ cpx cp_mul_2i(cpx z) { return {p_scale(z.y, -2.f), p_scale(z.x, 2.f)}; }
+
+template <bool AE>
+__device__ __forceinline__ void slow_pair_unequal(const dfl (&r)[3][3], const dfl (&kr)[3],
+                                               const dfl (&fo)[3], const cpx (&E)[3],
+                                               const cpx (&A0)[3], dfl omL, int tdi,
+                                               const float4 *__restrict__ sct, cpx out[3])
+{
+    dfl ell[3];
+    cpx A[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const dfl e2 = p_dot3(r[a][0], r[a][0], r[a][1], r[a][1], r[a][2], r[a][2]);
+        const float sq = sqrtf(e2.h);
+        ell[a] = df_fast(sq, (fmaf(-sq, sq, e2.h) + e2.l) * (0.5f / sq));
+        A[a] = cp_scale(A0[a], df_recip(ell[a]));
+    }
+    cpx G[6];
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+        const int arm = q < 3 ? q : q - 3;
+        const int s = q < 3 ? q : (q - 2) % 3;
+        const dfl k = q < 3 ? kr[arm] : df_neg(kr[arm]);
+        const dfl a = p_scale(p_mul(fo[s], p_addf(ell[arm], k)), 0.5f);
+        dfl S, C;
+        sinc_cos_pair(a, sct, S, C);
+        const cpx T = {p_mul(S, C), df_neg(p_mul(p_mul(a, S), S))};
+        G[q] = cp_mul(cp_mul(T, A[arm]), E[s]);
+    }
+    cpx D[3];
+    dfl sn[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        dfl c;
+        sincos_pair_acc(p_mul(omL, ell[a]), sct, c, sn[a]);
+        D[a] = {c, df_neg(sn[a])};
+    }
+    // s_a D_a (G_q1 + D_b G_q2)
+    auto term = [&](int a, int b, int q1, int q2) {
+        return cp_scale(cp_mul(D[a], cp_add(G[q1], cp_mul(D[b], G[q2]))), sn[a]);
+    };
+    cpx X = cp_sub(term(2, 0, 3, 0), term(0, 2, 2, 5));
+    cpx Y = cp_sub(term(0, 1, 4, 1), term(1, 0, 0, 3));
+    cpx Z = cp_sub(term(1, 2, 5, 2), term(2, 1, 1, 4));
+    if (tdi & GBX_TDI2_BIT) {
+        // 2i sin(x_a + x_b) D_a D_b
+        auto fac = [&](int a, int b) {
+            const dfl sab = p_dot2(sn[a], D[b].x, D[a].x, sn[b]);
+            return cp_mul_2i(cp_scale(cp_mul(D[a], D[b]), sab));
+        };
+        X = cp_mul(fac(0, 2), X);
+        Y = cp_mul(fac(1, 0), Y);
+        Z = cp_mul(fac(2, 1), Z);
+    }
+    const dfl w = p_scale(omL, 4.f);
+    X = cp_scale(X, w);
+    Y = cp_scale(Y, w);
+    Z = cp_scale(Z, w);
+    if constexpr (AE) {
+        out[0] = cp_scale(cp_sub(Z, X), dconst(0.70710678118654752440));
+        out[1] = cp_scale(cp_add(cp_sub(X, cp_pow2(Y, 2.f)), Z), dconst(0.40824829046386301637));
+    } else {
+        out[0] = X;
+        out[1] = Y;
+        out[2] = Z;
+    }
+}
+
 // ---------------------------------------------------------------- slow part
 // The slow part at one sample (gbgpu.py:399-540 and 348-375), as slow_mixed
 // but every quantity a pair.  AE: out[0], out[1] = A, E (formed before the
@@ -170,10 +273,10 @@ __device__ __forceinline__ void sinc_cos_pair(dfl a, const float4 *__restrict__ 
 // they carry: with P_q = T_q A_arm(q) (T = sinc(a) e^{-ia} / 4) and
 // F_s = fc (P_q - P_q') for the two links of spacecraft s,
 //   X = fc2 (F_1 E_1 + P_21 E_2 - P_31 E_3), Y and Z cyclic.
-template <bool AE>
+template <bool AE, bool UNEQ>
 __device__ __forceinline__ void slow_pair(const Bin &B, int n, int N, dfl step, dfl Loc,
                                           const double *__restrict__ tab,
-                                          const float4 *__restrict__ sct, cpx out[3])
+                                          const float4 *__restrict__ sct, cpx out[3], int tdi)
 {
     const float *tabf = reinterpret_cast<const float *>(tab + (size_t)18 * N);
     dfl r[3][3];
@@ -231,6 +334,10 @@ __device__ __forceinline__ void slow_pair(const Bin &B, int n, int N, dfl step, 
         const dfl pp = p_scale(p_dot2(rv, rv, df_neg(ru), ru), 0.25f);
         const dfl cc = p_scale(p_mul(ru, rv), 0.5f);
         A[a] = {p_dot2(pp, B.pr.DP.x, cc, B.pr.DC.x), p_dot2(pp, B.pr.DP.y, cc, B.pr.DC.y)};
+    }
+    if constexpr (UNEQ) {
+        slow_pair_unequal<AE>(r, kr, fo, E, A, p_addf(base, dfl{B.w2 * tf * tf, 0.f}), tdi, sct, out);
+        return;
     }
     // links (ij, arm, spacecraft): 12,23,31 (+k.r), 21,32,13 (-k.r)
     cpx P[6];
@@ -371,7 +478,7 @@ __device__ __forceinline__ void fft_dif_pair(cpx *buf, int nsub, int lg)
 // arrays (the transformed pairs rounded once to FP64, then the FP64 scale
 // and AET), MODE_LL folds the window into <d|h> and <h|h> (pairs).  Shared memory: the binaries' constants, the reduction
 // scratch, the sin/cos table and the transform buffers.
-template <int MODE>
+template <int MODE, bool UNEQ>
 __global__ void __launch_bounds__(kBlock, 2) pair_kernel(const KParams K)
 {
     constexpr int NCH = MODE == MODE_WAVE ? 3 : 2;
@@ -445,7 +552,7 @@ __global__ void __launch_bounds__(kBlock, 2) pair_kernel(const KParams K)
             if (!B.valid) {
                 o[0] = o[1] = o[2] = cp_zero();
             } else {
-                slow_pair<NCH == 2>(B, n, N, stepd, K.Locd, tab, sct, o);
+                slow_pair<NCH == 2, UNEQ>(B, n, N, stepd, K.Locd, tab, sct, o, a.tdi2);
             }
 #pragma unroll
             for (int c = 0; c < NCH; c++) buf[(p * NCH + c) * N + swz(n, lg)] = o[c];

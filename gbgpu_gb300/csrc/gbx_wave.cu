@@ -501,7 +501,7 @@ __device__ void setup_bin(Bin &B, const KParams &K, int b, int N, int mode)
     // output scaling (gbgpu.py:298-309): amp * 0.5 T / N [* 2i sin 2wL e^{-2iwL}]
     double fc = 0.5 * T / (double)N;
     double2 sc = make_double2(amp * fc, 0.0);
-    if (a.tdi2) {
+    if (a.tdi2 == GBX_TDI2_BIT) {
         double omL = 2.0 * kPi * f0 * (a.armlength / kCSI);
         double s2, c2;
         sincos(2.0 * omL, &s2, &c2);
@@ -561,11 +561,76 @@ __device__ void setup_bin(Bin &B, const KParams &K, int b, int N, int mode)
 }
 
 // ----------------------------------------------------------------------------
+// Unequal arms (no counterpart in the reference, whose TDI assumes one
+// armlength, gbgpu.py:167-170): arm a = 12, 23, 31 has length ell_a L at the
+// sample, ell_a = |r_a| with r_a = (P_j - P_i)/L from the orbit table.  Each
+// link carries its own arm: transfer argument a = (f/f*)(ell_a +- k.r_a)/2 (the
+// reference's (f/f*)(1 +- k.r)/2 times ell_a with r normalised), antenna
+// pattern r.e.r / ell_a^2 and amplitude ell_a; the TDI delays are the phase
+// factors D_a = exp(-i omL ell_a) at the instantaneous frequency
+// (quasi-static: the slow part is not re-sampled at the delayed times):
+//   X = -2i omL [(1 - D_31^2)(G21 + D_12 G12) - (1 - D_12^2)(G31 + D_31 G13)]
+// with Y, Z cyclic, and TDI-2 multiplies X by (1 - D_12^2 D_31^2) (Y, Z
+// cyclic).  With every ell_a = 1 this is the reference's fctr2 [G21 - G31 +
+// (G12 - G13) fctr] (gbgpu.py:362-372), since -2i omL (1 - D^2) = 4 omL
+// sin(omL) e^{-i omL}, and its TDI-2 factor 1 - D^4 = 2i sin 2wL e^{-2iwL}
+// (gbgpu.py:298-309) evaluated at f(t) instead of f0.
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ double2 one_minus(double2 z) { return make_double2(1.0 - z.x, -z.y); }
+
+__device__ __forceinline__ void slow_unequal_fp64(const Bin &B, double tm, double fstar,
+                                               const double (&r)[3][3], const double (&kdotr)[3],
+                                               const double (&fonfs)[3], const double (&kp)[3],
+                                               const double2 (&A)[3], int tdi, double2 out[3])
+{
+    double ell[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) ell[a] = sqrt(r[a][0] * r[a][0] + r[a][1] * r[a][1] + r[a][2] * r[a][2]);
+    double2 G[6];
+    const int arm[6] = {0, 1, 2, 0, 1, 2};
+    const int sc[6] = {0, 1, 2, 1, 2, 0};
+    const double sg[6] = {1.0, 1.0, 1.0, -1.0, -1.0, -1.0};
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+        const double arg = 0.5 * fonfs[sc[q]] * (ell[arm[q]] + sg[q] * kdotr[arm[q]]);
+        double sn, cs;
+        sincos(arg + kp[sc[q]], &sn, &cs);
+        const double amp = 0.25 * sin(arg) / arg / ell[arm[q]];
+        G[q] = cmul(make_double2(amp * cs, -amp * sn), A[arm[q]]);
+    }
+    const double f = B.f0 + B.fdot * tm + 0.5 * B.fddot * tm * tm;
+    const double omL = f / fstar;
+    double2 D[3], D2[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        double sn, cs;
+        sincos(omL * ell[a], &sn, &cs);
+        D[a] = make_double2(cs, -sn);
+        D2[a] = cmul(D[a], D[a]);
+    }
+    double2 X = csub(cmul(one_minus(D2[2]), cadd(G[3], cmul(D[0], G[0]))),
+                     cmul(one_minus(D2[0]), cadd(G[2], cmul(D[2], G[5]))));
+    double2 Y = csub(cmul(one_minus(D2[0]), cadd(G[4], cmul(D[1], G[1]))),
+                     cmul(one_minus(D2[1]), cadd(G[0], cmul(D[0], G[3]))));
+    double2 Z = csub(cmul(one_minus(D2[1]), cadd(G[5], cmul(D[2], G[2]))),
+                     cmul(one_minus(D2[2]), cadd(G[1], cmul(D[1], G[4]))));
+    if (tdi & GBX_TDI2_BIT) {
+        X = cmul(one_minus(cmul(D2[0], D2[2])), X);
+        Y = cmul(one_minus(cmul(D2[1], D2[0])), Y);
+        Z = cmul(one_minus(cmul(D2[2], D2[1])), Z);
+    }
+    const double2 pre = make_double2(0.0, -2.0 * omL);
+    out[0] = cmul(pre, X);
+    out[1] = cmul(pre, Y);
+    out[2] = cmul(pre, Z);
+}
+
+// ----------------------------------------------------------------------------
 // slow part at one sample (gbgpu.py:399-540 and 348-375)
 // writes fctr2 * {X, Y, Z} (amplitude divided out) into out[0..2]
 // ----------------------------------------------------------------------------
-template <bool THIRD>
-__device__ __forceinline__ void slow_fp64(const Bin &B, int n, int N, double tm, double inv_c_unused,
+template <bool THIRD, bool UNEQ>
+__device__ __forceinline__ void slow_fp64(const Bin &B, int n, int N, double tm, int tdi,
                                           const double *__restrict__ tab, double fstar,
                                           const double *psi, const double *vl, double2 out[3])
 {
@@ -605,6 +670,10 @@ __device__ __forceinline__ void slow_fp64(const Bin &B, int n, int N, double tm,
     const int arm[6] = {0, 1, 2, 0, 1, 2};
     const int sc[6] = {0, 1, 2, 1, 2, 0};
     const double sg[6] = {1.0, 1.0, 1.0, -1.0, -1.0, -1.0};
+    if constexpr (UNEQ) {
+        slow_unequal_fp64(B, tm, fstar, r, kdotr, fonfs, kp, A, tdi, out);
+        return;
+    }
 #pragma unroll
     for (int q = 0; q < 6; q++) {
         double arg = 0.5 * fonfs[sc[q]] * (1.0 + sg[q] * kdotr[arm[q]]);
@@ -1039,7 +1108,7 @@ __device__ __forceinline__ void third_prepass_mixed(const Bin *bins, const doubl
     __syncthreads();
 }
 
-template <typename R, int MODE, bool THIRD>
+template <typename R, int MODE, bool THIRD, bool UNEQ>
 __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(const KParams K)
 {
     using V = typename C2<R>::T;
@@ -1154,7 +1223,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                 o[0] = o[1] = o[2] = V{0, 0};
             } else if constexpr (sizeof(R) == 8) {
                 double vd[3] = {(double)vv[0], (double)vv[1], (double)vv[2]};
-                slow_fp64<THIRD>(B, n, N, tm, 0.0, tab, fstar, ps, vd, reinterpret_cast<double2 *>(o));
+                slow_fp64<THIRD, UNEQ>(B, n, N, tm, a.tdi2, tab, fstar, ps, vd, reinterpret_cast<double2 *>(o));
             } else {
                 float vf[3] = {(float)vv[0], (float)vv[1], (float)vv[2]};
                 slow_mixed<THIRD>(B, n, N, stepd, Loc, tab, psf, vf, reinterpret_cast<float2 *>(o));
@@ -1595,12 +1664,12 @@ static int launch_tiles(void (*kern)(const KParams), size_t sm, const KParams &K
     return GBX_OK;
 }
 
-template <typename R, int MODE, bool THIRD>
+template <typename R, int MODE, bool THIRD, bool UNEQ = false>
 static int launch_one(const KParams &K, int maxS, cudaStream_t st)
 {
     const size_t sm = smem_bytes(sizeof(R) == 8 ? GBX_FP64 : GBX_MIXED, THIRD, maxS,
                                  MODE == MODE_WAVE ? 3 : 2, K.maxP);
-    return launch_tiles<MODE>(wave_kernel<R, MODE, THIRD>, sm, K, st);
+    return launch_tiles<MODE>(wave_kernel<R, MODE, THIRD, UNEQ>, sm, K, st);
 }
 
 // most binaries in one tile of this launch (the shared memory holds their constants)
@@ -1619,16 +1688,20 @@ static int dispatch(KParams &K, int maxS, cudaStream_t st)
     K.maxS = maxS;
     K.maxP = max_pack(&K.a, MODE == MODE_SWAP ? 2 : 1);
     const bool third = K.a.nparams >= 14;
+    // unequal arms are a separate instantiation: the equal-arm kernels carry none of it
+    const bool uneq = (K.a.tdi2 & GBX_TDI_UNEQUAL) != 0;
+    if (uneq && third) return set_error(GBX_ERR_UNSUPPORTED, "unequal arms cover the 9-parameter model");
     if (K.a.precision == GBX_PAIR) {
         if constexpr (MODE == MODE_WAVE || MODE == MODE_LL) {
             if (third) return set_error(GBX_ERR_UNSUPPORTED, "the pair form covers the 9-parameter model");
-            return launch_tiles<MODE>(pair_kernel<MODE>,
+            return launch_tiles<MODE>(uneq ? pair_kernel<MODE, true> : pair_kernel<MODE, false>,
                                       pair_smem_bytes(maxS, MODE == MODE_WAVE ? 3 : 2, K.maxP), K, st);
         } else {
             return set_error(GBX_ERR_UNSUPPORTED, "the pair form covers gbx_waveform and gbx_waveform_ll");
         }
     }
     if (K.a.precision == GBX_FP64) {
+        if (uneq) return launch_one<double, MODE, false, true>(K, maxS, st);
         return third ? launch_one<double, MODE, true>(K, maxS, st)
                      : launch_one<double, MODE, false>(K, maxS, st);
     }
@@ -1646,6 +1719,10 @@ static int check_wave(const gbx_wave_args *a, int *maxS)
         return set_error(GBX_ERR_ARG, "unknown precision %d", a->precision);
     if (!(a->T > 0.0) || !(a->armlength > 0.0)) return set_error(GBX_ERR_ARG, "T and armlength must be > 0");
     if (a->nparams == 14 && !(a->year > 0.0)) return set_error(GBX_ERR_ARG, "year must be > 0");
+    if (a->tdi2 < 0 || a->tdi2 > (GBX_TDI2_BIT | GBX_TDI_UNEQUAL))
+        return set_error(GBX_ERR_ARG, "tdi2=%d: bits GBX_TDI2_BIT and GBX_TDI_UNEQUAL only", a->tdi2);
+    if ((a->tdi2 & GBX_TDI_UNEQUAL) && a->precision == GBX_MIXED)
+        return set_error(GBX_ERR_UNSUPPORTED, "unequal arms are computed in the FP64 and pair forms only");
     if (a->workspace) {
         if (((uintptr_t)a->workspace & 15) != 0) return set_error(GBX_ERR_ARG, "workspace must be 16-byte aligned");
         if (a->workspace_bytes < gbx_wave_workspace_bytes(a->num_bin))

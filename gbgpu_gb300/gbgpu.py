@@ -128,7 +128,7 @@ class WavePlan:
         self.owner = owner
         self.T = float(T)
         self.precision = precision
-        self.tdi2 = bool(tdi2)
+        self.tdi2 = int(tdi2)              # GBX_TDI2_BIT | GBX_TDI_UNEQUAL
         self.nparams = nparams
         self.tile = int(tile)
         self.blocks_per_sm = int(blocks_per_sm)
@@ -168,7 +168,7 @@ class WavePlan:
         a.nparams = params.shape[0]
         a.N = self.N
         a.precision = _PRECISIONS[self.precision]
-        a.tdi2 = int(self.tdi2)
+        a.tdi2 = self.tdi2
         a.start_freq_ind = int(start_freq_ind)
         a.T = self.T
         a.armlength = float(self.owner.orbits.armlength)
@@ -201,8 +201,14 @@ class GBGPUBase(abc.ABC):
         orbits: object with ``get_pos(t, sc)``, ``armlength`` and ``t_base``
             (default: analytic ``EqualArmlengthOrbits``).
         force_backend: accepted for API compatibility; only the GPU exists.
-        precision: ``"fp64"`` (plain form) or ``"mixed"`` (FP64 phase, FP32
-            slow part and FFT) for the fused likelihood / fill kernels.
+        precision: ``"fp64"`` (plain form), ``"pair"`` (float-pair slow part,
+            FFT and sums, within ~1e-9 of FP64) or ``"mixed"`` (FP64 phase,
+            FP32 slow part and FFT) for the fused likelihood / fill kernels.
+        unequal_arms: take each arm's length from the orbit at every sample
+            (|P_j - P_i|) in the link transfer functions, antenna patterns and
+            TDI delays, instead of the single ``orbits.armlength`` of the
+            reference's equal-arm TDI (gbgpu.py:167-170); FP64 and pair forms.
+            With equal arms both give the same windows.
         autotune: pick the fused kernels' launch shape (samples per tile,
             blocks per SM) by timing candidates on the first batch of each
             workload (cached per device); default from ``GBX_AUTOTUNE=1``.
@@ -211,8 +217,9 @@ class GBGPUBase(abc.ABC):
     NPARAMS = 9
 
     def __init__(self, orbits: Orbits = None, force_backend=None, precision="fp64", device=None,
-                 autotune=None):
+                 autotune=None, unequal_arms=False):
         self._backend = get_backend(force_backend)
+        self.unequal_arms = bool(unequal_arms)
         # launch shapes picked by timing (gbgpu_gb300.autotune); default from
         # the environment variable GBX_AUTOTUNE=1, else the kernels' defaults
         self.autotune = (os.environ.get("GBX_AUTOTUNE", "0") == "1") if autotune is None \
@@ -314,11 +321,14 @@ class GBGPUBase(abc.ABC):
         buffer, not yet verified against the contents, and serves only to find
         an existing plan: a new plan is always filed under the key of the
         contents it was built from."""
+        # TDI code of the kernels: bit 0 TDI-2, bit 1 unequal arms
+        tdi = (nat.GBX_TDI2_BIT if tdi2 else 0) | \
+            (nat.GBX_TDI_UNEQUAL if getattr(self, "unequal_arms", False) else 0)
         if np.ndim(N) == 0:
-            key = (int(N), float(T), precision, bool(tdi2), nparams, tile, blocks_per_sm)
+            key = (int(N), float(T), precision, tdi, nparams, tile, blocks_per_sm)
         else:
             arr = np.ascontiguousarray(N, dtype=np.int64)
-            rest = (arr.shape[0], float(T), precision, bool(tdi2), nparams, tile, blocks_per_sm)
+            rest = (arr.shape[0], float(T), precision, tdi, nparams, tile, blocks_per_sm)
             if nkey is None or (not trusted and (nkey,) + rest not in self._plans):
                 nkey = _array_key(arr)
             key = (nkey,) + rest
@@ -328,7 +338,7 @@ class GBGPUBase(abc.ABC):
             # gbx_wave_args built from it does (WavePlan.args keeps a reference)
             while len(self._plans) >= _PLAN_CACHE:
                 self._plans.pop(next(iter(self._plans)))
-            plan = WavePlan(self, N, T, precision, tdi2, nparams, tile, blocks_per_sm)
+            plan = WavePlan(self, N, T, precision, tdi, nparams, tile, blocks_per_sm)
         self._plans[key] = plan
         return plan
 

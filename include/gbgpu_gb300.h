@@ -41,6 +41,10 @@ extern "C" {
 
 #define GBX_MAX_LOG2N 13       /* N = 2^k, 5 <= k <= 13 (FP64 form: k <= 12) */
 
+/* ---- bits of gbx_wave_args.tdi2 ---- */
+#define GBX_TDI2_BIT 1         /* second-generation TDI */
+#define GBX_TDI_UNEQUAL 2      /* per-sample arm lengths |P_j - P_i| (no counterpart in the reference) */
+
 int gbx_version(void);
 
 /* Message for the most recent non-zero status returned on this host thread. */
@@ -175,8 +179,12 @@ typedef struct gbx_wave_args {
     int num_bin;
     int nparams;                 /* 9, or 14 for the third-body model */
     int N;                       /* uniform N (power of two) or 0 with tiles */
-    int precision;               /* GBX_FP64 or GBX_MIXED */
-    int tdi2;                    /* 0: TDI 1st generation, 1: multiply by 2i sin(2wL) e^{-2iwL} */
+    int precision;               /* GBX_FP64, GBX_MIXED or GBX_PAIR */
+    int tdi2;                    /* bit 0 (GBX_TDI2_BIT): TDI-2; bit 1 (GBX_TDI_UNEQUAL): unequal arms.
+                                    0: TDI-1.5, 1: times 2i sin(2wL) e^{-2iwL} at f0 (the reference's
+                                    equal-arm forms); 2, 3: per-sample arm lengths from the orbit
+                                    table (FP64 and pair forms, 9 parameters; otherwise
+                                    GBX_ERR_UNSUPPORTED) */
     int start_freq_ind;          /* subtracted from every start index */
     double T;                    /* observation time, already int(T/dt)*dt */
     double armlength;            /* m */

@@ -139,11 +139,18 @@ def third_body_phase(f0, fdot, fddot, xi, A2, varpi, e2, n2, T2):
 # Waveform (gbgpu/gbgpu.py:108-540)
 # ----------------------------------------------------------------------------
 def waveform(params, N, T=4 * YRSID_SI, dt=10.0, tdi2=False, orbits=None,
-             third=None):
+             third=None, unequal_arms=False):
     """FastGB X/Y/Z and A/E/T for a batch sharing one N.
 
     ``params`` is (9, B): amp, f0, fdot, fddot, phi0, iota, psi, lam, beta.
     ``third`` is None or (A2, varpi, e2, P2[yr], T2[yr]) arrays of length B.
+    ``unequal_arms``: the library's unequal-arm model (no counterpart in the
+    reference, whose TDI takes one armlength, gbgpu.py:167-170): arm a has
+    length ell_a L with ell_a = |r_a| at each sample; transfer argument
+    (f/f*)(ell_a +- k.r_a)/2, antenna pattern r.e.r / ell_a^2 times ell_a,
+    delays D_a = exp(-i omL ell_a),
+    X = -2i omL [(1 - D31^2)(G21 + D12 G12) - (1 - D12^2)(G31 + D31 G13)]
+    (Y, Z cyclic), TDI-2 per sample: X (1 - D12^2 D31^2) (cyclic).
     Returns dict(XYZf=(B,3,N) c128, AETf=(B,3,N) c128, start_inds=(B,) int64,
     T=T_used, df=1/T_used).
     """
@@ -210,27 +217,44 @@ def waveform(params, N, T=4 * YRSID_SI, dt=10.0, tdi2=False, orbits=None,
         argS = argS + third_body_phase(f0, fdot, fddot, xi, A2, varpi, e2, n2, T2s)
     kp = om[:, None, None] * kdotP - argS
 
+    ell = {ij: (np.linalg.norm(r[ij], axis=-1) if unequal_arms else np.ones(N))
+           for ij in ("12", "23", "31")}
     G = {}
     for ij, sym, s in (("12", "12", 0), ("23", "23", 1), ("31", "31", 2),
                        ("21", "12", 1), ("32", "23", 2), ("13", "31", 0)):
-        a = 0.5 * fonfs[:, s, :] * (1 + kdotr[ij])
-        G[ij] = 0.25 * np.sin(a) / a * np.exp(-1.0j * (a + kp[:, s])) * Aij[sym]
+        a = 0.5 * fonfs[:, s, :] * (ell[sym] + kdotr[ij])
+        G[ij] = 0.25 * np.sin(a) / a * np.exp(-1.0j * (a + kp[:, s])) * Aij[sym] / ell[sym]
 
     # TDI assembly + FFT (gbgpu.py:348-388)
     f = f0[:, None] + fdot[:, None] * tm[None, :] + 1 / 2 * fddot[:, None] * tm[None, :] ** 2
     omL = f / fstar
-    fc = np.exp(-1.0j * omL)
-    fc2 = 4.0 * omL * np.sin(omL) * fc / amp[:, None]
-    X = G["21"] - G["31"] + (G["12"] - G["13"]) * fc
-    Y = G["32"] - G["12"] + (G["23"] - G["21"]) * fc
-    Z = G["13"] - G["23"] + (G["31"] - G["32"]) * fc
-    sl = fc2[:, None, :] * np.stack([X, Y, Z], axis=1)
+    if unequal_arms:
+        D = {a: np.exp(-1.0j * omL * ell[a]) for a in ("12", "23", "31")}
+        X = ((1 - D["31"] ** 2) * (G["21"] + D["12"] * G["12"])
+             - (1 - D["12"] ** 2) * (G["31"] + D["31"] * G["13"]))
+        Y = ((1 - D["12"] ** 2) * (G["32"] + D["23"] * G["23"])
+             - (1 - D["23"] ** 2) * (G["12"] + D["12"] * G["21"]))
+        Z = ((1 - D["23"] ** 2) * (G["13"] + D["31"] * G["31"])
+             - (1 - D["31"] ** 2) * (G["23"] + D["23"] * G["32"]))
+        if tdi2:
+            X = X * (1 - D["12"] ** 2 * D["31"] ** 2)
+            Y = Y * (1 - D["23"] ** 2 * D["12"] ** 2)
+            Z = Z * (1 - D["31"] ** 2 * D["23"] ** 2)
+        pre = -2.0j * omL / amp[:, None]
+        sl = pre[:, None, :] * np.stack([X, Y, Z], axis=1)
+    else:
+        fc = np.exp(-1.0j * omL)
+        fc2 = 4.0 * omL * np.sin(omL) * fc / amp[:, None]
+        X = G["21"] - G["31"] + (G["12"] - G["13"]) * fc
+        Y = G["32"] - G["12"] + (G["23"] - G["21"]) * fc
+        Z = G["13"] - G["23"] + (G["31"] - G["32"]) * fc
+        sl = fc2[:, None, :] * np.stack([X, Y, Z], axis=1)
     XYZf = np.fft.fftshift(amp[:, None, None] * np.fft.fft(sl, axis=-1), axes=-1)
     fmin = (q - N / 2) / T
     start_inds = np.round(fmin / df).astype(int)            # gbgpu.py:296-297
 
     fctr = np.full(B, 0.5 * T / N, dtype=np.complex128)      # gbgpu.py:298-309
-    if tdi2:
+    if tdi2 and not unequal_arms:
         omegaL = 2 * np.pi * f0 * (L / C_SI)
         fctr = fctr * (2.0j * np.sin(2 * omegaL) * np.exp(-2j * omegaL))
     XYZf = XYZf * fctr[:, None, None]
@@ -318,9 +342,11 @@ def point_major(X):
 # ----------------------------------------------------------------------------
 def get_ll(params, data, psd, N, T=4 * YRSID_SI, dt=10.0, tdi2=False, d_d=0.0,
            start_freq_ind=0, data_index=None, noise_index=None, orbits=None,
-           third=None, phase_marginalize=False, return_terms=False, parallel=False):
+           third=None, phase_marginalize=False, return_terms=False, parallel=False,
+           unequal_arms=False):
     """GBGPUBase.get_ll semantics (gbgpu.py:580-735) on the oracle waveform."""
-    w = waveform(params, N, T=T, dt=dt, tdi2=tdi2, orbits=orbits, third=third)
+    w = waveform(params, N, T=T, dt=dt, tdi2=tdi2, orbits=orbits, third=third,
+                 unequal_arms=unequal_arms)
     B = w["AETf"].shape[0]
     data = [np.asarray(x) for x in data]
     psd = [np.asarray(x) for x in psd]
