@@ -888,10 +888,30 @@ def swap_bench(seed, W=4096, K=500, N=512, steps=100, replays=3):
     torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / replays
+    # swap likelihood with its gradient in the proposal (both launches of
+    # gbx_swap_ll_grad) for every walker's first proposal, on the current state
+    k0 = ks[0]
+    old = smp.params[:, :, k0].contiguous()
+    prop = props[0].contiguous()
+    kw = dict(data_index=smp.walkers, start_freq_ind=s0, N=N, T=T_OBS, dt=DT, return_tensor=True)
+    for _ in range(3):
+        gb.swap_likelihood(old, prop, [smp.res[0], smp.res[1]], [Sd, Sd], grad=True, **kw)
+    torch.cuda.synchronize()
+    reps = 20
+    e0.record()
+    for _ in range(reps):
+        gb.swap_likelihood(old, prop, [smp.res[0], smp.res[1]], [Sd, Sd], grad=True, **kw)
+    e1.record()
+    torch.cuda.synchronize()
+    gms = e0.elapsed_time(e1) / reps
     return {"workload": f"GBGPUThirdBody, {W} walkers x {K} sources, N={N}, dt=5 s; "
                         f"{steps} swap steps per CUDA graph", "graph_ms": ms,
             "swaps_per_s": W * steps / (ms / 1e3),
-            "acceptance": float(smp.accepted.sum().item()) / (W * steps * (replays + 1))}
+            "acceptance": float(smp.accepted.sum().item()) / (W * steps * (replays + 1)),
+            "swap_grad_ms": gms,
+            "swaps_with_grad_per_s": W / (gms / 1e3),
+            "swap_grad_note": f"{W} (old, new) pairs per call: dlogL and its 14-parameter "
+                              "gradient in the proposal (mixed form, eager calls)"}
 
 
 HEADLINE = "pair"      # the precision whose logL meets <= 1e-6 max(1, <h|h>) on this data

@@ -488,7 +488,13 @@ __host__ __device__ constexpr size_t grad_smem_bytes(bool third, int maxS, int m
            (size_t)maxS * (5 * sizeof(float2) + (third ? 3 * (sizeof(double) + 2 * sizeof(float)) : 0));
 }
 
-template <bool THIRD>
+// SWAP: binaries 2j (the current source, h_o) and 2j+1 (the proposal, h) of
+// each tile form a pair, both transformed in the forward pass; only the
+// proposal is differentiated, against the data r + h_o (r: the residual row),
+// since d/dtheta [Re<r|h - h_o> - 1/2 <h - h_o|h - h_o>] = Re<r + h_o - h|dh>.
+// Its gradient goes to column j of grad (num_bin / 2 columns), and d_h, h_h
+// (when given) receive <r + h_o|h> and <h|h>.
+template <bool THIRD, bool SWAP>
 __global__ void __launch_bounds__(kBlock, 2) grad_kernel(const GradParams GP)
 {
     using V = float2;
@@ -544,9 +550,9 @@ __global__ void __launch_bounds__(kBlock, 2) grad_kernel(const GradParams GP)
         const int N = 1 << lg;
         const double *tab = (lg >= 5 && lg <= GBX_MAX_LOG2N)
                                 ? reinterpret_cast<const double *>(a.orbit[lg]) : nullptr;
-        const int maxcnt = tile_pack(a.tile, lg, 1);
+        const int maxcnt = tile_pack(a.tile, lg, SWAP ? 2 : 1);
         if (tab == nullptr || cnt < 1 || cnt > maxcnt || first < 0 || first + cnt > a.num_bin ||
-            (cnt << lg) > K.maxS) {
+            (cnt << lg) > K.maxS || (SWAP && ((cnt | first) & 1))) {
             flag(a.status, GBX_FLAG_TILE);
             __syncthreads();
             continue;
@@ -587,11 +593,15 @@ __global__ void __launch_bounds__(kBlock, 2) grad_kernel(const GradParams GP)
         __syncthreads();
         fft_dif<float>(buf, 2 * cnt, lg);
 
-        // residual weights, likelihood terms, Qf; conj(w) written in place
-        const int Tpb = kBlock / maxcnt;
+        // residual weights, likelihood terms, Qf; conj(w) written in place.
+        // Tpb threads per differentiated binary p (with SWAP, the odd ones)
+        const int Tpb = (SWAP ? 2 : 1) * (kBlock / maxcnt);
         const int width = Tpb < 32 ? Tpb : 32;
-        const int p = tid / Tpb;
-        const int i0 = tid - p * Tpb;
+        const int pq = tid / Tpb;
+        const int p = SWAP ? 2 * pq + 1 : pq;
+        const int i0 = tid - pq * Tpb;
+        const int nproc = SWAP ? cnt >> 1 : cnt;
+        const bool valid = p < cnt && bins[p].valid && (!SWAP || bins[p - 1].valid);
         float acc[kGradAcc];
 #pragma unroll
         for (int k = 0; k < kGradAcc; k++) acc[k] = 0.0f;
@@ -600,20 +610,34 @@ __global__ void __launch_bounds__(kBlock, 2) grad_kernel(const GradParams GP)
             bool out = false;
             // scale 2^eD as a float complex: h in the data's scaled units
             const float2 sc = make_float2(d2f_scaled(B.scale.x, B.eD), d2f_scaled(B.scale.y, B.eD));
+            // SWAP: the current source's scale in the same units
+            const Bin &Bo = bins[SWAP ? p - 1 : p];
+            const float2 so = make_float2(d2f_scaled(Bo.scale.x, B.eD), d2f_scaled(Bo.scale.y, B.eD));
             for (int i = i0; i < N; i += Tpb) {
                 const int j = B.start + i;
                 const int pos = bitrev((i + (N >> 1)) & (N - 1), lg);
                 const int sp = swz(pos, lg);
                 const V hA = buf[(p * 2 + 0) * N + sp], hE = buf[(p * 2 + 1) * N + sp];
                 float2 uA = {0.f, 0.f}, uE = {0.f, 0.f};
-                if (B.valid && j >= 0 && j < K.L) {
+                if (valid && j >= 0 && j < K.L) {
                     const size_t jd = (size_t)B.di * K.L + j, jn = (size_t)B.ni * K.L + j;
                     const double2 dA = __ldg(K.A_data + jd), dE = __ldg(K.E_data + jd);
                     const double SA = __ldg(K.A_psd + jn), SE = __ldg(K.E_psd + jn);
                     const float wA = __frcp_rn(d2f_scaled(SA, B.eS));
                     const float wE = __frcp_rn(d2f_scaled(SE, B.eS));
-                    const float aR = d2f_scaled(dA.x, B.eD), aI = d2f_scaled(dA.y, B.eD);
-                    const float eR = d2f_scaled(dE.x, B.eD), eI = d2f_scaled(dE.y, B.eD);
+                    float aR = d2f_scaled(dA.x, B.eD), aI = d2f_scaled(dA.y, B.eD);
+                    float eR = d2f_scaled(dE.x, B.eD), eI = d2f_scaled(dE.y, B.eD);
+                    if (SWAP) {
+                        // data r + h_o: the current source on the windows' overlap
+                        const int k = j - Bo.start;
+                        if (k >= 0 && k < N) {
+                            const int pk = swz(bitrev((k + (N >> 1)) & (N - 1), lg), lg);
+                            const float2 oA = cmul(so, buf[((p - 1) * 2 + 0) * N + pk]);
+                            const float2 oE = cmul(so, buf[((p - 1) * 2 + 1) * N + pk]);
+                            aR += oA.x; aI += oA.y;
+                            eR += oE.x; eI += oE.y;
+                        }
+                    }
                     acc[0] += fmaf(aR, hA.x, aI * hA.y) * wA + fmaf(eR, hE.x, eI * hE.y) * wE;
                     acc[1] += fmaf(aR, hA.y, -aI * hA.x) * wA + fmaf(eR, hE.y, -eI * hE.x) * wE;
                     acc[2] += fmaf(hA.x, hA.x, hA.y * hA.y) * wA + fmaf(hE.x, hE.x, hE.y * hE.y) * wE;
@@ -625,7 +649,7 @@ __global__ void __launch_bounds__(kBlock, 2) grad_kernel(const GradParams GP)
                     // X, Y, Z weights are the A, E ones mapped back)
                     acc[3] += fmaf(uA.x, hA.x, fmaf(uA.y, hA.y, fmaf(uE.x, hE.x, uE.y * hE.y)));
                     acc[4] += fmaf(uA.x, hA.y, fmaf(-uA.y, hA.x, fmaf(uE.x, hE.y, -uE.y * hE.x)));
-                } else if (B.valid) {
+                } else if (valid) {
                     out = true;
                 }
                 buf[(p * 2 + 0) * N + sp] = make_float2(uA.x, -uA.y);
@@ -640,7 +664,7 @@ __global__ void __launch_bounds__(kBlock, 2) grad_kernel(const GradParams GP)
         if (p < cnt) {
             const Bin &B = bins[p];
             const GradExtra &Gx = gxs[p];
-            if (B.valid) {
+            if (valid) {
                 for (int n = i0; n < N; n += Tpb) {
                     float2 Yc[3], Es[3];
                     float2 *ep = es + 3 * ((size_t)(p << lg) + n);
@@ -676,7 +700,8 @@ __global__ void __launch_bounds__(kBlock, 2) grad_kernel(const GradParams GP)
             // suffix sums R_k = sum_{n >= k} cph_n along every (binary, spacecraft) row
             const int warp = tid >> 5, lane = tid & 31;
             const int chunk = N >> 5;
-            for (int row = warp; row < 3 * cnt; row += kBlock / 32) {
+            for (int rr = warp; rr < 3 * nproc; rr += kBlock / 32) {
+                const int row = SWAP ? 3 * (2 * (rr / 3) + 1) + rr % 3 : rr;
                 V *rp = cphs + (size_t)row * N;
                 const int c0 = lane * chunk;
                 float2 t = {0.f, 0.f};
@@ -695,7 +720,7 @@ __global__ void __launch_bounds__(kBlock, 2) grad_kernel(const GradParams GP)
                 }
             }
             __syncthreads();
-            if (p < cnt && bins[p].valid) {
+            if (valid) {
                 const Bin &B = bins[p];
                 const GradExtra &Gx = gxs[p];
                 for (int k = i0; k < N; k += Tpb) {
@@ -730,7 +755,7 @@ __global__ void __launch_bounds__(kBlock, 2) grad_kernel(const GradParams GP)
         __syncthreads();
         {
             const int per = Tpb / width;
-            for (int t = tid; t < cnt * kGradAcc; t += kBlock) {
+            for (int t = tid; t < nproc * kGradAcc; t += kBlock) {
                 const int q = t / kGradAcc, k = t - q * kGradAcc;
                 dfl x = {0.f, 0.f};
                 for (int g = q * per; g < (q + 1) * per; g++) {
@@ -743,22 +768,25 @@ __global__ void __launch_bounds__(kBlock, 2) grad_kernel(const GradParams GP)
         __syncthreads();
         {
             constexpr int kOut = (THIRD ? 14 : 9) + 1;   // gradient rows + (d_h, h_h)
-            for (int t = tid; t < cnt * kOut; t += kBlock) {
+            for (int t = tid; t < nproc * kOut; t += kBlock) {
                 const int q = t / kOut, j = t - q * kOut;
-                const Bin &B = bins[q];
+                const int bq = SWAP ? 2 * q + 1 : q;
+                const Bin &B = bins[bq];
                 if (B.b < 0) continue;
-                const GradExtra &Gx = gxs[q];
+                const bool ok = B.valid && (!SWAP || (bins[bq - 1].valid && bins[bq - 1].b >= 0));
+                const int col = SWAP ? B.b >> 1 : B.b;
+                const GradExtra &Gx = gxs[bq];
                 const double *ts = tsum + q * kGradAcc;
                 const double s4 = 4.0 * K.df;
                 // weights were 4 df r / S in units of 2^(eS - eD): cu converts sums of w
                 const double cu = s4 * exp2_int(B.eS - B.eD);
                 const double2 sc = B.scale;
-                const double nb = a.num_bin;
+                const size_t nb = SWAP ? a.num_bin >> 1 : a.num_bin;
                 if (j == kOut - 1) {
                     const double ch = s4 * exp2_int(B.eS) * (sc.x * sc.x + sc.y * sc.y);
                     const double2 dh = cmul(make_double2(cu * ts[0], cu * ts[1]), sc);
-                    K.d_h[B.b] = B.valid ? dh : make_double2(0.0, 0.0);
-                    K.h_h[B.b] = B.valid ? make_double2(ch * ts[2], 0.0) : make_double2(0.0, 0.0);
+                    if (K.d_h) K.d_h[col] = ok ? dh : make_double2(0.0, 0.0);
+                    if (K.h_h) K.h_h[col] = ok ? make_double2(ch * ts[2], 0.0) : make_double2(0.0, 0.0);
                     continue;
                 }
                 double g;
@@ -778,7 +806,7 @@ __global__ void __launch_bounds__(kBlock, 2) grad_kernel(const GradParams GP)
                     const int k = j == 2 ? 11 : j == 3 ? 13 : j == 7 ? 15 : j == 8 ? 17 : 19 + 2 * (j - 9);
                     g = cmul(sc, make_double2(cu * ts[k], cu * ts[k + 1])).x;
                 }
-                GP.grad[(size_t)j * (size_t)nb + B.b] = B.valid ? g : 0.0;
+                GP.grad[(size_t)j * nb + col] = ok ? g : 0.0;
             }
         }
         __syncthreads();

@@ -1885,37 +1885,31 @@ extern "C" size_t gbx_grad_workspace_bytes(int num_bin)
     return ((size_t)num_bin * (sizeof(Bin) + sizeof(GradExtra)) + 255) & ~(size_t)255;
 }
 
-extern "C" int gbx_waveform_ll_grad(const gbx_wave_args *a, const gbx_ll_args *l, void *d_h,
-                                    void *h_h, double *grad, void *stream)
+// validates the gradient entry points' arguments (b: a copy of the caller's,
+// workspace checked here, not by check_wave); *maxS as check_wave
+static int check_grad(gbx_wave_args &b, const gbx_ll_args *l, int *maxS)
 {
-    int maxS = 0;
-    gbx_wave_args b = a ? *a : gbx_wave_args{};
-    if (!a) return set_error(GBX_ERR_ARG, "NULL wave args");
-    // the per-binary workspace of this entry point is larger; validate it here
     const void *ws = b.workspace;
     const size_t wsb = b.workspace_bytes;
     b.workspace = nullptr;
-    int rc = check_wave(&b, &maxS);
+    int rc = check_wave(&b, maxS);
     if (rc) return rc;
     if (b.precision != GBX_MIXED) return set_error(GBX_ERR_UNSUPPORTED, "gradients are computed in the mixed form only");
     if (b.nparams != 9 && b.nparams != 14)
         return set_error(GBX_ERR_UNSUPPORTED, "gradients cover the 9-parameter model and the 14-parameter third-body model");
     if (!ws || ((uintptr_t)ws & 15) != 0 || wsb < gbx_grad_workspace_bytes(b.num_bin))
         return set_error(GBX_ERR_ARG, "gradients need a 16-byte aligned workspace of gbx_grad_workspace_bytes(num_bin)");
-    if (!l || !l->A_data || !l->E_data || !l->A_psd || !l->E_psd || !d_h || !h_h || !grad)
-        return set_error(GBX_ERR_ARG, "NULL likelihood / gradient pointer");
+    if (!l || !l->A_data || !l->E_data || !l->A_psd || !l->E_psd)
+        return set_error(GBX_ERR_ARG, "NULL likelihood pointer");
     if (l->data_length <= 0 || l->num_data < 1 || l->num_psd < 1)
         return set_error(GBX_ERR_ARG, "data_length / num_data / num_psd must be positive");
-    if (b.num_bin == 0) return GBX_OK;
-    cudaStream_t st = (cudaStream_t)stream;
-    rc = ensure_init(st);
-    if (rc) return rc;
     b.workspace = const_cast<void *>(ws);
     b.workspace_bytes = wsb;
-    GradParams G;
-    memset(&G, 0, sizeof(G));
-    G.K = base_params(&b);
-    KParams &K = G.K;
+    return GBX_OK;
+}
+
+static void set_ll(KParams &K, const gbx_ll_args *l)
+{
     K.A_data = (const double2 *)l->A_data;
     K.E_data = (const double2 *)l->E_data;
     K.A_psd = l->A_psd;
@@ -1926,13 +1920,29 @@ extern "C" int gbx_waveform_ll_grad(const gbx_wave_args *a, const gbx_ll_args *l
     K.data_index = l->data_index;
     K.noise_index = l->noise_index;
     K.df = l->df;
+}
+
+// prep_grad_kernel + grad_kernel<third, SWAP> over the validated arguments
+template <bool SWAP>
+static int launch_grad(const gbx_wave_args &b, const gbx_ll_args *l, void *d_h, void *h_h,
+                       double *grad, int maxS, cudaStream_t st)
+{
+    GradParams G;
+    memset(&G, 0, sizeof(G));
+    G.K = base_params(&b);
+    KParams &K = G.K;
+    set_ll(K, l);
     K.d_h = (double2 *)d_h;
     K.h_h = (double2 *)h_h;
+    if (SWAP) {
+        K.P = tile_pack(b.tile, 31 - __builtin_clz((unsigned)b.N), 2);
+        maxS = K.P * b.N;
+    }
     K.maxS = maxS;
-    K.maxP = max_pack(&K.a, 1);
+    K.maxP = max_pack(&K.a, SWAP ? 2 : 1);
     G.grad = grad;
     const bool third = b.nparams == 14;
-    auto kern = third ? grad_kernel<true> : grad_kernel<false>;
+    auto kern = third ? grad_kernel<true, SWAP> : grad_kernel<false, SWAP>;
     const size_t sm = grad_smem_bytes(third, maxS, K.maxP);
     if (sm > 227 * 1024) return set_error(GBX_ERR_UNSUPPORTED, "tile needs %zu B of shared memory", sm);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -1963,6 +1973,46 @@ extern "C" int gbx_waveform_ll_grad(const gbx_wave_args *a, const gbx_ll_args *l
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_error(e, "grad_kernel launch");
     return GBX_OK;
+}
+
+extern "C" int gbx_waveform_ll_grad(const gbx_wave_args *a, const gbx_ll_args *l, void *d_h,
+                                    void *h_h, double *grad, void *stream)
+{
+    if (!a) return set_error(GBX_ERR_ARG, "NULL wave args");
+    int maxS = 0;
+    gbx_wave_args b = *a;
+    int rc = check_grad(b, l, &maxS);
+    if (rc) return rc;
+    if (!d_h || !h_h || !grad) return set_error(GBX_ERR_ARG, "NULL likelihood / gradient pointer");
+    if (b.num_bin == 0) return GBX_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    rc = ensure_init(st);
+    if (rc) return rc;
+    return launch_grad<false>(b, l, d_h, h_h, grad, maxS, st);
+}
+
+extern "C" int gbx_swap_ll_grad(const gbx_wave_args *a, const gbx_ll_args *l, double *dlogl,
+                                double *grad, void *stream)
+{
+    if (!a) return set_error(GBX_ERR_ARG, "NULL wave args");
+    int maxS = 0;
+    gbx_wave_args b = *a;
+    int rc = check_grad(b, l, &maxS);
+    if (rc) return rc;
+    if (b.tiles || b.order) return set_error(GBX_ERR_ARG, "gbx_swap_ll_grad takes a uniform N and no order");
+    if (b.num_bin % 2) return set_error(GBX_ERR_ARG, "num_bin must be even: (old, new) pairs");
+    if (!grad) return set_error(GBX_ERR_ARG, "NULL gradient pointer");
+    if (b.num_bin == 0) return GBX_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (dlogl) {
+        // the change of log-likelihood itself: the swap kernel, as gbx_swap_ll
+        rc = gbx_swap_ll(&b, l, dlogl, stream);
+        if (rc) return rc;
+    } else {
+        rc = ensure_init(st);
+        if (rc) return rc;
+    }
+    return launch_grad<true>(b, l, nullptr, nullptr, grad, maxS, st);
 }
 
 // ----------------------------------------------------------------------------

@@ -787,7 +787,8 @@ class GBGPUBase(abc.ABC):
         return like, grad
 
     def swap_likelihood(self, params_old, params_new, data, psd, start_freq_ind=0,
-                        data_index=None, noise_index=None, return_tensor=False, **kwargs):
+                        data_index=None, noise_index=None, return_tensor=False, grad=False,
+                        **kwargs):
         """Change of log-likelihood when source ``params_old[:, j]`` is replaced by
         ``params_new[:, j]`` (no counterpart in this version of the reference).
 
@@ -796,8 +797,14 @@ class GBGPUBase(abc.ABC):
         ``dlogL_j = Re<r|Dh> - <Dh|Dh>/2`` over the union of both windows, in
         the inner product of the reference's likelihood.  Keywords as in
         ``get_ll`` (N must be a single power of two; ``precision``).
+
+        With ``grad=True`` returns ``(dlogL, grad)``, ``grad[k, j] = d dlogL_j /
+        d params_new[k, j]`` (= Re<r + h_old - h_new | d h_new>, the likelihood
+        gradient at the proposal against r + h_old), both in the mixed form.
         """
-        precision = kwargs.pop("precision", self.precision)
+        precision = kwargs.pop("precision", "mixed" if grad else self.precision)
+        if grad and precision != "mixed":
+            raise ValueError("swap gradients are computed in the mixed form only")
         N = kwargs.pop("N", None)
         T = kwargs.pop("T", 4 * YRSID_SI)
         dt = kwargs.pop("dt", 10.0)
@@ -827,10 +834,11 @@ class GBGPUBase(abc.ABC):
         ni2 = None if ni is None else ni.repeat_interleave(2).contiguous()
         dd, pp, L, di2, ni2 = self._prepare_data(data, psd, di2, ni2, 2 * B)
         out = torch.empty(B, dtype=torch.float64, device=self.device)
+        gout = torch.zeros((self.NPARAMS, B), dtype=torch.float64, device=self.device) if grad else None
         if B:
             plan = self._plan(N, T, precision, tdi2, self.NPARAMS)
             self._status.zero_()
-            a = plan.args(prm, start_freq_ind, self._status)
+            a = plan.args(prm, start_freq_ind, self._status, grad=grad)
             la = nat.LLArgs()
             la.A_data, la.E_data = dd[0].data_ptr(), dd[1].data_ptr()
             la.A_psd, la.E_psd = pp[0].data_ptr(), pp[1].data_ptr()
@@ -840,14 +848,19 @@ class GBGPUBase(abc.ABC):
             la.data_index = di2.data_ptr()
             la.noise_index = ni2.data_ptr()
             la.df = 1.0 / T
-            rc = nat.lib().gbx_swap_ll(ctypes.byref(a), ctypes.byref(la), nat.ptr(out),
-                                       nat.stream_handle())
-            nat.check(rc, "gbx_swap_ll")
+            if grad:
+                rc = nat.lib().gbx_swap_ll_grad(ctypes.byref(a), ctypes.byref(la), nat.ptr(out),
+                                                nat.ptr(gout), nat.stream_handle())
+                nat.check(rc, "gbx_swap_ll_grad")
+            else:
+                rc = nat.lib().gbx_swap_ll(ctypes.byref(a), ctypes.byref(la), nat.ptr(out),
+                                           nat.stream_handle())
+                nat.check(rc, "gbx_swap_ll")
         if return_tensor:
-            return out
+            return (out, gout) if grad else out
         res = out.cpu().numpy()
         self._check_status()
-        return res
+        return (res, gout.cpu().numpy()) if grad else res
 
     # --------------------------------------------------------- global fill
     def fill_global_template(self, group_index, templates, A, E, start_inds, N=None,

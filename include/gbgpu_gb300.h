@@ -285,6 +285,19 @@ int gbx_waveform_ll_grad(const gbx_wave_args *a, const gbx_ll_args *l, void *d_h
                          double *grad, void *stream);
 
 /*
+ * Swap log-likelihood with its gradient (no counterpart in the reference):
+ * the pairs, residual rows and dlogl of gbx_swap_ll (dlogl may be NULL), and
+ * grad[k*(num_bin/2) + j] = d dlogl[j] / d params[k, 2j+1], the gradient with
+ * respect to the proposal, = Re<r + h_old - h_new | d h_new / d theta>
+ * (the likelihood gradient at the proposal against the data r + h_old).
+ * Mixed form only, uniform N, num_bin even, 9 or 14 parameters; the workspace
+ * must hold gbx_grad_workspace_bytes(num_bin) bytes.  Two launches: the swap
+ * kernel for dlogl, then the gradient kernel with each tile's pairs.
+ */
+int gbx_swap_ll_grad(const gbx_wave_args *a, const gbx_ll_args *l, double *dlogl, double *grad,
+                     void *stream);
+
+/*
  * gbx_waveform_ll without caller-provided scratch.  No counterpart in the
  * reference (its kernels use no scratch).  For callers that may not allocate
  * device memory: a plug-in inside an application that owns all device
