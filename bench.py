@@ -667,25 +667,38 @@ def dropin_kernels(gb, p, data, Sd, steps):
 
 
 def fisher_bench(gb, p, Tu):
-    """Per-binary 8x8 Fisher matrices of the 50k N = 256 binaries (FP64
-    five-point differences of the batched waveform, TDI-2)."""
+    """Per-binary 8x8 Fisher matrices of the 50k N = 256 binaries (TDI-2):
+    in-kernel forward mode (one gbx_fisher launch) and, for comparison, FP64
+    five-point differences of the batched waveform."""
     import torch
     B = p.shape[1]
-    # untimed call on a slice: one-time costs (library kernels loaded on first
-    # use by the batched inner products, plans, orbit tables) stay out of the timing
-    gb.fisher_matrices(p[:, :512], N=256, T=T_OBS, dt=DT, tdi2=True, inds=FREE8, return_gpu=True)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    torch.cuda.nvtx.range_push("n256_fisher")
-    F = gb.fisher_matrices(p, N=256, T=T_OBS, dt=DT, tdi2=True, inds=FREE8, return_gpu=True)
-    torch.cuda.synchronize()
-    torch.cuda.nvtx.range_pop()
-    dt_s = time.perf_counter() - t0
-    ok = bool(torch.isfinite(F).all().item())
-    return {"binaries": B, "params": len(FREE8), "seconds": dt_s, "binaries_per_s": B / dt_s,
-            "finite": ok, "note": "5-point FP64 differences: 32 batched FP64 waveform launches "
-                                  "+ one inner-product einsum; after one untimed call on 512 "
-                                  "binaries"}
+    out = {"binaries": B, "params": len(FREE8)}
+    Fs = {}
+    for method in ("forward", "differences"):
+        # untimed call on a slice: one-time costs (library kernels loaded on first
+        # use, plans, orbit tables) stay out of the timing
+        gb.fisher_matrices(p[:, :512], N=256, T=T_OBS, dt=DT, tdi2=True, inds=FREE8,
+                           return_gpu=True, method=method)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        torch.cuda.nvtx.range_push(f"n256_fisher_{method}")
+        Fs[method] = gb.fisher_matrices(p, N=256, T=T_OBS, dt=DT, tdi2=True, inds=FREE8,
+                                        return_gpu=True, method=method)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        dt_s = time.perf_counter() - t0
+        out[f"{method}_seconds"] = dt_s
+        out[f"{method}_binaries_per_s"] = B / dt_s
+    d = torch.sqrt(torch.diagonal(Fs["differences"], dim1=1, dim2=2))
+    diff = (Fs["forward"] - Fs["differences"]).abs() / (d[:, :, None] * d[:, None, :])
+    out.update({"seconds": out["forward_seconds"], "binaries_per_s": out["forward_binaries_per_s"],
+                "finite": bool(torch.isfinite(Fs["forward"]).all().item()),
+                "max_forward_vs_differences": float(diff.max().item()),
+                "note": "forward: one gbx_fisher launch (14 transforms per binary, 45 products "
+                        "per channel and bin) plus prep; differences: 32 batched FP64 waveform launches + one "
+                        "einsum; host wall time after one untimed call on 512 binaries; "
+                        "difference normalised by sqrt(F_ii F_jj)"})
+    return out
 
 
 def hmc_bench(gb, p, data, Sd, seed, B=4096, transitions=100, n_leapfrog=10, step=0.2):

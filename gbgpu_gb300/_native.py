@@ -28,7 +28,7 @@ EXPORTS = (
     "gbx_orbit_table_bytes", "gbx_orbit_table",
     "gbx_waveform", "gbx_waveform_ll", "gbx_waveform_fill", "gbx_wave_workspace_bytes",
     "gbx_waveform_ll_noalloc", "gbx_waveform_ll_grad", "gbx_grad_workspace_bytes",
-    "gbx_swap_ll", "gbx_swap_ll_grad", "gbx_fill_global_det", "gbx_math_selftest",
+    "gbx_swap_ll", "gbx_swap_ll_grad", "gbx_fisher", "gbx_fill_global_det", "gbx_math_selftest",
 )
 
 _vp = ctypes.c_void_p
@@ -95,6 +95,8 @@ def lib():
     L.gbx_grad_workspace_bytes.restype = ctypes.c_size_t
     L.gbx_swap_ll.argtypes = [ctypes.POINTER(WaveArgs), ctypes.POINTER(LLArgs), _vp, _vp]
     L.gbx_swap_ll_grad.argtypes = [ctypes.POINTER(WaveArgs), ctypes.POINTER(LLArgs), _vp, _vp, _vp]
+    L.gbx_fisher.argtypes = [ctypes.POINTER(WaveArgs), _vp, _vp, _i, _i, _vp, ctypes.c_double,
+                             _vp, _vp]
     L.gbx_waveform_fill.argtypes = [ctypes.POINTER(WaveArgs), _vp, _vp, _vp, _i, _i, _ll, _vp]
     L.gbx_math_selftest.argtypes = [_vp, _vp, _i, _i, _i, _vp]
     for name in EXPORTS:

@@ -1600,6 +1600,7 @@ __global__ void __launch_bounds__(kPrepBlock) prep_kernel(const KParams K)
 constexpr int kPairMaxLog2N = 12;  // pair form: N <= 4096 (two 16-byte channels of 4096 fit)
 #include "gbx_pair.cuh"
 #include "gbx_grad.cuh"
+#include "gbx_fisher.cuh"
 
 // ----------------------------------------------------------------------------
 // host side
@@ -2013,6 +2014,78 @@ extern "C" int gbx_swap_ll_grad(const gbx_wave_args *a, const gbx_ll_args *l, do
         if (rc) return rc;
     }
     return launch_grad<true>(b, l, nullptr, nullptr, grad, maxS, st);
+}
+
+extern "C" int gbx_fisher(const gbx_wave_args *a, const double *A_psd, const double *E_psd,
+                          int psd_length, int num_psd, const int *noise_index, double df,
+                          double *fisher, void *stream)
+{
+    if (!a) return set_error(GBX_ERR_ARG, "NULL wave args");
+    int maxS = 0;
+    gbx_wave_args b = *a;
+    gbx_ll_args l;
+    memset(&l, 0, sizeof(l));
+    // the likelihood arguments' checks, with the PSD rows standing in for the
+    // data (never read)
+    l.A_data = A_psd;
+    l.E_data = E_psd;
+    l.A_psd = A_psd;
+    l.E_psd = E_psd;
+    l.data_length = psd_length;
+    l.num_data = 1;
+    l.num_psd = num_psd;
+    l.noise_index = noise_index;
+    l.df = df;
+    int rc = check_grad(b, &l, &maxS);
+    if (rc) return rc;
+    if (b.nparams != 9) return set_error(GBX_ERR_UNSUPPORTED, "Fisher matrices cover the 9-parameter model");
+    if (b.tdi2 & GBX_TDI_UNEQUAL) return set_error(GBX_ERR_UNSUPPORTED, "Fisher matrices take equal arms");
+    if (!fisher) return set_error(GBX_ERR_ARG, "NULL Fisher output");
+    if (b.num_bin == 0) return GBX_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    rc = ensure_init(st);
+    if (rc) return rc;
+    FisherParams F;
+    memset(&F, 0, sizeof(F));
+    F.K = base_params(&b);
+    KParams &K = F.K;
+    set_ll(K, &l);
+    K.A_data = nullptr;
+    K.E_data = nullptr;
+    K.data_index = nullptr;
+    K.maxS = maxS;
+    K.maxP = max_pack(&K.a, 1);
+    F.fisher = fisher;
+    const size_t sm = fisher_smem_bytes(maxS, K.maxP);
+    if (sm > 227 * 1024) return set_error(GBX_ERR_UNSUPPORTED, "tile needs %zu B of shared memory (use a smaller tile)", sm);
+    cudaError_t e = cudaFuncSetAttribute(fisher_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(fisher)");
+    e = cudaFuncSetAttribute(fisher_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(fisher carveout)");
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fisher_kernel, kBlock, sm);
+    if (e != cudaSuccess) return cuda_error(e, "occupancy(fisher)");
+    if (b.blocks_per_sm > 0 && per_sm > b.blocks_per_sm) per_sm = b.blocks_per_sm;
+    if (per_sm < 1) per_sm = 1;
+    const int ntiles = b.tiles ? b.ntiles : (b.num_bin + K.P - 1) / K.P;
+    int grid = per_sm * num_sms();
+    if (grid > ntiles) grid = ntiles;
+    if (grid < 1) return GBX_OK;
+    if (b.queue) {
+        e = cudaMemsetAsync(b.queue, 0, sizeof(int), st);
+        if (e != cudaSuccess) return cuda_error(e, "queue reset");
+    }
+    const size_t psm = (sizeof(Bin) + sizeof(GradExtra)) * kPrepBlock;
+    e = cudaFuncSetAttribute(prep_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psm);
+    if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute(prep_grad)");
+    prep_grad_kernel<<<(b.num_bin + kPrepBlock - 1) / kPrepBlock, kPrepBlock, psm, st>>>(K);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_error(e, "prep_grad_kernel launch");
+    fisher_kernel<<<grid, kBlock, sm, st>>>(F);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_error(e, "fisher_kernel launch");
+    return GBX_OK;
 }
 
 // ----------------------------------------------------------------------------

@@ -1149,21 +1149,29 @@ class GBGPUBase(abc.ABC):
         return info
 
     def fisher_matrices(self, params, N, T=4 * YRSID_SI, dt=10.0, tdi2=False, inds=None,
-                        psd_func=None, psd_kwargs={}, return_gpu=False):
+                        psd_func=None, psd_kwargs={}, return_gpu=False, method="auto"):
         """Per-binary Fisher matrices F_ij = <dh/dtheta_i | dh/dtheta_j> (A and E)
-        for a whole batch, by five-point FP64 central differences of the
-        batched waveform in absolute parameter steps.
+        for a whole batch.
+
+        ``method="forward"``: forward-mode derivatives in one launch
+        (``gbx_fisher``: the bases of the two polarisations and five slow-part
+        tangents transformed per binary, the 45 products summed per bin; mixed
+        form, the 9-parameter model, equal arms, N <= 1024).
+        ``method="differences"``: five-point FP64 central differences of the
+        batched waveform in absolute parameter steps (any model, 4 waveform
+        launches per parameter).  ``"auto"`` takes the first where it applies.
 
         Unlike ``information_matrix`` (the reference's, gbgpu.py:957-1138: steps
         relative to each parameter, and every binary of a call must share one
         start bin), binaries may sit anywhere: each derivative is taken on the
-        binary's own window; the f0 stencil stays inside the binary's carrier
-        bin rint(f0 T) (shortened near a bin edge), and a step that still moves
-        the window is aligned before differencing.  ``params`` is (nparams, B); ``inds``
-        selects the parameters (default all 9 / 14).  Steps: amp 1e-6 amp;
-        f0 1e-4/T; fdot 1e-4/T^2; fddot 1e-4/T^3 (phase-equivalent); angles
-        1e-6 rad; third body: A2, P2 relative 1e-6, varpi, e2, T2 1e-6.  Returns (B, n, n)
-        NumPy (or a CUDA tensor with ``return_gpu``).
+        binary's own window.  With differences the f0 stencil stays inside the
+        binary's carrier bin rint(f0 T) (shortened near a bin edge), and a step
+        that still moves the window is aligned before differencing.  ``params``
+        is (nparams, B); ``inds`` selects the parameters (default all 9 / 14).
+        Steps: amp 1e-6 amp; f0 1e-4/T; fdot 1e-4/T^2; fddot 1e-4/T^3
+        (phase-equivalent); angles 1e-6 rad; third body: A2, P2 relative 1e-6,
+        varpi, e2, T2 1e-6.  Returns (B, n, n) NumPy (or a CUDA tensor with
+        ``return_gpu``).
         """
         if psd_func is None:
             from .sensitivity import A1TDISens
@@ -1175,6 +1183,17 @@ class GBGPUBase(abc.ABC):
         inds = list(range(npar)) if inds is None else [int(i) for i in inds]
         Tu = int(T / dt) * dt
         N = int(N)
+        if method not in ("auto", "forward", "differences"):
+            raise ValueError("method must be 'auto', 'forward' or 'differences'")
+        fwd_ok = npar == 9 and not self.unequal_arms and N <= 1024
+        if method == "forward" and not fwd_ok:
+            raise ValueError("forward-mode Fisher matrices cover the 9-parameter model, equal "
+                             "arms and N <= 1024")
+        if method == "forward" or (method == "auto" and fwd_ok):
+            F = self._fisher_forward(prm, N, T, Tu, tdi2, psd_func, psd_kwargs)
+            ix = torch.as_tensor(inds, device=self.device)
+            F = F[:, ix][:, :, ix].contiguous()
+            return F if return_gpu else F.cpu().numpy()
         absolute = {1: 1e-4 / Tu, 2: 1e-4 / Tu ** 2, 3: 1e-4 / Tu ** 3, 4: 1e-6, 5: 1e-6,
                     6: 1e-6, 7: 1e-6, 8: 1e-6, 10: 1e-6, 11: 1e-6, 13: 1e-6}
 
@@ -1223,6 +1242,28 @@ class GBGPUBase(abc.ABC):
         F = torch.einsum("bicn,bjcn->bij", dh.conj() * w[:, None, None, :], dh).real
         F = 0.5 * (F + F.transpose(1, 2))
         return F if return_gpu else F.cpu().numpy()
+
+    def _fisher_forward(self, prm, N, T, Tu, tdi2, psd_func, psd_kwargs):
+        """(B, 9, 9) Fisher matrices from gbx_fisher on the PSD of the union
+        of the binaries' windows (one host evaluation per distinct bin)."""
+        B = prm.shape[1]
+        F = torch.zeros((B, 9, 9), dtype=torch.float64, device=self.device)
+        if B == 0:
+            return F
+        self._check_T(Tu)
+        q = torch.round(prm[1] * Tu).to(torch.int64) - N // 2
+        lo = int(q.min().item()) - N
+        hi = int(q.max().item()) + 2 * N
+        grid = np.asarray(psd_func((lo + np.arange(hi - lo)) / Tu, **psd_kwargs), dtype=np.float64)
+        psd = torch.as_tensor(grid, device=self.device).contiguous()
+        plan = self._plan(N, Tu, "mixed", tdi2, 9)
+        self._status.zero_()
+        a = plan.args(prm, lo, self._status, grad=True)
+        rc = nat.lib().gbx_fisher(ctypes.byref(a), psd.data_ptr(), psd.data_ptr(), int(hi - lo), 1,
+                                  None, 1.0 / Tu, nat.ptr(F), nat.stream_handle())
+        nat.check(rc, "gbx_fisher")
+        self._check_status()
+        return F
 
     # ----------------------------------------------------------------- hooks
     @abc.abstractmethod

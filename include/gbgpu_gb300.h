@@ -298,6 +298,19 @@ int gbx_swap_ll_grad(const gbx_wave_args *a, const gbx_ll_args *l, double *dlogl
                      void *stream);
 
 /*
+ * Per-binary Fisher matrices by forward mode in one launch (the reference
+ * forms them from five-point differences of run_wave, gbgpu/gbgpu.py:957-1138):
+ * fisher[b*81 + 9*i + j] = 4 df sum_{A,E} Re conj(dh/dp_i) dh/dp_j / S over the
+ * binary's window, p = (amp, f0, fdot, fddot, phi0, iota, psi, lam, beta),
+ * with S the PSD rows A_psd / E_psd (num_psd rows of psd_length bins, row
+ * noise_index[b] or 0; bin j of a row is bin j + start_freq_ind of the grid).
+ * Mixed form, 9 parameters, equal arms; the workspace must hold
+ * gbx_grad_workspace_bytes(num_bin) bytes; tiles of at most 1024 samples.
+ */
+int gbx_fisher(const gbx_wave_args *a, const double *A_psd, const double *E_psd, int psd_length,
+               int num_psd, const int *noise_index, double df, double *fisher, void *stream);
+
+/*
  * gbx_waveform_ll without caller-provided scratch.  No counterpart in the
  * reference (its kernels use no scratch).  For callers that may not allocate
  * device memory: a plug-in inside an application that owns all device
