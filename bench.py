@@ -516,6 +516,71 @@ def dropin_section(args):
     return out
 
 
+def fill_section(args):
+    """The template fills alone (``--section fill``): the 50k N = 256 TDI-2
+    batch (f0 on [1e-3, 5e-3] Hz) into 64 group templates over the batch's
+    band (about 1 GB of templates), group of each binary drawn at random: the
+    fused waveform + atomic fill (gbx_waveform_fill, mixed form) and the
+    deterministic gather (waveform windows, then fill_det_kernel); one
+    untimed call and ``--steps`` timed ones each; one JSON line.  A small
+    case for profiling the fill kernels."""
+    import torch
+    from gbgpu_gb300 import GBGPU
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    p = n256_params(args.seed)
+    B, N, G = p.shape[1], 256, 64
+    Tu = int(T_OBS / DT) * DT
+    q = np.rint(p[1] * Tu).astype(np.int64) - N // 2
+    s0 = int(q.min()) - N
+    Lb = int(q.max()) + 2 * N - s0
+    gb = GBGPU(precision="mixed")
+    gi = torch.as_tensor(np.random.default_rng(args.seed + 6).integers(0, G, B), dtype=torch.int32,
+                         device="cuda")
+    tmpl = torch.zeros((G, 2, Lb), dtype=torch.complex128, device="cuda")
+    pT = torch.as_tensor(p.T.copy(), device="cuda")
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    out = {"section": "fill", "binaries": B, "N": N, "groups": G, "band_bins": Lb}
+
+    def timed(run, name):
+        run()
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push(name)
+        ev[0].record()
+        for _ in range(max(1, args.steps)):
+            run()
+        ev[1].record()
+        torch.cuda.nvtx.range_pop()
+        torch.cuda.synchronize()
+        return ev[0].elapsed_time(ev[1]) / max(1, args.steps)
+
+    for mode, sort in (("atomic", False), ("atomic", True), ("deterministic", False)):
+        key = mode + ("_sorted" if sort else "")
+        out[f"{key}_ms"] = timed(lambda: gb.generate_global_template(
+            pT, gi, tmpl, N=N, T=T_OBS, dt=DT, tdi2=True, start_freq_ind=s0, fill_mode=mode,
+            sort=sort), f"fill_{key}")
+    # dense: the swap sampler's residuals, 512 walkers x 500 sources of N = 512
+    # in a 34,000-bin band, added into (A, E) rows of each walker
+    W, K, Nd, Ld = 512, 500, 512, 34_000
+    rng = np.random.default_rng(args.seed + 8)
+    sd = int(2e-3 * Tu)
+    f0 = (sd + 1024 + rng.uniform(0, Ld - 2048, W * K)) / Tu
+    fdot = 10 ** rng.uniform(-18, -16, W * K)
+    pd = torch.as_tensor(np.array([10 ** rng.uniform(-23, -21, W * K), f0, fdot,
+                                   11 / 3 * fdot ** 2 / f0, rng.uniform(0, 2 * np.pi, W * K),
+                                   np.arccos(rng.uniform(-1, 1, W * K)),
+                                   rng.uniform(0, np.pi, W * K), rng.uniform(0, 2 * np.pi, W * K),
+                                   np.arcsin(rng.uniform(-1, 1, W * K))]), device="cuda")
+    gw = torch.arange(W, device="cuda", dtype=torch.int32).repeat_interleave(K)
+    rA = torch.zeros((W, Ld), dtype=torch.complex128, device="cuda")
+    rE = torch.zeros_like(rA)
+    out["dense"] = {"workload": f"{W} groups x {K} sources, N={Nd}, {Ld}-bin band, mixed form"}
+    for sort in (False, True):
+        out["dense"]["sorted_ms" if sort else "unsorted_ms"] = timed(
+            lambda: gb.add_to_templates(pd, gw, (rA, rE), N=Nd, T=T_OBS, dt=DT, start_freq_ind=sd,
+                                        sort=sort), "dense_sorted" if sort else "dense_unsorted")
+    return out
+
+
 def pair_section(args):
     """The headline kernel alone (``--section pair``): the uneven-N workload's
     first ``--binaries`` binaries (20,000 gives a small case of about 1 GB on
@@ -1248,7 +1313,7 @@ def main():
     ap.add_argument("--no-mcmc-bench", action="store_true")
     ap.add_argument("--no-autotune", action="store_true",
                     help="use the kernels' default launch shape instead of the autotuner's")
-    ap.add_argument("--section", choices=["dropin", "pair"], default=None,
+    ap.add_argument("--section", choices=["dropin", "pair", "fill"], default=None,
                     help="run one sub-benchmark alone (not the bench line)")
     args = ap.parse_args()
     if args.section == "dropin":
@@ -1256,6 +1321,9 @@ def main():
         return
     if args.section == "pair":
         print(json.dumps(pair_section(args)), flush=True)
+        return
+    if args.section == "fill":
+        print(json.dumps(fill_section(args)), flush=True)
         return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

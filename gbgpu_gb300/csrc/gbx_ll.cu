@@ -136,6 +136,80 @@ __global__ void __launch_bounds__(256) fill_global_kernel(
     }
 }
 
+// Point-major templates (t_stride_b == 1, the reference's i * num_bin + b):
+// one CTA per chunk of 32 binaries.  Slabs of 32 samples x 32 binaries are
+// read one row per warp instruction (512 contiguous bytes), transposed
+// through shared memory, and each warp then adds one binary's 32 consecutive
+// bins with one reduction per lane and component, so the loads and the L2
+// reductions of a warp instruction both cover contiguous addresses.  (One
+// warp per binary on point-major rows reads 16 bytes per lane at a stride of
+// num_bin x 16 bytes: half of every sector, and a long dependent chain.)
+constexpr int kFillRows = 32;
+
+__global__ void __launch_bounds__(256) fill_global_pm_kernel(
+    double2 *__restrict__ A_g, double2 *__restrict__ E_g, const double2 *__restrict__ A_t,
+    const double2 *__restrict__ E_t, const int *__restrict__ start_ind, int M, int num_bin,
+    const int *__restrict__ group_index, int L, long long gstride, long long tsi, int num_groups,
+    int *status)
+{
+    __shared__ double2 tA[kFillRows][33], tE[kFillRows][33];
+    __shared__ long long s_goff[32];
+    __shared__ int s_start[32], s_ok[32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nchunks = (num_bin + 31) >> 5;
+    for (int c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const int b0 = c << 5;
+        if (threadIdx.x < 32) {
+            const int b = b0 + threadIdx.x;
+            int ok = 0, s = 0;
+            long long goff = 0;
+            if (b < num_bin) {
+                s = start_ind[b];
+                const int g = group_index[b];
+                if (num_groups > 0 && (g < 0 || g >= num_groups)) {
+                    flag(status, GBX_FLAG_INDEX);
+                } else {
+                    ok = 1;
+                    goff = (long long)g * gstride;
+                }
+            }
+            s_start[threadIdx.x] = s;
+            s_goff[threadIdx.x] = goff;
+            s_ok[threadIdx.x] = ok;
+        }
+        for (int i0 = 0; i0 < M; i0 += kFillRows) {
+            __syncthreads();
+            const int b = b0 + lane;
+#pragma unroll
+            for (int r = warp; r < kFillRows; r += 8) {
+                const int i = i0 + r;
+                double2 a = make_double2(0.0, 0.0), e = make_double2(0.0, 0.0);
+                if (i < M && b < num_bin) {
+                    a = __ldg(A_t + (size_t)i * tsi + b);
+                    e = __ldg(E_t + (size_t)i * tsi + b);
+                }
+                tA[r][lane] = a;
+                tE[r][lane] = e;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int q = warp; q < 32; q += 8) {
+                const int i = i0 + lane;
+                const int j = s_start[q] + i;
+                // gbgpu_utils.cu:88-91: bins outside the data are skipped
+                if (!s_ok[q] || i >= M || j < 0 || j >= L) continue;
+                const double2 a = tA[lane][q], e = tE[lane][q];
+                const size_t o = (size_t)(s_goff[q] + j);
+                atomicAdd(&A_g[o].x, a.x);
+                atomicAdd(&A_g[o].y, a.y);
+                atomicAdd(&E_g[o].x, e.x);
+                atomicAdd(&E_g[o].y, e.y);
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // Deterministic fill: one CTA per (chunk of kDetChunk output bins, group).
 // Binaries of a group are visited in the order given by `order` (sorted by
 // start index), so every output bin is the same sum in the same order on
@@ -263,10 +337,20 @@ extern "C" int gbx_fill_global_ex(void *A_glob, void *E_glob, const void *A_temp
     if (group_stride < data_length) return set_error(GBX_ERR_ARG, "group_stride < data_length");
     int rc = ensure_init((cudaStream_t)stream);
     if (rc) return rc;
-    fill_global_kernel<<<grid_for(num_bin), 256, 0, (cudaStream_t)stream>>>(
-        (double2 *)A_glob, (double2 *)E_glob, (const double2 *)A_template,
-        (const double2 *)E_template, start_ind, M, num_bin, group_index, data_length,
-        group_stride, t_stride_i, t_stride_b, num_groups, status);
+    if (t_stride_b == 1 && t_stride_i >= num_bin) {
+        // point-major templates: coalesced slabs through shared memory
+        const int chunks = (num_bin + 31) / 32;
+        const int cap = num_sms() * 6;
+        fill_global_pm_kernel<<<chunks < cap ? chunks : cap, 256, 0, (cudaStream_t)stream>>>(
+            (double2 *)A_glob, (double2 *)E_glob, (const double2 *)A_template,
+            (const double2 *)E_template, start_ind, M, num_bin, group_index, data_length,
+            group_stride, t_stride_i, num_groups, status);
+    } else {
+        fill_global_kernel<<<grid_for(num_bin), 256, 0, (cudaStream_t)stream>>>(
+            (double2 *)A_glob, (double2 *)E_glob, (const double2 *)A_template,
+            (const double2 *)E_template, start_ind, M, num_bin, group_index, data_length,
+            group_stride, t_stride_i, t_stride_b, num_groups, status);
+    }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_error(e, "fill_global launch");
     return GBX_OK;

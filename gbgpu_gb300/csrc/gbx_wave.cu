@@ -1400,16 +1400,55 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                 if (Bn.b >= 0) K.dlogl[Bn.b >> 1] = ok ? (rn - ro - 0.5 * (hn + ho) + cx) : 0.0;
             }
         } else if (MODE == MODE_FILL) {
-            for (int m = tid; m < S; m += kBlock) {
-                const int p = m >> lg, i = m & (N - 1);
-                const Bin &B = bins[p];
-                const int j = B.start + i;
-                if (!B.valid || j < 0 || j >= K.L) continue;
-                const int pos = bitrev((i + (N >> 1)) & (N - 1), lg);
-                const V hA = buf[(p * 2 + 0) * N + swz(pos, lg)], hE = buf[(p * 2 + 1) * N + swz(pos, lg)];
-                double2 Ah = cmul(make_double2((double)hA.x, (double)hA.y), B.scale);
-                double2 Eh = cmul(make_double2((double)hE.x, (double)hE.y), B.scale);
-                const size_t o = (size_t)B.gi * K.gstride + j;
+            // Pre-reduction: a run of consecutive tile slots with one group and
+            // ascending starts less than N apart covers one contiguous span of
+            // output bins; every bin of the span is summed over the run's
+            // windows here and added with one atomic per component, instead of
+            // one per window (a tile of binaries sorted by group and frequency
+            // in a dense band needs a fraction of the atomics).  Unsorted
+            // input gives runs of one binary: one atomic per window bin.
+            __shared__ int s_run[kMaxPack + 1], s_lo[kMaxPack], s_off[kMaxPack + 1];
+            __shared__ int s_nruns;
+            if (tid == 0) {
+                int nr = 0, off = 0, hi = 0;
+                for (int p = 0; p < cnt; p++) {
+                    const Bin &B = bins[p];
+                    const bool join = nr > 0 && B.valid && bins[p - 1].valid && B.gi == bins[p - 1].gi &&
+                                      B.start >= bins[p - 1].start && B.start - bins[p - 1].start < N;
+                    if (!join) {
+                        if (nr > 0) off += hi - s_lo[nr - 1];
+                        s_off[nr] = off;
+                        s_run[nr] = p;
+                        s_lo[nr] = B.start;
+                        nr++;
+                    }
+                    // a run's last member ends its span; an invalid binary's run is empty
+                    hi = B.valid ? B.start + N : s_lo[nr - 1];
+                }
+                off += hi - s_lo[nr - 1];
+                s_off[nr] = off;
+                s_run[nr] = cnt;
+                s_nruns = nr;
+            }
+            __syncthreads();
+            const int nr = s_nruns;
+            const int U = s_off[nr];
+            for (int m = tid; m < U; m += kBlock) {
+                int r = 0;
+                while (r + 1 < nr && s_off[r + 1] <= m) r++;
+                const int j = s_lo[r] + (m - s_off[r]);
+                if (j < 0 || j >= K.L) continue;
+                double2 Ah = make_double2(0.0, 0.0), Eh = make_double2(0.0, 0.0);
+                for (int p = s_run[r]; p < s_run[r + 1]; p++) {
+                    const Bin &B = bins[p];
+                    const int i = j - B.start;
+                    if (i < 0 || i >= N) continue;
+                    const int pos = bitrev((i + (N >> 1)) & (N - 1), lg);
+                    const V hA = buf[(p * 2 + 0) * N + swz(pos, lg)], hE = buf[(p * 2 + 1) * N + swz(pos, lg)];
+                    Ah = cadd(Ah, cmul(make_double2((double)hA.x, (double)hA.y), B.scale));
+                    Eh = cadd(Eh, cmul(make_double2((double)hE.x, (double)hE.y), B.scale));
+                }
+                const size_t o = (size_t)bins[s_run[r]].gi * K.gstride + j;
                 atomicAdd(&K.A_glob[o].x, Ah.x);
                 atomicAdd(&K.A_glob[o].y, Ah.y);
                 atomicAdd(&K.E_glob[o].x, Eh.x);

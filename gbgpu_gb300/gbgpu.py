@@ -956,11 +956,16 @@ class GBGPUBase(abc.ABC):
                                  **kwargs):
         """Waveforms straight into templates (gbgpu.py:839-878), fused on the GPU.
 
-        ``params`` is (B, nparams), transposed relative to ``get_ll``.
+        ``params`` is (B, nparams), transposed relative to ``get_ll``.  With
+        ``sort=True`` (atomic mode, one N) the binaries are launched in order
+        of (group, carrier bin), so that a tile holds frequency neighbours of
+        one group and the kernel adds their overlapping windows once (fewer
+        atomics in dense bands; the sum is the same up to FP64 rounding).
         """
         templates = _native(templates)
         precision = kwargs.pop("precision", self.precision)
         fill_mode = kwargs.pop("fill_mode", "atomic")
+        sort = bool(kwargs.pop("sort", False))
         if fill_mode not in ("atomic", "deterministic"):
             raise ValueError("fill_mode must be 'atomic' or 'deterministic'")
         N = kwargs.pop("N", None)
@@ -1003,8 +1008,10 @@ class GBGPUBase(abc.ABC):
         work[:, 0:2].zero_()
         self._status.zero_()
         if B:
-            plan = self._plan(N, T, precision, tdi2, prm.shape[0])
+            plan = self._plan(N, T, precision, tdi2, prm.shape[0], self._fill_tile(N, sort))
             a = plan.args(prm, start_freq_ind, self._status)
+            if sort:
+                self._fill_order(a, prm, gi, T, N)
             rc = nat.lib().gbx_waveform_fill(
                 ctypes.byref(a), ctypes.c_void_p(work[0, 0].data_ptr()),
                 ctypes.c_void_p(work[0, 1].data_ptr()), ctypes.c_void_p(gi.data_ptr()),
@@ -1030,6 +1037,7 @@ class GBGPUBase(abc.ABC):
         T = kwargs.pop("T", 4 * YRSID_SI)
         dt = kwargs.pop("dt", 10.0)
         tdi2 = kwargs.pop("tdi2", False)
+        sort = bool(kwargs.pop("sort", False))
         if kwargs:
             raise TypeError(f"unexpected keyword arguments {list(kwargs)}")
         T = int(T / dt) * dt
@@ -1049,13 +1057,34 @@ class GBGPUBase(abc.ABC):
         B = params.shape[1]
         if B == 0:
             return
-        plan = self._plan(N, T, precision, tdi2, params.shape[0])
+        plan = self._plan(N, T, precision, tdi2, params.shape[0], self._fill_tile(N, sort))
         a = plan.args(params, start_freq_ind, self._status)
+        if sort:
+            self._fill_order(a, params, group_index, T, N)
         rc = nat.lib().gbx_waveform_fill(
             ctypes.byref(a), ctypes.c_void_p(pA), ctypes.c_void_p(pE),
             ctypes.c_void_p(group_index.data_ptr()), int(G), int(L), int(gstride),
             nat.stream_handle())
         nat.check(rc, "gbx_waveform_fill")
+
+    @staticmethod
+    def _fill_tile(N, sort):
+        """Samples per tile of a fill: sorted fills pack up to 16 binaries (at
+        most 4096 samples) so that neighbours share a tile; else the default."""
+        if not sort or np.ndim(N) != 0:
+            return 0
+        return int(min(16 * int(N), 4096))
+
+    @staticmethod
+    def _fill_order(a, prm, gi, T, N):
+        """Launch order by (group, carrier bin rint(f0 T)) for a fill of one N
+        (device sort; the order tensor is kept alive with the arguments)."""
+        if np.ndim(N) != 0:
+            raise NotImplementedError("sorted fills take one N per call")
+        key = gi.to(torch.int64) * (1 << 40) + torch.round(prm[1] * T).to(torch.int64)
+        order = torch.argsort(key).to(torch.int32).contiguous()
+        a.order = order.data_ptr()
+        a._keep = tuple(a._keep) + (order,)
 
     # ------------------------------------------------------------- injection
     def inject_signal(self, *args, fmax=None, T=4.0 * YRSID_SI, dt=10.0, **kwargs):

@@ -61,3 +61,52 @@ def test_deterministic_fill_is_bit_reproducible_and_matches_atomic(precision):
     assert rel_err(out[0], out[2]) < (1e-13 if precision == "fp64" else 1e-6)
     # the windows cover ~500 of the 2000 bins of each group; the rest is 0
     assert 0.2 * out[0].size < np.count_nonzero(out[0]) < 0.3 * out[0].size
+
+
+@pytest.mark.parametrize("precision,N", [("fp64", 256), ("mixed", 256), ("mixed", 64)])
+def test_sorted_fill_prereduces_and_matches(precision, N):
+    """Binaries launched in (group, carrier bin) order: the fused fill adds each
+    tile's overlapping same-group windows once per output bin.  Same templates
+    as the unsorted launch and the deterministic gather (FP64 rounding of the
+    summation order only); a group boundary and windows past both ends of the
+    data inside one tile; windows of invalid (out-of-range group) binaries
+    are dropped and flagged."""
+    from gbgpu_gb300 import GBGPU
+    rng = np.random.default_rng(91 + N)
+    B, G = 3000, 3
+    T, dt = 4 * 31557600.0, 10.0
+    f0 = rng.uniform(1.0e-3, 1.001e-3, B)
+    fdot = 10 ** rng.uniform(-18, -16, B)
+    p = np.array([10 ** rng.uniform(-23, -21, B), f0, fdot, 11 / 3 * fdot ** 2 / f0,
+                  rng.uniform(0, 2 * np.pi, B), np.arccos(rng.uniform(-1, 1, B)),
+                  rng.uniform(0, np.pi, B), rng.uniform(0, 2 * np.pi, B),
+                  np.arcsin(rng.uniform(-1, 1, B))])
+    gi = rng.integers(0, G, B).astype(np.int32)
+    q = np.rint(f0 * T)
+    s0 = int(q.min()) + 20                  # the lowest windows start before bin 0
+    L = int(q.max()) - s0 - 10              # and the highest end past the last bin
+    gb = GBGPU()
+    out = {}
+    for key, mode, sort in (("unsorted", "atomic", False), ("sorted", "atomic", True),
+                            ("det", "deterministic", False)):
+        t = torch.zeros((G, 2, L), dtype=torch.complex128, device="cuda")
+        gb.generate_global_template(p.T, dev(gi), t, N=N, T=T, dt=dt, start_freq_ind=s0,
+                                    precision=precision, fill_mode=mode, sort=sort)
+        out[key] = t.cpu().numpy()
+    scale = np.max(np.abs(out["det"]))
+    assert np.max(np.abs(out["sorted"] - out["unsorted"])) <= 1e-12 * scale
+    if precision == "fp64":
+        assert np.max(np.abs(out["sorted"] - out["det"])) <= 1e-12 * scale
+    # add_to_templates with the same option, on top of the sorted result
+    tA = torch.as_tensor(out["sorted"][:, 0].copy(), device="cuda")
+    tE = torch.as_tensor(out["sorted"][:, 1].copy(), device="cuda")
+    gb.add_to_templates(torch.as_tensor(p, device="cuda"), dev(gi), (tA, tE), N=N, T=T, dt=dt,
+                        start_freq_ind=s0, precision=precision, sort=True)
+    assert np.max(np.abs(tA.cpu().numpy() - 2 * out["sorted"][:, 0])) <= 2e-12 * scale
+    # an out-of-range group drops that binary's window and raises on the status
+    bad = gi.copy()
+    bad[5] = G + 3
+    t = torch.zeros((G, 2, L), dtype=torch.complex128, device="cuda")
+    with pytest.raises(ValueError):
+        gb.generate_global_template(p.T, dev(bad), t, N=N, T=T, dt=dt, start_freq_ind=s0,
+                                    precision=precision, sort=True)
