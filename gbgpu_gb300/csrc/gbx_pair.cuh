@@ -153,6 +153,26 @@ __device__ __forceinline__ void sincos_pair_acc(dfl x, const float4 *__restrict_
     s = p_add(p_add(Ts, p_mul(Ts, em)), p_mul(Tc, sd));
 }
 
+// sin(a)/a alone: the S half of sinc_cos_pair.
+__device__ __forceinline__ dfl sinc_pair(dfl a, const float4 *__restrict__ tab)
+{
+    const dfl x = p_sqr(a);
+    const float xf = x.h;
+    if (xf < 2.56f) {
+        constexpr dfl s2 = dconst(1.0 / 120.0), s1 = dconst(-1.0 / 6.0);
+        float q = fmaf(xf, -1.0f / 1307674368000.0f, 1.0f / 6227020800.0f);
+        q = fmaf(q, xf, -1.0f / 39916800.0f);
+        q = fmaf(q, xf, 1.0f / 362880.0f);
+        q = fmaf(q, xf, -1.0f / 5040.0f);
+        dfl r = p_addf(s2, dfl{xf * q, 0.f});
+        r = p_addf(s1, p_mul(x, r));
+        return p_addf(dfl{1.f, 0.f}, p_mul(x, r));
+    }
+    dfl c, sn;
+    sincos_pair(a, tab, c, sn);
+    return p_div(sn, a);
+}
+
 // sin(a)/a and cos(a) for a pair a >= 0: Taylor series in x = a^2 for
 // x < 2.56 (terms to x^7; truncation below 5e-12 and 9e-11), the leading three
 // coefficients as pairs and the rest as an FP32 tail (at most 4e-10 of the
@@ -269,10 +289,14 @@ __device__ __forceinline__ void slow_pair_unequal(const dfl (&r)[3][3], const df
 // but every quantity a pair.  AE: out[0], out[1] = A, E (formed before the
 // transform); otherwise out[0..2] = X, Y, Z.  Amplitude divided out.
 //
-// The six links are grouped by the spacecraft whose carrier exp(-i phi_s)
-// they carry: with P_q = T_q A_arm(q) (T = sinc(a) e^{-ia} / 4) and
-// F_s = fc (P_q - P_q') for the two links of spacecraft s,
-//   X = fc2 (F_1 E_1 + P_21 E_2 - P_31 E_3), Y and Z cyclic.
+// Each link carries its spacecraft's carrier in one exponential:
+//   G_q = sinc(a_q) exp(-i (a_q + phi_s)) A_arm / 4
+// (one sincos of the summed angle instead of exp(-i a_q) times
+// exp(-i phi_s)), and with X' = G21 - G31, D_1 = G12 - G13 (cyclic) the TDI
+// combination X = fc2 (X' + fc D_1) (gbgpu.py:370-375) gives
+//   A = fc2/sqrt2 [(Z' - X') + fc (D_3 - D_1)],
+//   E = fc2/sqrt6 [(X' - 2Y' + Z') + fc (D_1 - 2 D_2 + D_3)]:
+// four complex products for A and E.
 template <bool AE, bool UNEQ>
 __device__ __forceinline__ void slow_pair(const Bin &B, int n, int N, dfl step, dfl Loc,
                                           const double *__restrict__ tab,
@@ -311,15 +335,18 @@ __device__ __forceinline__ void slow_pair(const Bin &B, int n, int N, dfl step, 
     // fdot = 1e-15 that term is 1e-3 of w0, and omL enters fc2 squared
     const dfl base = p_addf(dfl{B.w0h, B.w0l}, p_mul(dfl{B.w1, B.w1l}, tm));
     cpx E[3];
-    dfl fo[3];
+    dfl fo[3], phs[3];
 #pragma unroll
     for (int s = 0; s < 3; s++) {
         dfl ph = s == 0 ? ph0 : p_add(ph0, p_mul(dk[s], wt));
         const float kPf = kP0.h + dk[s].h;
         ph.l += kPf * kPf * fmaf(kPf, B.p3d.h, -(float)kPi * fdt);   // below 1e-8 rad
-        dfl cs, sn;
-        sincos_pair(ph, sct, cs, sn);
-        E[s] = {cs, df_neg(sn)};
+        phs[s] = ph;
+        if constexpr (UNEQ) {
+            dfl cs, sn;
+            sincos_pair(ph, sct, cs, sn);
+            E[s] = {cs, df_neg(sn)};
+        }
         // f(xi)/fstar at xi = t - kP: - w1 kP + w2 xi^2 are below 3e-6 of w0
         const float xf = tf - kPf;
         fo[s] = p_addf(base, dfl{fmaf(B.w2 * xf, xf, -B.w1 * kPf), 0.f});
@@ -340,17 +367,17 @@ __device__ __forceinline__ void slow_pair(const Bin &B, int n, int N, dfl step, 
         return;
     }
     // links (ij, arm, spacecraft): 12,23,31 (+k.r), 21,32,13 (-k.r)
-    cpx P[6];
+    cpx G[6];
 #pragma unroll
     for (int q = 0; q < 6; q++) {
         const int arm = q < 3 ? q : q - 3;
         const int s = q < 3 ? q : (q - 2) % 3;
         const dfl k = q < 3 ? kr[arm] : df_neg(kr[arm]);
         const dfl a = p_scale(p_mul(fo[s], p_addf(dfl{1.f, 0.f}, k)), 0.5f);
-        dfl S, C;
-        sinc_cos_pair(a, sct, S, C);
-        const cpx T = {p_mul(S, C), df_neg(p_mul(p_mul(a, S), S))};   // sinc(a) e^{-ia}
-        P[q] = cp_mul(T, A[arm]);
+        const dfl S = sinc_pair(a, sct);
+        dfl c, sn;
+        sincos_pair(p_add(a, phs[s]), sct, c, sn);
+        G[q] = cp_mul(cpx{p_mul(S, c), df_neg(p_mul(S, sn))}, A[arm]);
     }
     // omega L, fc = e^{-i omL}, fc2 = 4 omL sin(omL) fc (gbgpu.py:362-368)
     const dfl omL = p_addf(base, dfl{B.w2 * tf * tf, 0.f});
@@ -358,28 +385,22 @@ __device__ __forceinline__ void slow_pair(const Bin &B, int n, int N, dfl step, 
     sincos_pair(omL, sct, co, so);
     const cpx fc = {co, df_neg(so)};
     const dfl g4 = p_scale(p_mul(omL, so), 4.f);
-    const cpx fc2 = {p_mul(g4, co), df_neg(p_mul(g4, so))};
-    // F_s = fc (P12 - P13), fc (P23 - P21), fc (P31 - P32)
-    const cpx F0 = cp_mul(fc, cp_sub(P[0], P[5]));
-    const cpx F1 = cp_mul(fc, cp_sub(P[1], P[3]));
-    const cpx F2 = cp_mul(fc, cp_sub(P[2], P[4]));
+    const cpx D1 = cp_sub(G[0], G[5]), D2 = cp_sub(G[1], G[3]), D3 = cp_sub(G[2], G[4]);
+    const cpx X0 = cp_sub(G[3], G[2]), Y0 = cp_sub(G[4], G[0]), Z0 = cp_sub(G[5], G[1]);
     if constexpr (AE) {
         // A = (Z - X)/sqrt2, E = (X - 2Y + Z)/sqrt6 (utility.py:24-38)
-        const cpx a0 = cp_sub(P[5], F0), a1 = cp_neg(cp_add(P[1], P[3])), a2 = cp_add(F2, P[2]);
-        const cpx b0 = cp_add(cp_add(F0, P[5]), cp_pow2(P[0], 2.f));
-        const cpx b1 = cp_sub(cp_sub(P[3], P[1]), cp_pow2(F1, 2.f));
-        const cpx b2 = cp_sub(F2, cp_add(P[2], cp_pow2(P[4], 2.f)));
-        const cpx sA = cp_add(cp_add(cp_mul(a0, E[0]), cp_mul(a1, E[1])), cp_mul(a2, E[2]));
-        const cpx sE = cp_add(cp_add(cp_mul(b0, E[0]), cp_mul(b1, E[1])), cp_mul(b2, E[2]));
-        out[0] = cp_mul(cp_scale(fc2, dconst(0.70710678118654752440)), sA);
-        out[1] = cp_mul(cp_scale(fc2, dconst(0.40824829046386301637)), sE);
+        const cpx wA = cp_add(cp_sub(Z0, X0), cp_mul(fc, cp_sub(D3, D1)));
+        const cpx wE = cp_add(cp_add(cp_sub(X0, cp_pow2(Y0, 2.f)), Z0),
+                              cp_mul(fc, cp_add(cp_sub(D1, cp_pow2(D2, 2.f)), D3)));
+        const dfl gA = p_mul(g4, dconst(0.70710678118654752440));
+        const dfl gE = p_mul(g4, dconst(0.40824829046386301637));
+        out[0] = cp_mul(cpx{p_mul(gA, co), df_neg(p_mul(gA, so))}, wA);
+        out[1] = cp_mul(cpx{p_mul(gE, co), df_neg(p_mul(gE, so))}, wE);
     } else {
-        const cpx X = cp_add(cp_mul(F0, E[0]), cp_sub(cp_mul(P[3], E[1]), cp_mul(P[2], E[2])));
-        const cpx Y = cp_add(cp_mul(F1, E[1]), cp_sub(cp_mul(P[4], E[2]), cp_mul(P[0], E[0])));
-        const cpx Z = cp_add(cp_mul(F2, E[2]), cp_sub(cp_mul(P[5], E[0]), cp_mul(P[1], E[1])));
-        out[0] = cp_mul(fc2, X);
-        out[1] = cp_mul(fc2, Y);
-        out[2] = cp_mul(fc2, Z);
+        const cpx fc2 = {p_mul(g4, co), df_neg(p_mul(g4, so))};
+        out[0] = cp_mul(fc2, cp_add(X0, cp_mul(fc, D1)));
+        out[1] = cp_mul(fc2, cp_add(Y0, cp_mul(fc, D2)));
+        out[2] = cp_mul(fc2, cp_add(Z0, cp_mul(fc, D3)));
     }
 }
 
