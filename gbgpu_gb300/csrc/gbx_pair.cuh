@@ -461,35 +461,52 @@ __device__ __forceinline__ void fft_dif_pair(cpx *buf, int nsub, int lg)
         hl -= rb;
         __syncthreads();
     }
-    // last five stages inside a warp (lane l holds element 32c + l): the
-    // lower lane of a pair keeps x + y, the upper one (y - x) W
+    // Last five stages (half-spans 16 ... 1) on 32-element blocks, one block
+    // per half-warp, lane l holding two elements: first positions l and
+    // l + 16 (the span-16 butterfly in registers), then before each later
+    // stage of half-span h the lane trades one element with lane l ^ h so
+    // that it holds the pair (e, e + h) of the in-place transform (e = l mod
+    // h plus multiples of 2h), and ends with positions 2l, 2l + 1.  Same
+    // operations and operand order as stage-by-stage butterflies, two
+    // elements per lane: no butterfly is computed twice.
     const int lane = threadIdx.x & 31;
+    const int l = lane & 15;
     cpx w[4];
-    float sg[5];
 #pragma unroll
-    for (int k = 0; k < 5; k++) {
+    for (int k = 0; k < 4; k++) {
         const int hh = 4 - k;
-        const bool up = (lane & (16 >> k)) != 0;
-        sg[k] = up ? -1.f : 1.f;
-        if (k < 4) {
-            const int rp = lane & ((1 << hh) - 1);
-            w[k] = up ? tw_pair(rp * (kTwN >> (hh + 1))) : cpx{{1.f, 0.f}, {0.f, 0.f}};
-        }
+        w[k] = tw_pair((l & ((1 << hh) - 1)) * (kTwN >> (hh + 1)));
     }
-    const int chunks = (nsub << lg) >> 5;
-    for (int c = threadIdx.x >> 5; c < chunks; c += kBlock >> 5) {
-        const int e = (c << 5) + lane;
-        const int idx = ((e >> lg) << lg) + swz(e & ((1 << lg) - 1), lg);
-        cpx x = buf[idx];
-#pragma unroll
-        for (int k = 0; k < 5; k++) {
-            const int o = 16 >> k;
-            const cpx y = {{shfl4(x.x.h, o), shfl4(x.x.l, o)}, {shfl4(x.y.h, o), shfl4(x.y.l, o)}};
-            const cpx sx = {{sg[k] * x.x.h, sg[k] * x.x.l}, {sg[k] * x.y.h, sg[k] * x.y.l}};
-            const cpx d = cp_add(sx, y);
-            x = (k < 4) ? cp_mul(d, w[k < 4 ? k : 0]) : d;
+    const int blocks = (nsub << lg) >> 5;
+    const int npairs = (blocks + 1) >> 1;
+    for (int c = threadIdx.x >> 5; c < npairs; c += kBlock >> 5) {
+        const int blk = 2 * c + (lane >> 4);
+        const bool live = blk < blocks;
+        const int e0 = (live ? blk : blocks - 1) << 5;   // a spare half-warp repeats the last block
+        cpx *sub = buf + ((e0 >> lg) << lg);
+        const int off = e0 & ((1 << lg) - 1);
+        cpx u = sub[swz(off + l, lg)], v = sub[swz(off + l + 16, lg)];
+        {
+            const cpx t = cp_sub(u, v);
+            u = cp_add(u, v);
+            v = cp_mul(t, w[0]);
         }
-        buf[idx] = x;
+#pragma unroll
+        for (int k = 1; k < 5; k++) {
+            const int h = 16 >> k;
+            const bool bit = (l & h) != 0;
+            const cpx snd = bit ? u : v;
+            const cpx rcv = {{shfl4(snd.x.h, h), shfl4(snd.x.l, h)}, {shfl4(snd.y.h, h), shfl4(snd.y.l, h)}};
+            if (bit) u = rcv;
+            else v = rcv;
+            const cpx t = cp_sub(u, v);
+            u = cp_add(u, v);
+            v = k < 4 ? cp_mul(t, w[k < 4 ? k : 0]) : t;
+        }
+        if (live) {
+            sub[swz(off + 2 * l, lg)] = u;
+            sub[swz(off + 2 * l + 1, lg)] = v;
+        }
     }
     __syncthreads();
 }
