@@ -366,18 +366,36 @@ __device__ __forceinline__ void slow_pair(const Bin &B, int n, int N, dfl step, 
         slow_pair_unequal<AE>(r, kr, fo, E, A, p_addf(base, dfl{B.w2 * tf * tf, 0.f}), tdi, sct, out);
         return;
     }
-    // links (ij, arm, spacecraft): 12,23,31 (+k.r), 21,32,13 (-k.r)
+    // links (ij, arm, spacecraft): 12,23,31 (+k.r) and 21,32,13 (-k.r); the two
+    // links of arm a (spacecraft a and a+1) carry angles th+ = a+ + phi_a and
+    // th- = a- + phi_(a+1) that differ by
+    //   d = (fo_(a+1) - fo_a)/2 + k.r (f(t)/f* - (fo_a + fo_(a+1))/2) + (k.P^2 terms),
+    // |d| < 1e-7 rad (fdot k.P/f* and the phase's k.P^2 terms), so
+    // exp(-i th-) A_a = exp(-i th+) A_a (1 - i d) to 1e-14: one pair sincos
+    // and one complex product per arm.  (|d| >= 1e-4 would take the full
+    // sincos; it does not occur for equal arms.)
     cpx G[6];
 #pragma unroll
-    for (int q = 0; q < 6; q++) {
-        const int arm = q < 3 ? q : q - 3;
-        const int s = q < 3 ? q : (q - 2) % 3;
-        const dfl k = q < 3 ? kr[arm] : df_neg(kr[arm]);
-        const dfl a = p_scale(p_mul(fo[s], p_addf(dfl{1.f, 0.f}, k)), 0.5f);
-        const dfl S = sinc_pair(a, sct);
+    for (int a = 0; a < 3; a++) {
+        const int s2 = a == 2 ? 0 : a + 1;
+        const dfl ap = p_scale(p_mul(fo[a], p_addf(dfl{1.f, 0.f}, kr[a])), 0.5f);
+        const dfl am = p_scale(p_mul(fo[s2], p_addf(dfl{1.f, 0.f}, df_neg(kr[a]))), 0.5f);
+        const dfl Sp = sinc_pair(ap, sct), Sm = sinc_pair(am, sct);
+        const dfl thp = p_add(ap, phs[a]), thm = p_add(am, phs[s2]);
         dfl c, sn;
-        sincos_pair(p_add(a, phs[s]), sct, c, sn);
-        G[q] = cp_mul(cpx{p_mul(S, c), df_neg(p_mul(S, sn))}, A[arm]);
+        sincos_pair(thp, sct, c, sn);
+        const cpx eA = cp_mul(cpx{c, df_neg(sn)}, A[a]);
+        G[a] = {p_mul(Sp, eA.x), p_mul(Sp, eA.y)};
+        const dfl dl = p_sub(thm, thp);
+        const float d = dl.h + dl.l;
+        cpx eAm;
+        if (fabsf(d) < 1e-4f) {
+            eAm = {p_add(eA.x, dfl{d * eA.y.h, 0.f}), p_add(eA.y, dfl{-d * eA.x.h, 0.f})};
+        } else {
+            sincos_pair(thm, sct, c, sn);
+            eAm = cp_mul(cpx{c, df_neg(sn)}, A[a]);
+        }
+        G[a + 3] = {p_mul(Sm, eAm.x), p_mul(Sm, eAm.y)};
     }
     // omega L, fc = e^{-i omL}, fc2 = 4 omL sin(omL) fc (gbgpu.py:362-368)
     const dfl omL = p_addf(base, dfl{B.w2 * tf * tf, 0.f});
