@@ -303,17 +303,22 @@ __device__ __forceinline__ void slow_pair(const Bin &B, int n, int N, dfl step, 
                                           const float4 *__restrict__ sct, cpx out[3], int tdi)
 {
     const float *tabf = reinterpret_cast<const float *>(tab + (size_t)18 * N);
+    // arm vectors r_12, r_23, r_31 = (P_j - P_i)/L close (sum to zero to
+    // ~1e-14): with equal arms, arm 3's projections are minus the sum of the
+    // other two; the unequal-arm model reads all three (it needs |r_a|)
+    constexpr int NA = UNEQ ? 3 : 2;
     dfl r[3][3];
 #pragma unroll
-    for (int a = 0; a < 3; a++)
+    for (int a = 0; a < NA; a++)
 #pragma unroll
         for (int c = 0; c < 3; c++)
             r[a][c] = {__ldg(tabf + (size_t)(3 * a + c) * N + n),
                        __ldg(tabf + (size_t)(27 + 3 * a + c) * N + n)};
     dfl kr[3];
 #pragma unroll
-    for (int a = 0; a < 3; a++)
+    for (int a = 0; a < NA; a++)
         kr[a] = p_dot3(B.kd[0], r[a][0], B.kd[1], r[a][1], B.kd[2], r[a][2]);
+    if constexpr (!UNEQ) kr[2] = df_neg(p_add(kr[0], kr[1]));
     const dfl tm = p_mulf(step, (float)n);                 // n T/N
     const float tf = tm.h;
     const dfl tm2 = p_sqr(tm);
@@ -354,10 +359,21 @@ __device__ __forceinline__ void slow_pair(const Bin &B, int n, int N, dfl step, 
     // antenna patterns per arm, with the 1/4 of the transfer functions:
     // r.e+.r = (r.v)^2 - (r.u)^2, r.ex.r = 2 (r.u)(r.v)
     cpx A[3];
+    dfl rus[2], rvs[2];
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        const dfl ru = p_dot3(B.pr.ud[0], r[a][0], B.pr.ud[1], r[a][1], B.pr.ud[2], r[a][2]);
-        const dfl rv = p_dot2(B.pr.vd[0], r[a][0], B.pr.vd[1], r[a][1]);
+        dfl ru, rv;
+        if (a < NA) {
+            ru = p_dot3(B.pr.ud[0], r[a][0], B.pr.ud[1], r[a][1], B.pr.ud[2], r[a][2]);
+            rv = p_dot2(B.pr.vd[0], r[a][0], B.pr.vd[1], r[a][1]);
+        } else {
+            ru = df_neg(p_add(rus[0], rus[1]));
+            rv = df_neg(p_add(rvs[0], rvs[1]));
+        }
+        if (a < 2) {
+            rus[a] = ru;
+            rvs[a] = rv;
+        }
         const dfl pp = p_scale(p_dot2(rv, rv, df_neg(ru), ru), 0.25f);
         const dfl cc = p_scale(p_mul(ru, rv), 0.5f);
         A[a] = {p_dot2(pp, B.pr.DP.x, cc, B.pr.DC.x), p_dot2(pp, B.pr.DP.y, cc, B.pr.DC.y)};
