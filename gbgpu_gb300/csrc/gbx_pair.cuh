@@ -419,18 +419,24 @@ __device__ __forceinline__ void slow_pair(const Bin &B, int n, int N, dfl step, 
     sincos_pair(omL, sct, co, so);
     const cpx fc = {co, df_neg(so)};
     const dfl g4 = p_scale(p_mul(omL, so), 4.f);
-    const cpx D1 = cp_sub(G[0], G[5]), D2 = cp_sub(G[1], G[3]), D3 = cp_sub(G[2], G[4]);
-    const cpx X0 = cp_sub(G[3], G[2]), Y0 = cp_sub(G[4], G[0]), Z0 = cp_sub(G[5], G[1]);
     if constexpr (AE) {
-        // A = (Z - X)/sqrt2, E = (X - 2Y + Z)/sqrt6 (utility.py:24-38)
-        const cpx wA = cp_add(cp_sub(Z0, X0), cp_mul(fc, cp_sub(D3, D1)));
-        const cpx wE = cp_add(cp_add(cp_sub(X0, cp_pow2(Y0, 2.f)), Z0),
-                              cp_mul(fc, cp_add(cp_sub(D1, cp_pow2(D2, 2.f)), D3)));
+        // A = (Z - X)/sqrt2, E = (X - 2Y + Z)/sqrt6 (utility.py:24-38), with
+        //   Z' - X' = (G31 + G13) - (G23 + G21),  D3 - D1 = (G31 + G13) - (G12 + G32),
+        //   X' - 2Y' + Z' = 2 (G12 - G32) + (G21 - G23) + (G13 - G31),
+        //   D1 - 2 D2 + D3 = (G12 - G32) + 2 (G21 - G23) - (G13 - G31)
+        const cpx s25 = cp_add(G[2], G[5]);
+        const cpx ga = cp_sub(G[0], G[4]), gb = cp_sub(G[3], G[1]), gc = cp_sub(G[5], G[2]);
+        const cpx wA = cp_add(cp_sub(s25, cp_add(G[1], G[3])),
+                              cp_mul(fc, cp_sub(s25, cp_add(G[0], G[4]))));
+        const cpx wE = cp_add(cp_add(cp_pow2(ga, 2.f), cp_add(gb, gc)),
+                              cp_mul(fc, cp_sub(cp_add(ga, cp_pow2(gb, 2.f)), gc)));
         const dfl gA = p_mul(g4, dconst(0.70710678118654752440));
         const dfl gE = p_mul(g4, dconst(0.40824829046386301637));
         out[0] = cp_mul(cpx{p_mul(gA, co), df_neg(p_mul(gA, so))}, wA);
         out[1] = cp_mul(cpx{p_mul(gE, co), df_neg(p_mul(gE, so))}, wE);
     } else {
+        const cpx D1 = cp_sub(G[0], G[5]), D2 = cp_sub(G[1], G[3]), D3 = cp_sub(G[2], G[4]);
+        const cpx X0 = cp_sub(G[3], G[2]), Y0 = cp_sub(G[4], G[0]), Z0 = cp_sub(G[5], G[1]);
         const cpx fc2 = {p_mul(g4, co), df_neg(p_mul(g4, so))};
         out[0] = cp_mul(fc2, cp_add(X0, cp_mul(fc, D1)));
         out[1] = cp_mul(fc2, cp_add(Y0, cp_mul(fc, D2)));
