@@ -8,20 +8,16 @@
 
 namespace gbx {
 
-// conj(d) h w and |h|^2 w of one bin of one channel, accumulated into the
-// float pairs dr, di, hh
-__device__ __forceinline__ void ll_bin(double2 d, double2 hv, double S, int eD, int eS, dfl &dr,
-                                       dfl &di, dfl &hh)
+// Re conj(d) h, Im conj(d) h and |h|^2 of one bin of one channel, before the
+// PSD weight (float pairs, unnormalised sums: a tail stays below 2^-23 of the
+// largest product, so a later product keeps ~1e-14 of sum |terms|)
+__device__ __forceinline__ void ll_terms(double2 d, double2 hv, int eD, dfl &re, dfl &im, dfl &sq)
 {
     const dfl dR = d2ff_scaled(d.x, eD), dI = d2ff_scaled(d.y, eD);
     const dfl hR = d2ff_scaled(hv.x, eD), hI = d2ff_scaled(hv.y, eD);
-    const dfl w = df_recip(d2ff_scaled(S, eS));
-    const dfl re = df_sum(df_prod(dR, hR), df_prod(dI, hI));
-    const dfl im = df_sum(df_prod(dR, hI), df_neg(df_prod(dI, hR)));
-    const dfl sq = df_sum(df_prod(hR, hR), df_prod(hI, hI));
-    dr = df_add(dr, df_prod(re, w));         // accumulators stay normalised
-    di = df_add(di, df_prod(im, w));
-    hh = df_add(hh, df_prod(sq, w));
+    re = df_sum(df_prod(dR, hR), df_prod(dI, hI));
+    im = df_sum(df_prod(dR, hI), df_neg(df_prod(dI, hR)));
+    sq = df_sum(df_prod(hR, hR), df_prod(hI, hI));
 }
 
 // sum over the 16 lanes of the same parity (the lanes of one binary)
@@ -79,6 +75,8 @@ __global__ void __launch_bounds__(256) get_ll_kernel(
         dfl dr = {0.f, 0.f}, di = {0.f, 0.f}, hh = {0.f, 0.f};
         bool out = false;
         const int Mh = use ? M : 0;
+        // one PSD array for both channels (the usual call): one weight per bin
+        const bool same = A_p == E_p;
 #pragma unroll 2
         for (int i = q; i < Mh; i += 16) {
             const int j = s + i;
@@ -89,9 +87,22 @@ __global__ void __launch_bounds__(256) get_ll_kernel(
             const double2 hA = __ldg(A_t + i * tsi + b * tsb);
             const double2 hE = __ldg(E_t + i * tsi + b * tsb);
             const double2 dA = __ldg(A_d + doff + j), dE = __ldg(E_d + doff + j);
-            const double SA = __ldg(A_p + noff + j), SE = __ldg(E_p + noff + j);
-            ll_bin(dA, hA, SA, eD, eS, dr, di, hh);
-            ll_bin(dE, hE, SE, eD, eS, dr, di, hh);
+            dfl reA, imA, sqA, reE, imE, sqE;
+            ll_terms(dA, hA, eD, reA, imA, sqA);
+            ll_terms(dE, hE, eD, reE, imE, sqE);
+            // accumulators stay normalised
+            if (same) {
+                const dfl w = df_recip(d2ff_scaled(__ldg(A_p + noff + j), eS));
+                dr = df_add(dr, df_prod(df_sum(reA, reE), w));
+                di = df_add(di, df_prod(df_sum(imA, imE), w));
+                hh = df_add(hh, df_prod(df_sum(sqA, sqE), w));
+            } else {
+                const dfl wA = df_recip(d2ff_scaled(__ldg(A_p + noff + j), eS));
+                const dfl wE = df_recip(d2ff_scaled(__ldg(E_p + noff + j), eS));
+                dr = df_add(dr, df_sum(df_prod(reA, wA), df_prod(reE, wE)));
+                di = df_add(di, df_sum(df_prod(imA, wA), df_prod(imE, wE)));
+                hh = df_add(hh, df_sum(df_prod(sqA, wA), df_prod(sqE, wE)));
+            }
         }
         dr = pair_sum_df(dr);
         di = pair_sum_df(di);

@@ -110,6 +110,16 @@ def test_backend_get_ll_dropin_matches_oracle(gbgpu):
                       dev(ni), L)
     np.testing.assert_allclose(d_h.cpu().numpy(), ref_dh, rtol=1e-12)
     np.testing.assert_allclose(h_h.cpu().numpy().real, ref_hh.real, rtol=1e-12)
+    # one PSD array for both channels (the kernel then forms one weight per bin)
+    ref_dh, ref_hh = O.get_ll_native(A_pm, E_pm, g["A_data"].ravel(), g["E_data"].ravel(),
+                                     g["A_psd"].ravel(), g["A_psd"].ravel(), W["df"], si,
+                                     int(g["N"]), B, di, ni, L)
+    S = dev(g["A_psd"].ravel())
+    gb.backend.get_ll(d_h, h_h, dev(A_pm), dev(E_pm), dev(g["A_data"].ravel()),
+                      dev(g["E_data"].ravel()), S, S, W["df"], dev(si), int(g["N"]), B, dev(di),
+                      dev(ni), L)
+    np.testing.assert_allclose(d_h.cpu().numpy(), ref_dh, rtol=1e-12)
+    np.testing.assert_allclose(h_h.cpu().numpy().real, ref_hh.real, rtol=1e-12)
 
 
 def test_backend_get_ll_edges_odd_batch(gbgpu):
