@@ -675,6 +675,7 @@ __global__ void __launch_bounds__(kBlock, 2) pair_kernel(const KParams K)
             const int p = tid / Tpb;
             const int i0 = tid - p * Tpb;
             dfl sr = {0.f, 0.f}, si = {0.f, 0.f}, xh = {0.f, 0.f};
+            const bool samepsd = K.A_psd == K.E_psd;
             if (p < cnt) {
                 const Bin &B = bins[p];
                 bool out = false;
@@ -689,18 +690,32 @@ __global__ void __launch_bounds__(kBlock, 2) pair_kernel(const KParams K)
                         const cpx tA = buf[(p * 2 + 0) * N + pos], tE = buf[(p * 2 + 1) * N + pos];
                         const size_t jd = (size_t)B.di * K.L + j, jn = (size_t)B.ni * K.L + j;
                         const double2 dA = __ldg(K.A_data + jd), dE = __ldg(K.E_data + jd);
-                        const dfl wA = df_recip(d2ff_scaled(__ldg(K.A_psd + jn), B.eS));
-                        const dfl wE = df_recip(d2ff_scaled(__ldg(K.E_psd + jn), B.eS));
-                        // conj(d) h / S  (gbgpu_utils.cu:172-178), d / S first
-                        const dfl ar = p_mul(d2ff_scaled(dA.x, B.eD), wA);
-                        const dfl ai = p_mul(d2ff_scaled(dA.y, B.eD), wA);
-                        const dfl er = p_mul(d2ff_scaled(dE.x, B.eD), wE);
-                        const dfl ei = p_mul(d2ff_scaled(dE.y, B.eD), wE);
-                        sr = p_add(sr, p_add(p_dot2(ar, tA.x, ai, tA.y), p_dot2(er, tE.x, ei, tE.y)));
-                        si = p_add(si, p_add(p_dot2(ar, tA.y, df_neg(ai), tA.x),
-                                               p_dot2(er, tE.y, df_neg(ei), tE.x)));
-                        xh = p_add(xh, p_dot2(p_dot2(tA.x, tA.x, tA.y, tA.y), wA,
-                                               p_dot2(tE.x, tE.x, tE.y, tE.y), wE));
+                        if (samepsd) {
+                            // one PSD for both channels: the channels' terms summed, then
+                            // one weight (gbgpu_utils.cu:172-178)
+                            const dfl w = df_recip(d2ff_scaled(__ldg(K.A_psd + jn), B.eS));
+                            const dfl ar = d2ff_scaled(dA.x, B.eD), ai = d2ff_scaled(dA.y, B.eD);
+                            const dfl er = d2ff_scaled(dE.x, B.eD), ei = d2ff_scaled(dE.y, B.eD);
+                            sr = p_add(sr, p_mul(p_add(p_dot2(ar, tA.x, ai, tA.y),
+                                                       p_dot2(er, tE.x, ei, tE.y)), w));
+                            si = p_add(si, p_mul(p_add(p_dot2(ar, tA.y, df_neg(ai), tA.x),
+                                                       p_dot2(er, tE.y, df_neg(ei), tE.x)), w));
+                            xh = p_add(xh, p_mul(p_add(p_dot2(tA.x, tA.x, tA.y, tA.y),
+                                                       p_dot2(tE.x, tE.x, tE.y, tE.y)), w));
+                        } else {
+                            const dfl wA = df_recip(d2ff_scaled(__ldg(K.A_psd + jn), B.eS));
+                            const dfl wE = df_recip(d2ff_scaled(__ldg(K.E_psd + jn), B.eS));
+                            // conj(d) h / S  (gbgpu_utils.cu:172-178), d / S first
+                            const dfl ar = p_mul(d2ff_scaled(dA.x, B.eD), wA);
+                            const dfl ai = p_mul(d2ff_scaled(dA.y, B.eD), wA);
+                            const dfl er = p_mul(d2ff_scaled(dE.x, B.eD), wE);
+                            const dfl ei = p_mul(d2ff_scaled(dE.y, B.eD), wE);
+                            sr = p_add(sr, p_add(p_dot2(ar, tA.x, ai, tA.y), p_dot2(er, tE.x, ei, tE.y)));
+                            si = p_add(si, p_add(p_dot2(ar, tA.y, df_neg(ai), tA.x),
+                                                   p_dot2(er, tE.y, df_neg(ei), tE.x)));
+                            xh = p_add(xh, p_dot2(p_dot2(tA.x, tA.x, tA.y, tA.y), wA,
+                                                   p_dot2(tE.x, tE.x, tE.y, tE.y), wE));
+                        }
                     }
                 }
                 if (out) flag(a.status, GBX_FLAG_WINDOW);

@@ -89,6 +89,27 @@ def test_get_ll_matches_reference(gbgpu, case, precision):
     np.testing.assert_array_equal(gb.start_inds.cpu().numpy(), g["start_inds"])
 
 
+@pytest.mark.parametrize("precision", ["fp64", "pair", "mixed"])
+def test_get_ll_one_psd_array_for_both_channels(gbgpu, precision):
+    """The same PSD tensor for A and E (the kernels then form one weight per
+    bin): the oracle's likelihood with that PSD in both channels."""
+    g = load_golden("ll_multi")
+    S = dev(g["A_psd"])
+    kw = dict(N=int(g["N"]), T=float(g["T"]), dt=float(g["dt"]), tdi2=bool(g["tdi2"]),
+              start_freq_ind=int(g["start_freq_ind"]))
+    _, d_h, h_h, _ = O.get_ll(g["params"], [g["A_data"], g["E_data"]], [g["A_psd"], g["A_psd"]],
+                              data_index=g["data_index"], noise_index=g["noise_index"],
+                              return_terms=True, **kw)
+    gb = gbgpu()
+    gb.d_d = 0.0
+    gb.get_ll(g["params"], [dev(g["A_data"]), dev(g["E_data"])], [S, S], precision=precision,
+              data_index=dev(g["data_index"], torch.int32),
+              noise_index=dev(g["noise_index"], torch.int32), **kw)
+    tol = {"fp64": FP64_TOL, "pair": 1e-9, "mixed": 1e-5}[precision]
+    np.testing.assert_allclose(gb.d_h.cpu().numpy(), d_h, rtol=tol, atol=tol * np.abs(d_h).max())
+    np.testing.assert_allclose(gb.h_h.real.cpu().numpy(), h_h.real, rtol=tol, atol=0)
+
+
 def test_backend_get_ll_dropin_matches_oracle(gbgpu):
     """backend.get_ll with the reference's 15-argument list (gbgpu_utils_wrap.pyx:20-48)."""
     g = load_golden("ll_multi")
