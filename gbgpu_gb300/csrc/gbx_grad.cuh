@@ -622,9 +622,12 @@ __global__ void __launch_bounds__(kBlock, 2) grad_kernel(const GradParams GP)
                 if (valid && j >= 0 && j < K.L) {
                     const size_t jd = (size_t)B.di * K.L + j, jn = (size_t)B.ni * K.L + j;
                     const double2 dA = __ldg(K.A_data + jd), dE = __ldg(K.E_data + jd);
-                    const double SA = __ldg(K.A_psd + jn), SE = __ldg(K.E_psd + jn);
+                    // one PSD array for both channels: one weight, and the
+                    // likelihood terms summed as the fused likelihood sums them
+                    const bool samepsd = K.A_psd == K.E_psd;
+                    const double SA = __ldg(K.A_psd + jn);
                     const float wA = __frcp_rn(d2f_scaled(SA, B.eS));
-                    const float wE = __frcp_rn(d2f_scaled(SE, B.eS));
+                    const float wE = samepsd ? wA : __frcp_rn(d2f_scaled(__ldg(K.E_psd + jn), B.eS));
                     float aR = d2f_scaled(dA.x, B.eD), aI = d2f_scaled(dA.y, B.eD);
                     float eR = d2f_scaled(dE.x, B.eD), eI = d2f_scaled(dE.y, B.eD);
                     if (SWAP) {
@@ -638,9 +641,15 @@ __global__ void __launch_bounds__(kBlock, 2) grad_kernel(const GradParams GP)
                             eR += oE.x; eI += oE.y;
                         }
                     }
-                    acc[0] += fmaf(aR, hA.x, aI * hA.y) * wA + fmaf(eR, hE.x, eI * hE.y) * wE;
-                    acc[1] += fmaf(aR, hA.y, -aI * hA.x) * wA + fmaf(eR, hE.y, -eI * hE.x) * wE;
-                    acc[2] += fmaf(hA.x, hA.x, hA.y * hA.y) * wA + fmaf(hE.x, hE.x, hE.y * hE.y) * wE;
+                    if (samepsd) {
+                        acc[0] = fmaf(fmaf(aR, hA.x, aI * hA.y) + fmaf(eR, hE.x, eI * hE.y), wA, acc[0]);
+                        acc[1] = fmaf(fmaf(aR, hA.y, -aI * hA.x) + fmaf(eR, hE.y, -eI * hE.x), wA, acc[1]);
+                        acc[2] = fmaf(fmaf(hA.x, hA.x, hA.y * hA.y) + fmaf(hE.x, hE.x, hE.y * hE.y), wA, acc[2]);
+                    } else {
+                        acc[0] += fmaf(aR, hA.x, aI * hA.y) * wA + fmaf(eR, hE.x, eI * hE.y) * wE;
+                        acc[1] += fmaf(aR, hA.y, -aI * hA.x) * wA + fmaf(eR, hE.y, -eI * hE.x) * wE;
+                        acc[2] += fmaf(hA.x, hA.x, hA.y * hA.y) * wA + fmaf(hE.x, hE.x, hE.y * hE.y) * wE;
+                    }
                     // r' = d' - sc h ; u = r' / S'
                     const float2 shA = cmul(sc, hA), shE = cmul(sc, hE);
                     uA = make_float2((aR - shA.x) * wA, (aI - shA.y) * wA);

@@ -1467,6 +1467,9 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
             const int i0 = tid - p * Tpb;
             typedef typename std::conditional<sizeof(R) == 8, double, float>::type Acc;
             Acc sr = 0, si = 0, sh = 0;
+            // one PSD array for both channels (the usual call): the channels'
+            // terms are summed, then weighted once
+            const bool samepsd = K.A_psd == K.E_psd;
             if (p < cnt) {
                 const Bin &B = bins[p];
                 bool out = false;
@@ -1481,6 +1484,25 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                         const V tA = buf[(p * 2 + 0) * N + swz(pos, lg)], tE = buf[(p * 2 + 1) * N + swz(pos, lg)];
                         const size_t jd = (size_t)B.di * K.L + j, jn = (size_t)B.ni * K.L + j;
                         const double2 dA = __ldg(K.A_data + jd), dE = __ldg(K.E_data + jd);
+                        if (samepsd) {
+                            const double S = __ldg(K.A_psd + jn);
+                            if constexpr (sizeof(R) == 8) {
+                                const double2 hA = cmul(make_double2(tA.x, tA.y), B.scale);
+                                const double2 hE = cmul(make_double2(tE.x, tE.y), B.scale);
+                                const double w = 1.0 / S;
+                                sr += ((dA.x * hA.x + dA.y * hA.y) + (dE.x * hE.x + dE.y * hE.y)) * w;
+                                si += ((dA.x * hA.y - dA.y * hA.x) + (dE.x * hE.y - dE.y * hE.x)) * w;
+                                sh += ((hA.x * hA.x + hA.y * hA.y) + (hE.x * hE.x + hE.y * hE.y)) * w;
+                            } else {
+                                const float w = __frcp_rn(d2f_scaled(S, B.eS));
+                                const float aR = d2f_scaled(dA.x, B.eD), aI = d2f_scaled(dA.y, B.eD);
+                                const float eR = d2f_scaled(dE.x, B.eD), eI = d2f_scaled(dE.y, B.eD);
+                                sr = fmaf(fmaf(aR, tA.x, aI * tA.y) + fmaf(eR, tE.x, eI * tE.y), w, sr);
+                                si = fmaf(fmaf(aR, tA.y, -aI * tA.x) + fmaf(eR, tE.y, -eI * tE.x), w, si);
+                                sh = fmaf(fmaf(tA.x, tA.x, tA.y * tA.y) + fmaf(tE.x, tE.x, tE.y * tE.y), w, sh);
+                            }
+                            continue;
+                        }
                         const double SA = __ldg(K.A_psd + jn), SE = __ldg(K.E_psd + jn);
                         if constexpr (sizeof(R) == 8) {
                             double2 hA = cmul(make_double2(tA.x, tA.y), B.scale);
