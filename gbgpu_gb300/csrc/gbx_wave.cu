@@ -1409,6 +1409,11 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
             // input gives runs of one binary: one atomic per window bin.
             __shared__ int s_run[kMaxPack + 1], s_lo[kMaxPack], s_off[kMaxPack + 1];
             __shared__ int s_nruns;
+            // mixed form: the scale in FP32 (the values carry FP32 accuracy),
+            // the product widened to FP64 on the integer pipe, as MODE_WAVE
+            __shared__ float2 s_scf[kMaxPack];
+            if (sizeof(R) == 4 && tid < cnt)
+                s_scf[tid] = make_float2(d2f_scaled(bins[tid].scale.x, 0), d2f_scaled(bins[tid].scale.y, 0));
             if (tid == 0) {
                 int nr = 0, off = 0, hi = 0;
                 for (int p = 0; p < cnt; p++) {
@@ -1439,14 +1444,30 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
                 const int j = s_lo[r] + (m - s_off[r]);
                 if (j < 0 || j >= K.L) continue;
                 double2 Ah = make_double2(0.0, 0.0), Eh = make_double2(0.0, 0.0);
+                bool any = false;
                 for (int p = s_run[r]; p < s_run[r + 1]; p++) {
                     const Bin &B = bins[p];
                     const int i = j - B.start;
                     if (i < 0 || i >= N) continue;
                     const int pos = bitrev((i + (N >> 1)) & (N - 1), lg);
                     const V hA = buf[(p * 2 + 0) * N + swz(pos, lg)], hE = buf[(p * 2 + 1) * N + swz(pos, lg)];
-                    Ah = cadd(Ah, cmul(make_double2((double)hA.x, (double)hA.y), B.scale));
-                    Eh = cadd(Eh, cmul(make_double2((double)hE.x, (double)hE.y), B.scale));
+                    double2 a2, e2;
+                    if constexpr (sizeof(R) == 4) {
+                        a2 = f2d(cmul(hA, s_scf[p]));
+                        e2 = f2d(cmul(hE, s_scf[p]));
+                    } else {
+                        a2 = cmul(make_double2(hA.x, hA.y), B.scale);
+                        e2 = cmul(make_double2(hE.x, hE.y), B.scale);
+                    }
+                    // the first window adds nothing in FP64; later ones add in FP64
+                    if (any) {
+                        Ah = cadd(Ah, a2);
+                        Eh = cadd(Eh, e2);
+                    } else {
+                        Ah = a2;
+                        Eh = e2;
+                        any = true;
+                    }
                 }
                 const size_t o = (size_t)bins[s_run[r]].gi * K.gstride + j;
                 atomicAdd(&K.A_glob[o].x, Ah.x);
