@@ -712,6 +712,9 @@ def dropin_kernels(gb, p, data, Sd, steps):
 
     ms_ll = timeit(lambda: be.get_ll(d_h, h_h, A_pm, E_pm, data[0], data[1], Sd, Sd, 1.0 / Tu,
                                      start, N, B, zeros, zeros, L), "dropin_get_ll")
+    ms_ll64 = timeit(lambda: be.get_ll(d_h, h_h, A_pm, E_pm, data[0], data[1], Sd, Sd, 1.0 / Tu,
+                                       start, N, B, zeros, zeros, L, fp64=True),
+                     "dropin_get_ll_fp64")
     G = 256
     Lf = int(start.max().item()) + N + 1
     glob = torch.zeros((2, G * Lf), dtype=torch.complex128, device="cuda")
@@ -725,6 +728,7 @@ def dropin_kernels(gb, p, data, Sd, steps):
     return {"workload": f"{B} binaries, N={N}, point-major FP64 templates",
             "get_ll_ms": ms_ll, "get_ll_GBps": ll_bytes / (ms_ll / 1e3) / 1e9,
             "get_ll_frac": ll_bytes / (ms_ll / 1e3) / 1e9 / peak,
+            "get_ll_fp64_ms": ms_ll64,
             "fill_global_ms": ms_fill, "fill_global_GBps": fill_bytes / (ms_fill / 1e3) / 1e9,
             "fill_global_frac": fill_bytes / (ms_fill / 1e3) / 1e9 / peak,
             "peak_GBps": peak, "note": f"peak {src}; algorithmic bytes (80 N + 44 and 96 N per "

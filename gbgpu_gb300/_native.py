@@ -24,7 +24,7 @@ GBX_FLAG_TILE = 4
 
 EXPORTS = (
     "gbx_version", "gbx_last_error", "gbx_device_info", "gbx_init",
-    "gbx_get_ll", "gbx_get_ll_ex", "gbx_fill_global", "gbx_fill_global_ex",
+    "gbx_get_ll", "gbx_get_ll_ex", "gbx_get_ll_fp64", "gbx_fill_global", "gbx_fill_global_ex",
     "gbx_orbit_table_bytes", "gbx_orbit_table",
     "gbx_waveform", "gbx_waveform_ll", "gbx_waveform_fill", "gbx_wave_workspace_bytes",
     "gbx_waveform_ll_noalloc", "gbx_waveform_ll_grad", "gbx_grad_workspace_bytes",
@@ -77,6 +77,7 @@ def lib():
     L.gbx_get_ll.argtypes = [_vp] * 8 + [_d, _vp, _i, _i, _vp, _vp, _i, _vp, _vp]
     L.gbx_get_ll_ex.argtypes = [_vp] * 8 + [_d, _vp, _i, _i, _vp, _vp, _i, _ll, _ll, _i, _i,
                                             _vp, _vp]
+    L.gbx_get_ll_fp64.argtypes = L.gbx_get_ll_ex.argtypes
     L.gbx_fill_global.argtypes = [_vp] * 5 + [_i, _i, _vp, _i, _vp, _vp]
     L.gbx_fill_global_ex.argtypes = [_vp] * 5 + [_i, _i, _vp, _i, _i, _ll, _ll, _ll, _vp, _vp]
     L.gbx_fill_global_det.argtypes = [_vp] * 5 + [_i, _i, _vp, _vp, _i, _i, _ll, _ll, _ll, _vp]

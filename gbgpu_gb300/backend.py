@@ -54,16 +54,20 @@ class GB300Backend:
         nat.check(self._lib.gbx_init(), "gbx_init")
 
     def get_ll(self, d_h, h_h, A_template, E_template, A_data, E_data, A_psd, E_psd, df,
-               start_ind, M, num_bin, data_index, noise_index, data_length, status=None):
+               start_ind, M, num_bin, data_index, noise_index, data_length, status=None,
+               fp64=False):
         """gbx_get_ll with the reference's method-table arguments (gbgpu_utils_wrap.pyx:20-48).
 
         When the data and PSD arrive as arrays (not raw addresses) their row
         counts are passed on, so out-of-range data_index / noise_index rows are
-        flagged in ``status`` and skipped instead of being read."""
+        flagged in ``status`` and skipped instead of being read.  ``fp64=True``
+        sums in FP64 as the reference does (gbx_get_ll_fp64) instead of in
+        float pairs (within 1e-12 of sum |terms|)."""
         rows = lambda x: (_numel(x) // int(data_length)) if data_length else 0
         nd = min(rows(A_data), rows(E_data))
         npsd = min(rows(A_psd), rows(E_psd))
-        rc = self._lib.gbx_get_ll_ex(
+        fn = self._lib.gbx_get_ll_fp64 if fp64 else self._lib.gbx_get_ll_ex
+        rc = fn(
             _addr(d_h), _addr(h_h), _addr(A_template), _addr(E_template), _addr(A_data),
             _addr(E_data), _addr(A_psd), _addr(E_psd), float(df), _addr(start_ind), int(M),
             int(num_bin), _addr(data_index), _addr(noise_index), int(data_length),

@@ -42,6 +42,9 @@ __device__ __forceinline__ dfl pair_sum_df(dfl v)
 // sum |terms| of the FP64 result); one FP64 conversion per output.  A
 // negative row, or one at or above num_data / num_psd when those are
 // positive, is flagged (GBX_FLAG_INDEX), never read, and gives zero outputs.
+// FP64: the same mapping with the reference's arithmetic, FP64 products and
+// sums (gbgpu_utils.cu:167-179, the division by S as a product with 1/S).
+template <bool FP64>
 __global__ void __launch_bounds__(256) get_ll_kernel(
     double2 *__restrict__ d_h, double2 *__restrict__ h_h, const double2 *__restrict__ A_t,
     const double2 *__restrict__ E_t, const double2 *__restrict__ A_d,
@@ -73,12 +76,30 @@ __global__ void __launch_bounds__(256) get_ll_kernel(
         const int lgS = (hS > 0 && exS > 0 && exS < 0x7ff) ? exS - 1023 : 0;
         const int eS = -lgS, eD = -(lgS >> 1) - 14;
         dfl dr = {0.f, 0.f}, di = {0.f, 0.f}, hh = {0.f, 0.f};
+        double xr = 0.0, xi = 0.0, xh = 0.0;
         bool out = false;
         const int Mh = use ? M : 0;
         // one PSD array for both channels (the usual call): one weight per bin
         const bool same = A_p == E_p;
+        if constexpr (FP64) {
+            for (int i = q; i < Mh; i += 16) {
+                const int j = s + i;
+                if (j < 0 || j >= L) {
+                    out = true;
+                    continue;
+                }
+                const double2 hA = __ldg(A_t + i * tsi + b * tsb);
+                const double2 hE = __ldg(E_t + i * tsi + b * tsb);
+                const double2 dA = __ldg(A_d + doff + j), dE = __ldg(E_d + doff + j);
+                const double wA = 1.0 / __ldg(A_p + noff + j);
+                const double wE = same ? wA : 1.0 / __ldg(E_p + noff + j);
+                xr += (dA.x * hA.x + dA.y * hA.y) * wA + (dE.x * hE.x + dE.y * hE.y) * wE;
+                xi += (dA.x * hA.y - dA.y * hA.x) * wA + (dE.x * hE.y - dE.y * hE.x) * wE;
+                xh += (hA.x * hA.x + hA.y * hA.y) * wA + (hE.x * hE.x + hE.y * hE.y) * wE;
+            }
+        }
 #pragma unroll 2
-        for (int i = q; i < Mh; i += 16) {
+        for (int i = q; i < (FP64 ? 0 : Mh); i += 16) {
             const int j = s + i;
             if (j < 0 || j >= L) {
                 out = true;
@@ -104,16 +125,30 @@ __global__ void __launch_bounds__(256) get_ll_kernel(
                 hh = df_add(hh, df_sum(df_prod(sqA, wA), df_prod(sqE, wE)));
             }
         }
-        dr = pair_sum_df(dr);
-        di = pair_sum_df(di);
-        hh = pair_sum_df(hh);
+        if constexpr (FP64) {
+#pragma unroll
+            for (int o = 16; o > 1; o >>= 1) {
+                xr += __shfl_xor_sync(0xffffffffu, xr, o);
+                xi += __shfl_xor_sync(0xffffffffu, xi, o);
+                xh += __shfl_xor_sync(0xffffffffu, xh, o);
+            }
+        } else {
+            dr = pair_sum_df(dr);
+            di = pair_sum_df(di);
+            hh = pair_sum_df(hh);
+        }
         if (__any_sync(0xffffffffu, out) && lane == 0) flag(status, GBX_FLAG_WINDOW);
         if (q == 0 && has) {
-            // undo the scalings: terms carry 2^(2 eD - eS)
-            const double s4 = 4. * df * __hiloint2double((eS - 2 * eD + 1023) << 20, 0);
-            d_h[b] = make_double2(s4 * ((double)dr.h + (double)dr.l),
-                                  s4 * ((double)di.h + (double)di.l));
-            h_h[b] = make_double2(s4 * ((double)hh.h + (double)hh.l), 0.0);
+            if constexpr (FP64) {
+                d_h[b] = make_double2(4. * df * xr, 4. * df * xi);
+                h_h[b] = make_double2(4. * df * xh, 0.0);
+            } else {
+                // undo the scalings: terms carry 2^(2 eD - eS)
+                const double s4 = 4. * df * __hiloint2double((eS - 2 * eD + 1023) << 20, 0);
+                d_h[b] = make_double2(s4 * ((double)dr.h + (double)dr.l),
+                                      s4 * ((double)di.h + (double)di.l));
+                h_h[b] = make_double2(s4 * ((double)hh.h + (double)hh.l), 0.0);
+            }
         }
     }
 }
@@ -300,13 +335,13 @@ static int grid_for(int num_bin)
 
 using namespace gbx;
 
-extern "C" int gbx_get_ll_ex(void *d_h, void *h_h, const void *A_template,
-                             const void *E_template, const void *A_data, const void *E_data,
-                             const double *A_psd, const double *E_psd, double df,
-                             const int *start_ind, int M, int num_bin, const int *data_index,
-                             const int *noise_index, int data_length, long long t_stride_i,
-                             long long t_stride_b, int num_data, int num_psd, int *status,
-                             void *stream)
+template <bool FP64>
+static int get_ll_launch(void *d_h, void *h_h, const void *A_template, const void *E_template,
+                         const void *A_data, const void *E_data, const double *A_psd,
+                         const double *E_psd, double df, const int *start_ind, int M, int num_bin,
+                         const int *data_index, const int *noise_index, int data_length,
+                         long long t_stride_i, long long t_stride_b, int num_data, int num_psd,
+                         int *status, void *stream)
 {
     if (num_bin < 0 || M < 0 || data_length < 0) return set_error(GBX_ERR_ARG, "negative size");
     if (num_bin == 0) return GBX_OK;
@@ -315,13 +350,39 @@ extern "C" int gbx_get_ll_ex(void *d_h, void *h_h, const void *A_template,
         return set_error(GBX_ERR_ARG, "NULL pointer");
     int rc = ensure_init((cudaStream_t)stream);
     if (rc) return rc;
-    get_ll_kernel<<<grid_for((num_bin + 1) / 2), 256, 0, (cudaStream_t)stream>>>(
+    get_ll_kernel<FP64><<<grid_for((num_bin + 1) / 2), 256, 0, (cudaStream_t)stream>>>(
         (double2 *)d_h, (double2 *)h_h, (const double2 *)A_template, (const double2 *)E_template,
         (const double2 *)A_data, (const double2 *)E_data, A_psd, E_psd, df, start_ind, M, num_bin,
         data_index, noise_index, data_length, t_stride_i, t_stride_b, num_data, num_psd, status);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_error(e, "get_ll launch");
     return GBX_OK;
+}
+
+extern "C" int gbx_get_ll_ex(void *d_h, void *h_h, const void *A_template,
+                             const void *E_template, const void *A_data, const void *E_data,
+                             const double *A_psd, const double *E_psd, double df,
+                             const int *start_ind, int M, int num_bin, const int *data_index,
+                             const int *noise_index, int data_length, long long t_stride_i,
+                             long long t_stride_b, int num_data, int num_psd, int *status,
+                             void *stream)
+{
+    return get_ll_launch<false>(d_h, h_h, A_template, E_template, A_data, E_data, A_psd, E_psd,
+                                df, start_ind, M, num_bin, data_index, noise_index, data_length,
+                                t_stride_i, t_stride_b, num_data, num_psd, status, stream);
+}
+
+extern "C" int gbx_get_ll_fp64(void *d_h, void *h_h, const void *A_template,
+                               const void *E_template, const void *A_data, const void *E_data,
+                               const double *A_psd, const double *E_psd, double df,
+                               const int *start_ind, int M, int num_bin, const int *data_index,
+                               const int *noise_index, int data_length, long long t_stride_i,
+                               long long t_stride_b, int num_data, int num_psd, int *status,
+                               void *stream)
+{
+    return get_ll_launch<true>(d_h, h_h, A_template, E_template, A_data, E_data, A_psd, E_psd,
+                               df, start_ind, M, num_bin, data_index, noise_index, data_length,
+                               t_stride_i, t_stride_b, num_data, num_psd, status, stream);
 }
 
 extern "C" int gbx_get_ll(void *d_h, void *h_h, const void *A_template, const void *E_template,

@@ -141,6 +141,12 @@ def test_backend_get_ll_dropin_matches_oracle(gbgpu):
                       dev(ni), L)
     np.testing.assert_allclose(d_h.cpu().numpy(), ref_dh, rtol=1e-12)
     np.testing.assert_allclose(h_h.cpu().numpy().real, ref_hh.real, rtol=1e-12)
+    # the FP64 variant: the reference's arithmetic, to FP64 rounding
+    gb.backend.get_ll(d_h, h_h, dev(A_pm), dev(E_pm), dev(g["A_data"].ravel()),
+                      dev(g["E_data"].ravel()), S, S, W["df"], dev(si), int(g["N"]), B, dev(di),
+                      dev(ni), L, fp64=True)
+    np.testing.assert_allclose(d_h.cpu().numpy(), ref_dh, rtol=1e-14, atol=1e-14 * np.abs(ref_dh).max())
+    np.testing.assert_allclose(h_h.cpu().numpy().real, ref_hh.real, rtol=1e-14)
 
 
 def test_backend_get_ll_edges_odd_batch(gbgpu):
@@ -189,6 +195,16 @@ def test_backend_get_ll_edges_odd_batch(gbgpu):
     assert np.all(np.abs(got_dh - ref_dh) <= 1e-12 * bound_dh + 1e-300)
     assert np.all(np.abs(got_hh.real - ref_hh) <= 1e-12 * bound_hh + 1e-300)
     assert got_dh[2] == 0 and got_hh[2] == 0
+    assert int(st.item()) & nat.GBX_FLAG_WINDOW
+    # the FP64 variant under the same edges: FP64 rounding of the same sums
+    st.zero_()
+    gb.backend.get_ll(d_h, h_h, dev(O.point_major(A_t)), dev(O.point_major(E_t)),
+                      dev(A_d.ravel()), dev(E_d.ravel()), dev(A_p.ravel()), dev(E_p.ravel()),
+                      df, dev(s), M, B, dev(di), dev(ni), L, status=st, fp64=True)
+    f_dh, f_hh = d_h.cpu().numpy(), h_h.cpu().numpy()
+    assert np.all(np.abs(f_dh - ref_dh) <= 1e-14 * bound_dh + 1e-300)
+    assert np.all(np.abs(f_hh.real - ref_hh) <= 1e-14 * bound_hh + 1e-300)
+    assert f_dh[2] == 0 and f_hh[2] == 0
     assert int(st.item()) & nat.GBX_FLAG_WINDOW
     # windows inside the data raise no flag
     st.zero_()
