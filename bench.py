@@ -864,7 +864,7 @@ def fill_bench(gb, seed, B=1_000_000, G=256, N=256, steps=3):
     """Global templates of 1e6 binaries: f0 density f^(-11/3) on [1e-4, 1e-2] Hz,
     amp ~ f0^(2/3) with log-normal scatter (sigma 0.3), N = 256, group index
     uniform over 256 walkers, templates (256, 2, 12,623,041) complex128
-    (103.4 GB).  Times the fused FP64 atomic fill and the deterministic fill
+    (103.4 GB).  Times the fused atomic fill and the deterministic fill
     (waveforms, sort by (group, start), ordered gather); the zeroing of the
     templates that the atomic mode needs is timed separately."""
     import torch
@@ -903,7 +903,7 @@ def fill_bench(gb, seed, B=1_000_000, G=256, N=256, steps=3):
         return ev[0].elapsed_time(ev[1]) / steps
 
     ms_zero = timeit(lambda: tmpl.zero_(), "fill_zero")
-    for prec in ("fp64", "mixed"):
+    for prec in ("fp64", "pair", "mixed"):
         for mode in ("atomic", "deterministic"):
             ms = timeit(lambda: gb.generate_global_template(pT, gi, tmpl, N=N, T=T_OBS, dt=DT,
                                                             precision=prec, fill_mode=mode),
@@ -911,9 +911,9 @@ def fill_bench(gb, seed, B=1_000_000, G=256, N=256, steps=3):
             out[f"{prec}_{mode}_ms"] = ms
             out[f"{prec}_{mode}_binaries_per_s"] = B / (ms / 1e3)
     out["zeroing_ms"] = ms_zero
-    out["note"] = ("templates accumulate in FP64 in every variant; fp64/mixed is the waveform "
-                   "precision.  atomic includes zeroing channels 0/1 (the reference's overwrite "
-                   "semantics); deterministic writes every bin itself")
+    out["note"] = ("templates accumulate in FP64 in every variant; fp64/pair/mixed is the "
+                   "waveform precision.  atomic includes zeroing channels 0/1 (the reference's "
+                   "overwrite semantics); deterministic writes every bin itself")
     del tmpl
     torch.cuda.empty_cache()
     return out

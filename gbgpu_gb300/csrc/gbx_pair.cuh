@@ -666,6 +666,46 @@ __global__ void __launch_bounds__(kBlock, 2) pair_kernel(const KParams K)
                 }
                 if (i == 0 && K.start_out) K.start_out[B.b] = B.start;
             }
+        } else if constexpr (MODE == MODE_FILL) {
+            // as wave_kernel's MODE_FILL: each run of same-group binaries with
+            // ascending, overlapping windows is summed once per bin of its span;
+            // the pairs are rounded once to FP64 and scaled in FP64
+            __shared__ int s_run[kMaxPack + 1], s_lo[kMaxPack], s_off[kMaxPack + 1];
+            __shared__ int s_nruns;
+            if (tid == 0) s_nruns = fill_runs(bins, cnt, N, s_run, s_lo, s_off);
+            __syncthreads();
+            const int nr = s_nruns;
+            const int U = s_off[nr];
+            for (int m = tid; m < U; m += kBlock) {
+                int r = 0;
+                while (r + 1 < nr && s_off[r + 1] <= m) r++;
+                const int j = s_lo[r] + (m - s_off[r]);
+                if (j < 0 || j >= K.L) continue;
+                double2 Ah = make_double2(0.0, 0.0), Eh = make_double2(0.0, 0.0);
+                bool any = false;
+                for (int p = s_run[r]; p < s_run[r + 1]; p++) {
+                    const Bin &B = bins[p];
+                    const int i = j - B.start;
+                    if (i < 0 || i >= N) continue;
+                    const int pos = swz(bitrev((i + (N >> 1)) & (N - 1), lg), lg);
+                    const cpx tA = buf[(p * 2 + 0) * N + pos], tE = buf[(p * 2 + 1) * N + pos];
+                    const double2 a2 = cmul(make_double2(pd(tA.x), pd(tA.y)), B.scale);
+                    const double2 e2 = cmul(make_double2(pd(tE.x), pd(tE.y)), B.scale);
+                    if (any) {
+                        Ah = cadd(Ah, a2);
+                        Eh = cadd(Eh, e2);
+                    } else {
+                        Ah = a2;
+                        Eh = e2;
+                        any = true;
+                    }
+                }
+                const size_t o = (size_t)bins[s_run[r]].gi * K.gstride + j;
+                atomicAdd(&K.A_glob[o].x, Ah.x);
+                atomicAdd(&K.A_glob[o].y, Ah.y);
+                atomicAdd(&K.E_glob[o].x, Eh.x);
+                atomicAdd(&K.E_glob[o].y, Eh.y);
+            }
         } else {
             // Threads [p Tpb, (p+1) Tpb) own binary p and stride its window (a
             // warp reads contiguous runs of data and PSD).  <d|h> and <h|h> per

@@ -1108,6 +1108,34 @@ __device__ __forceinline__ void third_prepass_mixed(const Bin *bins, const doubl
     __syncthreads();
 }
 
+// Runs of a fill tile (MODE_FILL, called by one thread): consecutive tile
+// slots with one group and ascending starts less than N apart cover one
+// contiguous span of output bins.  Run r holds slots run[r] .. run[r+1]-1,
+// spans lo[r] .. lo[r] + off[r+1] - off[r] - 1; an invalid binary's run is
+// empty; returns the number of runs.
+__device__ __forceinline__ int fill_runs(const Bin *bins, int cnt, int N, int *run, int *lo, int *off)
+{
+    int nr = 0, acc = 0, hi = 0;
+    for (int p = 0; p < cnt; p++) {
+        const Bin &B = bins[p];
+        const bool join = nr > 0 && B.valid && bins[p - 1].valid && B.gi == bins[p - 1].gi &&
+                          B.start >= bins[p - 1].start && B.start - bins[p - 1].start < N;
+        if (!join) {
+            if (nr > 0) acc += hi - lo[nr - 1];
+            off[nr] = acc;
+            run[nr] = p;
+            lo[nr] = B.start;
+            nr++;
+        }
+        // a run's last member ends its span; an invalid binary's run is empty
+        hi = B.valid ? B.start + N : lo[nr - 1];
+    }
+    acc += hi - lo[nr - 1];
+    off[nr] = acc;
+    run[nr] = cnt;
+    return nr;
+}
+
 template <typename R, int MODE, bool THIRD, bool UNEQ>
 __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(const KParams K)
 {
@@ -1414,27 +1442,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 3 : 2) wave_kernel(co
             __shared__ float2 s_scf[kMaxPack];
             if (sizeof(R) == 4 && tid < cnt)
                 s_scf[tid] = make_float2(d2f_scaled(bins[tid].scale.x, 0), d2f_scaled(bins[tid].scale.y, 0));
-            if (tid == 0) {
-                int nr = 0, off = 0, hi = 0;
-                for (int p = 0; p < cnt; p++) {
-                    const Bin &B = bins[p];
-                    const bool join = nr > 0 && B.valid && bins[p - 1].valid && B.gi == bins[p - 1].gi &&
-                                      B.start >= bins[p - 1].start && B.start - bins[p - 1].start < N;
-                    if (!join) {
-                        if (nr > 0) off += hi - s_lo[nr - 1];
-                        s_off[nr] = off;
-                        s_run[nr] = p;
-                        s_lo[nr] = B.start;
-                        nr++;
-                    }
-                    // a run's last member ends its span; an invalid binary's run is empty
-                    hi = B.valid ? B.start + N : s_lo[nr - 1];
-                }
-                off += hi - s_lo[nr - 1];
-                s_off[nr] = off;
-                s_run[nr] = cnt;
-                s_nruns = nr;
-            }
+            if (tid == 0) s_nruns = fill_runs(bins, cnt, N, s_run, s_lo, s_off);
             __syncthreads();
             const int nr = s_nruns;
             const int U = s_off[nr];
@@ -1775,12 +1783,12 @@ static int dispatch(KParams &K, int maxS, cudaStream_t st)
     const bool uneq = (K.a.tdi2 & GBX_TDI_UNEQUAL) != 0;
     if (uneq && third) return set_error(GBX_ERR_UNSUPPORTED, "unequal arms cover the 9-parameter model");
     if (K.a.precision == GBX_PAIR) {
-        if constexpr (MODE == MODE_WAVE || MODE == MODE_LL) {
+        if constexpr (MODE == MODE_WAVE || MODE == MODE_LL || MODE == MODE_FILL) {
             if (third) return set_error(GBX_ERR_UNSUPPORTED, "the pair form covers the 9-parameter model");
             return launch_tiles<MODE>(uneq ? pair_kernel<MODE, true> : pair_kernel<MODE, false>,
                                       pair_smem_bytes(maxS, MODE == MODE_WAVE ? 3 : 2, K.maxP), K, st);
         } else {
-            return set_error(GBX_ERR_UNSUPPORTED, "the pair form covers gbx_waveform and gbx_waveform_ll");
+            return set_error(GBX_ERR_UNSUPPORTED, "the pair form covers gbx_waveform, gbx_waveform_ll and gbx_waveform_fill");
         }
     }
     if (K.a.precision == GBX_FP64) {

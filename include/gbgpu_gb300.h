@@ -37,7 +37,8 @@ extern "C" {
 #define GBX_FP64 0             /* every step in FP64 (the plain form) */
 #define GBX_MIXED 1            /* FP64 carrier phase, delays and reductions; FP32 slow part + FFT */
 #define GBX_PAIR 2             /* slow part, FFT and <d|h> in float pairs (FP32 pipe, ~44 bits);
-                                  gbx_waveform and gbx_waveform_ll only, 9 parameters, N <= 4096 */
+                                  gbx_waveform, gbx_waveform_ll and gbx_waveform_fill,
+                                  9 parameters, N <= 4096 */
 
 #define GBX_MAX_LOG2N 13       /* N = 2^k, 5 <= k <= 13 (FP64 form: k <= 12) */
 

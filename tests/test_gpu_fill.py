@@ -63,7 +63,8 @@ def test_deterministic_fill_is_bit_reproducible_and_matches_atomic(precision):
     assert 0.2 * out[0].size < np.count_nonzero(out[0]) < 0.3 * out[0].size
 
 
-@pytest.mark.parametrize("precision,N", [("fp64", 256), ("mixed", 256), ("mixed", 64)])
+@pytest.mark.parametrize("precision,N", [("fp64", 256), ("mixed", 256), ("mixed", 64),
+                                         ("pair", 256), ("pair", 64)])
 def test_sorted_fill_prereduces_and_matches(precision, N):
     """Binaries launched in (group, carrier bin) order: the fused fill adds each
     tile's overlapping same-group windows once per output bin.  Same templates
@@ -97,6 +98,13 @@ def test_sorted_fill_prereduces_and_matches(precision, N):
     assert np.max(np.abs(out["sorted"] - out["unsorted"])) <= 1e-12 * scale
     if precision == "fp64":
         assert np.max(np.abs(out["sorted"] - out["det"])) <= 1e-12 * scale
+    if precision == "pair":
+        # the pair form's fill against the FP64 form's gather (1e-10 per window)
+        t = torch.zeros((G, 2, L), dtype=torch.complex128, device="cuda")
+        gb.generate_global_template(p.T, dev(gi), t, N=N, T=T, dt=dt, start_freq_ind=s0,
+                                    precision="fp64", fill_mode="deterministic")
+        ref = t.cpu().numpy()
+        assert np.max(np.abs(out["unsorted"] - ref)) <= 1e-10 * np.max(np.abs(ref))
     # add_to_templates with the same option, on top of the sorted result
     tA = torch.as_tensor(out["sorted"][:, 0].copy(), device="cuda")
     tE = torch.as_tensor(out["sorted"][:, 1].copy(), device="cuda")
