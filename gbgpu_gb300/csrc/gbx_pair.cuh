@@ -596,7 +596,7 @@ __global__ void __launch_bounds__(kBlock, 2) pair_kernel(const KParams K)
         const int N = 1 << lg;
         const double *tab = (lg >= 5 && lg <= kPairMaxLog2N)
                                 ? reinterpret_cast<const double *>(a.orbit[lg]) : nullptr;
-        const int maxcnt = tile_pack(a.tile, lg, 1);
+        const int maxcnt = tile_pack(a.tile, lg, MODE == MODE_SWAP ? 2 : 1);
         if (tab == nullptr || cnt < 1 || cnt > maxcnt || first < 0 || first + cnt > a.num_bin ||
             (cnt << lg) > K.maxS) {
             flag(a.status, GBX_FLAG_TILE);
@@ -665,6 +665,106 @@ __global__ void __launch_bounds__(kBlock, 2) pair_kernel(const KParams K)
                     K.AET[o + 2 * N] = make_double2((Xd.x + Yd.x + Zd.x) * i3, (Xd.y + Yd.y + Zd.y) * i3);
                 }
                 if (i == 0 && K.start_out) K.start_out[B.b] = B.start;
+            }
+        } else if constexpr (MODE == MODE_SWAP) {
+            // as wave_kernel's MODE_SWAP: binaries 2j (current) and 2j+1
+            // (proposal) of the tile form a pair, threads [j Tp2, (j+1) Tp2)
+            // walk both windows; with r the residual row and Dh = h_new - h_old
+            //   dlogL = Re<r|h_new> - Re<r|h_old> - (<h_new|h_new> + <h_old|h_old>)/2
+            //           + Re<h_old|h_new>   (cross term on the windows' overlap),
+            // every term summed in pairs
+            const int Tp2 = 2 * (kBlock / maxcnt);
+            const int width = Tp2 < 32 ? Tp2 : 32;
+            const int pr = tid / Tp2;
+            const int i0 = tid - pr * Tp2;
+            const bool samepsd = K.A_psd == K.E_psd;
+            dfl acc8[8];   // Crn (2), Cro (2), Hn, Ho, Cx (2)
+#pragma unroll
+            for (int k = 0; k < 8; k++) acc8[k] = dfl{0.f, 0.f};
+            if (2 * pr + 1 < cnt) {
+                const Bin &Bo = bins[2 * pr], &Bn = bins[2 * pr + 1];
+                const int po = 2 * pr, pn = 2 * pr + 1;
+                if (Bo.valid && Bn.valid) {
+                    bool out = false;
+                    for (int e = i0; e < 2 * N; e += Tp2) {
+                        const bool isnew = e < N;
+                        const int i = isnew ? e : e - N;
+                        const Bin &Bw = isnew ? Bn : Bo;
+                        const int pw = isnew ? pn : po;
+                        const int j = Bw.start + i;
+                        if (j < 0 || j >= K.L) {
+                            out = true;
+                            continue;
+                        }
+                        const int pos = swz(bitrev((i + (N >> 1)) & (N - 1), lg), lg);
+                        const cpx hA = buf[(pw * 2 + 0) * N + pos], hE = buf[(pw * 2 + 1) * N + pos];
+                        const size_t jd = (size_t)Bn.di * K.L + j, jn = (size_t)Bn.ni * K.L + j;
+                        const double2 dA = __ldg(K.A_data + jd), dE = __ldg(K.E_data + jd);
+                        const dfl wA = df_recip(d2ff_scaled(__ldg(K.A_psd + jn), Bn.eS));
+                        const dfl wE = samepsd ? wA : df_recip(d2ff_scaled(__ldg(K.E_psd + jn), Bn.eS));
+                        const dfl ar = p_mul(d2ff_scaled(dA.x, Bn.eD), wA);
+                        const dfl ai = p_mul(d2ff_scaled(dA.y, Bn.eD), wA);
+                        const dfl er = p_mul(d2ff_scaled(dE.x, Bn.eD), wE);
+                        const dfl ei = p_mul(d2ff_scaled(dE.y, Bn.eD), wE);
+                        // conj(r) h / S and |h|^2 / S
+                        const dfl cr = p_add(p_dot2(ar, hA.x, ai, hA.y), p_dot2(er, hE.x, ei, hE.y));
+                        const dfl ci = p_add(p_dot2(ar, hA.y, df_neg(ai), hA.x),
+                                             p_dot2(er, hE.y, df_neg(ei), hE.x));
+                        const dfl hh2 = p_dot2(p_dot2(hA.x, hA.x, hA.y, hA.y), wA,
+                                               p_dot2(hE.x, hE.x, hE.y, hE.y), wE);
+                        if (isnew) {
+                            acc8[0] = p_add(acc8[0], cr);
+                            acc8[1] = p_add(acc8[1], ci);
+                            acc8[4] = p_add(acc8[4], hh2);
+                            const int k = j - Bo.start;
+                            if (k >= 0 && k < N) {
+                                const int pk = swz(bitrev((k + (N >> 1)) & (N - 1), lg), lg);
+                                const cpx oA = buf[(po * 2 + 0) * N + pk], oE = buf[(po * 2 + 1) * N + pk];
+                                // conj(h_old) h_new / S
+                                acc8[6] = p_add(acc8[6], p_dot2(p_dot2(oA.x, hA.x, oA.y, hA.y), wA,
+                                                                p_dot2(oE.x, hE.x, oE.y, hE.y), wE));
+                                acc8[7] = p_add(acc8[7], p_dot2(p_dot2(oA.x, hA.y, df_neg(oA.y), hA.x), wA,
+                                                                p_dot2(oE.x, hE.y, df_neg(oE.y), hE.x), wE));
+                            }
+                        } else {
+                            acc8[2] = p_add(acc8[2], cr);
+                            acc8[3] = p_add(acc8[3], ci);
+                            acc8[5] = p_add(acc8[5], hh2);
+                        }
+                    }
+                    if (out) flag(a.status, GBX_FLAG_WINDOW);
+                }
+            }
+            {
+                // group trees in pairs; the leaders write FP64 partials
+                const bool leader = (tid & (width - 1)) == 0;
+                const int g = tid / width;
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    dfl x = acc8[k];
+                    for (int o = width >> 1; o > 0; o >>= 1)
+                        x = p_add(x, dfl{shfl4(x.h, o), shfl4(x.l, o)});
+                    if (leader) red[8 * g + k] = pd(x);
+                }
+            }
+            __syncthreads();
+            if (2 * tid + 1 < cnt) {
+                const Bin &Bo = bins[2 * tid], &Bn = bins[2 * tid + 1];
+                const int per = Tp2 / width;
+                double t[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                for (int g = tid * per; g < (tid + 1) * per; g++)
+#pragma unroll
+                    for (int k = 0; k < 8; k++) t[k] += red[8 * g + k];
+                const double cdh = 4.0 * K.df * exp2_int(Bn.eS - Bn.eD);
+                const double chh = 4.0 * K.df * exp2_int(Bn.eS);
+                const double2 so = Bo.scale, sn = Bn.scale;
+                const double rn = cmul(sn, make_double2(t[0], t[1])).x * cdh;
+                const double ro = cmul(so, make_double2(t[2], t[3])).x * cdh;
+                const double hn = (sn.x * sn.x + sn.y * sn.y) * t[4] * chh;
+                const double ho = (so.x * so.x + so.y * so.y) * t[5] * chh;
+                const double cx = cmul(make_double2(so.x, -so.y), cmul(sn, make_double2(t[6], t[7]))).x * chh;
+                const bool ok = Bo.valid && Bn.valid && Bo.b >= 0 && Bn.b >= 0;
+                if (Bn.b >= 0) K.dlogl[Bn.b >> 1] = ok ? (rn - ro - 0.5 * (hn + ho) + cx) : 0.0;
             }
         } else if constexpr (MODE == MODE_FILL) {
             // as wave_kernel's MODE_FILL: each run of same-group binaries with

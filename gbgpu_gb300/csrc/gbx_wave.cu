@@ -1783,12 +1783,12 @@ static int dispatch(KParams &K, int maxS, cudaStream_t st)
     const bool uneq = (K.a.tdi2 & GBX_TDI_UNEQUAL) != 0;
     if (uneq && third) return set_error(GBX_ERR_UNSUPPORTED, "unequal arms cover the 9-parameter model");
     if (K.a.precision == GBX_PAIR) {
-        if constexpr (MODE == MODE_WAVE || MODE == MODE_LL || MODE == MODE_FILL) {
+        if constexpr (MODE == MODE_WAVE || MODE == MODE_LL || MODE == MODE_FILL || MODE == MODE_SWAP) {
             if (third) return set_error(GBX_ERR_UNSUPPORTED, "the pair form covers the 9-parameter model");
             return launch_tiles<MODE>(uneq ? pair_kernel<MODE, true> : pair_kernel<MODE, false>,
                                       pair_smem_bytes(maxS, MODE == MODE_WAVE ? 3 : 2, K.maxP), K, st);
         } else {
-            return set_error(GBX_ERR_UNSUPPORTED, "the pair form covers gbx_waveform, gbx_waveform_ll and gbx_waveform_fill");
+            return set_error(GBX_ERR_UNSUPPORTED, "the pair form covers the waveform, likelihood, fill and swap entry points");
         }
     }
     if (K.a.precision == GBX_FP64) {

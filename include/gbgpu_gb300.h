@@ -37,7 +37,7 @@ extern "C" {
 #define GBX_FP64 0             /* every step in FP64 (the plain form) */
 #define GBX_MIXED 1            /* FP64 carrier phase, delays and reductions; FP32 slow part + FFT */
 #define GBX_PAIR 2             /* slow part, FFT and <d|h> in float pairs (FP32 pipe, ~44 bits);
-                                  gbx_waveform, gbx_waveform_ll and gbx_waveform_fill,
+                                  waveform, likelihood, fill and swap entry points,
                                   9 parameters, N <= 4096 */
 
 #define GBX_MAX_LOG2N 13       /* N = 2^k, 5 <= k <= 13 (FP64 form: k <= 12) */
@@ -282,7 +282,8 @@ int gbx_waveform_fill(const gbx_wave_args *a, void *A_glob, void *E_glob,
  *   dlogl[j] = Re<r|Dh> - 1/2 <Dh|Dh>
  * with <a|b> = 4 df sum_{A,E} conj(a) b / S over the union of both windows
  * (the inner product of gbgpu/cutils/gbgpu_utils.cu:172-183).  Uniform N,
- * num_bin even; both precisions; circular or third-body parameters.
+ * num_bin even; FP64, pair and FP32 forms (the pair form for 9 parameters);
+ * circular or third-body parameters.
  */
 int gbx_swap_ll(const gbx_wave_args *a, const gbx_ll_args *l, double *dlogl, void *stream);
 
