@@ -261,6 +261,43 @@ def test_c_abi_rejects_bad_arguments_before_touching_a_device():
                                     None) == ERR_ARG
     assert "workspace" in msg()
     assert lib.gbx_wave_workspace_bytes(0) == 0 and lib.gbx_wave_workspace_bytes(3) % 256 == 0
+    # TDI bits: only TDI-2 and unequal arms; unequal arms not in the FP32 form
+    for a, code, text in [(args(tdi2=4), ERR_ARG, "GBX_TDI"),
+                          (args(tdi2=nat.GBX_TDI_UNEQUAL), ERR_UNSUPPORTED, "unequal arms")]:
+        assert lib.gbx_waveform_ll(ctypes.byref(a), ctypes.byref(la), fake, fake, None) == code
+        assert text in msg(), (text, msg())
+    # swap gradient: mixed form, aligned workspace, uniform N, even num_bin, a gradient buffer
+    lib.gbx_swap_ll_grad.argtypes = [vp, vp, vp, vp, vp]
+    lib.gbx_grad_workspace_bytes.restype = ctypes.c_size_t
+    lib.gbx_grad_workspace_bytes.argtypes = [i]
+    ws = dict(workspace=fake.value, workspace_bytes=lib.gbx_grad_workspace_bytes(8))
+    swap_cases = [
+        (args(precision=nat.GBX_FP64, **ws), fake, ERR_UNSUPPORTED, "mixed"),
+        (args(), fake, ERR_ARG, "workspace"),
+        (args(num_bin=5, **ws), fake, ERR_ARG, "even"),
+        (args(order=fake.value, **ws), fake, ERR_ARG, "uniform N"),
+        (args(**ws), None, ERR_ARG, "gradient"),
+    ]
+    for a, gbuf, code, text in swap_cases:
+        assert lib.gbx_swap_ll_grad(ctypes.byref(a), ctypes.byref(la), fake, gbuf, None) == code, text
+        assert text in msg(), (text, msg())
+    # forward-mode Fisher matrices: 9 parameters, equal arms, an output buffer
+    lib.gbx_fisher.argtypes = [vp, vp, vp, i, i, vp, d, vp, vp]
+    fisher_cases = [
+        (args(nparams=14, year=3.15e7, **ws), fake, ERR_UNSUPPORTED, "9-parameter"),
+        (args(precision=nat.GBX_FP64, **ws), fake, ERR_UNSUPPORTED, "mixed"),
+        (args(**ws), None, ERR_ARG, "Fisher"),
+        (args(), fake, ERR_ARG, "workspace"),
+    ]
+    for a, out, code, text in fisher_cases:
+        assert lib.gbx_fisher(ctypes.byref(a), fake, fake, 100, 1, None, 1e-7, out, None) == code, text
+        assert text in msg(), (text, msg())
+    # the FP64 drop-in: the same checks as gbx_get_ll_ex
+    lib.gbx_get_ll_fp64.argtypes = lib.gbx_get_ll_ex.argtypes
+    assert lib.gbx_get_ll_fp64(*ptrs, 1.0, fake, 16, -1, None, None, 100, 1, 1, 0, 0,
+                               None, None) == ERR_ARG
+    assert lib.gbx_get_ll_fp64(*ptrs, 1.0, fake, 16, 0, None, None, 100, 0, 1, 0, 0,
+                               None, None) == 0
 
 
 def test_tabulated_orbits_interpolate_the_analytic_orbit(tmp_path):
