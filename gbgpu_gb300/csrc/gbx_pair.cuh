@@ -416,7 +416,7 @@ __device__ __forceinline__ void slow_pair(const Bin &B, int n, int N, dfl step, 
     // omega L, fc = e^{-i omL}, fc2 = 4 omL sin(omL) fc (gbgpu.py:362-368)
     const dfl omL = p_addf(base, dfl{B.w2 * tf * tf, 0.f});
     dfl co, so;
-    sincos_pair(omL, sct, co, so);
+    sincos_pair_acc(omL, sct, co, so);   // sin(omL) scales the window: relative accuracy at low f
     const cpx fc = {co, df_neg(so)};
     const dfl g4 = p_scale(p_mul(omL, so), 4.f);
     if constexpr (AE) {

@@ -405,7 +405,7 @@ def test_uneven_N_persistent_kernel(gbgpu, precision):
 
 
 @pytest.mark.parametrize("N,precision", [(32, "fp64"), (4096, "fp64"), (8192, "mixed"),
-                                         (1024, "mixed")])
+                                         (1024, "mixed"), (32, "pair"), (4096, "pair")])
 def test_ll_extreme_N(gbgpu, N, precision):
     B = 5
     p, _, data, S, s0 = _ll_setup(B, N, 7, f_lo=1e-2, f_hi=1.001e-2)
@@ -415,8 +415,29 @@ def test_ll_extreme_N(gbgpu, N, precision):
                      dt=5.0, start_freq_ind=s0, precision=precision)
     ref, _, hh, _ = O.get_ll(p, data, [S, S], N, T=4 * 31557600.0, dt=5.0, start_freq_ind=s0,
                              return_terms=True)
-    tol = FP64_TOL if precision == "fp64" else MIXED_LL_TOL
+    tol = {"fp64": FP64_TOL, "pair": PAIR_LL_TOL}.get(precision, MIXED_LL_TOL)
     assert np.max(np.abs(like - ref) / np.maximum(1.0, hh.real)) < tol
+
+
+@pytest.mark.parametrize("N,B", [(32, 5), (64, 3), (32, 1)])
+def test_pair_waveform_small_N_odd_batch(gbgpu, N, B):
+    """The pair transform's last five stages run on half-warps, one 32-element
+    block each: an odd number of blocks (three channels, odd batches at N = 32,
+    64) leaves a spare half-warp that repeats the last block and stores
+    nothing.  Windows against the oracle, start indices bit-exact."""
+    rng = np.random.default_rng(40 + N + B)
+    f0 = rng.uniform(2e-4, 4e-4, B)
+    fd = 10 ** rng.uniform(-18, -17, B)
+    p = np.array([10 ** rng.uniform(-23, -21, B), f0, fd, 11 / 3 * fd ** 2 / f0,
+                  rng.uniform(0, 2 * np.pi, B), np.arccos(rng.uniform(-1, 1, B)),
+                  rng.uniform(0, np.pi, B), rng.uniform(0, 2 * np.pi, B),
+                  np.arcsin(rng.uniform(-1, 1, B))])
+    gb = gbgpu()
+    gb.run_wave(*p, N=N, T=4 * 31557600.0, dt=10.0, precision="pair")
+    W = O.waveform(p, N, T=4 * 31557600.0, dt=10.0)
+    np.testing.assert_array_equal(gb.start_inds.cpu().numpy(), W["start_inds"])
+    assert np.max(rel_err(gb.XYZf.cpu().numpy(), W["XYZf"], axis=(1, 2))) < 1e-10
+    assert np.max(rel_err(gb.AETf.cpu().numpy(), W["AETf"], axis=(1, 2))) < 1e-10
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
