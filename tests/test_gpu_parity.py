@@ -440,6 +440,31 @@ def test_pair_waveform_small_N_odd_batch(gbgpu, N, B):
     assert np.max(rel_err(gb.AETf.cpu().numpy(), W["AETf"], axis=(1, 2))) < 1e-10
 
 
+@pytest.mark.parametrize("N,tdi2", [(64, False), (256, True), (1024, False), (4096, True)])
+def test_pair_waveform_across_the_band(gbgpu, N, tdi2):
+    """Pair windows against the oracle for binaries spread log-uniformly over
+    1e-4 .. 2.5e-2 Hz (omega L from 0.005 to 1.3), all angles random, fdot up
+    to 1e-15: the stated 1e-10 normwise bound over the whole band."""
+    rng = np.random.default_rng(900 + N)
+    B = 60
+    f0 = 10 ** rng.uniform(-4, np.log10(2.5e-2), B)
+    fd = 10 ** rng.uniform(-19, -15, B)
+    p = np.array([10 ** rng.uniform(-23, -21, B), f0, fd, 11 / 3 * fd ** 2 / f0,
+                  rng.uniform(0, 2 * np.pi, B), np.arccos(rng.uniform(-1, 1, B)),
+                  rng.uniform(0, np.pi, B), rng.uniform(0, 2 * np.pi, B),
+                  np.arcsin(rng.uniform(-1, 1, B))])
+    if tdi2:
+        p[2], p[3] = 0.0, 0.0      # the reference's TDI-2 factor is taken at f0
+    gb = gbgpu()
+    gb.run_wave(*p, N=N, T=4 * 31557600.0, dt=5.0, tdi2=tdi2, precision="pair")
+    W = O.waveform(p, N, T=4 * 31557600.0, dt=5.0, tdi2=tdi2)
+    np.testing.assert_array_equal(gb.start_inds.cpu().numpy(), W["start_inds"])
+    err = rel_err(gb.XYZf.cpu().numpy(), W["XYZf"], axis=(1, 2))
+    print(f"pair N={N} tdi2={tdi2}: worst window error {err.max():.2e} "
+          f"(f0 {p[1][np.argmax(err)]:.2e} Hz)")
+    assert np.max(err) < 1e-10
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_third_body_ll(precision):
     from gbgpu_gb300 import GBGPUThirdBody
