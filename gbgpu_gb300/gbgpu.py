@@ -1120,19 +1120,49 @@ class GBGPUBase(abc.ABC):
 
     def information_matrix(self, params, eps=1e-9, parameter_transforms={}, inds=None, N=1024,
                            psd_func=None, psd_kwargs={}, easy_central_difference=False,
-                           return_gpu=False, **kwargs):
-        """Fisher matrices from central differences of run_wave (gbgpu.py:957-1138)."""
+                           return_gpu=False, method="auto", **kwargs):
+        """Fisher matrices of the reference's information_matrix (gbgpu.py:957-1138).
+
+        The reference differentiates with relative steps, h(theta (1 +- eps)), so
+        its matrices are in the logarithms of the parameters: F_ij = <theta_i
+        dh/dtheta_i | theta_j dh/dtheta_j>.  ``method="forward"`` forms them from
+        the forward-mode kernel (``gbx_fisher``: one launch, exact derivatives;
+        the 9-parameter model without parameter transforms, equal arms, N <=
+        1024); ``"differences"`` runs the reference's central differences of
+        run_wave; ``"auto"`` takes the first where it applies.
+        """
         if psd_func is None:
             from .sensitivity import A1TDISens
             psd_func = A1TDISens.get_Sn
         if N is None:
             raise ValueError("N must be provided up front for Infromation Matrix.")
-        kwargs["N"] = N
+        if method not in ("auto", "forward", "differences"):
+            raise ValueError("method must be 'auto', 'forward' or 'differences'")
         params = np.atleast_2d(_to_host(params))
         num_params = len(params)
         num_bins = len(params[0])
         if inds is None:
             inds = np.arange(num_params)
+        fwd_ok = (not parameter_transforms and num_params == 9 and not self.unequal_arms and
+                  np.ndim(N) == 0 and int(N) <= 1024 and
+                  set(kwargs) <= {"T", "dt", "tdi2", "oversample"})
+        if method == "forward" and not fwd_ok:
+            raise ValueError("forward-mode information matrices cover the 9-parameter model "
+                             "without parameter transforms, equal arms and N <= 1024")
+        if method == "forward" or (method == "auto" and fwd_ok):
+            T = kwargs.get("T", 4 * YRSID_SI)
+            dt = kwargs.get("dt", 10.0)
+            Tu = int(T / dt) * dt
+            prm = torch.as_tensor(np.ascontiguousarray(params, dtype=np.float64),
+                                  device=self.device)
+            F = self._fisher_forward(prm, int(N), Tu, Tu, bool(kwargs.get("tdi2", False)),
+                                     psd_func, psd_kwargs)
+            th = prm.T
+            F = F * th[:, :, None] * th[:, None, :]          # d/d ln theta, as the reference
+            ix = torch.as_tensor(np.asarray(inds, dtype=np.int64), device=self.device)
+            F = F[:, ix][:, :, ix].contiguous()
+            return F if return_gpu else F.cpu().numpy()
+        kwargs["N"] = N
         num_derivs = len(inds)
         info = torch.zeros((num_bins, num_derivs, num_derivs), dtype=torch.float64,
                            device=self.device)

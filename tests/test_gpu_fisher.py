@@ -114,3 +114,37 @@ def test_forward_fisher_declines_the_third_body():
     p = np.zeros((14, 2))
     with pytest.raises(ValueError, match="9-parameter"):
         GBGPUThirdBody().fisher_matrices(p, N=256, method="forward")
+
+
+def test_information_matrix_forward_mode_is_the_log_parameter_fisher():
+    """The reference's information_matrix differentiates with relative steps,
+    so its matrices are in ln theta; the forward-mode path equals the exact
+    Fisher matrix scaled by theta_i theta_j (2e-6 of sqrt(F_ii F_jj)) and the
+    reference's differences to their own noise (eps = 1e-9 relative steps
+    leave ~1e-3)."""
+    from gbgpu_gb300 import GBGPU
+    rng = np.random.default_rng(19)
+    B, N = 8, 256
+    Tu = int(T_OBS / DT) * DT
+    q = np.rint(rng.uniform(2e-3, 4e-3, B) * Tu)
+    f0 = (q + rng.uniform(-0.3, 0.3, B)) / Tu
+    fdot = 10 ** rng.uniform(-17, -16, B)
+    p = np.array([10 ** rng.uniform(-22.3, -21.7, B), f0, fdot, 11 / 3 * fdot ** 2 / f0,
+                  rng.uniform(0.5, 5.5, B), np.arccos(rng.uniform(-0.9, 0.9, B)),
+                  rng.uniform(0.3, 2.8, B), rng.uniform(0.5, 5.5, B),
+                  np.arcsin(rng.uniform(-0.9, 0.9, B))])
+    inds = [0, 1, 2, 4, 5, 6, 7, 8]
+    gb = GBGPU()
+    Ff = gb.information_matrix(p.copy(), inds=inds, N=N, T=T_OBS, dt=DT, method="forward")
+    ref = _exact_fisher(p, None, N) * p.T[:, :, None] * p.T[:, None, :]
+    ref = ref[:, inds][:, :, inds]
+    d = np.sqrt(np.einsum("bii->bi", ref))
+    err = np.abs(Ff - ref) / (d[:, :, None] * d[:, None, :])
+    print(f"information_matrix forward vs exact: {err.max():.2e}")
+    assert err.max() < 2e-6
+    # the reference's differences require one start bin per call: one binary each
+    Fd = np.concatenate([gb.information_matrix(p[:, b:b + 1].copy(), inds=inds, N=N, T=T_OBS,
+                                               dt=DT, method="differences") for b in range(B)])
+    errd = np.abs(Fd - ref) / (d[:, :, None] * d[:, None, :])
+    print(f"information_matrix differences vs exact: {errd.max():.2e}")
+    assert errd.max() < 1e-2
