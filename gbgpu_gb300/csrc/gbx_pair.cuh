@@ -90,7 +90,6 @@ __device__ __forceinline__ dfl p_div(dfl n, dfl d)
 
 __device__ __forceinline__ cpx cp_add(cpx a, cpx b) { return {p_add(a.x, b.x), p_add(a.y, b.y)}; }
 __device__ __forceinline__ cpx cp_sub(cpx a, cpx b) { return {p_sub(a.x, b.x), p_sub(a.y, b.y)}; }
-__device__ __forceinline__ cpx cp_neg(cpx a) { return {df_neg(a.x), df_neg(a.y)}; }
 __device__ __forceinline__ cpx cp_pow2(cpx a, float s) { return {p_scale(a.x, s), p_scale(a.y, s)}; }
 __device__ __forceinline__ cpx cp_mul(cpx a, cpx b)
 {
