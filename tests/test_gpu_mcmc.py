@@ -89,3 +89,38 @@ def test_graph_replay_equals_eager_and_residuals_stay_consistent():
     assert err < 1e-6 * eager.res.abs().max().item()
     np.testing.assert_allclose(graph.res.cpu().numpy(), eager.res.cpu().numpy(), rtol=0,
                                atol=1e-9 * eager.res.abs().max().item())
+
+
+def test_swap_sampler_in_the_pair_form():
+    """The same sampler on the 9-parameter model in the pair form (swap
+    likelihood and residual updates both in pairs): accepted swaps' dlogL
+    equals the change of -1/2 <r|r> to 1e-8 of |logL| (the FP32 form: 1e-5),
+    and the incrementally updated residuals equal d minus the sum of the
+    current sources recomputed from scratch."""
+    from gbgpu_gb300 import GBGPU
+    from gbgpu_gb300.mcmc import SwapSampler, random_proposals, log_uniforms
+    _, p, data, psd, s0, N, _ = _setup(seed=5)
+    gb = GBGPU()
+    kw = dict(N=N, T=T_OBS, dt=DT, start_freq_ind=s0, precision="pair")
+    s = SwapSampler(gb, p[:9].contiguous().clone(), data, psd, **kw)
+    g = torch.Generator(device="cuda").manual_seed(17)
+    scale = torch.tensor([0.05, 2e-9, 0, 0, 0.2, 0.1, 0.1, 0.02, 0.02], dtype=torch.float64,
+                         device="cuda")
+    steps = 8
+    lus = log_uniforms(s.W, steps, g, "cuda")
+    accepted = 0
+    for i in range(steps):
+        k = i % s.K
+        prop = random_proposals(s.params[:, :, k], scale, g)
+        ll0 = s.log_likelihood()
+        dl = s.step(k, prop, lus[i])
+        ll1 = s.log_likelihood()
+        a = (lus[i] < dl).cpu().numpy()
+        d_ll, dl_n = (ll1 - ll0).cpu().numpy(), dl.cpu().numpy()
+        tol = 1e-8 * np.maximum(1.0, np.abs(ll0.cpu().numpy()))
+        assert np.all(np.abs(d_ll[a] - dl_n[a]) < tol[a])
+        assert np.all(np.abs(d_ll[~a]) < tol[~a])
+        accepted += int(a.sum())
+    assert accepted > 0
+    fresh = SwapSampler(gb, s.params.clone(), data, psd, **kw)
+    assert (fresh.res - s.res).abs().max().item() < 1e-9 * s.res.abs().max().item()
