@@ -15,13 +15,14 @@
 // This file is included inside namespace gbx by gbx_wave.cu.
 
 // ---------------------------------------------------------------- arithmetic
-// Sums are renormalised (Fast2Sum of head and tail): after a cancellation
+// p_ sums are renormalised (Fast2Sum of head and tail): after a cancellation
 // the tail of an unnormalised sum can reach the size of its head, and a later
-// product would then round its cross term on that tail to FP32 precision.
-// Products are not: their tail is the exact rounding error of the head plus
-// the operands' cross terms, within a few units in the last place of the
-// head, so the next operation keeps ~44 significant bits without the three
-// instructions of a renormalisation.
+// product would then round its cross term on that tail to FP32 precision
+// relative to the (small) result; the u_ forms below skip it where that does
+// not matter.  Products are not renormalised: their tail is the exact
+// rounding error of the head plus the operands' cross terms, within a few
+// units in the last place of the head, so the next operation keeps ~44
+// significant bits without the three instructions of a renormalisation.
 __device__ __forceinline__ dfl p_add(dfl a, dfl b) { return df_add(a, b); }
 __device__ __forceinline__ dfl p_sub(dfl a, dfl b) { return p_add(a, dfl{-b.h, -b.l}); }
 
@@ -97,6 +98,58 @@ __device__ __forceinline__ cpx cp_mul(cpx a, cpx b)
 }
 __device__ __forceinline__ cpx cp_scale(cpx a, dfl r) { return {p_mul(a.x, r), p_mul(a.y, r)}; }
 __device__ __forceinline__ cpx cp_zero() { return {{0.f, 0.f}, {0.f, 0.f}}; }
+
+// Where an operation's error is judged against the size of its inputs (the
+// transform's butterflies, the TDI combination, the projections and
+// antenna patterns, series and link angles) the renormalisation adds
+// nothing: after a cancellation the unnormalised tail is at most a few units
+// in the last place of the INPUTS' heads, so the FP32 rounding of the later
+// tail additions and cross terms stays below 2^-48 of the input size, the
+// error the inputs already carry.  These u_ forms keep TwoSum's exact error
+// and skip the closing Fast2Sum (3 of 11 instructions).  Sums stay
+// renormalised where a head alone is read: the carrier phase before its
+// reduction mod 2 pi (a phase of 1e3 rad would leave a tail of 1e-4 rad,
+// and sincos picks its table entry from the head) and sincos's outputs.
+__device__ __forceinline__ dfl u_add(dfl a, dfl b)
+{
+    const dfl s = df_two_sum(a.h, b.h);
+    return {s.h, s.l + (a.l + b.l)};
+}
+__device__ __forceinline__ dfl u_sub(dfl a, dfl b) { return u_add(a, dfl{-b.h, -b.l}); }
+__device__ __forceinline__ dfl u_dot2(dfl a, dfl b, dfl c, dfl d)
+{
+    const float p = a.h * b.h, q = c.h * d.h;
+    float e = fmaf(a.h, b.h, -p);
+    float f = fmaf(c.h, d.h, -q);
+    e = fmaf(a.h, b.l, fmaf(a.l, b.h, e));
+    f = fmaf(c.h, d.l, fmaf(c.l, d.h, f));
+    const dfl s = df_two_sum(p, q);
+    return {s.h, s.l + (e + f)};
+}
+// a b + c d + e f, unnormalised
+__device__ __forceinline__ dfl u_dot3(dfl a, dfl b, dfl c, dfl d, dfl e, dfl f)
+{
+    const float p = a.h * b.h, q = c.h * d.h, r = e.h * f.h;
+    float ep = fmaf(a.h, b.h, -p), eq = fmaf(c.h, d.h, -q), er = fmaf(e.h, f.h, -r);
+    ep = fmaf(a.h, b.l, fmaf(a.l, b.h, ep));
+    eq = fmaf(c.h, d.l, fmaf(c.l, d.h, eq));
+    er = fmaf(e.h, f.l, fmaf(e.l, f.h, er));
+    const dfl s1 = df_two_sum(p, q);
+    const dfl s2 = df_two_sum(s1.h, r);
+    return {s2.h, (s1.l + s2.l) + (ep + (eq + er))};
+}
+// a + b when |a.h| >= |b.h| (or a = 0), unnormalised
+__device__ __forceinline__ dfl u_addf(dfl a, dfl b)
+{
+    const float s = a.h + b.h;
+    return {s, (b.h - (s - a.h)) + (a.l + b.l)};
+}
+__device__ __forceinline__ cpx cu_add(cpx a, cpx b) { return {u_add(a.x, b.x), u_add(a.y, b.y)}; }
+__device__ __forceinline__ cpx cu_sub(cpx a, cpx b) { return {u_sub(a.x, b.x), u_sub(a.y, b.y)}; }
+__device__ __forceinline__ cpx cu_mul(cpx a, cpx b)
+{
+    return {u_dot2(a.x, b.x, df_neg(a.y), b.y), u_dot2(a.x, b.y, a.y, b.x)};
+}
 __device__ __forceinline__ double pd(dfl a) { return (double)a.h + (double)a.l; }
 
 // ---------------------------------------------------------------- functions
@@ -122,8 +175,8 @@ __device__ __forceinline__ void sincos_pair(dfl x, const float4 *__restrict__ ta
     const dfl sd = {d.h, fmaf(d.h * d2, -1.0f / 6.0f, d.l)};
     const float eps = d2 * fmaf(d2, 1.0f / 24.0f, -0.5f);   // cos d - 1
     const dfl Tc = {t.x, t.y}, Ts = {t.z, t.w};
-    const dfl cc = p_add(Tc, df_neg(p_mul(Ts, sd)));
-    const dfl ss = p_add(Ts, p_mul(Tc, sd));
+    const dfl cc = u_add(Tc, df_neg(p_mul(Ts, sd)));
+    const dfl ss = u_add(Ts, p_mul(Tc, sd));
     c = df_fast(cc.h, fmaf(Tc.h, eps, cc.l));
     s = df_fast(ss.h, fmaf(Ts.h, eps, ss.l));
 }
@@ -148,8 +201,8 @@ __device__ __forceinline__ void sincos_pair_acc(dfl x, const float4 *__restrict_
     const dfl em = df_fast(-0.5f * d2, fmaf(d2 * d2, fmaf(d2, -1.0f / 720.0f, 1.0f / 24.0f),
                                             -0.5f * d2l));
     const dfl Tc = {t.x, t.y}, Ts = {t.z, t.w};
-    c = p_add(p_add(Tc, p_mul(Tc, em)), df_neg(p_mul(Ts, sd)));
-    s = p_add(p_add(Ts, p_mul(Ts, em)), p_mul(Tc, sd));
+    c = p_add(u_add(Tc, p_mul(Tc, em)), df_neg(p_mul(Ts, sd)));
+    s = p_add(u_add(Ts, p_mul(Ts, em)), p_mul(Tc, sd));
 }
 
 // sin(a)/a alone: the S half of sinc_cos_pair.
@@ -163,9 +216,9 @@ __device__ __forceinline__ dfl sinc_pair(dfl a, const float4 *__restrict__ tab)
         q = fmaf(q, xf, -1.0f / 39916800.0f);
         q = fmaf(q, xf, 1.0f / 362880.0f);
         q = fmaf(q, xf, -1.0f / 5040.0f);
-        dfl r = p_addf(s2, dfl{xf * q, 0.f});
-        r = p_addf(s1, p_mul(x, r));
-        return p_addf(dfl{1.f, 0.f}, p_mul(x, r));
+        dfl r = u_addf(s2, dfl{xf * q, 0.f});
+        r = u_addf(s1, p_mul(x, r));
+        return u_addf(dfl{1.f, 0.f}, p_mul(x, r));
     }
     dfl c, sn;
     sincos_pair(a, tab, c, sn);
@@ -316,8 +369,8 @@ __device__ __forceinline__ void slow_pair(const Bin &B, int n, int N, dfl step, 
     dfl kr[3];
 #pragma unroll
     for (int a = 0; a < NA; a++)
-        kr[a] = p_dot3(B.kd[0], r[a][0], B.kd[1], r[a][1], B.kd[2], r[a][2]);
-    if constexpr (!UNEQ) kr[2] = df_neg(p_add(kr[0], kr[1]));
+        kr[a] = u_dot3(B.kd[0], r[a][0], B.kd[1], r[a][1], B.kd[2], r[a][2]);
+    if constexpr (!UNEQ) kr[2] = df_neg(u_add(kr[0], kr[1]));
     const dfl tm = p_mulf(step, (float)n);                 // n T/N
     const float tf = tm.h;
     const dfl tm2 = p_sqr(tm);
@@ -337,7 +390,7 @@ __device__ __forceinline__ void slow_pair(const Bin &B, int n, int N, dfl step, 
     const dfl dk[3] = {dfl{0.f, 0.f}, p_mul(Loc, kr[0]), df_neg(p_mul(Loc, kr[2]))};
     // f(t)/fstar = w0 + w1 t + w2 t^2 with w1 t a pair: at f0 = 1e-4 Hz and
     // fdot = 1e-15 that term is 1e-3 of w0, and omL enters fc2 squared
-    const dfl base = p_addf(dfl{B.w0h, B.w0l}, p_mul(dfl{B.w1, B.w1l}, tm));
+    const dfl base = u_addf(dfl{B.w0h, B.w0l}, p_mul(dfl{B.w1, B.w1l}, tm));
     cpx E[3];
     dfl fo[3], phs[3];
 #pragma unroll
@@ -353,7 +406,7 @@ __device__ __forceinline__ void slow_pair(const Bin &B, int n, int N, dfl step, 
         }
         // f(xi)/fstar at xi = t - kP: - w1 kP + w2 xi^2 are below 3e-6 of w0
         const float xf = tf - kPf;
-        fo[s] = p_addf(base, dfl{fmaf(B.w2 * xf, xf, -B.w1 * kPf), 0.f});
+        fo[s] = u_addf(base, dfl{fmaf(B.w2 * xf, xf, -B.w1 * kPf), 0.f});
     }
     // antenna patterns per arm, with the 1/4 of the transfer functions:
     // r.e+.r = (r.v)^2 - (r.u)^2, r.ex.r = 2 (r.u)(r.v)
@@ -363,19 +416,19 @@ __device__ __forceinline__ void slow_pair(const Bin &B, int n, int N, dfl step, 
     for (int a = 0; a < 3; a++) {
         dfl ru, rv;
         if (a < NA) {
-            ru = p_dot3(B.pr.ud[0], r[a][0], B.pr.ud[1], r[a][1], B.pr.ud[2], r[a][2]);
-            rv = p_dot2(B.pr.vd[0], r[a][0], B.pr.vd[1], r[a][1]);
+            ru = u_dot3(B.pr.ud[0], r[a][0], B.pr.ud[1], r[a][1], B.pr.ud[2], r[a][2]);
+            rv = u_dot2(B.pr.vd[0], r[a][0], B.pr.vd[1], r[a][1]);
         } else {
-            ru = df_neg(p_add(rus[0], rus[1]));
-            rv = df_neg(p_add(rvs[0], rvs[1]));
+            ru = df_neg(u_add(rus[0], rus[1]));
+            rv = df_neg(u_add(rvs[0], rvs[1]));
         }
         if (a < 2) {
             rus[a] = ru;
             rvs[a] = rv;
         }
-        const dfl pp = p_scale(p_dot2(rv, rv, df_neg(ru), ru), 0.25f);
+        const dfl pp = p_scale(u_dot2(rv, rv, df_neg(ru), ru), 0.25f);
         const dfl cc = p_scale(p_mul(ru, rv), 0.5f);
-        A[a] = {p_dot2(pp, B.pr.DP.x, cc, B.pr.DC.x), p_dot2(pp, B.pr.DP.y, cc, B.pr.DC.y)};
+        A[a] = {u_dot2(pp, B.pr.DP.x, cc, B.pr.DC.x), u_dot2(pp, B.pr.DP.y, cc, B.pr.DC.y)};
     }
     if constexpr (UNEQ) {
         slow_pair_unequal<AE>(r, kr, fo, E, A, p_addf(base, dfl{B.w2 * tf * tf, 0.f}), tdi, sct, out);
@@ -396,24 +449,24 @@ __device__ __forceinline__ void slow_pair(const Bin &B, int n, int N, dfl step, 
         const dfl ap = p_scale(p_mul(fo[a], p_addf(dfl{1.f, 0.f}, kr[a])), 0.5f);
         const dfl am = p_scale(p_mul(fo[s2], p_addf(dfl{1.f, 0.f}, df_neg(kr[a]))), 0.5f);
         const dfl Sp = sinc_pair(ap, sct), Sm = sinc_pair(am, sct);
-        const dfl thp = p_add(ap, phs[a]), thm = p_add(am, phs[s2]);
+        const dfl thp = u_add(ap, phs[a]), thm = u_add(am, phs[s2]);
         dfl c, sn;
         sincos_pair(thp, sct, c, sn);
-        const cpx eA = cp_mul(cpx{c, df_neg(sn)}, A[a]);
+        const cpx eA = cu_mul(cpx{c, df_neg(sn)}, A[a]);
         G[a] = {p_mul(Sp, eA.x), p_mul(Sp, eA.y)};
-        const dfl dl = p_sub(thm, thp);
+        const dfl dl = u_sub(thm, thp);
         const float d = dl.h + dl.l;
         cpx eAm;
         if (fabsf(d) < 1e-4f) {
-            eAm = {p_add(eA.x, dfl{d * eA.y.h, 0.f}), p_add(eA.y, dfl{-d * eA.x.h, 0.f})};
+            eAm = {u_add(eA.x, dfl{d * eA.y.h, 0.f}), u_add(eA.y, dfl{-d * eA.x.h, 0.f})};
         } else {
             sincos_pair(thm, sct, c, sn);
-            eAm = cp_mul(cpx{c, df_neg(sn)}, A[a]);
+            eAm = cu_mul(cpx{c, df_neg(sn)}, A[a]);
         }
         G[a + 3] = {p_mul(Sm, eAm.x), p_mul(Sm, eAm.y)};
     }
     // omega L, fc = e^{-i omL}, fc2 = 4 omL sin(omL) fc (gbgpu.py:362-368)
-    const dfl omL = p_addf(base, dfl{B.w2 * tf * tf, 0.f});
+    const dfl omL = u_addf(base, dfl{B.w2 * tf * tf, 0.f});
     dfl co, so;
     sincos_pair_acc(omL, sct, co, so);   // sin(omL) scales the window: relative accuracy at low f
     const cpx fc = {co, df_neg(so)};
@@ -423,23 +476,23 @@ __device__ __forceinline__ void slow_pair(const Bin &B, int n, int N, dfl step, 
         //   Z' - X' = (G31 + G13) - (G23 + G21),  D3 - D1 = (G31 + G13) - (G12 + G32),
         //   X' - 2Y' + Z' = 2 (G12 - G32) + (G21 - G23) + (G13 - G31),
         //   D1 - 2 D2 + D3 = (G12 - G32) + 2 (G21 - G23) - (G13 - G31)
-        const cpx s25 = cp_add(G[2], G[5]);
-        const cpx ga = cp_sub(G[0], G[4]), gb = cp_sub(G[3], G[1]), gc = cp_sub(G[5], G[2]);
-        const cpx wA = cp_add(cp_sub(s25, cp_add(G[1], G[3])),
-                              cp_mul(fc, cp_sub(s25, cp_add(G[0], G[4]))));
-        const cpx wE = cp_add(cp_add(cp_pow2(ga, 2.f), cp_add(gb, gc)),
-                              cp_mul(fc, cp_sub(cp_add(ga, cp_pow2(gb, 2.f)), gc)));
+        const cpx s25 = cu_add(G[2], G[5]);
+        const cpx ga = cu_sub(G[0], G[4]), gb = cu_sub(G[3], G[1]), gc = cu_sub(G[5], G[2]);
+        const cpx wA = cu_add(cu_sub(s25, cu_add(G[1], G[3])),
+                              cu_mul(fc, cu_sub(s25, cu_add(G[0], G[4]))));
+        const cpx wE = cu_add(cu_add(cp_pow2(ga, 2.f), cu_add(gb, gc)),
+                              cu_mul(fc, cu_sub(cu_add(ga, cp_pow2(gb, 2.f)), gc)));
         const dfl gA = p_mul(g4, dconst(0.70710678118654752440));
         const dfl gE = p_mul(g4, dconst(0.40824829046386301637));
-        out[0] = cp_mul(cpx{p_mul(gA, co), df_neg(p_mul(gA, so))}, wA);
-        out[1] = cp_mul(cpx{p_mul(gE, co), df_neg(p_mul(gE, so))}, wE);
+        out[0] = cu_mul(cpx{p_mul(gA, co), df_neg(p_mul(gA, so))}, wA);
+        out[1] = cu_mul(cpx{p_mul(gE, co), df_neg(p_mul(gE, so))}, wE);
     } else {
-        const cpx D1 = cp_sub(G[0], G[5]), D2 = cp_sub(G[1], G[3]), D3 = cp_sub(G[2], G[4]);
-        const cpx X0 = cp_sub(G[3], G[2]), Y0 = cp_sub(G[4], G[0]), Z0 = cp_sub(G[5], G[1]);
+        const cpx D1 = cu_sub(G[0], G[5]), D2 = cu_sub(G[1], G[3]), D3 = cu_sub(G[2], G[4]);
+        const cpx X0 = cu_sub(G[3], G[2]), Y0 = cu_sub(G[4], G[0]), Z0 = cu_sub(G[5], G[1]);
         const cpx fc2 = {p_mul(g4, co), df_neg(p_mul(g4, so))};
-        out[0] = cp_mul(fc2, cp_add(X0, cp_mul(fc, D1)));
-        out[1] = cp_mul(fc2, cp_add(Y0, cp_mul(fc, D2)));
-        out[2] = cp_mul(fc2, cp_add(Z0, cp_mul(fc, D3)));
+        out[0] = cu_mul(fc2, cu_add(X0, cu_mul(fc, D1)));
+        out[1] = cu_mul(fc2, cu_add(Y0, cu_mul(fc, D2)));
+        out[2] = cu_mul(fc2, cu_add(Z0, cu_mul(fc, D3)));
     }
 }
 
@@ -478,8 +531,8 @@ __device__ __forceinline__ void fft_reg_pass_pair(cpx *buf, int nsub, int lg, in
                 if (m & dm) continue;
                 const int rp = r + ((m & (dm - 1)) << q);
                 const cpx u = x[m], v = x[m + dm];
-                x[m] = cp_add(u, v);
-                x[m + dm] = cp_mul(cp_sub(u, v), tw_pair(rp * ts));
+                x[m] = cu_add(u, v);
+                x[m + dm] = cu_mul(cu_sub(u, v), tw_pair(rp * ts));
             }
         }
 #pragma unroll
@@ -510,9 +563,11 @@ __device__ __forceinline__ void fft_dif_pair(cpx *buf, int nsub, int lg)
     // elements per lane: no butterfly is computed twice.
     const int lane = threadIdx.x & 31;
     const int l = lane & 15;
-    cpx w[4];
+    // half-span 2 takes W^0 = 1 and W^(kTwN/4) = -i (sincospi is exact
+    // there): a swap and a sign instead of a product, with the same result
+    cpx w[3];
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
+    for (int k = 0; k < 3; k++) {
         const int hh = 4 - k;
         w[k] = tw_pair((l & ((1 << hh) - 1)) * (kTwN >> (hh + 1)));
     }
@@ -526,9 +581,9 @@ __device__ __forceinline__ void fft_dif_pair(cpx *buf, int nsub, int lg)
         const int off = e0 & ((1 << lg) - 1);
         cpx u = sub[swz(off + l, lg)], v = sub[swz(off + l + 16, lg)];
         {
-            const cpx t = cp_sub(u, v);
-            u = cp_add(u, v);
-            v = cp_mul(t, w[0]);
+            const cpx t = cu_sub(u, v);
+            u = cu_add(u, v);
+            v = cu_mul(t, w[0]);
         }
 #pragma unroll
         for (int k = 1; k < 5; k++) {
@@ -538,9 +593,11 @@ __device__ __forceinline__ void fft_dif_pair(cpx *buf, int nsub, int lg)
             const cpx rcv = {{shfl4(snd.x.h, h), shfl4(snd.x.l, h)}, {shfl4(snd.y.h, h), shfl4(snd.y.l, h)}};
             if (bit) u = rcv;
             else v = rcv;
-            const cpx t = cp_sub(u, v);
-            u = cp_add(u, v);
-            v = k < 4 ? cp_mul(t, w[k < 4 ? k : 0]) : t;
+            const cpx t = cu_sub(u, v);
+            u = cu_add(u, v);
+            if (k < 3) v = cu_mul(t, w[k]);
+            else if (k == 3) v = (l & 1) ? cpx{t.y, df_neg(t.x)} : t;
+            else v = t;
         }
         if (live) {
             sub[swz(off + 2 * l, lg)] = u;
@@ -706,11 +763,11 @@ __global__ void __launch_bounds__(kBlock, 2) pair_kernel(const KParams K)
                         const dfl er = p_mul(d2ff_scaled(dE.x, Bn.eD), wE);
                         const dfl ei = p_mul(d2ff_scaled(dE.y, Bn.eD), wE);
                         // conj(r) h / S and |h|^2 / S
-                        const dfl cr = p_add(p_dot2(ar, hA.x, ai, hA.y), p_dot2(er, hE.x, ei, hE.y));
-                        const dfl ci = p_add(p_dot2(ar, hA.y, df_neg(ai), hA.x),
-                                             p_dot2(er, hE.y, df_neg(ei), hE.x));
-                        const dfl hh2 = p_dot2(p_dot2(hA.x, hA.x, hA.y, hA.y), wA,
-                                               p_dot2(hE.x, hE.x, hE.y, hE.y), wE);
+                        const dfl cr = u_add(u_dot2(ar, hA.x, ai, hA.y), u_dot2(er, hE.x, ei, hE.y));
+                        const dfl ci = u_add(u_dot2(ar, hA.y, df_neg(ai), hA.x),
+                                             u_dot2(er, hE.y, df_neg(ei), hE.x));
+                        const dfl hh2 = u_dot2(u_dot2(hA.x, hA.x, hA.y, hA.y), wA,
+                                               u_dot2(hE.x, hE.x, hE.y, hE.y), wE);
                         if (isnew) {
                             acc8[0] = p_add(acc8[0], cr);
                             acc8[1] = p_add(acc8[1], ci);
@@ -720,10 +777,10 @@ __global__ void __launch_bounds__(kBlock, 2) pair_kernel(const KParams K)
                                 const int pk = swz(bitrev((k + (N >> 1)) & (N - 1), lg), lg);
                                 const cpx oA = buf[(po * 2 + 0) * N + pk], oE = buf[(po * 2 + 1) * N + pk];
                                 // conj(h_old) h_new / S
-                                acc8[6] = p_add(acc8[6], p_dot2(p_dot2(oA.x, hA.x, oA.y, hA.y), wA,
-                                                                p_dot2(oE.x, hE.x, oE.y, hE.y), wE));
-                                acc8[7] = p_add(acc8[7], p_dot2(p_dot2(oA.x, hA.y, df_neg(oA.y), hA.x), wA,
-                                                                p_dot2(oE.x, hE.y, df_neg(oE.y), hE.x), wE));
+                                acc8[6] = p_add(acc8[6], u_dot2(u_dot2(oA.x, hA.x, oA.y, hA.y), wA,
+                                                                u_dot2(oE.x, hE.x, oE.y, hE.y), wE));
+                                acc8[7] = p_add(acc8[7], u_dot2(u_dot2(oA.x, hA.y, df_neg(oA.y), hA.x), wA,
+                                                                u_dot2(oE.x, hE.y, df_neg(oE.y), hE.x), wE));
                             }
                         } else {
                             acc8[2] = p_add(acc8[2], cr);
@@ -835,12 +892,12 @@ __global__ void __launch_bounds__(kBlock, 2) pair_kernel(const KParams K)
                             const dfl w = df_recip(d2ff_scaled(__ldg(K.A_psd + jn), B.eS));
                             const dfl ar = d2ff_scaled(dA.x, B.eD), ai = d2ff_scaled(dA.y, B.eD);
                             const dfl er = d2ff_scaled(dE.x, B.eD), ei = d2ff_scaled(dE.y, B.eD);
-                            sr = p_add(sr, p_mul(p_add(p_dot2(ar, tA.x, ai, tA.y),
-                                                       p_dot2(er, tE.x, ei, tE.y)), w));
-                            si = p_add(si, p_mul(p_add(p_dot2(ar, tA.y, df_neg(ai), tA.x),
-                                                       p_dot2(er, tE.y, df_neg(ei), tE.x)), w));
-                            xh = p_add(xh, p_mul(p_add(p_dot2(tA.x, tA.x, tA.y, tA.y),
-                                                       p_dot2(tE.x, tE.x, tE.y, tE.y)), w));
+                            sr = p_add(sr, p_mul(u_add(u_dot2(ar, tA.x, ai, tA.y),
+                                                       u_dot2(er, tE.x, ei, tE.y)), w));
+                            si = p_add(si, p_mul(u_add(u_dot2(ar, tA.y, df_neg(ai), tA.x),
+                                                       u_dot2(er, tE.y, df_neg(ei), tE.x)), w));
+                            xh = p_add(xh, p_mul(u_add(u_dot2(tA.x, tA.x, tA.y, tA.y),
+                                                       u_dot2(tE.x, tE.x, tE.y, tE.y)), w));
                         } else {
                             const dfl wA = df_recip(d2ff_scaled(__ldg(K.A_psd + jn), B.eS));
                             const dfl wE = df_recip(d2ff_scaled(__ldg(K.E_psd + jn), B.eS));
@@ -849,11 +906,11 @@ __global__ void __launch_bounds__(kBlock, 2) pair_kernel(const KParams K)
                             const dfl ai = p_mul(d2ff_scaled(dA.y, B.eD), wA);
                             const dfl er = p_mul(d2ff_scaled(dE.x, B.eD), wE);
                             const dfl ei = p_mul(d2ff_scaled(dE.y, B.eD), wE);
-                            sr = p_add(sr, p_add(p_dot2(ar, tA.x, ai, tA.y), p_dot2(er, tE.x, ei, tE.y)));
-                            si = p_add(si, p_add(p_dot2(ar, tA.y, df_neg(ai), tA.x),
-                                                   p_dot2(er, tE.y, df_neg(ei), tE.x)));
-                            xh = p_add(xh, p_dot2(p_dot2(tA.x, tA.x, tA.y, tA.y), wA,
-                                                   p_dot2(tE.x, tE.x, tE.y, tE.y), wE));
+                            sr = p_add(sr, u_add(u_dot2(ar, tA.x, ai, tA.y), u_dot2(er, tE.x, ei, tE.y)));
+                            si = p_add(si, u_add(u_dot2(ar, tA.y, df_neg(ai), tA.x),
+                                                   u_dot2(er, tE.y, df_neg(ei), tE.x)));
+                            xh = p_add(xh, u_dot2(u_dot2(tA.x, tA.x, tA.y, tA.y), wA,
+                                                   u_dot2(tE.x, tE.x, tE.y, tE.y), wE));
                         }
                     }
                 }
