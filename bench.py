@@ -1205,6 +1205,7 @@ def run_gpu(args, rank, world):
                              "arithmetic; issue_active_frac from ncu), so the HBM fraction is "
                              "low by construction"},
         "compute": compute_roofline(Ns, t_max, clk),
+        "issue": issue_roofline(Ns, ms_head, clk),
         "e2e": {"value": world * B / e2e_max, "unit": "binaries/s",
                 "h2d_bytes_per_step": int(p.nbytes), "d2h_bytes_per_step": int(B * 8)},
         "clocks": clk.summary(),
@@ -1242,10 +1243,34 @@ def compute_roofline(Ns, ms, clk):
                     "peak = nominal FP32 (SMs x 128 x 2 x max SM clock), not measured"}
 
 
+def issue_roofline(Ns, ms, clk):
+    """The bound of the issue-limited pair kernel: its warp instructions per
+    step (``warp_instr_per_sample`` of the committed ncu summary, counted on a
+    20k-binary slice of the same workload, times the step's samples) over the
+    timed step, against the SMs' issue ceiling of one warp instruction per
+    cycle on each of an SM's four schedulers at the median SM clock sampled
+    during the timed steps."""
+    import torch
+    per = profiled("warp_instr_per_sample")
+    if per is None:
+        return None
+    props = torch.cuda.get_device_properties(torch.cuda.current_device())
+    summ = clk.summary() or {}
+    mhz = summ.get("sm_mhz") or summ.get("sm_max_mhz") or 2070.0
+    peak = props.multi_processor_count * 4 * mhz * 1e6
+    achieved = per * float(np.sum(Ns)) / (ms / 1e3)
+    return {"warp_instr_per_sample": per, "achieved": achieved, "unit": "warp instructions/s",
+            "peak": peak, "frac": achieved / peak,
+            "note": "peak = SMs x 4 schedulers x 1 warp instruction per cycle x median SM clock "
+                    "under load; the pair kernel's FP32 float-pair arithmetic is bound here, "
+                    "not by HBM"}
+
+
 def profiled(key, name="pair_ll_200k.txt"):
     """A figure of the committed ncu summary of the headline kernel (a line
     ``key: value``): ``dram_bytes_per_launch`` (dram__bytes_read.sum +
-    dram__bytes_write.sum per full-size launch) or ``issue_active_frac``."""
+    dram__bytes_write.sum per full-size launch), ``issue_active_frac`` or
+    ``warp_instr_per_sample``."""
     path = os.path.join(ROOT, "profiles", name)
     try:
         for line in open(path):
