@@ -205,6 +205,31 @@ __device__ __forceinline__ void sinc_cos_f(float a, float &S, float &C)
     }
 }
 
+// sin(a)/a alone: the S half of sinc_cos_f (same series and ranges).
+__device__ __forceinline__ float sinc_f(float a)
+{
+    const float x = a * a;
+    if (x < 0.0256f) return fmaf(fmaf(x, 1.0f / 120.0f, -1.0f / 6.0f), x, 1.0f);
+    if (x < 0.25f) {
+        float s = fmaf(x, -1.0f / 5040.0f, 1.0f / 120.0f);
+        s = fmaf(s, x, -1.0f / 6.0f);
+        return fmaf(s, x, 1.0f);
+    }
+    if (x < 2.56f) {
+        float s = -1.0f / 1307674368000.0f;
+        s = fmaf(s, x, 1.0f / 6227020800.0f);
+        s = fmaf(s, x, -1.0f / 39916800.0f);
+        s = fmaf(s, x, 1.0f / 362880.0f);
+        s = fmaf(s, x, -1.0f / 5040.0f);
+        s = fmaf(s, x, 1.0f / 120.0f);
+        s = fmaf(s, x, -1.0f / 6.0f);
+        return fmaf(s, x, 1.0f);
+    }
+    float sn, cs;
+    sincos_mod(a, sn, cs);
+    return sn / a;
+}
+
 // Shared-memory position swizzle for one length-2^lg sub-array: the low k
 // bits are XOR-ed with the top k bits (k = 4 for lg >= 8).  Bit-reversed reads
 // (the FFT output order) then spread over the banks instead of hitting one;
@@ -730,15 +755,18 @@ __device__ __forceinline__ void slow_mixed(const Bin &B, int n, int N, dfl step,
     const float *tabf = reinterpret_cast<const float *>(tab + (size_t)18 * N);
     const dfl twopi = df_from(kTwoPi);
     const float inv2pi = (float)kInvTwoPi;
-    float r[3][3];
+    // arm vectors r_12, r_23 from the table; r_31 = -(r_12 + r_23) closes the
+    // triangle, so arm 3's projections are minus the sum of the other two
+    float r[2][3];
 #pragma unroll
-    for (int a = 0; a < 3; a++)
+    for (int a = 0; a < 2; a++)
 #pragma unroll
         for (int c = 0; c < 3; c++) r[a][c] = __ldg(tabf + (size_t)(3 * a + c) * N + n);
-    float kdotr[3], fonfs[3], phh[3], phl[3];
+    float kdotr[3], fonfs[3], phh[3], phl[3], dlt[3], sml[3];
 #pragma unroll
-    for (int a = 0; a < 3; a++)
+    for (int a = 0; a < 2; a++)
         kdotr[a] = fmaf(B.kf[0], r[a][0], fmaf(B.kf[1], r[a][1], B.kf[2] * r[a][2]));
+    kdotr[2] = -(kdotr[0] + kdotr[1]);
     const dfl tm = df_mul_f(step, (float)n);                 // n T/N
     // With xi = tm - kP the carrier phase om kP - argS (gbgpu.py:495-505)
     // expands exactly into a spacecraft-independent part and powers of kP:
@@ -783,48 +811,97 @@ __device__ __forceinline__ void slow_mixed(const Bin &B, int n, int N, dfl step,
         }
         phh[s] = ph.h;
         phl[s] = ph.l;
-        // FP32: instantaneous frequency over the transfer frequency
+        // FP32: instantaneous frequency over the transfer frequency, and
+        // f(t)/f* - f(xi)/f* = kP (w1 + w2 (t + xi)) formed directly (tiny)
         const float xf = tf - kPf;
         float fo = B.w0h + fmaf(fmaf(B.w2, xf, B.w1), xf, B.w0l);
         if (THIRD) fo *= 1.0f + vl[s] * (float)(1.0 / kCSI);
         fonfs[s] = fo;
+        dlt[s] = kPf * fmaf(B.w2, tf + xf, B.w1);
+        sml[s] = small;
     }
     float2 A[3];
+    float rus[2], rvs[2];
 #pragma unroll
     for (int a = 0; a < 3; a++) {
         // r.e+.r = (r.v)^2 - (r.u)^2, r.ex.r = 2 (r.u)(r.v)  (v has no z component)
-        const float ru = fmaf(B.uf[0], r[a][0], fmaf(B.uf[1], r[a][1], B.uf[2] * r[a][2]));
-        const float rv = fmaf(B.vf[0], r[a][0], B.vf[1] * r[a][1]);
+        float ru, rv;
+        if (a < 2) {
+            ru = fmaf(B.uf[0], r[a][0], fmaf(B.uf[1], r[a][1], B.uf[2] * r[a][2]));
+            rv = fmaf(B.vf[0], r[a][0], B.vf[1] * r[a][1]);
+            rus[a] = ru;
+            rvs[a] = rv;
+        } else {
+            ru = -(rus[0] + rus[1]);
+            rv = -(rvs[0] + rvs[1]);
+        }
         const float pp = fmaf(rv, rv, -ru * ru);
         const float cc = 2.0f * ru * rv;
         A[a] = make_float2(fmaf(pp, B.DPf.x, cc * B.DCf.x), fmaf(pp, B.DPf.y, cc * B.DCf.y));
     }
-    // exp(-i phase_s) per spacecraft, the pair's low part applied to first order
-    float Er[3], Ei[3];
-#pragma unroll
-    for (int s = 0; s < 3; s++) {
-        float sn, cs;
-        sincos_mod(phh[s], sn, cs);
-        Er[s] = fmaf(sn, -phl[s], cs);
-        Ei[s] = -fmaf(cs, phl[s], sn);
-        if (STORE_E) Eout[s] = make_float2(Er[s], Ei[s]);
-    }
-    // links: G = 1/4 sinc(a) exp(-i a) exp(-i phase_s) A_arm  (gbgpu.py:509-525)
+    // links 12, 23, 31, 21, 32, 13: G = 1/4 sinc(a) exp(-i a) exp(-i phase_s)
+    // A_arm (gbgpu.py:509-525)
     float2 G[6];
-    const int arm[6] = {0, 1, 2, 0, 1, 2};
-    const int sc[6] = {0, 1, 2, 1, 2, 0};
-    const float sg[6] = {1.f, 1.f, 1.f, -1.f, -1.f, -1.f};
+    if constexpr (THIRD) {
+        // exp(-i phase_s) per spacecraft (the Doppler phases differ between
+        // spacecraft), the pair's low part applied to first order
+        float Er[3], Ei[3];
 #pragma unroll
-    for (int q = 0; q < 6; q++) {
-        const int s = sc[q];
-        float a = 0.5f * fonfs[s] * fmaf(sg[q], kdotr[arm[q]], 1.0f);
-        float S, C;
-        sinc_cos_f(a, S, C);
-        const float aS = a * S;          // sin(a)
-        const float t = 0.25f * S;
-        // (C - i aS)(Er + i Ei)
-        float2 e = make_float2(t * fmaf(C, Er[s], aS * Ei[s]), t * fmaf(C, Ei[s], -aS * Er[s]));
-        G[q] = cmul(e, A[arm[q]]);
+        for (int s = 0; s < 3; s++) {
+            float sn, cs;
+            sincos_mod(phh[s], sn, cs);
+            Er[s] = fmaf(sn, -phl[s], cs);
+            Ei[s] = -fmaf(cs, phl[s], sn);
+            if (STORE_E) Eout[s] = make_float2(Er[s], Ei[s]);
+        }
+        const int arm[6] = {0, 1, 2, 0, 1, 2};
+        const int sc[6] = {0, 1, 2, 1, 2, 0};
+        const float sg[6] = {1.f, 1.f, 1.f, -1.f, -1.f, -1.f};
+#pragma unroll
+        for (int q = 0; q < 6; q++) {
+            const int s = sc[q];
+            float a = 0.5f * fonfs[s] * fmaf(sg[q], kdotr[arm[q]], 1.0f);
+            float S, C;
+            sinc_cos_f(a, S, C);
+            const float aS = a * S;          // sin(a)
+            const float t = 0.25f * S;
+            // (C - i aS)(Er + i Ei)
+            float2 e = make_float2(t * fmaf(C, Er[s], aS * Ei[s]), t * fmaf(C, Ei[s], -aS * Er[s]));
+            G[q] = cmul(e, A[arm[q]]);
+        }
+    } else {
+        // Each link carries its spacecraft's carrier in one exponential of the
+        // summed angle a + phase_s (the angle's FP32 rounding and the phase's
+        // low part applied to first order).  The two links of arm 12 -> (a+1)
+        // carry angles a+ + phase_a and a- + phase_(a+1) whose difference is
+        //   d = [dlt_a (1 + k.r) - dlt_(a+1) (1 - k.r)] / 2 + (kP^2 terms),
+        // with dlt_s = f(t)/f* - f(xi_s)/f* (the phases differ by (L/c) k.r
+        // w(t) = k.r f(t)/f*), |d| < 1e-7 rad: the second exponential is the
+        // first one times (1 - i d), d formed from its small parts.
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const int s2 = a == 2 ? 0 : a + 1;
+            const float ap = 0.5f * fonfs[a] * (1.0f + kdotr[a]);
+            const float am = 0.5f * fonfs[s2] * (1.0f - kdotr[a]);
+            const dfl th = df_two_sum(phh[a], ap);
+            const float thl = th.l + phl[a];
+            float sn, cs;
+            sincos_mod(th.h, sn, cs);
+            const float2 eA = cmul(make_float2(fmaf(sn, -thl, cs), -fmaf(cs, thl, sn)), A[a]);
+            const float tp = 0.25f * sinc_f(ap), tq = 0.25f * sinc_f(am);
+            G[a] = make_float2(tp * eA.x, tp * eA.y);
+            const float d = fmaf(0.5f * dlt[a], 1.0f + kdotr[a], -0.5f * dlt[s2] * (1.0f - kdotr[a])) +
+                            (sml[s2] - sml[a]);
+            G[a + 3] = make_float2(tq * fmaf(d, eA.y, eA.x), tq * fmaf(-d, eA.x, eA.y));
+        }
+        if (STORE_E) {
+#pragma unroll
+            for (int s = 0; s < 3; s++) {
+                float sn, cs;
+                sincos_mod(phh[s], sn, cs);
+                Eout[s] = make_float2(fmaf(sn, -phl[s], cs), -fmaf(cs, phl[s], sn));
+            }
+        }
     }
     float omL = B.w0h + fmaf(fmaf(B.w2, tf, B.w1), tf, B.w0l);
     float so, co;
@@ -913,19 +990,22 @@ __device__ __forceinline__ void fft_dif(typename C2<R>::T *buf, int nsub, int lg
     // lower lane of a pair keeps x + y, the upper one (y - x) W: both are
     // (sg x + y) w' with sg = +-1 and w' = 1 on lower lanes (and in the last
     // stage, whose twiddles are all 1), so the stage is branch-free.
+    // Half-span 2 takes W^0 = 1 and W^(kTwN/4) = -i (sincospi is exact
+    // there): a swap and a sign on the upper odd lanes instead of a product.
     const int lane = threadIdx.x & 31;
-    V w[4];
+    V w[3];
     R sg[5];
 #pragma unroll
     for (int k = 0; k < 5; k++) {
         const int hh = 4 - k;                       // half-span 2^hh = 16 >> k
         const bool up = (lane & (16 >> k)) != 0;
         sg[k] = up ? (R)-1 : (R)1;
-        if (k < 4) {
+        if (k < 3) {
             const int rp = lane & ((1 << hh) - 1);
             w[k] = up ? tw<R>(rp * (kTwN >> (hh + 1))) : V{(R)1, (R)0};
         }
     }
+    const bool mi = (lane & 3) == 3;                // upper lane of half-span 2, W = -i
     const int chunks = (nsub << lg) >> 5;
     for (int c = threadIdx.x >> 5; c < chunks; c += kBlock >> 5) {
         const int e = (c << 5) + lane;
@@ -935,7 +1015,9 @@ __device__ __forceinline__ void fft_dif(typename C2<R>::T *buf, int nsub, int lg
         for (int k = 0; k < 5; k++) {
             const V y = shfl_c<R>(x, 16 >> k);
             const V d = {fma(sg[k], x.x, y.x), fma(sg[k], x.y, y.y)};
-            x = (k < 4) ? cmul(d, w[k < 4 ? k : 0]) : d;
+            if (k < 3) x = cmul(d, w[k]);
+            else if (k == 3) x = mi ? V{d.y, -d.x} : d;
+            else x = d;
         }
         buf[idx] = x;
     }
