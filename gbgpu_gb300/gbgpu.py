@@ -1110,6 +1110,30 @@ class GBGPUBase(abc.ABC):
         return A_out, E_out
 
     # ---------------------------------------------------- information matrix
+    def _transform_jacobian(self, params, parameter_transforms, step=1e-6):
+        """D[b, k, l] = theta_l dphi_k/dtheta_l for phi = T(theta): the
+        derivative of the transformed parameters along the reference's relative
+        step theta (1 + eps e_l), by five-point differences of the transforms on
+        the host (relative step 1e-6: truncation ~1e-24, rounding ~1e-11 of
+        the transforms' scale).  A parameter of value 0 has a zero column, as
+        the reference's relative step leaves it in place."""
+        th = np.array(params, dtype=np.float64)
+        n, B = th.shape
+        D = np.zeros((B, n, n))
+
+        def T(scale):
+            return np.asarray(self._apply_parameter_transforms(th * scale, parameter_transforms),
+                              dtype=np.float64)
+        for l in range(n):
+            sc = np.ones((n, 1))
+            v = {}
+            for k in (-2, -1, 1, 2):
+                sc[l, 0] = 1.0 + k * step
+                v[k] = T(sc)
+            with np.errstate(invalid="ignore"):
+                D[:, :, l] = ((8.0 * (v[1] - v[-1]) - (v[2] - v[-2])) / (12.0 * step)).T
+        return D
+
     def _apply_parameter_transforms(self, params, parameter_transforms):
         for ind_trans, trans in parameter_transforms.items():
             if isinstance(ind_trans, int):
@@ -1123,13 +1147,16 @@ class GBGPUBase(abc.ABC):
                            return_gpu=False, method="auto", **kwargs):
         """Fisher matrices of the reference's information_matrix (gbgpu.py:957-1138).
 
-        The reference differentiates with relative steps, h(theta (1 +- eps)), so
-        its matrices are in the logarithms of the parameters: F_ij = <theta_i
-        dh/dtheta_i | theta_j dh/dtheta_j>.  ``method="forward"`` forms them from
-        the forward-mode kernel (``gbx_fisher``: one launch, exact derivatives;
-        the 9-parameter model without parameter transforms, equal arms, N <=
-        1024); ``"differences"`` runs the reference's central differences of
-        run_wave; ``"auto"`` takes the first where it applies.
+        The reference differentiates with relative steps, h(T(theta (1 +- eps)))
+        with T the parameter transforms, so its matrices are in the logarithms
+        of the sampled parameters: F_ij = <theta_i dh/dtheta_i | theta_j
+        dh/dtheta_j>.  ``method="forward"`` forms them from the forward-mode
+        kernel (``gbx_fisher``: one launch, exact derivatives in the physical
+        parameters phi = T(theta); the 9-parameter model, equal arms, N <= 1024)
+        by the chain rule, F = D^T F_phi D with D_kl = theta_l dphi_k/dtheta_l
+        (``_transform_jacobian``; D = diag(theta) without transforms);
+        ``"differences"`` runs the reference's central differences of run_wave;
+        ``"auto"`` takes the first where it applies.
         """
         if psd_func is None:
             from .sensitivity import A1TDISens
@@ -1143,22 +1170,36 @@ class GBGPUBase(abc.ABC):
         num_bins = len(params[0])
         if inds is None:
             inds = np.arange(num_params)
-        fwd_ok = (not parameter_transforms and num_params == 9 and not self.unequal_arms and
+        fwd_ok = (num_params == 9 and not self.unequal_arms and
                   np.ndim(N) == 0 and int(N) <= 1024 and
                   set(kwargs) <= {"T", "dt", "tdi2", "oversample"})
+        D = None
+        if fwd_ok and method != "differences" and parameter_transforms:
+            D = self._transform_jacobian(params, parameter_transforms)
+            if not np.all(np.isfinite(D)):
+                fwd_ok = False      # a transform left its domain within the stencil
         if method == "forward" and not fwd_ok:
             raise ValueError("forward-mode information matrices cover the 9-parameter model "
-                             "without parameter transforms, equal arms and N <= 1024")
+                             "with equal arms and N <= 1024, and parameter transforms "
+                             "that are finite around the parameters")
         if method == "forward" or (method == "auto" and fwd_ok):
             T = kwargs.get("T", 4 * YRSID_SI)
             dt = kwargs.get("dt", 10.0)
             Tu = int(T / dt) * dt
-            prm = torch.as_tensor(np.ascontiguousarray(params, dtype=np.float64),
-                                  device=self.device)
+            phys = np.array(params, dtype=np.float64)
+            if parameter_transforms:
+                phys = np.asarray(self._apply_parameter_transforms(phys, parameter_transforms),
+                                  dtype=np.float64)
+            prm = torch.as_tensor(np.ascontiguousarray(phys), device=self.device)
             F = self._fisher_forward(prm, int(N), Tu, Tu, bool(kwargs.get("tdi2", False)),
                                      psd_func, psd_kwargs)
-            th = prm.T
-            F = F * th[:, :, None] * th[:, None, :]          # d/d ln theta, as the reference
+            if D is None:
+                th = torch.as_tensor(np.ascontiguousarray(params, dtype=np.float64).T,
+                                     device=self.device)
+                F = F * th[:, :, None] * th[:, None, :]      # d/d ln theta, as the reference
+            else:
+                Dd = torch.as_tensor(D, device=self.device)
+                F = torch.einsum("bki,bkl,blj->bij", Dd, F, Dd)
             ix = torch.as_tensor(np.asarray(inds, dtype=np.int64), device=self.device)
             F = F[:, ix][:, :, ix].contiguous()
             return F if return_gpu else F.cpu().numpy()

@@ -148,3 +148,46 @@ def test_information_matrix_forward_mode_is_the_log_parameter_fisher():
     errd = np.abs(Fd - ref) / (d[:, :, None] * d[:, None, :])
     print(f"information_matrix differences vs exact: {errd.max():.2e}")
     assert errd.max() < 1e-2
+
+
+def test_information_matrix_forward_mode_with_parameter_transforms():
+    """Sampled coordinates ln amp, cos iota, sin beta (the reference's
+    parameter_transforms): the forward path runs the kernel at the physical
+    parameters and applies D = theta_l dphi_k/dtheta_l, so it equals
+    D^T F_exact D of the exact FP64 Fisher matrix (2e-6 of sqrt(F_ii F_jj))
+    and the reference's differences to their own noise."""
+    from gbgpu_gb300 import GBGPU
+    rng = np.random.default_rng(23)
+    B, N = 6, 256
+    Tu = int(T_OBS / DT) * DT
+    q = np.rint(rng.uniform(2e-3, 4e-3, B) * Tu)
+    f0 = (q + rng.uniform(-0.3, 0.3, B)) / Tu
+    fdot = 10 ** rng.uniform(-17, -16, B)
+    phys = np.array([10 ** rng.uniform(-22.3, -21.7, B), f0, fdot, 11 / 3 * fdot ** 2 / f0,
+                     rng.uniform(0.5, 5.5, B), np.arccos(rng.uniform(-0.9, 0.9, B)),
+                     rng.uniform(0.3, 2.8, B), rng.uniform(0.5, 5.5, B),
+                     np.arcsin(rng.uniform(-0.9, 0.9, B))])
+    th = phys.copy()
+    th[0], th[5], th[8] = np.log(phys[0]), np.cos(phys[5]), np.sin(phys[8])
+    tr = {0: np.exp, 5: np.arccos, 8: np.arcsin}
+    inds = [0, 1, 2, 4, 5, 6, 7, 8]
+    gb = GBGPU()
+    Ff = gb.information_matrix(th.copy(), inds=inds, N=N, T=T_OBS, dt=DT,
+                               parameter_transforms=tr, method="forward")
+    D = np.zeros((B, 9, 9))
+    for b in range(B):
+        D[b] = np.diag(th[:, b])
+        D[b, 0, 0] = th[0, b] * phys[0, b]                       # d exp(x) = exp(x) dx
+        D[b, 5, 5] = -th[5, b] / np.sqrt(1 - th[5, b] ** 2)      # d arccos(x)
+        D[b, 8, 8] = th[8, b] / np.sqrt(1 - th[8, b] ** 2)       # d arcsin(x)
+    ref = np.einsum("bki,bkl,blj->bij", D, _exact_fisher(phys, None, N), D)[:, inds][:, :, inds]
+    d = np.sqrt(np.einsum("bii->bi", ref))
+    err = np.abs(Ff - ref) / (d[:, :, None] * d[:, None, :])
+    print(f"information_matrix forward with transforms vs exact: {err.max():.2e}")
+    assert err.max() < 2e-6
+    Fd = np.concatenate([gb.information_matrix(th[:, b:b + 1].copy(), inds=inds, N=N, T=T_OBS,
+                                               dt=DT, parameter_transforms=tr,
+                                               method="differences") for b in range(B)])
+    errd = np.abs(Fd - ref) / (d[:, :, None] * d[:, None, :])
+    print(f"information_matrix differences with transforms vs exact: {errd.max():.2e}")
+    assert errd.max() < 1e-2

@@ -445,3 +445,34 @@ def test_N_none_resolves_to_the_batch_maximum_as_the_reference():
     assert gb._resolve_N(256, g["amp"], g["f0"], YRSID_SI, (), 1) == 256
     Ns = gb._resolve_N(np.full(64, 128), g["amp"], g["f0"], YRSID_SI, (), 1)
     assert Ns.dtype == np.int64 and Ns.shape == (64,)
+
+
+def test_transform_jacobian_matches_analytic_derivatives():
+    """information_matrix's forward path: D[b, k, l] = theta_l dphi_k/dtheta_l
+    of the parameter transforms (integer and tuple keys), five-point
+    differences against the analytic derivatives, and a zero column for a
+    parameter of value 0 (the reference's relative step leaves it in place)."""
+    from gbgpu_gb300.gbgpu import GBGPUBase
+
+    class Host:
+        def _apply_parameter_transforms(self, p, t):
+            return GBGPUBase._apply_parameter_transforms(self, p, t)
+
+    rng = np.random.default_rng(1)
+    B = 5
+    th = np.array([rng.uniform(-51, -48, B), rng.uniform(1e-3, 3e-3, B),
+                   10 ** rng.uniform(-17, -16, B), np.zeros(B), rng.uniform(0.5, 5, B),
+                   rng.uniform(-0.9, 0.9, B), rng.uniform(0.3, 2.8, B), rng.uniform(0.5, 5, B),
+                   rng.uniform(-0.9, 0.9, B)])
+    tr = {0: np.exp, 5: np.arccos, 8: np.arcsin, (1, 2): lambda a, b: (a + 0.0 * b, 2.0 * b)}
+    D = GBGPUBase._transform_jacobian(Host(), th, tr)
+    for b in range(B):
+        exp = np.diag(th[:, b])
+        exp[0, 0] = th[0, b] * np.exp(th[0, b])
+        exp[5, 5] = -th[5, b] / np.sqrt(1 - th[5, b] ** 2)
+        exp[8, 8] = th[8, b] / np.sqrt(1 - th[8, b] ** 2)
+        exp[2, 2] = 2.0 * th[2, b]
+        nz = exp != 0
+        assert np.all(D[b][~nz] == 0.0)
+        assert np.max(np.abs(D[b][nz] - exp[nz]) / np.abs(exp[nz])) < 1e-8
+    assert np.all(D[:, :, 3] == 0.0)
