@@ -820,23 +820,20 @@ __device__ __forceinline__ void slow_mixed(const Bin &B, int n, int N, dfl step,
         dlt[s] = kPf * fmaf(B.w2, tf + xf, B.w1);
         sml[s] = small;
     }
+    // r.e+.r = (r.v)^2 - (r.u)^2, r.ex.r = 2 (r.u)(r.v)  (v has no z component)
+    float ru[3], rv[3];
+#pragma unroll
+    for (int a = 0; a < 2; a++) {
+        ru[a] = fmaf(B.uf[0], r[a][0], fmaf(B.uf[1], r[a][1], B.uf[2] * r[a][2]));
+        rv[a] = fmaf(B.vf[0], r[a][0], B.vf[1] * r[a][1]);
+    }
+    ru[2] = -(ru[0] + ru[1]);
+    rv[2] = -(rv[0] + rv[1]);
     float2 A[3];
-    float rus[2], rvs[2];
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        // r.e+.r = (r.v)^2 - (r.u)^2, r.ex.r = 2 (r.u)(r.v)  (v has no z component)
-        float ru, rv;
-        if (a < 2) {
-            ru = fmaf(B.uf[0], r[a][0], fmaf(B.uf[1], r[a][1], B.uf[2] * r[a][2]));
-            rv = fmaf(B.vf[0], r[a][0], B.vf[1] * r[a][1]);
-            rus[a] = ru;
-            rvs[a] = rv;
-        } else {
-            ru = -(rus[0] + rus[1]);
-            rv = -(rvs[0] + rvs[1]);
-        }
-        const float pp = fmaf(rv, rv, -ru * ru);
-        const float cc = 2.0f * ru * rv;
+        const float pp = fmaf(rv[a], rv[a], -ru[a] * ru[a]);
+        const float cc = 2.0f * ru[a] * rv[a];
         A[a] = make_float2(fmaf(pp, B.DPf.x, cc * B.DCf.x), fmaf(pp, B.DPf.y, cc * B.DCf.y));
     }
     // links 12, 23, 31, 21, 32, 13: G = 1/4 sinc(a) exp(-i a) exp(-i phase_s)
