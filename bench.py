@@ -1243,21 +1243,22 @@ def compute_roofline(Ns, ms, clk):
                     "peak = nominal FP32 (SMs x 128 x 2 x max SM clock), not measured"}
 
 
-def issue_roofline(Ns, ms, clk):
+def issue_roofline(Ns, ms, clk, sms=None):
     """The bound of the issue-limited pair kernel: its warp instructions per
     step (``warp_instr_per_sample`` of the committed ncu summary, counted on a
     20k-binary slice of the same workload, times the step's samples) over the
     timed step, against the SMs' issue ceiling of one warp instruction per
     cycle on each of an SM's four schedulers at the median SM clock sampled
     during the timed steps."""
-    import torch
     per = profiled("warp_instr_per_sample")
     if per is None:
         return None
-    props = torch.cuda.get_device_properties(torch.cuda.current_device())
+    if sms is None:
+        import torch
+        sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
     summ = clk.summary() or {}
     mhz = summ.get("sm_mhz") or summ.get("sm_max_mhz") or 2070.0
-    peak = props.multi_processor_count * 4 * mhz * 1e6
+    peak = sms * 4 * mhz * 1e6
     achieved = per * float(np.sum(Ns)) / (ms / 1e3)
     return {"warp_instr_per_sample": per, "achieved": achieved, "unit": "warp instructions/s",
             "peak": peak, "frac": achieved / peak,

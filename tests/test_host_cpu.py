@@ -476,3 +476,21 @@ def test_transform_jacobian_matches_analytic_derivatives():
         assert np.all(D[b][~nz] == 0.0)
         assert np.max(np.abs(D[b][nz] - exp[nz]) / np.abs(exp[nz])) < 1e-8
     assert np.all(D[:, :, 3] == 0.0)
+
+
+def test_issue_roofline_arithmetic():
+    """bench.issue_roofline: warp instructions per sample (from the committed
+    ncu summary) x samples / step time against SMs x 4 schedulers x clock."""
+    import bench
+
+    class Clk:
+        def summary(self):
+            return {"sm_mhz": 2000.0, "sm_max_mhz": 2070.0}
+
+    Ns = np.array([256] * 1000 + [2048] * 100)
+    r = bench.issue_roofline(Ns, 2.0, Clk(), sms=152)
+    per = bench.profiled("warp_instr_per_sample")
+    assert per is not None and r["warp_instr_per_sample"] == per
+    assert abs(r["peak"] - 152 * 4 * 2000e6) < 1.0
+    assert abs(r["achieved"] - per * Ns.sum() / 2e-3) < 1e-3 * r["achieved"]
+    assert abs(r["frac"] - r["achieved"] / r["peak"]) < 1e-12
